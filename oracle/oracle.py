@@ -1,0 +1,150 @@
+"""ctypes wrapper of the C oracle (oracle.c) -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may
+import this module.  It restates codeml's branch-site model A likelihood on
+the CPU (see oracle.c for the reference routine behind each function) and is
+the checker for the CUDA library, never the thing measured or shipped.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+
+
+class _Problem(C.Structure):
+    _fields_ = [
+        ("ns", C.c_int), ("nnode", C.c_int), ("root", C.c_int), ("npatt", C.c_int),
+        ("nson", C.POINTER(C.c_int)), ("sons", C.POINTER(C.c_int)),
+        ("label", C.POINTER(C.c_int)), ("bnode", C.POINTER(C.c_int)),
+        ("z", C.POINTER(C.c_ubyte)), ("fpatt", C.POINTER(C.c_double)),
+        ("pi", C.POINTER(C.c_double)), ("nthreads", C.c_int),
+    ]
+
+
+def build(force: bool = False) -> str:
+    src = os.path.join(HERE, "oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    return LIB_PATH
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        dp = C.POINTER(C.c_double)
+        L.oracle_lnL.restype = C.c_double
+        L.oracle_lnL.argtypes = [C.POINTER(_Problem), dp, C.c_int, dp, dp, C.POINTER(C.c_int)]
+        L.oracle_patterns.restype = C.c_int
+        L.oracle_patterns.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                      C.POINTER(C.c_ubyte), dp, dp]
+        L.oracle_set_params.restype = C.c_int
+        L.oracle_set_params.argtypes = [C.POINTER(_Problem), dp, C.c_int, dp, dp, dp, dp, dp]
+        L.oracle_gradientB.restype = C.c_int
+        L.oracle_gradientB.argtypes = [C.POINTER(_Problem), dp, C.c_int, C.c_int, C.c_int, dp]
+        L.oracle_build_q.restype = C.c_double
+        L.oracle_build_q.argtypes = [dp, C.c_double, C.c_double, dp]
+        L.oracle_pmat.restype = None
+        L.oracle_pmat.argtypes = [dp, C.c_double, dp, dp, dp]
+        L.oracle_max_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def patterns(codons: np.ndarray):
+    """codons [ns, ncodon] (0..60) -> (z [ns, npatt] uint8, fpatt [npatt], pi [61])."""
+    codons = np.ascontiguousarray(codons, dtype=np.int32)
+    ns, nc = codons.shape
+    z = np.zeros(ns * nc, dtype=np.uint8)
+    fp = np.zeros(nc)
+    pi = np.zeros(61)
+    npatt = C.c_int(0)
+    rc = lib().oracle_patterns(ns, nc, codons.ctypes.data_as(C.POINTER(C.c_int)), C.byref(npatt),
+                               z.ctypes.data_as(C.POINTER(C.c_ubyte)), _dp(fp), _dp(pi))
+    if rc:
+        raise ValueError(f"oracle_patterns failed rc={rc}")
+    n = npatt.value
+    return z[: ns * n].reshape(ns, n).copy(), fp[:n].copy(), pi
+
+
+class Problem:
+    """A tree + compressed patterns + codon frequencies, held for the C oracle."""
+
+    def __init__(self, tree, z: np.ndarray, fpatt: np.ndarray, pi: np.ndarray, nthreads: int = 0):
+        self.tree = tree
+        nn = tree.nnode
+        self.nson = np.array([len(tree.sons[i]) for i in range(nn)], dtype=np.int32)
+        sons = np.full((nn, 3), -1, dtype=np.int32)
+        for i in range(nn):
+            for k, s in enumerate(tree.sons[i]):
+                sons[i, k] = s
+        self.sons = sons.reshape(-1).copy()
+        self.label = np.ascontiguousarray(tree.label, dtype=np.int32)
+        self.bnode = np.ascontiguousarray(tree.branch_nodes(), dtype=np.int32)
+        self.z = np.ascontiguousarray(z, dtype=np.uint8)
+        self.fpatt = np.ascontiguousarray(fpatt, dtype=np.float64)
+        self.pi = np.ascontiguousarray(pi, dtype=np.float64)
+        self.npatt = int(self.fpatt.shape[0])
+        self.np = tree.nbranch + 5
+        ip = C.POINTER(C.c_int)
+        self._s = _Problem(tree.ns, nn, tree.root, self.npatt,
+                           self.nson.ctypes.data_as(ip), self.sons.ctypes.data_as(ip),
+                           self.label.ctypes.data_as(ip), self.bnode.ctypes.data_as(ip),
+                           self.z.ctypes.data_as(C.POINTER(C.c_ubyte)), _dp(self.fpatt),
+                           _dp(self.pi), int(nthreads))
+
+    def set_threads(self, n: int) -> None:
+        self._s.nthreads = int(n)
+
+    def neg_lnL(self, x, lastround: bool = True, want_fhK: bool = False):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        fhK = np.zeros(4 * self.npatt) if want_fhK else None
+        lnf = np.zeros(self.npatt) if want_fhK else None
+        nsc = C.c_int(0)
+        v = lib().oracle_lnL(C.byref(self._s), _dp(x), int(lastround),
+                             _dp(fhK) if fhK is not None else None,
+                             _dp(lnf) if lnf is not None else None, C.byref(nsc))
+        if want_fhK:
+            return v, fhK.reshape(4, self.npatt), lnf, nsc.value
+        return v
+
+    def set_params(self, x, lastround: bool = True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        U = np.zeros((3, 61, 61)); V = np.zeros((3, 61, 61)); R = np.zeros((3, 61))
+        qf = np.zeros(2); fk = np.zeros(4)
+        rc = lib().oracle_set_params(C.byref(self._s), _dp(x), int(lastround), _dp(U), _dp(V),
+                                     _dp(R), _dp(qf), _dp(fk))
+        if rc:
+            raise ValueError("parameter error")
+        return U, V, R, qf, fk
+
+    def gradientB(self, x, lastround: bool = True, central: bool = True):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        g = np.zeros(len(x))
+        lib().oracle_gradientB(C.byref(self._s), _dp(x), len(x), int(lastround), int(central), _dp(g))
+        return g
+
+
+def build_q(pi, kappa, omega):
+    Q = np.zeros((61, 61))
+    pi = np.ascontiguousarray(pi, dtype=np.float64)
+    mr = lib().oracle_build_q(_dp(pi), float(kappa), float(omega), _dp(Q))
+    return Q, mr
+
+
+def max_threads() -> int:
+    return int(lib().oracle_max_threads())

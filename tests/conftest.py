@@ -1,0 +1,38 @@
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built library")
+
+
+def golden_names():
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.endswith(".json"))
+
+
+def load_golden(name):
+    """Fixture dict plus parsed tree and codon matrix [ns, ncodon]."""
+    from cucodeml_gb300 import codon
+    from cucodeml_gb300.tree import parse_newick
+
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        fx = json.load(f)
+    tree = parse_newick(fx["newick"], fx["names"])
+    lut = {codon.codon_string(i): i for i in range(61)}
+    codons = np.array([[lut[c] for c in row.split()] for row in fx["codons"]], dtype=np.int64)
+    return fx, tree, codons
+
+
+@pytest.fixture(params=golden_names())
+def golden(request):
+    return load_golden(request.param)

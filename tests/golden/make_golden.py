@@ -1,0 +1,138 @@
+"""Generate golden fixtures by running the reference codeml (CPU build).
+
+Test infrastructure.  Needs the reference sources (REF, default
+/root/reference) to build oracle/_ref/codeml via `make -C oracle ref`; the
+fixtures it writes (tests/golden/*.json) are committed, so tests never need
+the reference at run time.
+
+For each case a seeded model-A alignment is simulated, written as PHYLIP +
+Newick (#1 on the foreground branch), and codeml is run at FIXED parameters:
+in.codeml starts with -1, so codeml evaluates lnL once at x with p0, p1
+untransformed (readx treesub.c:3927, Forestry codeml.c:646-673) and, with
+RateAncestor = -1, writes per-pattern log f to file `lnf` together with the
+pattern's codons and count (print_lnf_site treesub.c:7332-7340).  The
+fixture keeps: the codon alignment, tree, x, codeml's lnL (out file, 6 dp),
+per-pattern log f (10 dp), pattern codons and counts (pattern order), and the
+F3x4 codon frequencies (out file, 8 dp).
+
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+
+from cucodeml_gb300 import codon  # noqa: E402
+from cucodeml_gb300.simulate import ModelA, simulate, write_phylip  # noqa: E402
+
+CTL = """\
+      seqfile = seq.phy
+     treefile = tree.nwk
+      outfile = out.txt
+        noisy = 0
+      verbose = 1
+      runmode = 0
+      seqtype = 1
+    CodonFreq = 2
+        clock = 0
+       aaDist = 0
+        model = 2
+      NSsites = 2
+        icode = 0
+        Mgene = 0
+    fix_kappa = 0
+        kappa = 2
+    fix_omega = 0
+        omega = 1
+    fix_alpha = 1
+        alpha = 0
+       Malpha = 0
+        ncatG = 4
+        getSE = 0
+ RateAncestor = -1
+   Small_Diff = 1e-6
+    cleandata = 1
+  fix_blength = 0
+       method = 0
+"""
+
+# name, ns, ncodon, seed, simulation model, evaluation params (kappa,p0,p1,w0,w2), blen scale
+CASES = [
+    ("c8x300_s1", 8, 300, 1, ModelA(), (2.0, 0.5, 0.3, 0.3, 3.0), 1.0),
+    ("c8x300_s2", 8, 300, 2, ModelA(kappa=1.5, omega0=0.1, omega2=5.0, p0=0.6, p1=0.25),
+     (1.7, 0.55, 0.3, 0.15, 4.0), 1.3),
+    ("c5x120_s5", 5, 120, 5, ModelA(), (2.5, 0.4, 0.4, 0.5, 2.0), 0.7),
+    ("c24x400_s3", 24, 400, 3, ModelA(), (2.0, 0.5, 0.3, 0.3, 3.0), 1.0),
+    ("c40x200_s4", 40, 200, 4, ModelA(kappa=3.0, omega0=0.2, omega2=6.0, p0=0.45, p1=0.35),
+     (2.8, 0.45, 0.35, 0.25, 5.5), 1.0),
+    ("c12x150_s6_long", 12, 150, 6, ModelA(), (2.0, 0.5, 0.3, 0.3, 3.0), 6.0),
+]
+
+
+def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, zero_branch=False):
+    aln = simulate(ns, ncodon, seed=seed, model=model)
+    tree = aln.tree
+    xb = tree.x_branch_lengths() * bscale
+    if name.startswith("c5x120"):
+        xb[2] = 0.0          # internal branch with t = 0: P = I (PMatUVRoot, t < 1e-100)
+        xb[1] = 0.01         # short tip branch (P entries of order t^3 stay well-conditioned)
+    x = np.concatenate([xb, list(params)])
+    with tempfile.TemporaryDirectory() as d:
+        write_phylip(os.path.join(d, "seq.phy"), aln)
+        with open(os.path.join(d, "tree.nwk"), "w") as f:
+            f.write(f"{ns} 1\n{tree.to_newick()}\n")
+        with open(os.path.join(d, "in.codeml"), "w") as f:
+            f.write("-1 " + " ".join(repr(float(v)) for v in x) + "\n")
+        with open(os.path.join(d, "codeml.ctl"), "w") as f:
+            f.write(CTL)
+        subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True,
+                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        out = open(os.path.join(d, "out.txt")).read()
+        lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
+    m = re.search(r"lnL\(ntime:\s*(\d+)\s+np:\s*(\d+)\):\s*(-?\d+\.\d+)", out)
+    lnL = float(m.group(3))
+    i0 = out.index("Codon frequencies under model")
+    vals = [float(v) for v in out[i0:].split("\n", 1)[1].split()[:64]]
+    pi8 = [vals[k] for k in codon.SENSE64]
+    pats, fp, lnf = [], [], []
+    for ln in lnf_lines:
+        parts = ln.split()
+        if len(parts) > 5 and parts[0].isdigit() and re.match(r"^-?\d", parts[2]):
+            if int(parts[0]) == 1:       # codeml writes one block per lfundG call: keep the last
+                pats, fp, lnf = [], [], []
+            fp.append(float(parts[1]))
+            lnf.append(float(parts[2]))
+            pats.append([p for p in parts[5:] if not p.startswith("(")])
+    lut = [codon.codon_string(i) for i in range(61)]
+    return {
+        "name": name, "ns": ns, "ncodon": ncodon, "seed": seed,
+        "names": tree.names, "newick": tree.to_newick(digits=17),
+        "codons": [" ".join(lut[c] for c in row) for row in aln.codons],
+        "x": [float(v) for v in x], "lastround": 1,
+        "codeml_lnL": lnL, "codeml_np": int(m.group(2)),
+        "lnf": lnf, "fpatt": fp, "patterns": [" ".join(p) for p in pats], "pi_8dp": pi8,
+    }
+
+
+def main():
+    subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
+    codeml = os.path.join(ROOT, "oracle", "_ref", "codeml")
+    outdir = os.path.dirname(os.path.abspath(__file__))
+    for case in CASES:
+        fx = run_case(codeml, *case)
+        with open(os.path.join(outdir, fx["name"] + ".json"), "w") as f:
+            json.dump(fx, f, separators=(",", ":"))
+        print(fx["name"], "npatt", len(fx["lnf"]), "lnL", fx["codeml_lnL"])
+
+
+if __name__ == "__main__":
+    main()

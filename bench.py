@@ -1,0 +1,345 @@
+"""Benchmark: branch-site model A lnL+gradient evaluations per second on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision fast|fp64] [--ns 64] [--ncodon 5000]
+
+Workload (one "step"): one lnL + analytic-gradient evaluation of a 64-taxon x
+5000-codon alignment (seeded model-A simulation: random unrooted tree,
+branch lengths ~Exp(0.1), one foreground branch, F3x4 from Dirichlet(5),
+kappa=2, w0=0.3, w2=3, p0=0.5, p1=0.3), gradient w.r.t. all 125 branch
+lengths, kappa, w0, w2, p0, p1.
+
+* value  -- device-resident throughput: the evaluation's CUDA graphs replayed
+            K times with inputs already on the device (CUDA events).
+* e2e    -- the same metric through the public API (gb_eval with host arrays:
+            host model set-up, host->device parameter copy, device->host result
+            and gradient copies inside the timed region).
+* roofline -- the dominant kernel class, algorithmic FLOPs / its measured time.
+* cpu_baseline -- the oracle (CPU restatement of codeml's lnfundG path) on the
+            host cores, a bounded sample of lnL evaluations; a CPU lnL+gradient
+            costs np+1 lnL evaluations (codeml's forward-difference gradientB).
+--impl reference times that CPU implementation as the reference arm.
+Multi-GPU: replicas only (each rank evaluates its own copy); value sums ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "lnL+gradient evals/sec on 1 GB300 vs plain FP64 GPU & host CPU at |ΔlnL|≤1e-6"
+PARAMS = dict(kappa=2.0, omega0=0.3, omega2=3.0, p0=0.5, p1=0.3)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(ns: int, ncodon: int, seed: int = 2024):
+    from cucodeml_gb300 import api
+    from cucodeml_gb300.simulate import simulate
+    aln = simulate(ns, ncodon, seed=seed)
+    z, fpatt, pi = api.patterns(aln.codons)
+    return aln.tree, z, fpatt, pi
+
+
+def count_flops(lk_tree, z, fpatt):
+    """Algorithmic FLOPs of one lnL and one lnL+gradient evaluation.
+
+    Contractions: 2*61^2*npatt per (node, class, internal child) computed by the
+    minimal schedule (classes 0,1 at every node, 2a/2b only where a foreground
+    branch lies below); P(t): 2*61^3 per unique (branch, omega) pair.
+    lnL+gradient = 3 x lnL (forward, adjoint propagation, dlnL/dP)."""
+    tree = lk_tree
+    ns, nn = tree.ns, tree.nnode
+    dirty = np.zeros(nn, dtype=bool)
+    for n in tree.postorder():
+        for s in tree.sons[n]:
+            if tree.label[s] == 1 or dirty[s]:
+                dirty[n] = True
+    nc = 0
+    for a in range(ns, nn):
+        ncls = 4 if (dirty[a] or a == tree.root) else 2
+        nc += ncls * sum(1 for s in tree.sons[a] if s >= ns)
+    npair = sum(3 if tree.label[n] else 2 for n in range(nn) if n != tree.root)
+    P = len(fpatt)
+    f_contr = 2.0 * 61 * 61 * P * nc
+    f_pmat = 2.0 * 61 ** 3 * npair
+    return {"contractions": nc, "npair": npair, "flops_prune": f_contr, "flops_pmat": f_pmat,
+            "flops_lnL": f_contr + f_pmat, "flops_lnL_grad": 3 * (f_contr + f_pmat),
+            "flops_nominal_lnL": 4.0 * (nn - ns - 1) * 2 * 61 * 61 * P}
+
+
+def fp64_peak_tflops():
+    """FP64 GEMM throughput (cuBLAS DGEMM via torch), the FP64 roof of this GPU."""
+    import torch
+    n = 4096
+    a = torch.rand(n, n, dtype=torch.float64, device="cuda")
+    b = torch.rand(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(3):
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    del a, b
+    return best
+
+
+def cpu_baseline(tree, z, fpatt, pi, threads: int, seconds: float = 12.0, min_evals: int = 2):
+    """Time the oracle's lnL on the host cores; lnL+gradient = (np+1) lnL evals."""
+    from oracle import oracle as O
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=threads)
+    x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
+                                                  PARAMS["omega0"], PARAMS["omega2"]]])
+    pb.neg_lnL(x)       # warm-up
+    t0 = time.perf_counter()
+    n = 0
+    while n < min_evals or time.perf_counter() - t0 < seconds:
+        pb.neg_lnL(x)
+        n += 1
+        if time.perf_counter() - t0 > 3 * seconds:
+            break
+    dt = (time.perf_counter() - t0) / n
+    np_ = tree.nbranch + 5
+    return {"value": 1.0 / ((np_ + 1) * dt), "unit": "evals/s", "cores": threads, "kind": "port",
+            "sample": f"{n} lnL evaluations of the workload on {threads} threads, {dt:.3f} s each; "
+                      f"lnL+gradient = np+1 = {np_ + 1} lnL evaluations (forward-difference gradientB)",
+            "lnL_eval_s": dt}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    tree, z, fpatt, pi = make_workload(args.ns, args.ncodon)
+    from oracle import oracle as O
+    threads = O.max_threads()
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=threads)
+    x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
+                                                  PARAMS["omega0"], PARAMS["omega2"]]])
+    for _ in range(args.warmup):
+        pb.neg_lnL(x)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pb.neg_lnL(x)
+    dt = (time.perf_counter() - t0) / args.steps
+    np_ = tree.nbranch + 5
+    value = 1.0 / ((np_ + 1) * dt)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 * (np_ + 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded model-A simulation)",
+        "config": {"workload": f"lnL+gradient, {args.ns} taxa x {args.ncodon} codons, branch-site model A",
+                   "npatt": int(len(fpatt)), "np": np_},
+        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} lnL evaluations per run on {threads} threads "
+                                   f"({dt:.3f} s each); lnL+gradient = np+1 lnL evaluations "
+                                   "(codeml's forward-difference gradientB)"},
+        "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="best", choices=["best", "fast", "fp64"])
+    ap.add_argument("--ns", type=int, default=64)
+    ap.add_argument("--ncodon", type=int, default=5000)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = local if torch.cuda.is_available() else 0
+    torch.cuda.set_device(dev)
+
+    from cucodeml_gb300 import api
+    tree, z, fpatt, pi = make_workload(args.ns, args.ncodon)
+    fl = count_flops(tree, z, fpatt)
+    precision = "fp64" if args.precision in ("best", "fp64") else "fast"
+    try:
+        if args.precision == "best":
+            api.Likelihood(tree, z, fpatt, pi, precision="fast", device=dev).close()
+            precision = "fast"
+    except Exception:
+        precision = "fp64"
+    lk = api.Likelihood(tree, z, fpatt, pi, precision=precision, device=dev)
+    bl0 = tree.branch.copy()
+    rng = np.random.default_rng(7)
+
+    def step_params(i):
+        return bl0 * (1.0 + 0.01 * rng.standard_normal(bl0.shape)).clip(0.5, 1.5)
+
+    # warm-up through the public API (builds the graphs)
+    for i in range(args.warmup):
+        r = lk.evaluate(step_params(i), grad=True, **PARAMS)
+    # ---- e2e: public API with host buffers, K steps
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    h2d = d2h = 0.0
+    with ClockSampler(dev) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            r = lk.evaluate(step_params(i), grad=True, **PARAMS)
+            h2d += r.h2d_bytes
+            d2h += r.d2h_bytes
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+        # ---- value: device-resident replay of the evaluation's graphs
+        for _ in range(args.warmup):
+            lk.replay(1, True)
+        dev_ms = lk.replay(args.steps, True)
+    kernels_per_eval = r.kernels
+    if ws > 1:
+        t = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dev_ms, e2e_s = float(t[0]), float(t[1])
+    value = ws * args.steps / (dev_ms * 1e-3)
+    e2e_value = ws * args.steps / e2e_s
+
+    # ---- per-kernel-class times (outside the timed region)
+    prof = lk.profile(3, True)
+    tot = sum(v[0] for v in prof.values())
+    cls_flops = {"prune": fl["flops_prune"], "bwd": fl["flops_prune"], "gradP": fl["flops_prune"],
+                 "pmat": fl["flops_pmat"], "gradH": 2 * fl["flops_pmat"]}
+    top = max(prof, key=lambda k: prof[k][0])
+    top_ms_per_eval = prof[top][0] / 3
+    achieved = cls_flops.get(top, 0.0) / (top_ms_per_eval * 1e-3) / 1e12
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    if precision == "fp64":
+        peak = fp64_peak_tflops()
+        roof = {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe; no FP64 entry "
+                               "in the measured-peaks file)"}
+    else:
+        peak = peaks.get("bf16_tflops", 1928.4)
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": "bf16_tflops of measured" if peaks else "fallback"}
+    roof.update({"kernel": top, "share": prof[top][0] / tot if tot else None,
+                 "flops_per_eval": cls_flops.get(top, 0.0), "ms_per_eval": top_ms_per_eval,
+                 "classes_ms_per_eval": {k: v[0] / 3 for k, v in prof.items()}})
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f64+split",
+        "data": "synthetic (seeded model-A simulation, seed 2024)",
+        "config": {"workload": f"lnL+gradient, {args.ns} taxa x {args.ncodon} codons, branch-site model A",
+                   "npatt": int(len(fpatt)), "np": tree.nbranch + 5, "precision": precision,
+                   "l2": "working set per evaluation > L2 (no flush needed)",
+                   "parallelism": f"replicas x{ws}", "flops_lnL_grad_alg": fl["flops_lnL_grad"],
+                   "flops_nominal_lnL": fl["flops_nominal_lnL"]},
+        "roofline": roof,
+        "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": h2d / args.steps,
+                "d2h_bytes_per_step": d2h / args.steps},
+        "clocks": clk.summary(),
+        "gpu_launches": int(kernels_per_eval * args.steps),
+        "achieved_tflops_alg": fl["flops_lnL_grad"] * args.steps / (dev_ms * 1e-3) / 1e12,
+    }
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle as O
+        line["cpu_baseline"] = cpu_baseline(tree, z, fpatt, pi, O.max_threads())
+    lk.close()
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

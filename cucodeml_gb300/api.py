@@ -1,0 +1,189 @@
+"""Python host mirror of the library's C ABI, shaped like codeml's interface.
+
+`Likelihood` is one gb_handle: one tree + compressed alignment on one GPU.
+Its methods mirror the reference's calls on the model-A hot path:
+
+* `neg_lnL_uvr(...)`   codeml's CUDA_lfundG / CUDA_fx_r from host U, V, Root,
+                       Qfactor and class proportions (treesub.c:7397-7450,
+                       7554-7595); returns -lnL, com.fhK and per-pattern log f.
+* `evaluate(...)`      -lnL (and optionally its analytic gradient) from the
+                       natural parameters.
+* `dfun_x(x, ...)`     ming2's dfun hook over codeml's x vector
+                       (tools.c:6361-6363).
+
+All work runs in libgbcodeml.so; nothing here computes likelihoods.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from .tree import Tree
+
+_dp = C.POINTER(C.c_double)
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def patterns(codons: np.ndarray):
+    """Codon alignment [ns, ncodon] (sense codon ids) -> (z [ns, npatt], fpatt, pi)."""
+    L = _lib.load()
+    codons = np.ascontiguousarray(codons, dtype=np.int32)
+    ns, nc = codons.shape
+    z = np.zeros(ns * nc, dtype=np.uint8)
+    fp = np.zeros(nc)
+    pi = np.zeros(61)
+    npatt = C.c_int(0)
+    _lib.check(L.gb_patterns(ns, nc, codons.ctypes.data_as(C.POINTER(C.c_int)), C.byref(npatt),
+                             z.ctypes.data_as(C.POINTER(C.c_ubyte)), _ptr(fp), _ptr(pi)))
+    n = npatt.value
+    return z[: ns * n].reshape(ns, n).copy(), fp[:n].copy(), pi
+
+
+def model_setup(pi, kappa, omega0, omega2, p0, p1):
+    """(U [3,61,61], V [3,61,61], Root [3,61], qf [2], freqK [4]) computed by the library's host code."""
+    L = _lib.load()
+    pi = np.ascontiguousarray(pi, dtype=np.float64)
+    U = np.zeros((3, 61, 61)); V = np.zeros((3, 61, 61)); R = np.zeros((3, 61))
+    qf = np.zeros(2); fk = np.zeros(4)
+    _lib.check(L.gb_model_setup(_ptr(pi), kappa, omega0, omega2, p0, p1, _ptr(U), _ptr(V), _ptr(R),
+                                _ptr(qf), _ptr(fk)))
+    return U, V, R, qf, fk
+
+
+@dataclass
+class EvalResult:
+    neg_lnL: float
+    fhK: np.ndarray | None = None
+    lnf: np.ndarray | None = None
+    grad: dict | None = None
+    ms_device: float = 0.0
+    ms_host: float = 0.0
+    kernels: int = 0
+    h2d_bytes: float = 0.0
+    d2h_bytes: float = 0.0
+
+
+class Likelihood:
+    def __init__(self, tree: Tree, z: np.ndarray, fpatt: np.ndarray, pi: np.ndarray,
+                 precision: str = "fp64", device: int = 0, node_scale=None):
+        self._L = _lib.load()
+        self.tree = tree
+        self.ns, self.nnode = tree.ns, tree.nnode
+        self.npatt = int(len(fpatt))
+        self._father = np.ascontiguousarray(tree.father, dtype=np.int32)
+        self._label = np.ascontiguousarray(tree.label, dtype=np.int32)
+        self._z = np.ascontiguousarray(z, dtype=np.uint8)
+        self._fpatt = np.ascontiguousarray(fpatt, dtype=np.float64)
+        self._pi = np.ascontiguousarray(pi, dtype=np.float64)
+        self._scale = None
+        if node_scale is not None:
+            self._scale = np.ascontiguousarray(node_scale, dtype=np.int8).tobytes()
+        prec = {"fp64": _lib.GB_PREC_FP64, "fast": _lib.GB_PREC_FAST}[precision]
+        ip = C.POINTER(C.c_int)
+        self._prob = _lib.Problem(self.ns, self.nnode, tree.root, self._father.ctypes.data_as(ip),
+                                  self._label.ctypes.data_as(ip), self.npatt,
+                                  self._z.ctypes.data_as(C.POINTER(C.c_ubyte)), _ptr(self._fpatt),
+                                  _ptr(self._pi), self._scale, prec, device)
+        h = C.c_void_p()
+        _lib.check(self._L.gb_create(C.byref(self._prob), C.byref(h)))
+        self._h = h
+        self.bnode = np.ascontiguousarray(tree.branch_nodes(), dtype=np.int32)
+
+    @property
+    def nscale(self) -> int:
+        return int(self._L.gb_nscale(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.gb_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def neg_lnL_uvr(self, U, V, Root, qfactor, freqK, blength, want_site=True) -> EvalResult:
+        U = [np.ascontiguousarray(u, dtype=np.float64) for u in U]
+        V = [np.ascontiguousarray(v, dtype=np.float64) for v in V]
+        R = [np.ascontiguousarray(r, dtype=np.float64) for r in Root]
+        qf = np.ascontiguousarray(qfactor, dtype=np.float64)
+        fk = np.ascontiguousarray(freqK, dtype=np.float64)
+        bl = np.ascontiguousarray(blength, dtype=np.float64)
+        f = C.c_double(0)
+        fhK = np.zeros((4, self.npatt)) if want_site else None
+        lnf = np.zeros(self.npatt) if want_site else None
+        st = _lib.Stats()
+        arr3 = _dp * 3
+        _lib.check(self._L.gb_eval_uvr(self._h, arr3(*[_ptr(u) for u in U]), arr3(*[_ptr(v) for v in V]),
+                                       arr3(*[_ptr(r) for r in R]), _ptr(qf), _ptr(fk), _ptr(bl),
+                                       C.byref(f), _ptr(fhK) if want_site else None,
+                                       _ptr(lnf) if want_site else None, C.byref(st)))
+        return EvalResult(f.value, fhK, lnf, None, st.ms_device, st.ms_host, st.kernels)
+
+    def evaluate(self, blength, kappa, omega0, omega2, p0, p1, grad: bool = False,
+                 want_site: bool = False) -> EvalResult:
+        bl = np.ascontiguousarray(blength, dtype=np.float64)
+        prm = _lib.Params(_ptr(bl), kappa, omega0, omega2, p0, p1)
+        f = C.c_double(0)
+        st = _lib.Stats()
+        g = None
+        dbl = None
+        if grad:
+            dbl = np.zeros(self.nnode)
+            g = _lib.Grad(_ptr(dbl), 0, 0, 0, 0, 0)
+        fhK = np.zeros((4, self.npatt)) if want_site else None
+        lnf = np.zeros(self.npatt) if want_site else None
+        _lib.check(self._L.gb_eval(self._h, C.byref(prm), C.byref(f), C.byref(g) if grad else None,
+                                   _ptr(fhK) if want_site else None, _ptr(lnf) if want_site else None,
+                                   C.byref(st)))
+        gd = None
+        if grad:
+            gd = {"blength": dbl, "kappa": g.d_kappa, "omega0": g.d_omega0, "omega2": g.d_omega2,
+                  "p0": g.d_p0, "p1": g.d_p1}
+        return EvalResult(f.value, fhK, lnf, gd, st.ms_device, st.ms_host, st.kernels,
+                          st.h2d_bytes, st.d2h_bytes)
+
+    def replay(self, iters: int, with_grad: bool) -> float:
+        """Device ms for `iters` re-runs of the last evaluation with inputs resident."""
+        ms = C.c_double(0)
+        _lib.check(self._L.gb_replay(self._h, int(iters), int(with_grad), C.byref(ms)))
+        return ms.value
+
+    def profile(self, iters: int, with_grad: bool) -> dict:
+        """Per kernel class: (device ms summed over iters, launches)."""
+        ms = np.zeros(len(_lib.KCLASS))
+        n = np.zeros(len(_lib.KCLASS), dtype=np.int32)
+        _lib.check(self._L.gb_profile(self._h, int(iters), int(with_grad), _ptr(ms),
+                                      n.ctypes.data_as(C.POINTER(C.c_int))))
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_lib.KCLASS)}
+
+    def evaluate_x(self, x, lastround: bool = True, grad: bool = False) -> EvalResult:
+        """-lnL (and gradient in node order) from codeml's x vector."""
+        x = np.asarray(x, dtype=np.float64)
+        nb = self.nnode - 1
+        bl = np.zeros(self.nnode)
+        bl[self.bnode] = x[:nb]
+        kappa, w0, w2 = x[nb], x[nb + 3], x[nb + 4]
+        if lastround:
+            p0, p1 = x[nb + 1], x[nb + 2]
+        else:
+            e = np.exp(x[nb + 1:nb + 3])
+            p0, p1 = e / (1 + e.sum())
+        return self.evaluate(bl, kappa, w0, w2, p0, p1, grad=grad)
+
+    def dfun_x(self, x, lastround: bool = True):
+        """(f, dx) as ming2's dfun hook: f = -lnL, dx = d(-lnL)/dx in codeml's x space."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        f = C.c_double(0)
+        dx = np.zeros(len(x))
+        _lib.check(self._L.gb_dfun_x(self._h, self.bnode.ctypes.data_as(C.POINTER(C.c_int)),
+                                     int(lastround), _ptr(x), len(x), C.byref(f), _ptr(dx)))
+        return f.value, dx

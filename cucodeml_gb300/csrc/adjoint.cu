@@ -1,0 +1,581 @@
+// FP64 adjoint (reverse-mode) gradient of lnL for branch-site model A.
+//
+// The reference has no analytic gradient: codeml's optimiser ming2 takes a
+// gradient hook (tools.c:6361-6363) but is given NULL (codeml.c:688), so every
+// gradient costs np or 2np likelihood evaluations through gradientB
+// (tools.c:6326-6350).  This module differentiates the forward evaluation of
+// runtime.cu exactly:
+//
+//   forward  L_a = prod_i E_i,  E_i = P_i L~_{s_i}  (tips: rows of P),
+//            L~_a = L_a / m_a at scaled nodes, f~ = pi . L~_root,
+//            lnL = sum_h fpatt_h log sum_c freqK_c e^{S_c} f~_c.
+//   seeds    dlnL/dL~_root,c[h][j] = fpatt_h rho_c,h / f~_c,h * pi_j
+//            (rho = posterior of the site class).  Node scales m are held
+//            constant: lnL is invariant to them.
+//   sweep    top-down over the same levels: Ebar_i = (Abar_a / m_a) . prod_{i'!=i} E_i',
+//            Abar_{s_i} += Ebar_i P_i, and dlnL/dP_i += sum_h Ebar_i[h]^T L~_{s_i}[h].
+//            A child slot shared by two parent classes (class 2a = class 0 below
+//            the foreground path) accumulates both contributions.
+//   params   P = U e^{t' Root} V: dlnL/dt' = sum_m Root_m e^{t' Root_m} (U^T G V^T)_mm;
+//            kappa / omega through dP = U [(V dQ U) o Phi] V t' with
+//            Phi_mn = (e^{a_m} - e^{a_n}) / (a_m - a_n), a = t' Root;
+//            Qfactors, class proportions and branch lengths by the chain rule
+//            on the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "handle.h"
+
+namespace gb {
+
+namespace {
+
+constexpr int NCd = 61;
+constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP
+constexpr int kGradPSmem = (2 * TILE64 * 65 + 64 * 65) * sizeof(double);
+constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256) * sizeof(double);
+
+struct BItem {                // backward work: (node, class family) of one level
+    int node, ncls, is_root, nchild;
+    int cls[2], pslot[2], sslot[2];
+    int pidx[MAXC][2];        // pair of edge i under parent class k
+    int tslot[MAXC][2];       // child slot receiving the adjoint (-1: tip)
+};
+
+struct Contrib {              // one (parent slot, child) term of dlnL/dP for a pair
+    int ebar;                 // index into Ebar (= parent slot * MAXC + child index)
+    int tslot;                // child conP slot, or -1 for a tip
+    int tip;                  // tip node when tslot < 0
+};
+
+struct GradParams {
+    double dQk[3][61 * 61];
+    double dQw[3][61 * 61];
+};
+
+// ---------------------------------------------------------------- kernels
+
+// D matrices V dQ U for (kappa: w=0,1,2) and (omega: w=0,2), 64-padded
+__global__ void __launch_bounds__(256) dmat_kernel(const DevParams *__restrict__ prm,
+                                                   const GradParams *__restrict__ gp,
+                                                   double *__restrict__ Dm) {
+    __shared__ double T[61 * 62];
+    const int which = blockIdx.x;   // 0,1,2: kappa for w; 3: omega w0; 4: omega w2
+    const int w = which < 3 ? which : (which == 3 ? 0 : 2);
+    const double *dQ = which < 3 ? gp->dQk[w] : gp->dQw[w];
+    const double *U = prm->U[w];
+    const double *V = prm->V[w];
+    // T = dQ U
+    for (int i = threadIdx.x; i < 61 * 61; i += blockDim.x) {
+        int r = i / 61, c = i % 61;
+        double s = 0;
+        for (int k = 0; k < 61; k++) s = fma(dQ[r * 61 + k], U[k * 61 + c], s);
+        T[r * 62 + c] = s;
+    }
+    __syncthreads();
+    double *out = Dm + (size_t)which * 64 * 64;
+    for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
+        int r = i / 64, c = i % 64;
+        double s = 0;
+        if (r < 61 && c < 61)
+            for (int k = 0; k < 61; k++) s = fma(V[r * 61 + k], T[k * 62 + c], s);
+        out[i] = s;
+    }
+}
+
+// one CTA per (32-pattern tile, backward item)
+__global__ void __launch_bounds__(128) bwd_level_kernel(
+    const BItem *__restrict__ bitems, int npad, const double *__restrict__ Pt,
+    const double *__restrict__ E, double *__restrict__ Ebar, double *__restrict__ Abar,
+    const double *__restrict__ scaleF, const double *__restrict__ fpatt,
+    const double *__restrict__ post, const double *__restrict__ fbar, const double *__restrict__ pi) {
+    __shared__ double Bs[NCd * 65];  // P[j][k] (non-transposed), rows j < 61
+    __shared__ double Xs[TILE64 * 65];
+    const BItem it = bitems[blockIdx.y];
+    const int h0 = blockIdx.x * TILE64;
+    const int tid = threadIdx.x;
+    const int rg = tid >> 4, cg = tid & 15;
+    const int r0 = rg * 4, c0 = cg * 4;
+
+    double A[2][4][4];
+    for (int k = 0; k < it.ncls; k++) {
+        const int c = it.cls[k];
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+            const int h = h0 + r0 + r;
+            double sc = 1.0;
+            if (it.sslot[k] >= 0) {
+                const double sf = scaleF[(size_t)it.sslot[k] * npad + h];
+                sc = sf == -800.0 ? 0.0 : exp(-sf);
+            }
+            if (it.is_root) {
+                const double g = fpatt[h] * post[(size_t)c * npad + h] / fbar[(size_t)c * npad + h];
+#pragma unroll
+                for (int q = 0; q < 4; q++) A[k][r][q] = (c0 + q < NCd) ? g * pi[c0 + q] : 0.0;
+            } else {
+                const double4 v = *reinterpret_cast<const double4 *>(Abar + ((size_t)it.pslot[k] * npad + h) * 64 + c0);
+                A[k][r][0] = v.x * sc; A[k][r][1] = v.y * sc; A[k][r][2] = v.z * sc; A[k][r][3] = v.w * sc;
+            }
+        }
+    }
+
+    for (int i = 0; i < it.nchild; i++) {
+        double Eb[2][4][4];
+        for (int k = 0; k < it.ncls; k++) {
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) Eb[k][r][q] = A[k][r][q];
+            for (int i2 = 0; i2 < it.nchild; i2++) {
+                if (i2 == i) continue;
+                const double *e = E + ((size_t)(it.pslot[k] * MAXC + i2) * npad + h0 + r0) * 64 + c0;
+#pragma unroll
+                for (int r = 0; r < 4; r++) {
+                    const double4 v = *reinterpret_cast<const double4 *>(e + r * 64);
+                    Eb[k][r][0] *= v.x; Eb[k][r][1] *= v.y; Eb[k][r][2] *= v.z; Eb[k][r][3] *= v.w;
+                }
+            }
+            double *eb = Ebar + ((size_t)(it.pslot[k] * MAXC + i) * npad + h0 + r0) * 64 + c0;
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+                *reinterpret_cast<double4 *>(eb + r * 64) = make_double4(Eb[k][r][0], Eb[k][r][1], Eb[k][r][2], Eb[k][r][3]);
+        }
+        if (it.tslot[i][0] < 0) continue;   // tip child: only dlnL/dP (gradP kernel)
+        // adjoint of the child: one target if both classes share it, else one per class
+        const bool shared = it.ncls == 1 || it.tslot[i][0] == it.tslot[i][1];
+        const int ntarget = shared ? 1 : 2;
+        for (int tg = 0; tg < ntarget; tg++) {
+            double acc[4][4];
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[r][q] = 0.0;
+            const int kbeg = shared ? 0 : tg, kend = shared ? it.ncls : tg + 1;
+            for (int k = kbeg; k < kend; k++) {
+                const double *P = Pt + (size_t)it.pidx[i][k] * 64 * 64;
+                __syncthreads();
+                for (int idx = tid; idx < 64 * 64; idx += 128) {
+                    const int kk = idx >> 6, jj = idx & 63;   // Pt[kk][jj] = P[jj][kk]
+                    if (jj < NCd) Bs[jj * 65 + kk] = P[idx];
+                }
+#pragma unroll
+                for (int r = 0; r < 4; r++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) Xs[(r0 + r) * 65 + c0 + q] = Eb[k][r][q];
+                __syncthreads();
+#pragma unroll 4
+                for (int j = 0; j < NCd; j++) {
+                    double a[4], b[4];
+#pragma unroll
+                    for (int r = 0; r < 4; r++) a[r] = Xs[(r0 + r) * 65 + j];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) b[q] = Bs[j * 65 + c0 + q];
+#pragma unroll
+                    for (int r = 0; r < 4; r++)
+#pragma unroll
+                        for (int q = 0; q < 4; q++) acc[r][q] = fma(a[r], b[q], acc[r][q]);
+                }
+            }
+            double *o = Abar + ((size_t)it.tslot[i][tg] * npad + h0 + r0) * 64 + c0;
+#pragma unroll
+            for (int r = 0; r < 4; r++)
+                *reinterpret_cast<double4 *>(o + r * 64) = make_double4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+        }
+    }
+}
+
+// partial dlnL/dP of one pair over a chunk of patterns: G[j][k] = sum_h Ebar[h][j] X[h][k]
+__global__ void __launch_bounds__(128) gradP_kernel(const Contrib *__restrict__ contrib,
+                                                    const int *__restrict__ coff, int npatt, int npad,
+                                                    const double *__restrict__ Ebar,
+                                                    const double *__restrict__ conP,
+                                                    const unsigned char *__restrict__ z,
+                                                    double *__restrict__ Gpart, int nchunk) {
+    extern __shared__ double smg[];
+    double *Es = smg;                    // [32][65]
+    double *Xs = smg + TILE64 * 65;      // [32][65]
+    double *Gs = smg + 2 * TILE64 * 65;  // [64][65] tip scatter target
+    const int p = blockIdx.x, chunk = blockIdx.y;
+    const int tid = threadIdx.x;
+    // thread owns G rows j = 8*(tid/16) .. +7, cols k = 4*(tid%16) .. +3
+    const int j0 = (tid >> 4) * 8, k0 = (tid & 15) * 4;
+    double g[8][4];
+#pragma unroll
+    for (int a = 0; a < 8; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) g[a][b] = 0.0;
+    for (int i = tid; i < 64 * 65; i += 128) Gs[i] = 0.0;
+    const int hbeg = chunk * GCHUNK, hend = min(npatt, hbeg + GCHUNK);
+    for (int ci = coff[p]; ci < coff[p + 1]; ci++) {
+        const Contrib cb = contrib[ci];
+        for (int hb = hbeg; hb < hend; hb += TILE64) {
+            __syncthreads();
+            const double *eb = Ebar + ((size_t)cb.ebar * npad + hb) * 64;
+            for (int i = tid; i < TILE64 * 64; i += 128) Es[(i >> 6) * 65 + (i & 63)] = eb[i];
+            if (cb.tslot >= 0) {
+                const double *x = conP + ((size_t)cb.tslot * npad + hb) * 64;
+                for (int i = tid; i < TILE64 * 64; i += 128) Xs[(i >> 6) * 65 + (i & 63)] = x[i];
+            }
+            __syncthreads();
+            const int nh = min(TILE64, hend - hb);
+            if (cb.tslot >= 0) {
+                for (int hh = 0; hh < nh; hh++) {
+                    double a[8], b[4];
+#pragma unroll
+                    for (int q = 0; q < 8; q++) a[q] = Es[hh * 65 + j0 + q];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) b[q] = Xs[hh * 65 + k0 + q];
+#pragma unroll
+                    for (int q = 0; q < 8; q++)
+#pragma unroll
+                        for (int u = 0; u < 4; u++) g[q][u] = fma(a[q], b[u], g[q][u]);
+                }
+            } else if (tid < 64) {
+                // tip: X is one-hot at z[h]; thread tid owns row j = tid of Gs
+                const unsigned char *zz = z + (size_t)cb.tip * npad + hb;
+                for (int hh = 0; hh < nh; hh++) Gs[tid * 65 + zz[hh]] += Es[hh * 65 + tid];
+            }
+        }
+    }
+    __syncthreads();
+    double *out = Gpart + ((size_t)p * nchunk + chunk) * 64 * 64;
+#pragma unroll
+    for (int q = 0; q < 8; q++)
+#pragma unroll
+        for (int u = 0; u < 4; u++) out[(j0 + q) * 64 + k0 + u] = g[q][u] + Gs[(j0 + q) * 65 + k0 + u];
+}
+
+// per pair: G = sum of chunk partials; H = U^T G V^T; contributions to dlnL/dt',
+// dlnL/dkappa and dlnL/domega (out[pair][3])
+__global__ void __launch_bounds__(256) gradH_kernel(const PairDesc *__restrict__ pairs,
+                                                    const int *__restrict__ label,
+                                                    const double *__restrict__ tnode,
+                                                    const DevParams *__restrict__ prm,
+                                                    const double *__restrict__ Gpart, int nchunk,
+                                                    const double *__restrict__ Dm,
+                                                    double *__restrict__ out) {
+    extern __shared__ double smh[];
+    double *Gs = smh;                    // [61][62]
+    double *Ts = smh + 61 * 62;          // [61][62]
+    double (*red)[256] = reinterpret_cast<double (*)[256]>(smh + 2 * 61 * 62);
+    const int p = blockIdx.x;
+    const PairDesc pd = pairs[p];
+    const int w = pd.w;
+    const double tp = tnode[pd.node] * prm->qf[label[pd.node]];
+    const double *U = prm->U[w];
+    const double *V = prm->V[w];
+    const double *R = prm->Root[w];
+    for (int i = threadIdx.x; i < 61 * 61; i += blockDim.x) {
+        int j = i / 61, k = i % 61;
+        double s = 0;
+        for (int c = 0; c < nchunk; c++) s += Gpart[((size_t)p * nchunk + c) * 64 * 64 + j * 64 + k];
+        Gs[j * 62 + k] = s;
+    }
+    __syncthreads();
+    // T = G V^T : T[j][n] = sum_k G[j][k] V[n][k]
+    for (int i = threadIdx.x; i < 61 * 61; i += blockDim.x) {
+        int j = i / 61, n = i % 61;
+        double s = 0;
+        for (int k = 0; k < 61; k++) s = fma(Gs[j * 62 + k], V[n * 61 + k], s);
+        Ts[j * 62 + n] = s;
+    }
+    __syncthreads();
+    // H[m][n] = sum_j U[j][m] T[j][n]
+    double sdt = 0, sk = 0, sw = 0;
+    const double *Dk = Dm + (size_t)w * 64 * 64;
+    const double *Dw = w == 0 ? Dm + 3 * 64 * 64 : (w == 2 ? Dm + 4 * 64 * 64 : nullptr);
+    for (int i = threadIdx.x; i < 61 * 61; i += blockDim.x) {
+        int m = i / 61, n = i % 61;
+        double hmn = 0;
+        for (int j = 0; j < 61; j++) hmn = fma(U[j * 61 + m], Ts[j * 62 + n], hmn);
+        const double am = tp * R[m], an = tp * R[n];
+        double phi;
+        const double d = am - an;
+        if (fabs(d) < 1e-8) phi = exp(0.5 * (am + an)) * (1.0 + d * d / 24.0);
+        else phi = exp(an) * expm1(d) / d;
+        if (m == n) sdt += R[m] * exp(am) * hmn;
+        const double hp = hmn * phi * tp;
+        sk = fma(hp, Dk[m * 64 + n], sk);
+        if (Dw) sw = fma(hp, Dw[m * 64 + n], sw);
+    }
+    red[0][threadIdx.x] = sdt;
+    red[1][threadIdx.x] = sk;
+    red[2][threadIdx.x] = sw;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int q = 0; q < 3; q++) red[q][threadIdx.x] += red[q][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) out[p * 3 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// dlnL/dfreqK_c (up to the 1/freqK_c factor) : sum_h fpatt_h f_c / R_h
+__global__ void __launch_bounds__(256) freq_kernel(const double *__restrict__ fhK,
+                                                   const double *__restrict__ lnf,
+                                                   const double *__restrict__ fpatt, int npatt,
+                                                   int npad, int nscale, double *__restrict__ part) {
+    __shared__ double red[4][256];
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    double q[4] = {0, 0, 0, 0};
+    if (h < npatt && fpatt[h] > 0) {
+        const double L = lnf[h];
+        for (int c = 0; c < 4; c++) {
+            const double v = fhK[(size_t)c * npad + h];
+            q[c] = fpatt[h] * (nscale > 0 ? exp(v - L) : v / exp(L));
+        }
+    }
+    for (int c = 0; c < 4; c++) red[c][threadIdx.x] = q[c];
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int c = 0; c < 4; c++) red[c][threadIdx.x] += red[c][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+}  // namespace
+
+struct AdjointState {
+    std::vector<BItem> bitems;
+    std::vector<int> blevel_off;     // top-down order of levels
+    std::vector<Contrib> contrib;
+    std::vector<int> coff;
+    int nchunk = 1, nfreq_blocks = 1;
+    BItem *d_bitems = nullptr;
+    Contrib *d_contrib = nullptr;
+    int *d_coff = nullptr;
+    double *d_Ebar = nullptr, *d_Abar = nullptr, *d_Gpart = nullptr, *d_Dm = nullptr;
+    double *d_pout = nullptr, *d_fpart = nullptr;
+    GradParams *d_gp = nullptr, *h_gp = nullptr;
+    double *h_pout = nullptr, *h_fpart = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_kernels = 0;
+};
+
+void adjoint_free(AdjointState *a) {
+    if (!a) return;
+    if (a->graph) cudaGraphExecDestroy(a->graph);
+    void *dev[] = {a->d_bitems, a->d_contrib, a->d_coff, a->d_Ebar, a->d_Abar, a->d_Gpart,
+                   a->d_Dm, a->d_pout, a->d_fpart, a->d_gp};
+    for (void *p : dev)
+        if (p) cudaFree(p);
+    if (a->h_gp) cudaFreeHost(a->h_gp);
+    if (a->h_pout) cudaFreeHost(a->h_pout);
+    if (a->h_fpart) cudaFreeHost(a->h_fpart);
+    delete a;
+}
+
+namespace {
+
+int adjoint_init(gb_handle *h) {
+    AdjointState *a = new AdjointState();
+    h->adj = a;
+    const int ns = h->ns, nn = h->nnode;
+    auto ncls = [&](int n) { return (h->dirty[n] || n == h->root) ? 4 : 2; };
+    auto cls_of = [&](int s, int c) { return (h->dirty[s] || s == h->root) ? c : (c & 1); };
+    // backward items, levels from the root down
+    const int H = h->height[h->root];
+    a->blevel_off.clear();
+    for (int L = H; L >= 1; L--) {
+        a->blevel_off.push_back((int)a->bitems.size());
+        for (int n = ns; n < nn; n++) {
+            if (h->height[n] != L) continue;
+            for (int fam = 0; fam < 2; fam++) {
+                BItem b{};
+                b.node = n;
+                b.is_root = n == h->root;
+                b.nchild = h->nson[n];
+                b.ncls = ncls(n) == 4 ? 2 : 1;
+                for (int k = 0; k < 2; k++) {
+                    b.cls[k] = fam + 2 * k;
+                    b.pslot[k] = k < b.ncls ? h->slot_of[n * 4 + b.cls[k]] : -1;
+                    b.sslot[k] = (k < b.ncls && h->scale[n]) ? h->sslot_of[n * 4 + b.cls[k]] : -1;
+                }
+                for (int i = 0; i < MAXC; i++)
+                    for (int k = 0; k < 2; k++) { b.pidx[i][k] = -1; b.tslot[i][k] = -1; }
+                for (int i = 0; i < b.nchild; i++) {
+                    int s = h->sons[n * MAXC + i];
+                    for (int k = 0; k < b.ncls; k++) {
+                        int c = b.cls[k];
+                        int w = h->label[s] == 0 ? (c & 1) : (c <= 1 ? c : 2);
+                        b.pidx[i][k] = h->pair_of[s * 3 + w];
+                        b.tslot[i][k] = s < ns ? -1 : h->slot_of[s * 4 + cls_of(s, c)];
+                    }
+                    if (b.ncls == 1) { b.pidx[i][1] = b.pidx[i][0]; b.tslot[i][1] = b.tslot[i][0]; }
+                }
+                a->bitems.push_back(b);
+            }
+        }
+    }
+    a->blevel_off.push_back((int)a->bitems.size());
+    // dlnL/dP contributions per pair
+    std::vector<std::vector<Contrib>> per((size_t)h->pairs.size());
+    for (const Item &it : h->items)
+        for (int i = 0; i < it.nchild; i++) {
+            Contrib cb{it.slot * MAXC + i, it.cslot[i], it.child[i]};
+            per[it.pidx[i]].push_back(cb);
+        }
+    a->coff.assign(h->pairs.size() + 1, 0);
+    for (size_t p = 0; p < per.size(); p++) {
+        a->coff[p + 1] = a->coff[p] + (int)per[p].size();
+        for (auto &c : per[p]) a->contrib.push_back(c);
+    }
+    a->nchunk = (h->npatt + GCHUNK - 1) / GCHUNK;
+    a->nfreq_blocks = (h->npatt + 255) / 256;
+    const size_t npad = h->npad;
+    int rc;
+    if ((rc = dalloc(&a->d_bitems, a->bitems.size())) || (rc = dalloc(&a->d_contrib, a->contrib.size())) ||
+        (rc = dalloc(&a->d_coff, a->coff.size())) ||
+        (rc = dalloc(&a->d_Ebar, (size_t)h->nslot * MAXC * npad * 64)) ||
+        (rc = dalloc(&a->d_Abar, (size_t)h->nslot * npad * 64)) ||
+        (rc = dalloc(&a->d_Gpart, h->pairs.size() * a->nchunk * 64 * 64)) ||
+        (rc = dalloc(&a->d_Dm, 5 * 64 * 64)) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
+        (rc = dalloc(&a->d_fpart, a->nfreq_blocks * 4)) || (rc = dalloc(&a->d_gp, 1)))
+        return rc;
+    if (cudaMallocHost((void **)&a->h_gp, sizeof(GradParams)) ||
+        cudaMallocHost((void **)&a->h_pout, sizeof(double) * h->pairs.size() * 3) ||
+        cudaMallocHost((void **)&a->h_fpart, sizeof(double) * a->nfreq_blocks * 4))
+        return fail(GB_ERR_OOM, "cudaMallocHost (adjoint)");
+    CK(cudaMemcpy(a->d_bitems, a->bitems.data(), sizeof(BItem) * a->bitems.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a->d_contrib, a->contrib.data(), sizeof(Contrib) * std::max<size_t>(a->contrib.size(), 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(a->d_coff, a->coff.data(), sizeof(int) * a->coff.size(), cudaMemcpyHostToDevice));
+    // the Ebar rows of padded patterns must be zero for the dP reduction: they are
+    // written by the sweep with g = 0 (fpatt = 0) at the root and products below
+    CK(cudaMemset(a->d_Abar, 0, sizeof(double) * (size_t)h->nslot * npad * 64));
+    CK(cudaFuncSetAttribute(gradP_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradPSmem));
+    CK(cudaFuncSetAttribute(gradH_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHSmem));
+    return 0;
+}
+
+int record_backward(gb_handle *h) {
+    AdjointState *a = h->adj;
+    int nk = 0;
+    dmat_kernel<<<5, 256, 0, h->stream>>>(h->d_prm, a->d_gp, a->d_Dm);
+    prof_mark(h, GB_K_OTHER);
+    nk++;
+    for (size_t L = 0; L + 1 < a->blevel_off.size(); L++) {
+        int n = a->blevel_off[L + 1] - a->blevel_off[L];
+        if (!n) continue;
+        dim3 grid(h->ntile, n);
+        bwd_level_kernel<<<grid, 128, 0, h->stream>>>(a->d_bitems + a->blevel_off[L], h->npad, h->d_Pt,
+                                                      h->d_E, a->d_Ebar, a->d_Abar, h->d_scaleF,
+                                                      h->d_fpatt, h->d_post, h->d_fbar, h->d_pi);
+        prof_mark(h, GB_K_BWD);
+        nk++;
+    }
+    dim3 g2((unsigned)h->pairs.size(), a->nchunk);
+    gradP_kernel<<<g2, 128, kGradPSmem, h->stream>>>(a->d_contrib, a->d_coff, h->npatt, h->npad, a->d_Ebar,
+                                            h->d_conP, h->d_z, a->d_Gpart, a->nchunk);
+    prof_mark(h, GB_K_GRADP);
+    nk++;
+    gradH_kernel<<<(unsigned)h->pairs.size(), 256, kGradHSmem, h->stream>>>(h->d_pairs, h->d_label, h->d_tnode,
+                                                                   h->d_prm, a->d_Gpart, a->nchunk,
+                                                                   a->d_Dm, a->d_pout);
+    prof_mark(h, GB_K_GRADH);
+    nk++;
+    freq_kernel<<<a->nfreq_blocks, 256, 0, h->stream>>>(h->d_fhK, h->d_lnf, h->d_fpatt, h->npatt,
+                                                       h->npad, h->nscale, a->d_fpart);
+    prof_mark(h, GB_K_OTHER);
+    nk++;
+    return nk;
+}
+
+}  // namespace
+
+int adjoint_record(gb_handle *h) { return record_backward(h); }
+
+bool adjoint_ready(gb_handle *h) { return h->adj && h->adj->graph; }
+
+int adjoint_launch_graph(gb_handle *h) {
+    CK(cudaGraphLaunch(h->adj->graph, h->stream));
+    return 0;
+}
+
+int adjoint_run(gb_handle *h, const Derived *D, const ModelParams &m, const double *blength,
+                gb_grad *grad, gb_stats *stats) {
+    if (!h->adj) {
+        int rc = adjoint_init(h);
+        if (rc) return rc;
+    }
+    AdjointState *a = h->adj;
+    if (!a->graph) {
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+        a->graph_kernels = record_backward(h);
+        CK(cudaStreamEndCapture(h->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&a->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate (adjoint)");
+    }
+    std::memcpy(a->h_gp->dQk, D->dQk, sizeof(D->dQk));
+    std::memcpy(a->h_gp->dQw, D->dQw, sizeof(D->dQw));
+    CK(cudaEventRecord(h->ev0, h->stream));
+    CK(cudaMemcpyAsync(a->d_gp, a->h_gp, sizeof(GradParams), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaGraphLaunch(a->graph, h->stream));
+    const size_t np = h->pairs.size();
+    CK(cudaMemcpyAsync(a->h_pout, a->d_pout, sizeof(double) * np * 3, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(a->h_fpart, a->d_fpart, sizeof(double) * a->nfreq_blocks * 4, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaEventRecord(h->ev1, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    CK(cudaGetLastError());
+    h->kernels_last += a->graph_kernels;
+    if (stats) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+        stats->ms_device += ms;
+        stats->kernels += a->graph_kernels;
+        stats->h2d_bytes += sizeof(GradParams);
+        stats->d2h_bytes += sizeof(double) * (np * 3 + a->nfreq_blocks * 4);
+    }
+
+    // chain rule on the host (all derivatives of lnL; negated at the end)
+    const int nn = h->nnode;
+    std::vector<double> dtp(nn, 0.0);    // dlnL/dt' per node
+    double dk = 0, dw0 = 0, dw2 = 0;
+    for (size_t p = 0; p < np; p++) {
+        const PairDesc &pd = h->pairs[p];
+        dtp[pd.node] += a->h_pout[p * 3 + 0];
+        dk += a->h_pout[p * 3 + 1];
+        if (pd.w == 0) dw0 += a->h_pout[p * 3 + 2];
+        if (pd.w == 2) dw2 += a->h_pout[p * 3 + 2];
+    }
+    double dqf[2] = {0, 0};
+    for (int n = 0; n < nn; n++) {
+        if (n == h->root) continue;
+        const int b = h->label[n];
+        const double t = blength[n];
+        grad->d_blength[n] = -(dtp[n] * D->qf[b]);
+        dqf[b] += dtp[n] * t;
+    }
+    grad->d_blength[h->root] = 0.0;
+    double dfk[4] = {0, 0, 0, 0};   // sum_h fpatt f_c / R
+    for (int b = 0; b < a->nfreq_blocks; b++)
+        for (int c = 0; c < 4; c++) dfk[c] += a->h_fpart[b * 4 + c];
+    double gk = dk, gw0 = dw0, gw2 = dw2, gp0 = 0, gp1 = 0;
+    for (int b = 0; b < 2; b++) {
+        gk += dqf[b] * D->dqf[b][0];
+        gw0 += dqf[b] * D->dqf[b][1];
+        gw2 += dqf[b] * D->dqf[b][2];
+        gp0 += dqf[b] * D->dqf[b][3];
+        gp1 += dqf[b] * D->dqf[b][4];
+    }
+    for (int c = 0; c < 4; c++) {
+        gp0 += dfk[c] * D->dfreqK[c][0];
+        gp1 += dfk[c] * D->dfreqK[c][1];
+    }
+    (void)m;
+    grad->d_kappa = -gk;
+    grad->d_omega0 = -gw0;
+    grad->d_omega2 = -gw2;
+    grad->d_p0 = -gp0;
+    grad->d_p1 = -gp1;
+    return 0;
+}
+
+}  // namespace gb

@@ -1,0 +1,113 @@
+// The handle (gb_handle) and helpers shared by the host-side modules of the
+// library: runtime.cu (schedule, forward), adjoint.cu (gradient) and fast.cu
+// (split-precision path).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "gbcodeml.h"
+#include "internal.h"
+#include "model.h"
+
+namespace gb {
+
+struct AdjointState;
+struct FastState;
+
+int fail(int code, const std::string &msg);
+double now_ms();
+int cuda_fail(cudaError_t e, const char *what);
+
+template <class T>
+int dalloc(T **p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    return 0;
+}
+
+#define CK(call)                                     \
+    do {                                             \
+        cudaError_t e_ = (call);                     \
+        if (e_ != cudaSuccess) return ::gb::cuda_fail(e_, #call); \
+    } while (0)
+
+int adjoint_run(gb_handle *h, const Derived *D, const ModelParams &m, const double *blength,
+                gb_grad *grad, gb_stats *stats);
+int adjoint_record(gb_handle *h);          // backward launches on h->stream (profiling)
+int adjoint_launch_graph(gb_handle *h);    // replay the captured backward graph
+bool adjoint_ready(gb_handle *h);
+
+// profiling: when h->prof is set, launch sites call prof_mark after each kernel
+struct ProfRec {
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> cls;
+};
+void prof_mark(gb_handle *h, int cls);
+void adjoint_free(AdjointState *a);
+int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg_lnL, gb_grad *grad,
+              double *fhK, double *lnf, gb_stats *stats);
+int fast_replay(gb_handle *h, int iters, int with_grad, double *ms);
+int fast_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches);
+void fast_free(FastState *f);
+
+}  // namespace gb
+
+struct gb_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int ns = 0, nnode = 0, root = 0, npatt = 0, npad = 0, ntile = 0, precision = 0;
+    std::vector<int> father, label, nson, sons, height, dirty;
+    std::vector<char> scale;
+    std::vector<double> pi, fpatt;
+    int nscale = 0;
+
+    // schedule
+    std::vector<gb::Item> items;        // grouped by level
+    std::vector<int> level_off;     // items of level L: [level_off[L], level_off[L+1])
+    std::vector<gb::PairDesc> pairs;
+    std::vector<int> pair_of;       // [nnode*3] pair index of (node, w), -1 if absent
+    std::vector<int> slot_of;       // [nnode*4] conP slot of (node, class), -1 if absent
+    std::vector<int> sslot_of;      // [nnode*4] scale slot
+    std::vector<int> scale_list;    // [4*nscale] scale slot per root class and scaled node
+    int nslot = 0, nsslot = 0;
+
+    // device buffers
+    gb::Item *d_items = nullptr;
+    gb::PairDesc *d_pairs = nullptr;
+    int *d_label = nullptr, *d_scale_list = nullptr;
+    unsigned char *d_z = nullptr;
+    double *d_fpatt = nullptr, *d_pi = nullptr, *d_tnode = nullptr;
+    gb::DevParams *d_prm = nullptr;
+    double *d_Pt = nullptr, *d_conP = nullptr, *d_E = nullptr, *d_scaleF = nullptr;
+    double *d_fbar = nullptr, *d_ssum = nullptr, *d_fhK = nullptr, *d_lnf = nullptr, *d_post = nullptr;
+    double *d_partial = nullptr, *d_out = nullptr;
+    unsigned *d_ticket = nullptr;
+
+    // pinned staging
+    gb::DevParams *h_prm = nullptr;
+    double *h_tnode = nullptr, *h_out = nullptr;
+
+    // CUDA graphs of the forward evaluation (without / with E messages kept)
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int graph_kernels = 0;
+
+    gb::AdjointState *adj = nullptr;
+    gb::FastState *fast = nullptr;
+    int kernels_last = 0;
+    gb::ProfRec *prof = nullptr;
+};
+
+namespace gb {
+// forward pass on the handle's stream (runtime.cu); keepE keeps the edge
+// messages for the adjoint
+int run_forward(gb_handle *h, const Derived *D, const double *blength, bool keepE, double *neg_lnL,
+                double *fhK, double *lnf, gb_stats *stats);
+}  // namespace gb

@@ -1,0 +1,207 @@
+/*
+ * gbcodeml.h -- C ABI of libgbcodeml.so, a GB300 (sm_103a) implementation of
+ * PAML codeml's branch-site model A likelihood hot path.
+ *
+ * Everything here is plain C: pointers, sizes and status codes.  No call
+ * exits the process; every entry point returns GB_OK (0) or a negative
+ * GB_ERR_* code, and gb_last_error() gives a one-line reason.
+ *
+ * What each entry point replaces in the reference (paths relative to the
+ * reference project):
+ *
+ *   gb_create / gb_destroy   CUDA_Init / CUDA_FreeAll (cuda-codeml.cu:1106-1124,
+ *                            1162-1181) -- device set-up per tree and data set,
+ *                            but with all inputs passed explicitly instead of
+ *                            being read from codeml's globals (codeml.h:67-105).
+ *   gb_eval_uvr              CUDA_fx_r + CUDA_lfundG (treesub.c:7397-7450,
+ *                            7554-7595): P(t) for every branch from the host's
+ *                            U, V, Root (codeml's _UU/_VV/_Root, eigenQcodon
+ *                            codeml.c:2516-2520), pruning over the 4 site classes,
+ *                            node scaling, and the site-class mixture; fills
+ *                            fhK[4*npatt] exactly as CUDA_fx_r fills com.fhK and
+ *                            returns -lnL as CUDA_lfundG does.
+ *   gb_eval                  the same from the natural model-A parameters
+ *                            (branch lengths, kappa, w0, w2, p0, p1): the library
+ *                            builds Q, its eigen solution and the Qfactors
+ *                            (SetParametersNSsites codeml.c:2488-2521) itself.
+ *                            Optionally returns the analytic gradient of -lnL
+ *                            (the reference has none: ming2's dfun hook,
+ *                            tools.c:6361-6363, is passed NULL at codeml.c:688
+ *                            and gradientB tools.c:6326-6350 differentiates
+ *                            numerically).
+ *   gb_dfun_x                ming2's dfun signature (tools.c:6361-6363) over
+ *                            codeml's parameter vector x (branch lengths in
+ *                            codeml's branch order, kappa, p0/p1 in codeml's
+ *                            transformed or untransformed form, w0, w2).
+ *   gb_patterns              PatternWeight + EncodeSeqs (treesub.c:1075-1143,
+ *                            1302-1439) and F3x4 codon frequencies
+ *                            (codeml.c:3475-3570, 3732-3742) for clean codon data.
+ *
+ * The five symbols codeml.c itself calls (CUDA_Init, CUDA_lfundG, CUDA_fx_r,
+ * CUDA_ScheduleConditionalPNode, CUDA_FreeAll; codeml.h:67-85) are provided
+ * by the adapter cucodeml_gb300/csrc/codeml_adapter.c, declared in
+ * gbcodeml_codeml.h, which is compiled into codeml against its own headers.
+ *
+ * Threading: one handle per host thread; calls on one handle are not
+ * re-entrant.  The library owns device memory; the caller owns every host
+ * array passed in or out.
+ */
+#ifndef GBCODEML_H
+#define GBCODEML_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_OK            0
+#define GB_ERR_ARG      -1   /* malformed tree / data / sizes */
+#define GB_ERR_CUDA     -2   /* CUDA runtime error (message in gb_last_error) */
+#define GB_ERR_OOM      -3   /* device or host allocation failed */
+#define GB_ERR_PARAM    -4   /* parameter values outside the model (p0+p1 ~ 0, t < 0, ...) */
+#define GB_ERR_TIMEOUT  -5   /* a bounded device-side wait gave up */
+#define GB_ERR_STATE    -6   /* call on a destroyed / unfinished handle */
+#define GB_ERR_NODEVICE -7   /* no CUDA device */
+
+#define GB_NCODE 61           /* universal code, sense codons */
+
+/* precision of the pruning contraction */
+#define GB_PREC_FP64     0    /* FP64 throughout: the drop-in (<=1e-9 relative lnL) */
+#define GB_PREC_FAST     1    /* split-precision product path */
+
+typedef struct gb_handle gb_handle;
+
+typedef struct {
+    int ns;                       /* taxa; tips are nodes 0..ns-1 */
+    int nnode;                    /* nodes incl. root (2ns-2 for an unrooted binary tree) */
+    int root;                     /* root node id (>= ns) */
+    const int *father;            /* [nnode] father id, -1 for the root */
+    const int *label;             /* [nnode] branch label: 0 background, 1 foreground (#1) */
+    int npatt;                    /* site patterns */
+    const unsigned char *z;       /* [ns*npatt] sense codon 0..60 per tip and pattern */
+    const double *fpatt;          /* [npatt] pattern counts */
+    const double *pi;             /* [61] codon frequencies */
+    const char *node_scale;       /* [nnode] 1 = scale conditional likelihoods at this node
+                                     (codeml's com.nodeScale); NULL = codeml's own rule
+                                     (SetNodeScale, treesub.c:6917-6937) */
+    int precision;                /* GB_PREC_* */
+    int device;                   /* CUDA device ordinal */
+} gb_problem;
+
+typedef struct {
+    const double *blength;        /* [nnode] length of the branch above each node (root ignored) */
+    double kappa, omega0, omega2; /* omega1 is 1 */
+    double p0, p1;                /* untransformed proportions, p0 + p1 < 1 */
+} gb_params;
+
+typedef struct {
+    double *d_blength;            /* [nnode] d(-lnL)/d(branch length above node); root entry 0 */
+    double d_kappa, d_omega0, d_omega2, d_p0, d_p1;
+} gb_grad;
+
+typedef struct {
+    double ms_host;               /* host time in the call (set-up, copies, waits) */
+    double ms_device;             /* device time of the evaluation (CUDA events) */
+    int kernels;                  /* kernel launches made by the call */
+    int nscale;                   /* scaled nodes */
+    double h2d_bytes;             /* bytes copied host -> device by the call */
+    double d2h_bytes;             /* bytes copied device -> host by the call */
+} gb_stats;
+
+/* kernel classes reported by gb_profile */
+#define GB_K_PMAT     0           /* P(t) assembly */
+#define GB_K_PRUNE    1           /* pruning levels (forward contraction) */
+#define GB_K_MIX      2           /* site-class mixture, log, sum */
+#define GB_K_BWD      3           /* adjoint levels (backward contraction) */
+#define GB_K_GRADP    4           /* dlnL/dP accumulation over patterns */
+#define GB_K_GRADH    5           /* eigen-basis contraction to parameter derivatives */
+#define GB_K_OTHER    6           /* small set-up / reduction kernels */
+#define GB_NKCLASS    7
+
+/* Library version string. */
+const char *gb_version(void);
+
+/* One-line description of the last error on this thread. */
+const char *gb_last_error(void);
+
+/* Create a handle for one tree and data set; uploads everything that does not
+   change between evaluations.  Replaces CUDA_Init (cuda-codeml.cu:1106). */
+int gb_create(const gb_problem *prob, gb_handle **out);
+
+/* Free device memory and the handle.  Replaces CUDA_FreeAll (cuda-codeml.cu:1162). */
+int gb_destroy(gb_handle *h);
+
+/* Number of scaled nodes the handle uses (codeml's com.NnodeScale). */
+int gb_nscale(const gb_handle *h);
+
+/*
+ * Evaluate from the host's eigen solutions, as codeml's CUDA_lfundG does.
+ *   U[i], V[i]: 61x61 row-major (Q_i = U diag(Root_i) V), Root[i]: 61, for
+ *   i = 0,1,2 the w0, w1 = 1, w2 matrices (codeml's _UU/_VV/_Root);
+ *   qfactor[2]: Qfactor_NS_branch for background / foreground branches;
+ *   freqK[4]: site-class proportions; blength[nnode]: branch lengths.
+ * Outputs (each may be NULL): *neg_lnL; fhK[4*npatt] as codeml's com.fhK
+ * (log f + scale logs when any node is scaled, else f); lnf[npatt] per-pattern
+ * log f as codeml writes to its lnf file.
+ */
+int gb_eval_uvr(gb_handle *h, const double *const U[3], const double *const V[3],
+                const double *const Root[3], const double qfactor[2], const double freqK[4],
+                const double *blength, double *neg_lnL, double *fhK, double *lnf,
+                gb_stats *stats);
+
+/*
+ * Evaluate -lnL from natural parameters; if grad != NULL also the analytic
+ * gradient of -lnL (adjoint sweep).  fhK / lnf / stats may be NULL.
+ */
+int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad,
+            double *fhK, double *lnf, gb_stats *stats);
+
+/*
+ * ming2-compatible gradient hook over codeml's parameter vector
+ * x = [branch lengths by branch index (bnode[ib] is the node of branch ib),
+ *      kappa, p0', p1', w0, w2]; p' are codeml's f_and_x transforms
+ * (tools.c:1280-1305) unless lastround != 0, then p0, p1 themselves.
+ * Writes f = -lnL and dx = d(-lnL)/dx.  n must be nnode-1+5.
+ */
+int gb_dfun_x(gb_handle *h, const int *bnode, int lastround, const double *x, int n,
+              double *f, double *dx);
+
+/*
+ * Pattern compression of a clean codon alignment.
+ *   codons[ns*ncodon]: sense codon id 0..60 per species (row) and site.
+ * Outputs: *npatt; z[ns*ncodon] (first ns*npatt entries used, row stride
+ * npatt); fpatt[ncodon] (first npatt used); pi[61] F3x4 frequencies.
+ * Pattern order and counts are those codeml produces.
+ */
+int gb_patterns(int ns, int ncodon, const int *codons, int *npatt, unsigned char *z,
+                double *fpatt, double *pi);
+
+/*
+ * Measurement hooks (used by the benchmark):
+ *   gb_replay   re-runs the device work of the last gb_eval on this handle
+ *               `iters` times with its inputs resident on the device (no host
+ *               work, no copies) and returns the device time in *ms (CUDA
+ *               events on the handle's stream).  with_grad selects the
+ *               lnL+gradient work; it requires a previous gb_eval with grad.
+ *   gb_profile  runs the same work `iters` times as individual launches with
+ *               CUDA events around each one, and accumulates per kernel class
+ *               (GB_K_*) the device time ms[GB_NKCLASS] and launch count.
+ */
+int gb_replay(gb_handle *h, int iters, int with_grad, double *ms);
+int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches);
+
+/*
+ * Host-only model set-up (no GPU needed): for codon frequencies pi[61] and
+ * model-A parameters, the three eigen solutions U[i], V[i] (61x61 row-major),
+ * Root[i] for w0, w1 = 1, w2, the Qfactors qf[2] and class proportions
+ * freqK[4], as codeml's SetParametersNSsites computes them
+ * (codeml.c:2488-2521, eigenQcodon codeml.c:3103-3273).  Each output may be
+ * NULL.  U, V, Root point to arrays of 3*61*61, 3*61*61 and 3*61 doubles.
+ */
+int gb_model_setup(const double *pi, double kappa, double omega0, double omega2, double p0,
+                   double p1, double *U, double *V, double *Root, double *qf, double *freqK);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBCODEML_H */

@@ -1,0 +1,111 @@
+"""CPU-side checks of the C-ABI library (no GPU): it loads, exports every
+symbol include/*.h declares, and its host-only parts (pattern compression,
+model set-up, argument validation) agree with the oracle and golden fixtures."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from cucodeml_gb300 import _lib, api, codon
+from cucodeml_gb300.tree import parse_newick
+from oracle import oracle as O
+from tests.conftest import ROOT, golden_names, load_golden
+
+
+def header_functions():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(inc, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        if "extern \"C\"" not in text and f != "gbcodeml.h":
+            continue
+        names += re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(gb_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_exports_header_symbols():
+    L = _lib.load()
+    names = header_functions()
+    assert "gb_create" in names and "gb_eval" in names
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) <= set(_lib.SIGNATURES)
+    assert L.gb_version().decode().startswith("gbcodeml")
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_library_patterns_match_codeml(name):
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = api.patterns(codons)
+    got = [" ".join(codon.codon_string(int(c)) for c in z[:, h]) for h in range(z.shape[1])]
+    assert got == fx["patterns"]
+    assert np.array_equal(fpatt, np.array(fx["fpatt"]))
+    z2, fp2, pi2 = O.patterns(codons)
+    assert np.array_equal(z, z2) and np.array_equal(pi, pi2)
+
+
+def test_patterns_rejects_bad_codons():
+    with pytest.raises(_lib.GBError):
+        api.patterns(np.array([[0, 61], [1, 2], [3, 4]]))
+
+
+@pytest.mark.parametrize("name", ["c8x300_s1", "c40x200_s4"])
+def test_model_setup_matches_oracle(name):
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    pb = O.Problem(tree, z, fpatt, pi)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    U, V, R, qf, fk = api.model_setup(pi, x[nb], x[nb + 3], x[nb + 4], x[nb + 1], x[nb + 2])
+    Uo, Vo, Ro, qfo, fko = pb.set_params(x)
+    assert np.allclose(qf, qfo, rtol=1e-14, atol=0)
+    assert np.allclose(fk, fko, rtol=1e-14, atol=0)
+    for w in range(3):
+        for t in (0.01, 0.3, 2.0):
+            P1 = U[w] @ np.diag(np.exp(t * R[w])) @ V[w]
+            P2 = Uo[w] @ np.diag(np.exp(t * Ro[w])) @ Vo[w]
+            assert np.abs(P1 - P2).max() < 1e-12
+        assert np.abs(U[w] @ V[w] - np.eye(61)).max() < 1e-12
+
+
+def test_model_setup_rejects_bad_params():
+    pi = np.full(61, 1 / 61)
+    with pytest.raises(_lib.GBError) as e:
+        api.model_setup(pi, 2.0, 0.3, 3.0, 0.0, 0.0)
+    assert e.value.code == -4
+
+
+def _problem(tree, z, fpatt, pi, father=None):
+    return dict(tree=tree, z=z, fpatt=fpatt, pi=pi)
+
+
+def test_create_validates_before_device():
+    fx, tree, codons = load_golden("c8x300_s1")
+    z, fpatt, pi = O.patterns(codons)
+    bad = parse_newick(fx["newick"], fx["names"])
+    bad.label = bad.label.copy()
+    bad.label[0] = 2                       # labels must be 0/1
+    with pytest.raises(_lib.GBError) as e:
+        api.Likelihood(bad, z, fpatt, pi)
+    assert e.value.code == -1
+    zb = z.copy()
+    zb[0, 0] = 70                          # only clean data (sense codons)
+    with pytest.raises(_lib.GBError) as e:
+        api.Likelihood(tree, zb, fpatt, pi)
+    assert e.value.code == -1
+
+
+def test_create_without_gpu_fails_loudly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    fx, tree, codons = load_golden("c8x300_s1")
+    z, fpatt, pi = O.patterns(codons)
+    with pytest.raises(_lib.GBError) as e:
+        api.Likelihood(tree, z, fpatt, pi)
+    assert e.value.code in (-7, -2)

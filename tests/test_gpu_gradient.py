@@ -1,8 +1,9 @@
 """Adjoint gradient (FP64) through the C ABI against finite differences of the
 oracle and against codeml's own numerical gradient (gradientB restated).
 
-Bar: relative error <= 1e-5 against central differences (h = 1e-5 |x|+1e-5),
-measured as max |g - g_fd| / max(1, |g_fd|) over all np entries.
+Bar: relative error <= 1e-5 against a 5-point central difference of the
+oracle (step 1e-4 (|x_i| + 0.05), truncation O(h^4)), measured as
+max |g - g_fd| / max(1, |g_fd|) over all np entries.
 """
 import numpy as np
 import pytest
@@ -14,14 +15,16 @@ from tests.conftest import load_golden
 pytestmark = pytest.mark.gpu
 
 
-def fd_grad(pb, x, lastround, h=1e-5):
+def fd_grad(pb, x, lastround, h=1e-4):
     g = np.zeros(len(x))
     for i in range(len(x)):
-        e = h * (abs(x[i]) + 1)
-        xp, xm = x.copy(), x.copy()
-        xp[i] += e
-        xm[i] -= e
-        g[i] = (pb.neg_lnL(xp, lastround) - pb.neg_lnL(xm, lastround)) / (2 * e)
+        e = h * (abs(x[i]) + 0.05)
+        f = []
+        for k in (-2, -1, 1, 2):
+            xk = x.copy()
+            xk[i] += k * e
+            f.append(pb.neg_lnL(xk, lastround))
+        g[i] = (f[0] - 8 * f[1] + 8 * f[2] - f[3]) / (12 * e)
     return g
 
 
@@ -38,8 +41,7 @@ def test_dfun_matches_fd(name, lastround):
     x = np.array(fx["x"])
     nb = tree.nbranch
     if name.startswith("c5x120"):
-        x[tree.ibranch[tree.sons[tree.root][2]]] = 0.05   # keep every branch > 0 for the FD
-        x[:nb] = np.maximum(x[:nb], 0.02)
+        x[:nb] = np.maximum(x[:nb], 0.02)    # the FD needs every branch away from t = 0
     if not lastround:
         p0, p1 = x[nb + 1], x[nb + 2]
         x[nb + 1] = np.log(p0 / (1 - p0 - p1))
@@ -48,7 +50,9 @@ def test_dfun_matches_fd(name, lastround):
     f, g = lk.dfun_x(x, lastround)
     assert abs(f - pb.neg_lnL(x, lastround)) <= 1e-9 * abs(f)
     ref = fd_grad(pb, x, lastround)
-    assert rel_err(g, ref) <= 1e-5, (g, ref)
+    err = np.abs(g - ref) / np.maximum(1.0, np.abs(ref))
+    i = int(np.argmax(err))
+    assert err[i] <= 1e-5, (i, g[i], ref[i], err[i])
     lk.close()
 
 

@@ -1,0 +1,109 @@
+/*
+ * codeml_adapter.c -- links into codeml in place of cuda-codeml.o.
+ *
+ * Compiled together with codeml's own sources (it needs codeml's paml.h and
+ * codeml.h for the globals com, tree, nodes) and linked against
+ * libgbcodeml.so; see include/gbcodeml_codeml.h for what each function
+ * replaces.  It only marshals codeml's globals into the library's C ABI.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "paml.h"
+#include "codeml.h"
+#include "gbcodeml.h"
+#include "gbcodeml_codeml.h"
+
+/* codeml.c globals that are not declared in its headers */
+extern double *_UU[NBTYPE + 2], *_VV[NBTYPE + 2], *_Root[NBTYPE + 2];
+extern double Qfactor_NS_branch[NBTYPE];
+extern int LASTROUND;
+
+static gb_handle *g_h = NULL;
+static double *g_fhK = NULL;      /* [4*npatt] all classes of the current evaluation */
+static double *g_blen = NULL;     /* [nnode] */
+static int *g_bnode = NULL;       /* [nbranch] node of x[ib] */
+
+static void gb_die(const char *what, int rc) {
+    fprintf(stderr, "\ngbcodeml: %s failed (%d): %s\n", what, rc, gb_last_error());
+    exit(-1);
+}
+
+void CUDA_Init(double *x) {
+    int i, j, rc;
+    unsigned char *z;
+    int *father, *label;
+    char *scale = NULL;
+    gb_problem p;
+    (void)x;
+    if (com.ngene != 1) gb_die("CUDA_Init (one gene only)", GB_ERR_ARG);
+    if (!com.cleandata) gb_die("CUDA_Init (cleandata = 1 only)", GB_ERR_ARG);
+    if (com.ncode != GB_NCODE) gb_die("CUDA_Init (universal code only)", GB_ERR_ARG);
+    z = (unsigned char *)malloc((size_t)com.ns * com.npatt);
+    father = (int *)malloc(sizeof(int) * tree.nnode);
+    label = (int *)malloc(sizeof(int) * tree.nnode);
+    g_blen = (double *)malloc(sizeof(double) * tree.nnode);
+    g_bnode = (int *)malloc(sizeof(int) * tree.nnode);
+    g_fhK = (double *)malloc(sizeof(double) * 4 * com.npatt);
+    if (!z || !father || !label || !g_blen || !g_bnode || !g_fhK) gb_die("CUDA_Init (host memory)", GB_ERR_OOM);
+    for (j = 0; j < com.ns; j++) memcpy(z + (size_t)j * com.npatt, com.z[j], com.npatt);
+    for (i = 0; i < tree.nnode; i++) {
+        father[i] = nodes[i].father;
+        label[i] = (i == tree.root) ? 0 : (int)nodes[i].label;
+        if (i != tree.root) g_bnode[nodes[i].ibranch] = i;
+    }
+    if (com.NnodeScale) scale = com.nodeScale;
+    p.ns = com.ns;
+    p.nnode = tree.nnode;
+    p.root = tree.root;
+    p.father = father;
+    p.label = label;
+    p.npatt = com.npatt;
+    p.z = z;
+    p.fpatt = com.fpatt;
+    p.pi = com.pi;
+    p.node_scale = scale;
+    p.precision = GB_PREC_FP64;
+    p.device = 0;
+    if (!scale) {   /* codeml scales no node: tell the library so, rather than its own rule */
+        scale = (char *)calloc(tree.nnode, 1);
+        p.node_scale = scale;
+    }
+    rc = gb_create(&p, &g_h);
+    if (scale && scale != com.nodeScale) free(scale);
+    free(z);
+    free(father);
+    free(label);
+    if (rc) gb_die("gb_create", rc);
+}
+
+void CUDA_ScheduleConditionalPNode(int ir, int ig, double *x) {
+    int i, rc;
+    (void)x;
+    if (ir == 0) {   /* SetParameters ran in CUDA_fx_r: U, V, Root, Qfactor, freqK are current */
+        for (i = 0; i < tree.nnode; i++)
+            g_blen[i] = (i == tree.root) ? 0 : nodes[i].branch * com.rgene[ig];
+        rc = gb_eval_uvr(g_h, (const double *const *)_UU, (const double *const *)_VV,
+                         (const double *const *)_Root, Qfactor_NS_branch, com.freqK, g_blen, NULL,
+                         g_fhK, NULL, NULL);
+        if (rc) gb_die("gb_eval_uvr", rc);
+    }
+    memcpy(com.fhK + (size_t)ir * com.npatt, g_fhK + (size_t)ir * com.npatt, sizeof(double) * com.npatt);
+}
+
+void CUDA_FreeAll(void) {
+    if (g_h) gb_destroy(g_h);
+    g_h = NULL;
+    free(g_fhK);
+    free(g_blen);
+    free(g_bnode);
+    g_fhK = g_blen = NULL;
+    g_bnode = NULL;
+}
+
+int GB_dfun(double x[], double *f, double dx[], int n) {
+    int rc = gb_dfun_x(g_h, g_bnode, LASTROUND, x, n, f, dx);
+    if (rc) gb_die("gb_dfun_x", rc);
+    return 0;
+}

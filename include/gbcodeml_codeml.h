@@ -1,0 +1,43 @@
+/*
+ * gbcodeml_codeml.h -- the entry points codeml.c itself calls on its CUDA path,
+ * provided by cucodeml_gb300/csrc/codeml_adapter.c, which is compiled into
+ * codeml (against codeml's own paml.h / codeml.h) and links libgbcodeml.so.
+ *
+ *   CUDA_Init                      replaces cuda-codeml.cu:1106 (called at
+ *                                  codeml.c:684): creates the library handle from
+ *                                  codeml's globals (tree, com.z, com.fpatt,
+ *                                  com.pi, com.nodeScale).
+ *   CUDA_ScheduleConditionalPNode  replaces cuda-codeml.cu:1336 (called per site
+ *                                  class from CUDA_fx_r, treesub.c:7583): the
+ *                                  first class of an evaluation runs all four
+ *                                  classes on the GPU from codeml's _UU/_VV/_Root,
+ *                                  Qfactor_NS_branch and com.freqK; every call
+ *                                  copies its class into com.fhK + ir*npatt.
+ *   CUDA_FreeAll                   replaces cuda-codeml.cu:1162 (codeml.c:695).
+ *   GB_dfun                        new: ming2's gradient hook
+ *                                  (tools.c:6361-6363, `dfun`), the analytic
+ *                                  gradient of -lnL in codeml's x space; pass it
+ *                                  instead of NULL at codeml.c:688.
+ *
+ * CUDA_lfundG and CUDA_fx_r stay codeml's own (treesub.c:7397, 7554).  On any
+ * library error these functions print the library's message and exit(-1), as
+ * the reference's cutilSafeCall does (cuda-codeml.cu:20-39); the C ABI below
+ * them returns status codes instead.
+ */
+#ifndef GBCODEML_CODEML_H
+#define GBCODEML_CODEML_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+void CUDA_Init(double *x);
+void CUDA_ScheduleConditionalPNode(int ir, int ig, double *x);
+void CUDA_FreeAll(void);
+int GB_dfun(double x[], double *f, double dx[], int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBCODEML_CODEML_H */

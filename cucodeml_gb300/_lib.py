@@ -67,6 +67,9 @@ SIGNATURES = {
     "gb_patterns": (C.c_int, [C.c_int, C.c_int, _ip, _ip, C.POINTER(C.c_ubyte), _dp, _dp]),
     "gb_replay": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "gb_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),
+    "gb_lnL_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, C.c_char_p, C.c_int, C.c_void_p,
+                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                 C.c_void_p]),
     "gb_model_setup": (C.c_int, [_dp, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                  _dp, _dp, _dp, _dp, _dp]),
 }

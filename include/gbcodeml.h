@@ -200,6 +200,37 @@ int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches
 int gb_model_setup(const double *pi, double kappa, double omega0, double omega2, double p0,
                    double p1, double *U, double *V, double *Root, double *qf, double *freqK);
 
+/*
+ * gb_lnL_noalloc -- no counterpart in the reference.  The FP64 lnL of
+ * gb_eval_uvr for callers that cannot allocate device memory: their GPU
+ * memory is owned by another allocator (an application pool or arena that
+ * forbids outside allocations), or they cannot afford cudaMalloc/cudaFree,
+ * which synchronise the whole device.  This call allocates nothing, on the
+ * device or the host; its scratch is one static device array of
+ * GB_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until
+ * the process exits.  Problems needing more scratch (roughly npair * 32 KiB +
+ * nslot * npad * 512 B, i.e. tens of taxa and a few thousand patterns at
+ * most) are rejected with GB_ERR_ARG; at most 256 nodes.
+ *   Host arrays: father[nnode], label[nnode], node_scale[nnode] (may be NULL:
+ *   codeml's rule).  Device-accessible arrays owned by the caller: d_z
+ *   [ns*npatt] codon ids, d_fpatt [npatt], d_pi [61], d_model
+ *   [GB_MODEL_DOUBLES] = U[3][61*61], V[3][61*61], Root[3][61], qfactor[2],
+ *   freqK[4] (the arrays gb_eval_uvr takes, concatenated), d_blength
+ *   [nnode] (not checked: negative lengths act as 0); outputs d_neg_lnL [1]
+ *   and d_fhK [4*npatt] (may be NULL).
+ *   stream: a cudaStream_t (NULL = legacy default stream); the call returns
+ *   after that stream has finished the evaluation.
+ * The first call on a device (with it current) looks up the scratch array's
+ * device address; make it before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU race, so serialise them.
+ */
+#define GB_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+#define GB_MODEL_DOUBLES (6 * 61 * 61 + 3 * 61 + 2 + 4)
+int gb_lnL_noalloc(int ns, int nnode, int root, const int *father, const int *label,
+                   const char *node_scale, int npatt, const unsigned char *d_z,
+                   const double *d_fpatt, const double *d_pi, const double *d_model,
+                   const double *d_blength, double *d_neg_lnL, double *d_fhK, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

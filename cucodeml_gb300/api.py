@@ -84,7 +84,8 @@ class Likelihood:
         self._scale = None
         if node_scale is not None:
             self._scale = np.ascontiguousarray(node_scale, dtype=np.int8).tobytes()
-        prec = {"fp64": _lib.GB_PREC_FP64, "fast": _lib.GB_PREC_FAST}[precision]
+        prec = precision if isinstance(precision, int) else \
+            {"fp64": _lib.GB_PREC_FP64, "fast": _lib.GB_PREC_FAST}[precision]
         ip = C.POINTER(C.c_int)
         self._prob = _lib.Problem(self.ns, self.nnode, tree.root, self._father.ctypes.data_as(ip),
                                   self._label.ctypes.data_as(ip), self.npatt,

@@ -64,6 +64,7 @@ struct gb_handle {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int ns = 0, nnode = 0, root = 0, npatt = 0, npad = 0, ntile = 0, precision = 0;
+    int fast_slices = 8;            // digit planes per operand in the split-precision path
     std::vector<int> father, label, nson, sons, height, dirty;
     std::vector<char> scale;
     std::vector<double> pi, fpatt;

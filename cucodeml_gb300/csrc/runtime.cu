@@ -56,7 +56,9 @@ int build_schedule(gb_handle *h, const gb_problem *p) {
     if (p->root < ns || p->root >= nn || p->father[p->root] != -1)
         return fail(GB_ERR_ARG, "gb_problem: root must be an internal node with father -1");
     h->ns = ns; h->nnode = nn; h->root = p->root; h->npatt = p->npatt;
-    h->npad = (p->npatt + TILE64 - 1) / TILE64 * TILE64;
+    // pattern padding: 32-pattern tiles (FP64) or 128-pattern tiles (split precision)
+    const int unit = h->precision == GB_PREC_FP64 ? TILE64 : 128;
+    h->npad = (p->npatt + unit - 1) / unit * unit;
     h->ntile = h->npad / TILE64;
     h->father.assign(p->father, p->father + nn);
     h->label.assign(nn, 0);
@@ -308,12 +310,17 @@ const char *gb_last_error(void) { return g_err.c_str(); }
 int gb_create(const gb_problem *prob, gb_handle **out) {
     if (!prob || !out) return fail(GB_ERR_ARG, "null argument");
     *out = nullptr;
-    if (prob->precision != GB_PREC_FP64 && prob->precision != GB_PREC_FAST)
-        return fail(GB_ERR_ARG, "unknown precision");
+    int prec = prob->precision, slices = 8;
+    if (prec >= GB_PREC_FAST_NS(5) && prec <= GB_PREC_FAST_NS(8)) {
+        slices = prec - GB_PREC_FAST_NS(0);
+        prec = GB_PREC_FAST;
+    }
+    if (prec != GB_PREC_FP64 && prec != GB_PREC_FAST) return fail(GB_ERR_ARG, "unknown precision");
     // validate everything on the host before touching a device
     gb_handle *h = new gb_handle();
     h->device = -1;
-    h->precision = prob->precision;
+    h->precision = prec;
+    h->fast_slices = slices;
     int rc = build_schedule(h, prob);
     if (rc) { free_all(h); return rc; }
     for (size_t i = 0; i < (size_t)prob->ns * prob->npatt; i++)

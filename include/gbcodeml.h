@@ -66,7 +66,11 @@ extern "C" {
 
 /* precision of the pruning contraction */
 #define GB_PREC_FP64     0    /* FP64 throughout: the drop-in (<=1e-9 relative lnL) */
-#define GB_PREC_FAST     1    /* split-precision product path */
+#define GB_PREC_FAST     1    /* split precision: each operand cut into 7-bit digit planes
+                                 held exactly in bf16, digit products summed exactly in FP32
+                                 on the tensor cores, levels combined in double-float; P(t),
+                                 the root sum, logs and the lnL sum stay FP64 */
+#define GB_PREC_FAST_NS(n) (16 + (n))  /* GB_PREC_FAST with n = 5..8 digit planes (default 8) */
 
 typedef struct gb_handle gb_handle;
 

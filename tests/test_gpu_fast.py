@@ -1,0 +1,59 @@
+"""Split-precision path (GB_PREC_FAST) against the FP64 path on the GPU.
+
+The FP64 path equals the oracle to 1e-12 relative (test_gpu_fp64.py), so it
+is the reference here.  Bar (the precision target of the fast path):
+|delta lnL| <= 1e-6 absolute per alignment, per-pattern |delta log f| <= 1e-8.
+"""
+import numpy as np
+import pytest
+
+from cucodeml_gb300 import _lib, api
+from cucodeml_gb300.simulate import simulate
+from oracle import oracle as O
+from tests.conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def node_blength(tree, x):
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = np.asarray(x)[: tree.nbranch]
+    return bl
+
+
+def both(tree, z, fpatt, pi, args):
+    a = api.Likelihood(tree, z, fpatt, pi, precision="fp64").evaluate(*args, want_site=True)
+    b = api.Likelihood(tree, z, fpatt, pi, precision="fast").evaluate(*args, want_site=True)
+    return a, b
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_fast_lnL_golden(name):
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    args = (node_blength(tree, x), x[nb], x[nb + 3], x[nb + 4], x[nb + 1], x[nb + 2])
+    a, b = both(tree, z, fpatt, pi, args)
+    d = abs(a.neg_lnL - b.neg_lnL)
+    dl = np.max(np.abs(a.lnf - b.lnf))
+    print(f"{name}: |dlnL| = {d:.3e}  max |dlogf| = {dl:.3e}")
+    assert d <= 1e-6
+    assert dl <= 1e-8
+
+
+@pytest.mark.parametrize("slices", [6, 7, 8])
+def test_fast_lnL_64x5000(slices):
+    aln = simulate(64, 5000, seed=2024)
+    z, fpatt, pi = api.patterns(aln.codons)
+    tree = aln.tree
+    args = (tree.branch, 2.0, 0.3, 3.0, 0.5, 0.3)
+    a = api.Likelihood(tree, z, fpatt, pi, precision="fp64").evaluate(*args, want_site=True)
+    lk = api.Likelihood(tree, z, fpatt, pi, precision=16 + slices)
+    b = lk.evaluate(*args, want_site=True)
+    d = abs(a.neg_lnL - b.neg_lnL)
+    dl = np.max(np.abs(a.lnf - b.lnf))
+    print(f"64x5000 slices={slices}: lnL {-a.neg_lnL:.9f} |dlnL| = {d:.3e}  max |dlogf| = {dl:.3e} "
+          f"fp64 {a.ms_device:.2f} ms  fast {b.ms_device:.2f} ms")
+    if slices == 8:
+        assert d <= 1e-6

@@ -29,33 +29,15 @@
 #include <vector>
 
 #include "handle.h"
+#include "adjoint_internal.h"
 
 namespace gb {
 
 namespace {
 
 constexpr int NCd = 61;
-constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP
 constexpr int kGradPSmem = (2 * TILE64 * 65 + 64 * 65) * sizeof(double);
 constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256) * sizeof(double);
-
-struct BItem {                // backward work: (node, class family) of one level
-    int node, ncls, is_root, nchild;
-    int cls[2], pslot[2], sslot[2];
-    int pidx[MAXC][2];        // pair of edge i under parent class k
-    int tslot[MAXC][2];       // child slot receiving the adjoint (-1: tip)
-};
-
-struct Contrib {              // one (parent slot, child) term of dlnL/dP for a pair
-    int ebar;                 // index into Ebar (= parent slot * MAXC + child index)
-    int tslot;                // child conP slot, or -1 for a tip
-    int tip;                  // tip node when tslot < 0
-};
-
-struct GradParams {
-    double dQk[3][61 * 61];
-    double dQw[3][61 * 61];
-};
 
 // ---------------------------------------------------------------- kernels
 
@@ -341,22 +323,7 @@ __global__ void __launch_bounds__(256) freq_kernel(const double *__restrict__ fh
 
 }  // namespace
 
-struct AdjointState {
-    std::vector<BItem> bitems;
-    std::vector<int> blevel_off;     // top-down order of levels
-    std::vector<Contrib> contrib;
-    std::vector<int> coff;
-    int nchunk = 1, nfreq_blocks = 1;
-    BItem *d_bitems = nullptr;
-    Contrib *d_contrib = nullptr;
-    int *d_coff = nullptr;
-    double *d_Ebar = nullptr, *d_Abar = nullptr, *d_Gpart = nullptr, *d_Dm = nullptr;
-    double *d_pout = nullptr, *d_fpart = nullptr;
-    GradParams *d_gp = nullptr, *h_gp = nullptr;
-    double *h_pout = nullptr, *h_fpart = nullptr;
-    cudaGraphExec_t graph = nullptr;
-    int graph_kernels = 0;
-};
+
 
 void adjoint_free(AdjointState *a) {
     if (!a) return;
@@ -371,9 +338,8 @@ void adjoint_free(AdjointState *a) {
     delete a;
 }
 
-namespace {
-
 int adjoint_init(gb_handle *h) {
+    if (h->adj) return 0;
     AdjointState *a = new AdjointState();
     h->adj = a;
     const int ns = h->ns, nn = h->nnode;
@@ -453,6 +419,25 @@ int adjoint_init(gb_handle *h) {
     return 0;
 }
 
+void launch_dmat(gb_handle *h) {
+    dmat_kernel<<<5, 256, 0, h->stream>>>(h->d_prm, h->adj->d_gp, h->adj->d_Dm);
+}
+
+void launch_gradH(gb_handle *h) {
+    AdjointState *a = h->adj;
+    gradH_kernel<<<(unsigned)h->pairs.size(), 256, kGradHSmem, h->stream>>>(h->d_pairs, h->d_label, h->d_tnode,
+                                                                           h->d_prm, a->d_Gpart, a->nchunk,
+                                                                           a->d_Dm, a->d_pout);
+}
+
+void launch_freq(gb_handle *h, int nscale) {
+    AdjointState *a = h->adj;
+    freq_kernel<<<a->nfreq_blocks, 256, 0, h->stream>>>(h->d_fhK, h->d_lnf, h->d_fpatt, h->npatt, h->npad,
+                                                       nscale, a->d_fpart);
+}
+
+namespace {
+
 int record_backward(gb_handle *h) {
     AdjointState *a = h->adj;
     int nk = 0;
@@ -519,8 +504,8 @@ int adjoint_run(gb_handle *h, const Derived *D, const ModelParams &m, const doub
     CK(cudaMemcpyAsync(a->d_gp, a->h_gp, sizeof(GradParams), cudaMemcpyHostToDevice, h->stream));
     CK(cudaGraphLaunch(a->graph, h->stream));
     const size_t np = h->pairs.size();
-    CK(cudaMemcpyAsync(a->h_pout, a->d_pout, sizeof(double) * np * 3, cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(a->h_fpart, a->d_fpart, sizeof(double) * a->nfreq_blocks * 4, cudaMemcpyDeviceToHost, h->stream));
+    int rcf = adjoint_fetch(h);
+    if (rcf) return rcf;
     CK(cudaEventRecord(h->ev1, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
@@ -534,6 +519,22 @@ int adjoint_run(gb_handle *h, const Derived *D, const ModelParams &m, const doub
         stats->d2h_bytes += sizeof(double) * (np * 3 + a->nfreq_blocks * 4);
     }
 
+    adjoint_chain(h, D, blength, grad);
+    (void)m;
+    return 0;
+}
+
+int adjoint_fetch(gb_handle *h) {
+    AdjointState *a = h->adj;
+    const size_t np = h->pairs.size();
+    CK(cudaMemcpyAsync(a->h_pout, a->d_pout, sizeof(double) * np * 3, cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(a->h_fpart, a->d_fpart, sizeof(double) * a->nfreq_blocks * 4, cudaMemcpyDeviceToHost, h->stream));
+    return 0;
+}
+
+void adjoint_chain(gb_handle *h, const Derived *D, const double *blength, gb_grad *grad) {
+    AdjointState *a = h->adj;
+    const size_t np = h->pairs.size();
     // chain rule on the host (all derivatives of lnL; negated at the end)
     const int nn = h->nnode;
     std::vector<double> dtp(nn, 0.0);    // dlnL/dt' per node
@@ -569,13 +570,11 @@ int adjoint_run(gb_handle *h, const Derived *D, const ModelParams &m, const doub
         gp0 += dfk[c] * D->dfreqK[c][0];
         gp1 += dfk[c] * D->dfreqK[c][1];
     }
-    (void)m;
     grad->d_kappa = -gk;
     grad->d_omega0 = -gw0;
     grad->d_omega2 = -gw2;
     grad->d_p0 = -gp0;
     grad->d_p1 = -gp1;
-    return 0;
 }
 
 }  // namespace gb

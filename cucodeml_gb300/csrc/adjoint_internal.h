@@ -1,0 +1,61 @@
+// Adjoint structures shared by the FP64 adjoint (adjoint.cu) and the
+// split-precision adjoint (k_fast_bwd.cu, fast.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "gbcodeml.h"
+#include "internal.h"
+#include "model.h"
+
+struct gb_handle;
+
+namespace gb {
+
+constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP
+
+struct BItem {                // backward work: (node, class family) of one level
+    int node, ncls, is_root, nchild;
+    int cls[2], pslot[2], sslot[2];
+    int pidx[MAXC][2];        // pair of edge i under parent class k
+    int tslot[MAXC][2];       // child slot receiving the adjoint (-1: tip)
+};
+
+struct Contrib {              // one (parent slot, child) term of dlnL/dP for a pair
+    int ebar;                 // index into Ebar (= parent slot * MAXC + child index)
+    int tslot;                // child conP slot, or -1 for a tip
+    int tip;                  // tip node when tslot < 0
+};
+
+struct GradParams {
+    double dQk[3][61 * 61];
+    double dQw[3][61 * 61];
+};
+
+struct AdjointState {
+    std::vector<BItem> bitems;
+    std::vector<int> blevel_off;     // top-down order of levels
+    std::vector<Contrib> contrib;
+    std::vector<int> coff;
+    int nchunk = 1, nfreq_blocks = 1;
+    BItem *d_bitems = nullptr;
+    Contrib *d_contrib = nullptr;
+    int *d_coff = nullptr;
+    double *d_Ebar = nullptr, *d_Abar = nullptr, *d_Gpart = nullptr, *d_Dm = nullptr;
+    double *d_pout = nullptr, *d_fpart = nullptr;
+    GradParams *d_gp = nullptr, *h_gp = nullptr;
+    double *h_pout = nullptr, *h_fpart = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    int graph_kernels = 0;
+};
+
+int adjoint_init(gb_handle *h);               // host structures and device buffers
+void launch_dmat(gb_handle *h);
+void launch_gradH(gb_handle *h);
+void launch_freq(gb_handle *h, int nscale);
+void adjoint_chain(gb_handle *h, const Derived *D, const double *blength, gb_grad *grad);
+int adjoint_fetch(gb_handle *h);              // D2H of per-pair and class-weight sums (async)
+
+}  // namespace gb

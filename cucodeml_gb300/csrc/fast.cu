@@ -4,6 +4,7 @@
 
 #include <cstring>
 
+#include "adjoint_internal.h"
 #include "fast_internal.h"
 #include "handle.h"
 
@@ -14,15 +15,18 @@ struct FastState {
     float2 *Pdf = nullptr, *conP = nullptr, *E = nullptr;
     __nv_bfloat16 *Bf = nullptr, *Bb = nullptr;
     int *expo = nullptr, *expo_root = nullptr;
+    int *ebexp = nullptr, *aexp = nullptr;     // adjoint exponents
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    int graph_kernels = 0;
+    cudaGraphExec_t bwd_graph = nullptr;
+    int graph_kernels = 0, bwd_kernels = 0;
 };
 
 void fast_free(FastState *f) {
     if (!f) return;
     for (auto &g : f->graph)
         if (g) cudaGraphExecDestroy(g);
-    void *p[] = {f->Pdf, f->conP, f->E, f->Bf, f->Bb, f->expo, f->expo_root};
+    if (f->bwd_graph) cudaGraphExecDestroy(f->bwd_graph);
+    void *p[] = {f->Pdf, f->conP, f->E, f->Bf, f->Bb, f->expo, f->expo_root, f->ebexp, f->aexp};
     for (void *q : p)
         if (q) cudaFree(q);
     delete f;
@@ -95,6 +99,87 @@ int record_forward_fast(gb_handle *h, bool keepE) {
     return nk;
 }
 
+FastBwdArgs bwd_args(gb_handle *h) {
+    FastState *f = h->fast;
+    AdjointState *ad = h->adj;
+    FastBwdArgs b;
+    b.bitems = ad->d_bitems;
+    b.npad = h->npad;
+    b.npatt = h->npatt;
+    b.nchunk = ad->nchunk;
+    b.E = f->E;
+    b.conP = f->conP;
+    b.expo = f->expo;
+    b.expo_root = f->expo_root;
+    b.Bb = f->Bb;
+    // the FP64 adjoint's message buffers hold 8 bytes per element: reused as double-float
+    b.Ebar = reinterpret_cast<float2 *>(ad->d_Ebar);
+    b.ebexp = f->ebexp;
+    b.Abar = reinterpret_cast<float2 *>(ad->d_Abar);
+    b.aexp = f->aexp;
+    b.fpatt = h->d_fpatt;
+    b.post = h->d_post;
+    b.fbar = h->d_fbar;
+    b.pi = h->d_pi;
+    b.contrib = ad->d_contrib;
+    b.coff = ad->d_coff;
+    b.z = h->d_z;
+    b.Gpart = ad->d_Gpart;
+    return b;
+}
+
+int record_backward_fast(gb_handle *h) {
+    FastState *f = h->fast;
+    AdjointState *ad = h->adj;
+    int nk = 0;
+    launch_dmat(h);
+    prof_mark(h, GB_K_OTHER);
+    nk++;
+    FastBwdArgs b = bwd_args(h);
+    const int ntile = h->npad / FAST_MT;
+    for (size_t L = 0; L + 1 < ad->blevel_off.size(); L++) {
+        const int n = ad->blevel_off[L + 1] - ad->blevel_off[L];
+        if (!n) continue;
+        FastBwdArgs bl = b;
+        bl.bitems = ad->d_bitems + ad->blevel_off[L];
+        launch_bwd_fast(bl, f->ns, n, ntile, h->stream);
+        prof_mark(h, GB_K_BWD);
+        nk++;
+    }
+    launch_gradP_fast(b, f->ns, (int)h->pairs.size(), h->stream);
+    prof_mark(h, GB_K_GRADP);
+    nk++;
+    launch_gradH(h);
+    prof_mark(h, GB_K_GRADH);
+    nk++;
+    launch_freq(h, 1);
+    prof_mark(h, GB_K_OTHER);
+    nk++;
+    return nk;
+}
+
+int ensure_bwd_graph(gb_handle *h) {
+    FastState *f = h->fast;
+    if (f->bwd_graph) return 0;
+    int rc = adjoint_init(h);
+    if (rc) return rc;
+    if (!f->ebexp) {
+        if ((rc = dalloc(&f->ebexp, (size_t)h->nslot * MAXC * h->npad)) ||
+            (rc = dalloc(&f->aexp, (size_t)h->nslot * h->npad)))
+            return rc;
+        CK(cudaMemset(f->aexp, 0, sizeof(int) * h->nslot * h->npad));
+    }
+    CK(init_fast_bwd_kernels(f->ns));
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    f->bwd_kernels = record_backward_fast(h);
+    CK(cudaStreamEndCapture(h->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&f->bwd_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate (fast adjoint)");
+    return 0;
+}
+
 int ensure_fast_graph(gb_handle *h, bool keepE) {
     FastState *f = h->fast;
     cudaGraphExec_t &ge = f->graph[keepE ? 1 : 0];
@@ -117,7 +202,6 @@ int ensure_fast_graph(gb_handle *h, bool keepE) {
 
 int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg_lnL, gb_grad *grad,
               double *fhK, double *lnf, gb_stats *stats) {
-    if (grad) return fail(GB_ERR_STATE, "GB_PREC_FAST: the gradient is not available in this build");
     CK(cudaSetDevice(h->device));
     if (!h->fast) {
         int rc = fast_init(h);
@@ -137,13 +221,25 @@ int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg
         if (!(t >= 0.0)) return fail(GB_ERR_PARAM, "negative or non-finite branch length");
         h->h_tnode[n] = t;
     }
-    const bool keepE = false;
+    const bool keepE = grad != nullptr;
     int rc = ensure_fast_graph(h, keepE);
     if (rc) return rc;
+    if (grad) {
+        rc = ensure_bwd_graph(h);
+        if (rc) return rc;
+        std::memcpy(h->adj->h_gp->dQk, D->dQk, sizeof(D->dQk));
+        std::memcpy(h->adj->h_gp->dQw, D->dQw, sizeof(D->dQw));
+    }
     CK(cudaEventRecord(h->ev0, h->stream));
     CK(cudaMemcpyAsync(h->d_prm, h->h_prm, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_tnode, h->h_tnode, sizeof(double) * h->nnode, cudaMemcpyHostToDevice, h->stream));
+    if (grad) CK(cudaMemcpyAsync(h->adj->d_gp, h->adj->h_gp, sizeof(GradParams), cudaMemcpyHostToDevice, h->stream));
     CK(cudaGraphLaunch(f->graph[keepE ? 1 : 0], h->stream));
+    if (grad) {
+        CK(cudaGraphLaunch(f->bwd_graph, h->stream));
+        rc = adjoint_fetch(h);
+        if (rc) return rc;
+    }
     CK(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     if (fhK)
         CK(cudaMemcpy2DAsync(fhK, sizeof(double) * h->npatt, h->d_fhK, sizeof(double) * h->npad,
@@ -153,26 +249,32 @@ int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
     *neg_lnL = h->h_out[0];
-    h->kernels_last = f->graph_kernels;
+    h->kernels_last = f->graph_kernels + (grad ? f->bwd_kernels : 0);
+    if (grad) adjoint_chain(h, D, blength, grad);
     if (stats) {
         float ms = 0;
         cudaEventElapsedTime(&ms, h->ev0, h->ev1);
         stats->ms_device = ms;
         stats->ms_host = now_ms() - t0;
-        stats->kernels = f->graph_kernels;
+        stats->kernels = h->kernels_last;
         stats->nscale = h->nscale;
-        stats->h2d_bytes = sizeof(DevParams) + sizeof(double) * h->nnode;
-        stats->d2h_bytes = sizeof(double) * (1 + (fhK ? 4 * h->npatt : 0) + (lnf ? h->npatt : 0));
+        stats->h2d_bytes = sizeof(DevParams) + sizeof(double) * h->nnode + (grad ? sizeof(GradParams) : 0);
+        stats->d2h_bytes = sizeof(double) * (1 + (fhK ? 4 * h->npatt : 0) + (lnf ? h->npatt : 0)) +
+                           (grad ? sizeof(double) * (h->pairs.size() * 3 + h->adj->nfreq_blocks * 4) : 0);
     }
     return 0;
 }
 
 int fast_replay(gb_handle *h, int iters, int with_grad, double *ms) {
-    if (with_grad) return fail(GB_ERR_STATE, "GB_PREC_FAST: the gradient is not available in this build");
-    if (!h->fast || !h->fast->graph[0]) return fail(GB_ERR_STATE, "gb_replay: evaluate first");
+    FastState *f = h->fast;
+    if (!f || !f->graph[with_grad ? 1 : 0] || (with_grad && !f->bwd_graph))
+        return fail(GB_ERR_STATE, "gb_replay: evaluate first");
     CK(cudaSetDevice(h->device));
     CK(cudaEventRecord(h->ev0, h->stream));
-    for (int i = 0; i < iters; i++) CK(cudaGraphLaunch(h->fast->graph[0], h->stream));
+    for (int i = 0; i < iters; i++) {
+        CK(cudaGraphLaunch(f->graph[with_grad ? 1 : 0], h->stream));
+        if (with_grad) CK(cudaGraphLaunch(f->bwd_graph, h->stream));
+    }
     CK(cudaEventRecord(h->ev1, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     float t = 0;
@@ -182,13 +284,17 @@ int fast_replay(gb_handle *h, int iters, int with_grad, double *ms) {
 }
 
 int fast_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches) {
-    if (with_grad) return fail(GB_ERR_STATE, "GB_PREC_FAST: the gradient is not available in this build");
-    if (!h->fast || !h->fast->graph[0]) return fail(GB_ERR_STATE, "gb_profile: evaluate first");
+    FastState *f = h->fast;
+    if (!f || !f->graph[with_grad ? 1 : 0] || (with_grad && !f->bwd_graph))
+        return fail(GB_ERR_STATE, "gb_profile: evaluate first");
     CK(cudaSetDevice(h->device));
     ProfRec rec;
     h->prof = &rec;
     prof_mark(h, -1);
-    for (int i = 0; i < iters; i++) record_forward_fast(h, false);
+    for (int i = 0; i < iters; i++) {
+        record_forward_fast(h, with_grad != 0);
+        if (with_grad) record_backward_fast(h);
+    }
     h->prof = nullptr;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     for (int k = 0; k < GB_NKCLASS; k++) { ms[k] = 0; launches[k] = 0; }

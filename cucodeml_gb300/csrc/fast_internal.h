@@ -6,6 +6,7 @@
 #include <cuda_bf16.h>
 
 #include "internal.h"
+#include "adjoint_internal.h"
 
 namespace gb {
 
@@ -27,7 +28,28 @@ struct FastFwdArgs {
     int *expo_root;              // [4][npad]
 };
 
+struct FastBwdArgs {
+    const BItem *bitems;
+    int npad, npatt, nchunk;
+    const float2 *E;             // forward edge messages
+    const float2 *conP;          // forward normalised conditional likelihoods
+    const int *expo, *expo_root;
+    const __nv_bfloat16 *Bb;     // digit planes of Pt
+    float2 *Ebar;                // [nslot*3][npad][64] normalised dlnL/dE
+    int *ebexp;                  // [nslot*3][npad]
+    float2 *Abar;                // [nslot][npad][64] normalised dlnL/dL~
+    int *aexp;                   // [nslot][npad]
+    const double *fpatt, *post, *fbar, *pi;
+    const Contrib *contrib;
+    const int *coff;
+    const unsigned char *z;
+    double *Gpart;               // [npair][nchunk][64][64]
+};
+
 cudaError_t init_fast_kernels(int ns);
+cudaError_t init_fast_bwd_kernels(int ns);
+void launch_bwd_fast(const FastBwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st);
+void launch_gradP_fast(const FastBwdArgs &a, int ns, int npair, cudaStream_t st);
 void launch_pslice(const FastFwdArgs &a, int ns, int npair, cudaStream_t st);
 void launch_prune_fast(const FastFwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st);
 

@@ -57,3 +57,42 @@ def test_fast_lnL_64x5000(slices):
           f"fp64 {a.ms_device:.2f} ms  fast {b.ms_device:.2f} ms")
     if slices == 8:
         assert d <= 1e-6
+
+
+def grad_vec(r):
+    g = r.grad
+    return np.concatenate([g["blength"], [g["kappa"], g["omega0"], g["omega2"], g["p0"], g["p1"]]])
+
+
+@pytest.mark.parametrize("name", ["c8x300_s1", "c5x120_s5", "c24x400_s3", "c40x200_s4"])
+def test_fast_gradient_golden(name):
+    """Fast adjoint vs the FP64 adjoint (itself checked against finite differences)."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    args = (node_blength(tree, x), x[nb], x[nb + 3], x[nb + 4], x[nb + 1], x[nb + 2])
+    a = api.Likelihood(tree, z, fpatt, pi, precision="fp64").evaluate(*args, grad=True)
+    b = api.Likelihood(tree, z, fpatt, pi, precision="fast").evaluate(*args, grad=True)
+    ga, gb = grad_vec(a), grad_vec(b)
+    err = np.max(np.abs(ga - gb) / np.maximum(1.0, np.abs(ga)))
+    print(f"{name}: |dlnL| = {abs(a.neg_lnL - b.neg_lnL):.3e}  grad rel err = {err:.3e}")
+    assert abs(a.neg_lnL - b.neg_lnL) <= 1e-6
+    assert err <= 1e-5
+
+
+def test_fast_gradient_64x5000():
+    aln = simulate(64, 5000, seed=2024)
+    z, fpatt, pi = api.patterns(aln.codons)
+    tree = aln.tree
+    args = (tree.branch, 2.0, 0.3, 3.0, 0.5, 0.3)
+    a = api.Likelihood(tree, z, fpatt, pi, precision="fp64").evaluate(*args, grad=True)
+    lk = api.Likelihood(tree, z, fpatt, pi, precision="fast")
+    b = lk.evaluate(*args, grad=True)
+    b = lk.evaluate(*args, grad=True)
+    ga, gb = grad_vec(a), grad_vec(b)
+    err = np.max(np.abs(ga - gb) / np.maximum(1.0, np.abs(ga)))
+    print(f"64x5000 lnL+grad: |dlnL| = {abs(a.neg_lnL - b.neg_lnL):.3e} grad rel err = {err:.3e} "
+          f"fp64 {a.ms_device:.2f} ms fast {b.ms_device:.2f} ms")
+    assert abs(a.neg_lnL - b.neg_lnL) <= 1e-6
+    assert err <= 1e-5

@@ -160,6 +160,49 @@ def fp64_peak_tflops():
     return best
 
 
+def batched_leg(args, dev):
+    """Batched workload: args.batch independent genes (taxa U{12..48}, codons
+    log-uniform [100, 3000], per-gene kappa, w0, w2), lnL + gradient of every
+    gene per step, one CUDA-graph launch per step; split precision and FP64."""
+    from cucodeml_gb300 import api
+    from cucodeml_gb300.simulate import simulate_batch
+    alns = simulate_batch(args.batch, seed=4)
+    genes = []
+    for a in alns:
+        z, fp, pi = api.patterns(a.codons)
+        genes.append((a.tree, z, fp, pi))
+    prm = [{"blength": a.tree.branch, "kappa": a.model.kappa, "omega0": a.model.omega0,
+            "omega2": a.model.omega2, "p0": a.model.p0, "p1": a.model.p1} for a in alns]
+    out = {"genes": args.batch, "patterns": int(sum(len(g[2]) for g in genes)),
+           "workload": f"{args.batch} genes, taxa U{{12..48}}, codons log-uniform [100, 3000], lnL+gradient"}
+    res = {}
+    for prec in ("fast", "fp64"):
+        b = api.Batch(genes, precision=prec, device=dev)
+        f, g, st = b.evaluate(prm, grad=True)
+        f, g, st = b.evaluate(prm, grad=True)
+        res[prec] = (f, g)
+        import time as _t
+        t0 = _t.perf_counter()
+        for _ in range(args.batch_steps):
+            f, g, st = b.evaluate(prm, grad=True)
+        e2e = (_t.perf_counter() - t0) / args.batch_steps
+        ms = b.replay(args.batch_steps, True) / args.batch_steps
+        out[prec] = {"batch_evals_per_s": 1000.0 / ms, "gene_evals_per_s": args.batch * 1000.0 / ms,
+                     "ms_per_batch": ms, "e2e_batch_evals_per_s": 1.0 / e2e,
+                     "e2e_gene_evals_per_s": args.batch / e2e, "kernels_per_batch": st.kernels}
+        b.close()
+    out["speedup_vs_fp64"] = out["fast"]["batch_evals_per_s"] / out["fp64"]["batch_evals_per_s"]
+    out["e2e_speedup_vs_fp64"] = out["fast"]["e2e_batch_evals_per_s"] / out["fp64"]["e2e_batch_evals_per_s"]
+    out["max_abs_dlnL_vs_fp64"] = float(np.max(np.abs(res["fast"][0] - res["fp64"][0])))
+    err = 0.0
+    for a, b in zip(res["fp64"][1], res["fast"][1]):
+        va = np.concatenate([a["blength"], [a[k] for k in ("kappa", "omega0", "omega2", "p0", "p1")]])
+        vb = np.concatenate([b["blength"], [b[k] for k in ("kappa", "omega0", "omega2", "p0", "p1")]])
+        err = max(err, float(np.max(np.abs(va - vb) / np.maximum(1.0, np.abs(va)))))
+    out["max_grad_rel_err_vs_fp64"] = err
+    return out
+
+
 def cpu_baseline(tree, z, fpatt, pi, threads: int, seconds: float = 12.0, min_evals: int = 2):
     """Time the oracle's lnL on the host cores; lnL+gradient = (np+1) lnL evals."""
     from oracle import oracle as O
@@ -227,6 +270,8 @@ def main():
     ap.add_argument("--ns", type=int, default=64)
     ap.add_argument("--ncodon", type=int, default=5000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--batch", type=int, default=512, help="genes in the batched leg (0: skip it)")
+    ap.add_argument("--batch-steps", type=int, default=3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -332,6 +377,23 @@ def main():
         "gpu_launches": int(kernels_per_eval * args.steps),
         "achieved_tflops_alg": fl["flops_lnL_grad"] * args.steps / (dev_ms * 1e-3) / 1e12,
     }
+    # same lnL+gradient through the FP64 drop-in, for the speed-up of the fast path
+    if precision == "fast":
+        lk64 = api.Likelihood(tree, z, fpatt, pi, precision="fp64", device=dev)
+        for i in range(args.warmup):
+            r64 = lk64.evaluate(step_params(i), grad=True, **PARAMS)
+        ms64 = lk64.replay(max(3, args.steps // 4), True) / max(3, args.steps // 4)
+        rf = lk.evaluate(bl0, grad=True, **PARAMS)
+        r64 = lk64.evaluate(bl0, grad=True, **PARAMS)
+        g64 = np.concatenate([r64.grad["blength"], [r64.grad[k] for k in ("kappa", "omega0", "omega2", "p0", "p1")]])
+        gf = np.concatenate([rf.grad["blength"], [rf.grad[k] for k in ("kappa", "omega0", "omega2", "p0", "p1")]])
+        line["fp64_value"] = 1000.0 / ms64
+        line["speedup_vs_fp64"] = line["value"] / line["fp64_value"]
+        line["abs_dlnL_vs_fp64"] = abs(rf.neg_lnL - r64.neg_lnL)
+        line["grad_rel_err_vs_fp64"] = float(np.max(np.abs(gf - g64) / np.maximum(1.0, np.abs(g64))))
+        lk64.close()
+    if args.batch > 0:
+        line["batched"] = batched_leg(args, dev)
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         line["cpu_baseline"] = cpu_baseline(tree, z, fpatt, pi, O.max_threads())

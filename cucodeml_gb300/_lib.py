@@ -66,6 +66,11 @@ SIGNATURES = {
     "gb_dfun_x": (C.c_int, [C.c_void_p, _ip, C.c_int, _dp, C.c_int, _dp, _dp]),
     "gb_patterns": (C.c_int, [C.c_int, C.c_int, _ip, _ip, C.POINTER(C.c_ubyte), _dp, _dp]),
     "gb_replay": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
+    "gb_batch_create": (C.c_int, [C.c_int, C.POINTER(Problem), C.POINTER(C.c_void_p)]),
+    "gb_batch_size": (C.c_int, [C.c_void_p]),
+    "gb_batch_eval": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, C.POINTER(Grad), C.POINTER(Stats)]),
+    "gb_batch_replay": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
+    "gb_batch_destroy": (C.c_int, [C.c_void_p]),
     "gb_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),
     "gb_lnL_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, C.c_char_p, C.c_int, C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -188,3 +188,78 @@ class Likelihood:
         _lib.check(self._L.gb_dfun_x(self._h, self.bnode.ctypes.data_as(C.POINTER(C.c_int)),
                                      int(lastround), _ptr(x), len(x), C.byref(f), _ptr(dx)))
         return f.value, dx
+
+
+class Batch:
+    """Many independent alignments evaluated together (gb_batch_*): one CUDA
+    graph launch per evaluation, each gene an independent branch."""
+
+    def __init__(self, genes, precision: str = "fast", device: int = 0):
+        """genes: list of (tree, z, fpatt, pi)."""
+        self._L = _lib.load()
+        prec = precision if isinstance(precision, int) else \
+            {"fp64": _lib.GB_PREC_FP64, "fast": _lib.GB_PREC_FAST}[precision]
+        ip = C.POINTER(C.c_int)
+        self._keep = []
+        probs = (_lib.Problem * len(genes))()
+        self.trees = []
+        for i, (tree, z, fpatt, pi) in enumerate(genes):
+            father = np.ascontiguousarray(tree.father, dtype=np.int32)
+            label = np.ascontiguousarray(tree.label, dtype=np.int32)
+            z = np.ascontiguousarray(z, dtype=np.uint8)
+            fpatt = np.ascontiguousarray(fpatt, dtype=np.float64)
+            pi = np.ascontiguousarray(pi, dtype=np.float64)
+            self._keep += [father, label, z, fpatt, pi]
+            probs[i] = _lib.Problem(tree.ns, tree.nnode, tree.root, father.ctypes.data_as(ip),
+                                    label.ctypes.data_as(ip), len(fpatt),
+                                    z.ctypes.data_as(C.POINTER(C.c_ubyte)), _ptr(fpatt), _ptr(pi), None,
+                                    prec, device)
+            self.trees.append(tree)
+        h = C.c_void_p()
+        _lib.check(self._L.gb_batch_create(len(genes), probs, C.byref(h)))
+        self._h = h
+        self.n = len(genes)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gb_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def evaluate(self, params, grad: bool = False):
+        """params: list of dicts (blength, kappa, omega0, omega2, p0, p1) per gene.
+        Returns (neg_lnL [n], grads list or None, EvalResult stats)."""
+        n = self.n
+        pr = (_lib.Params * n)()
+        keep = []
+        for i, p in enumerate(params):
+            bl = np.ascontiguousarray(p["blength"], dtype=np.float64)
+            keep.append(bl)
+            pr[i] = _lib.Params(_ptr(bl), p["kappa"], p["omega0"], p["omega2"], p["p0"], p["p1"])
+        out = np.zeros(n)
+        gr = None
+        dbl = []
+        if grad:
+            gr = (_lib.Grad * n)()
+            for i in range(n):
+                d = np.zeros(self.trees[i].nnode)
+                dbl.append(d)
+                gr[i] = _lib.Grad(_ptr(d), 0, 0, 0, 0, 0)
+        st = _lib.Stats()
+        _lib.check(self._L.gb_batch_eval(self._h, pr, _ptr(out), gr, C.byref(st)))
+        grads = None
+        if grad:
+            grads = [{"blength": dbl[i], "kappa": gr[i].d_kappa, "omega0": gr[i].d_omega0,
+                      "omega2": gr[i].d_omega2, "p0": gr[i].d_p0, "p1": gr[i].d_p1} for i in range(n)]
+        return out, grads, EvalResult(float(out.sum()), None, None, None, st.ms_device, st.ms_host,
+                                      st.kernels, st.h2d_bytes, st.d2h_bytes)
+
+    def replay(self, iters: int, with_grad: bool) -> float:
+        ms = C.c_double(0)
+        _lib.check(self._L.gb_batch_replay(self._h, int(iters), int(with_grad), C.byref(ms)))
+        return ms.value

@@ -1,7 +1,11 @@
 // Host side of the split-precision path (GB_PREC_FAST): buffers, CUDA graphs
-// and launches; the kernels are in k_fast.cu (forward).
+// and launches.  Kernels: k_umma.cu (tcgen05 contractions, the default),
+// k_fast.cu / k_fast_bwd.cu (mma.sync contractions, P digit planes, dlnL/dP).
+// GBCODEML_MMA=sync in the environment selects the mma.sync contraction
+// kernels for the forward and adjoint levels.
 #include <cuda_runtime.h>
 
+#include <cstdlib>
 #include <cstring>
 
 #include "adjoint_internal.h"
@@ -16,6 +20,9 @@ struct FastState {
     __nv_bfloat16 *Bf = nullptr, *Bb = nullptr;
     int *expo = nullptr, *expo_root = nullptr;
     int *ebexp = nullptr, *aexp = nullptr;     // adjoint exponents
+    int *err = nullptr, *h_err = nullptr;      // bounded-wait failure flag (device, pinned host)
+    bool umma = true;                          // tcgen05 contractions (else mma.sync)
+    int nsb = 7;                               // digit planes in the adjoint contractions
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraphExec_t bwd_graph = nullptr;
     int graph_kernels = 0, bwd_kernels = 0;
@@ -26,7 +33,8 @@ void fast_free(FastState *f) {
     for (auto &g : f->graph)
         if (g) cudaGraphExecDestroy(g);
     if (f->bwd_graph) cudaGraphExecDestroy(f->bwd_graph);
-    void *p[] = {f->Pdf, f->conP, f->E, f->Bf, f->Bb, f->expo, f->expo_root, f->ebexp, f->aexp};
+    if (f->h_err) cudaFreeHost(f->h_err);
+    void *p[] = {f->Pdf, f->conP, f->E, f->Bf, f->Bb, f->expo, f->expo_root, f->ebexp, f->aexp, f->err};
     for (void *q : p)
         if (q) cudaFree(q);
     delete f;
@@ -45,7 +53,19 @@ int fast_init(gb_handle *h) {
         (rc = dalloc(&f->expo, (size_t)h->nslot * npad)) || (rc = dalloc(&f->expo_root, 4 * npad)))
         return rc;
     CK(cudaMemset(f->expo, 0, sizeof(int) * h->nslot * npad));
+    const char *mode = std::getenv("GBCODEML_MMA");
+    const char *nb = std::getenv("GBCODEML_ADJ_PLANES");
+    f->nsb = nb ? std::atoi(nb) : 7;
+    if (f->nsb < 4 || f->nsb > f->ns) f->nsb = f->ns < 7 ? f->ns : 7;
+    f->umma = !(mode && std::strcmp(mode, "sync") == 0) && f->ns >= 6;
+    if ((rc = dalloc(&f->err, 1))) return rc;
+    CK(cudaMemset(f->err, 0, sizeof(int)));
+    CK(cudaMallocHost((void **)&f->h_err, sizeof(int)));
     CK(init_fast_kernels(f->ns));
+    if (f->umma) {
+        CK(init_umma_kernels(f->ns));
+        CK(init_umma_kernels(f->nsb));
+    }
     return 0;
 }
 
@@ -67,6 +87,7 @@ FastFwdArgs fwd_args(gb_handle *h, bool keepE) {
     a.ssum = h->d_ssum;
     a.fhK = h->d_fhK;
     a.expo_root = f->expo_root;
+    a.err = f->err;
     return a;
 }
 
@@ -87,7 +108,8 @@ int record_forward_fast(gb_handle *h, bool keepE) {
         if (!n) continue;
         FastFwdArgs al = a;
         al.items = h->d_items + h->level_off[L];
-        launch_prune_fast(al, f->ns, n, ntile, h->stream);
+        if (f->umma) launch_prune_umma(al, f->ns, n, ntile, h->stream);
+        else launch_prune_fast(al, f->ns, n, ntile, h->stream);
         prof_mark(h, GB_K_PRUNE);
         nk++;
     }
@@ -125,6 +147,9 @@ FastBwdArgs bwd_args(gb_handle *h) {
     b.coff = ad->d_coff;
     b.z = h->d_z;
     b.Gpart = ad->d_Gpart;
+    b.err = f->err;
+    b.nsP = f->ns;
+    b.gchunk = GCHUNK;
     return b;
 }
 
@@ -142,11 +167,13 @@ int record_backward_fast(gb_handle *h) {
         if (!n) continue;
         FastBwdArgs bl = b;
         bl.bitems = ad->d_bitems + ad->blevel_off[L];
-        launch_bwd_fast(bl, f->ns, n, ntile, h->stream);
+        if (f->umma) launch_bwd_umma(bl, f->nsb, n, ntile, h->stream);
+        else launch_bwd_fast(bl, f->ns, n, ntile, h->stream);
         prof_mark(h, GB_K_BWD);
         nk++;
     }
-    launch_gradP_fast(b, f->ns, (int)h->pairs.size(), h->stream);
+    if (f->umma) launch_gradP_umma(b, f->nsb, (int)h->pairs.size(), h->stream);
+    else launch_gradP_fast(b, f->ns, (int)h->pairs.size(), h->stream);
     prof_mark(h, GB_K_GRADP);
     nk++;
     launch_gradH(h);
@@ -200,6 +227,43 @@ int ensure_fast_graph(gb_handle *h, bool keepE) {
 
 }  // namespace
 
+int fast_prepare(gb_handle *h, bool grad) {
+    CK(cudaSetDevice(h->device));
+    if (!h->fast) {
+        int rc = fast_init(h);
+        if (rc) return rc;
+    }
+    int rc = ensure_fast_graph(h, grad);
+    if (!rc && grad) rc = ensure_bwd_graph(h);
+    return rc;
+}
+
+int fast_record_eval(gb_handle *h, bool grad) {
+    FastState *f = h->fast;
+    CK(cudaMemcpyAsync(h->d_prm, h->h_prm, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_tnode, h->h_tnode, sizeof(double) * h->nnode, cudaMemcpyHostToDevice, h->stream));
+    if (grad) CK(cudaMemcpyAsync(h->adj->d_gp, h->adj->h_gp, sizeof(GradParams), cudaMemcpyHostToDevice, h->stream));
+    int nk = record_forward_fast(h, grad);
+    if (grad) {
+        nk += record_backward_fast(h);
+        int rc = adjoint_fetch(h);
+        if (rc) return -rc;
+    }
+    CK(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(f->h_err, f->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    return nk;
+}
+
+int fast_check_error(gb_handle *h) {
+    FastState *f = h->fast;
+    if (f && *f->h_err) {
+        cudaMemset(f->err, 0, sizeof(int));
+        *f->h_err = 0;
+        return fail(GB_ERR_TIMEOUT, "a tensor-core completion wait gave up (bounded mbarrier wait)");
+    }
+    return 0;
+}
+
 int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg_lnL, gb_grad *grad,
               double *fhK, double *lnf, gb_stats *stats) {
     CK(cudaSetDevice(h->device));
@@ -241,6 +305,7 @@ int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg
         if (rc) return rc;
     }
     CK(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(f->h_err, f->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     if (fhK)
         CK(cudaMemcpy2DAsync(fhK, sizeof(double) * h->npatt, h->d_fhK, sizeof(double) * h->npad,
                              sizeof(double) * h->npatt, 4, cudaMemcpyDeviceToHost, h->stream));
@@ -248,6 +313,10 @@ int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg
     CK(cudaEventRecord(h->ev1, h->stream));
     CK(cudaStreamSynchronize(h->stream));
     CK(cudaGetLastError());
+    if (*f->h_err) {
+        cudaMemset(f->err, 0, sizeof(int));
+        return fail(GB_ERR_TIMEOUT, "a tensor-core completion wait gave up (bounded mbarrier wait)");
+    }
     *neg_lnL = h->h_out[0];
     h->kernels_last = f->graph_kernels + (grad ? f->bwd_kernels : 0);
     if (grad) adjoint_chain(h, D, blength, grad);

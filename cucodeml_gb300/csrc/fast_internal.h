@@ -26,6 +26,7 @@ struct FastFwdArgs {
     const double *pi;
     double *fbar, *ssum, *fhK;   // [4][npad]
     int *expo_root;              // [4][npad]
+    int *err;                    // set to 1 by a CTA whose bounded wait gave up
 };
 
 struct FastBwdArgs {
@@ -44,10 +45,17 @@ struct FastBwdArgs {
     const int *coff;
     const unsigned char *z;
     double *Gpart;               // [npair][nchunk][64][64]
+    int *err;
+    int nsP;                     // digit planes stored per pair in Bb
+    int gchunk;                  // patterns per dlnL/dP partial
 };
 
 cudaError_t init_fast_kernels(int ns);
 cudaError_t init_fast_bwd_kernels(int ns);
+cudaError_t init_umma_kernels(int ns);
+void launch_prune_umma(const FastFwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st);
+void launch_bwd_umma(const FastBwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st);
+void launch_gradP_umma(const FastBwdArgs &a, int ns, int npair, cudaStream_t st);
 void launch_bwd_fast(const FastBwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st);
 void launch_gradP_fast(const FastBwdArgs &a, int ns, int npair, cudaStream_t st);
 void launch_pslice(const FastFwdArgs &a, int ns, int npair, cudaStream_t st);

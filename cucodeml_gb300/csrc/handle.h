@@ -107,6 +107,15 @@ struct gb_handle {
 };
 
 namespace gb {
+// host staging of one evaluation's parameters into the handle's pinned buffers
+int stage_params(gb_handle *h, const Derived *D, const double *blength);
+// record one evaluation's device work (copies in, kernels, copies out) on
+// h->stream; returns the kernel count or a negative GB_ERR_*
+int fp64_record_eval(gb_handle *h, bool grad);
+int fast_record_eval(gb_handle *h, bool grad);
+int fast_prepare(gb_handle *h, bool grad);     // allocations / kernel attributes before a capture
+int fp64_prepare(gb_handle *h, bool grad);
+int fast_check_error(gb_handle *h);
 // forward pass on the handle's stream (runtime.cu); keepE keeps the edge
 // messages for the adjoint
 int run_forward(gb_handle *h, const Derived *D, const double *blength, bool keepE, double *neg_lnL,

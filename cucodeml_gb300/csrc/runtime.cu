@@ -21,6 +21,7 @@
 #include "internal.h"
 #include "model.h"
 #include "handle.h"
+#include "adjoint_internal.h"
 
 using namespace gb;
 
@@ -284,6 +285,45 @@ int upload_and_run(gb_handle *h, const Derived *D, const double *blength, bool k
 }  // namespace
 
 namespace gb {
+int stage_params(gb_handle *h, const Derived *D, const double *blength) {
+    for (int i = 0; i < 3; i++) {
+        std::memcpy(h->h_prm->U[i], D->U[i], sizeof(double) * 61 * 61);
+        std::memcpy(h->h_prm->V[i], D->V[i], sizeof(double) * 61 * 61);
+        std::memcpy(h->h_prm->Root[i], D->Root[i], sizeof(double) * 61);
+    }
+    std::memcpy(h->h_prm->qf, D->qf, sizeof(double) * 2);
+    std::memcpy(h->h_prm->freqK, D->freqK, sizeof(double) * 4);
+    for (int n = 0; n < h->nnode; n++) {
+        double t = n == h->root ? 0.0 : blength[n];
+        if (!(t >= 0.0) || !std::isfinite(t)) return fail(GB_ERR_PARAM, "negative or non-finite branch length");
+        h->h_tnode[n] = t;
+    }
+    return 0;
+}
+
+int fp64_prepare(gb_handle *h, bool grad) {
+    CK(cudaSetDevice(h->device));
+    int rc = ensure_graph(h, grad);          // allocates the edge messages when grad
+    if (!rc && grad) rc = adjoint_init(h);
+    return rc;
+}
+
+// the device work of one FP64 evaluation on h->stream (for batch graphs):
+// parameter upload, forward, optional adjoint, result download
+int fp64_record_eval(gb_handle *h, bool grad) {
+    CK(cudaMemcpyAsync(h->d_prm, h->h_prm, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->d_tnode, h->h_tnode, sizeof(double) * h->nnode, cudaMemcpyHostToDevice, h->stream));
+    int nk = record_forward(h, grad);
+    if (grad) {
+        CK(cudaMemcpyAsync(h->adj->d_gp, h->adj->h_gp, sizeof(GradParams), cudaMemcpyHostToDevice, h->stream));
+        nk += adjoint_record(h);
+        int rc = adjoint_fetch(h);
+        if (rc) return -rc;
+    }
+    CK(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    return nk;
+}
+
 void prof_mark(gb_handle *h, int cls) {
     if (!h->prof) return;
     cudaEvent_t e;
@@ -347,7 +387,7 @@ int gb_create(const gb_problem *prob, gb_handle **out) {
         (rc = dalloc(&h->d_z, (size_t)h->ns * npad)) || (rc = dalloc(&h->d_fpatt, npad)) ||
         (rc = dalloc(&h->d_pi, 64)) || (rc = dalloc(&h->d_tnode, h->nnode)) || (rc = dalloc(&h->d_prm, 1)) ||
         (rc = dalloc(&h->d_Pt, h->pairs.size() * 64 * 64)) ||
-        (rc = dalloc(&h->d_conP, (size_t)h->nslot * npad * 64)) ||
+        (rc = dalloc(&h->d_conP, h->precision == GB_PREC_FP64 ? (size_t)h->nslot * npad * 64 : 1)) ||
         (rc = dalloc(&h->d_scaleF, (size_t)std::max(h->nsslot, 1) * npad)) ||
         (rc = dalloc(&h->d_fbar, 4 * npad)) || (rc = dalloc(&h->d_ssum, 4 * npad)) ||
         (rc = dalloc(&h->d_fhK, 4 * npad)) || (rc = dalloc(&h->d_lnf, npad)) ||

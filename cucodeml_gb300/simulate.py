@@ -80,15 +80,20 @@ def f3x4_pi(base_freqs: np.ndarray) -> np.ndarray:
     return pi / pi.sum()
 
 
-def transition_matrix(pi: np.ndarray, kappa: float, omega: float, t: float) -> np.ndarray:
-    """P(t) = exp(Q t) for the unscaled GY94 Q, via the symmetric eigenproblem."""
+def eigen_q(pi: np.ndarray, kappa: float, omega: float):
+    """(U, lam, V) with Q = U diag(lam) V for the unscaled GY94 Q."""
     Q, _ = codon.gy94_q(pi, kappa, omega)
     s = np.sqrt(pi)
     A = (s[:, None] * Q) / s[None, :]
     A = 0.5 * (A + A.T)
     lam, R = np.linalg.eigh(A)
-    P = (R / s[:, None]) @ np.diag(np.exp(lam * t)) @ (R.T * s[None, :])
-    return np.clip(P, 0.0, None)
+    return R / s[:, None], lam, R.T * s[None, :]
+
+
+def transition_matrix(pi: np.ndarray, kappa: float, omega: float, t: float, eig=None) -> np.ndarray:
+    """P(t) = exp(Q t) for the unscaled GY94 Q, via the symmetric eigenproblem."""
+    U, lam, V = eig if eig is not None else eigen_q(pi, kappa, omega)
+    return np.clip((U * np.exp(lam * t)[None, :]) @ V, 0.0, None)
 
 
 def simulate(ns: int, ncodon: int, seed: int, model: ModelA | None = None,
@@ -107,6 +112,7 @@ def simulate(ns: int, ncodon: int, seed: int, model: ModelA | None = None,
     # class -> omega index on background / foreground branches (Set_UVR_BranchSite)
     bg_w = [0, 1, 0, 1]
     fg_w = [0, 1, 2, 2]
+    eig = [eigen_q(pi, model.kappa, w[i]) for i in range(3)]
     stack = [tree.root]
     while stack:
         a = stack.pop()
@@ -118,7 +124,7 @@ def simulate(ns: int, ncodon: int, seed: int, model: ModelA | None = None,
                 if len(idx) == 0:
                     continue
                 wi = fg_w[k] if lab else bg_w[k]
-                P = transition_matrix(pi, model.kappa, w[wi], tt)
+                P = transition_matrix(pi, model.kappa, w[wi], tt, eig[wi])
                 cdf = np.cumsum(P, axis=1)
                 cdf /= cdf[:, -1:]
                 u = rng.random(len(idx))
@@ -135,3 +141,18 @@ def write_phylip(path: str, aln: Alignment) -> None:
         f.write(f"{aln.ns} {3 * aln.ncodon}\n")
         for nm, s in zip(aln.tree.names, seqs):
             f.write(f"{nm}    {s}\n")
+
+
+def simulate_batch(ngene: int, seed: int, taxa=(12, 48), codons=(100, 3000)):
+    """Independent alignments for the batched workload: taxa ~ U{12..48},
+    codons log-uniform in [100, 3000], and per gene kappa ~ LogN(ln 2, 0.3),
+    w0 ~ U(0.05, 0.8), w2 ~ U(1, 8) (p0 = 0.5, p1 = 0.3)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for g in range(ngene):
+        ns = int(rng.integers(taxa[0], taxa[1] + 1))
+        nc = int(round(np.exp(rng.uniform(np.log(codons[0]), np.log(codons[1])))))
+        m = ModelA(kappa=float(np.exp(rng.normal(np.log(2.0), 0.3))), omega0=float(rng.uniform(0.05, 0.8)),
+                   omega2=float(rng.uniform(1.0, 8.0)), p0=0.5, p1=0.3)
+        out.append(simulate(ns, nc, seed=int(rng.integers(1 << 31)), model=m))
+    return out

@@ -180,6 +180,22 @@ int gb_patterns(int ns, int ncodon, const int *codons, int *npatt, unsigned char
                 double *fpatt, double *pi);
 
 /*
+ * Batched evaluation of many independent alignments ("genes"), each with its
+ * own tree, patterns, codon frequencies and parameters (one device, one
+ * precision for the whole batch).  gb_batch_eval evaluates every gene
+ * (-lnL, and gradients when grads != NULL) with one CUDA-graph launch in
+ * which each gene's work is an independent branch; the host model set-up
+ * runs on all host cores.  prm, neg_lnL and grads are arrays of ngene.
+ * gb_batch_replay: as gb_replay, for the whole batch.
+ */
+typedef struct gb_batch gb_batch;
+int gb_batch_create(int ngene, const gb_problem *probs, gb_batch **out);
+int gb_batch_size(const gb_batch *b);
+int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *grads, gb_stats *stats);
+int gb_batch_replay(gb_batch *b, int iters, int with_grad, double *ms);
+int gb_batch_destroy(gb_batch *b);
+
+/*
  * Measurement hooks (used by the benchmark):
  *   gb_replay   re-runs the device work of the last gb_eval on this handle
  *               `iters` times with its inputs resident on the device (no host

@@ -8,10 +8,11 @@
 // (M = 128, N = 64, K = 16, bf16 x bf16 -> FP32) of every digit pair (i, j)
 // with i + j = L into that level's 64 TMEM columns (NS = 8: 8 levels = all
 // 512 columns), and commits to an mbarrier.  The level sums are exact integers
-// in FP32; each thread reads one row (TMEM lane) x 32 columns per level with
+// in FP32; each thread reads one row (TMEM lane) x 16 columns per level with
 // tcgen05.ld and combines the levels in double-float.
-// Warp w reads TMEM lanes 32 (w % 4) .. + 31 and columns 32 (w / 4) .. + 31, so
-// thread (w, lane) owns pattern row 32 (w % 4) + lane, states 32 (w / 4) + 0..31.
+// 16 warps (512 threads) per CTA: warp w reads TMEM lanes 32 (w % 4) .. + 31 and
+// columns 16 (w / 4) .. + 15, so thread (w, lane) owns pattern row
+// 32 (w % 4) + lane and states 16 (w / 4) + 0..15.
 // Every mbarrier wait is bounded; on timeout the CTA sets *err, skips its
 // remaining work and still frees its TMEM.
 #include <cuda_runtime.h>
@@ -28,6 +29,8 @@ namespace {
 
 using namespace fastdev;
 constexpr int NC = 61;
+constexpr int NT = 512;            // threads per CTA
+constexpr int NCOL = 16;           // states per thread in the epilogues
 constexpr int A_PLANE = 128 * 64 * 2;
 constexpr int B_PLANE = 64 * 64 * 2;
 
@@ -35,7 +38,7 @@ template <int NS>
 struct USm {
     static constexpr int OFF_B = NS * A_PLANE;
     static constexpr int OFF_MISC = OFF_B + NS * B_PLANE;
-    static constexpr int BYTES = OFF_MISC + 16 + 1024 + 2048;   // mbar, tmem slot, row max, row sums
+    static constexpr int BYTES = OFF_MISC + 16 + 2048 + 4096;   // mbar, tmem slot, row max [4][128], row sums [4][128]
 };
 
 // dlnL/dP kernel: A planes of 128 rows (rows 64..127 stay zero), B planes of 64 rows
@@ -52,8 +55,8 @@ __device__ __forceinline__ void slice_A_cm(const float2 *__restrict__ src, unsig
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = lane >> 2, kp = lane & 3;
 #pragma unroll 2
-    for (int q = 0; q < 16; q++) {
-        const int cmi = warp * 16 + q;                   // core matrix: row group cmi/8, k group cmi%8
+    for (int q = 0; q < 8; q++) {
+        const int cmi = warp * 8 + q;                    // core matrix: row group cmi/8, k group cmi%8
         const int row = (cmi >> 3) * 8 + rr, k = (cmi & 7) * 8 + 2 * kp;
         const float4 v = *reinterpret_cast<const float4 *>(src + (size_t)row * 64 + k);
         int d0[NS], d1[NS];
@@ -105,7 +108,7 @@ __device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t a_base, uin
 // success flag.
 template <int NS>
 __device__ __forceinline__ bool contract(unsigned char *sm, uint32_t tmem, uint64_t *mbar, uint32_t &phase,
-                                         float2 (&C)[32], int off_b = USm<NS>::OFF_B, bool b_top_only = false) {
+                                         float2 (&C)[NCOL], int off_b = USm<NS>::OFF_B, bool b_top_only = false) {
     umma::fence_proxy_async();
     umma::fence_before();
     __syncthreads();
@@ -121,61 +124,61 @@ __device__ __forceinline__ bool contract(unsigned char *sm, uint32_t tmem, uint6
     if (ok) {
         const int warp = threadIdx.x >> 5;
         const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-        const int col = 32 * (warp >> 2);
+        const int col = NCOL * (warp >> 2);
 #pragma unroll
-        for (int c = 0; c < 32; c++) C[c] = make_float2(0.f, 0.f);
+        for (int c = 0; c < NCOL; c++) C[c] = make_float2(0.f, 0.f);
 #pragma unroll 1
         for (int L = NS + 1; L >= 2; L--) {
-            float v[32];
-            umma::tmem_ld32(tmem + lane_base + (L - 2) * 64 + col, v);
+            float v[NCOL];
+            umma::tmem_ld16(tmem + lane_base + (L - 2) * 64 + col, v);
             const float w = scalbnf(1.0f, -7 * L);
 #pragma unroll
-            for (int c = 0; c < 32; c++) C[c] = df_add(C[c], make_float2(v[c] * w, 0.f));
+            for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(v[c] * w, 0.f));
         }
     }
     umma::fence_before();
     return ok;
 }
 
-__device__ __forceinline__ void load_row32(const float2 *p, float2 (&v)[32]) {
+__device__ __forceinline__ void load_row32(const float2 *p, float2 (&v)[NCOL]) {
 #pragma unroll
-    for (int c = 0; c < 16; c++) {
+    for (int c = 0; c < NCOL / 2; c++) {
         const float4 x = reinterpret_cast<const float4 *>(p)[c];
         v[2 * c] = make_float2(x.x, x.y);
         v[2 * c + 1] = make_float2(x.z, x.w);
     }
 }
 
-__device__ __forceinline__ void store_row32(float2 *p, const float2 (&v)[32]) {
+__device__ __forceinline__ void store_row32(float2 *p, const float2 (&v)[NCOL]) {
 #pragma unroll
-    for (int c = 0; c < 16; c++)
+    for (int c = 0; c < NCOL / 2; c++)
         reinterpret_cast<float4 *>(p)[c] = make_float4(v[2 * c].x, v[2 * c].y, v[2 * c + 1].x, v[2 * c + 1].y);
 }
 
-// row maximum over the valid states of the two threads sharing a row
-__device__ __forceinline__ float row_max(const float2 (&v)[32], int col0, float *rmax, int row, int ch) {
+// row maximum over the valid states of the four threads sharing a row
+__device__ __forceinline__ float row_max(const float2 (&v)[NCOL], int col0, float *rmax, int row, int ch) {
     float m = 0.f;
 #pragma unroll
-    for (int c = 0; c < 32; c++)
+    for (int c = 0; c < NCOL; c++)
         if (col0 + c < NC) m = fmaxf(m, v[c].x);
     rmax[ch * 128 + row] = m;
     __syncthreads();
-    m = fmaxf(rmax[row], rmax[128 + row]);
+    m = fmaxf(fmaxf(rmax[row], rmax[128 + row]), fmaxf(rmax[256 + row], rmax[384 + row]));
     __syncthreads();
     return m;
 }
 
 template <int NS>
-__global__ void __launch_bounds__(256, 1) prune_umma_kernel(FastFwdArgs a) {
+__global__ void __launch_bounds__(NT, 1) prune_umma_kernel(FastFwdArgs a) {
     extern __shared__ __align__(1024) unsigned char sm[];
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + USm<NS>::OFF_MISC);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + USm<NS>::OFF_MISC + 8);
     float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_MISC + 16);
-    double *rsum = reinterpret_cast<double *>(sm + USm<NS>::OFF_MISC + 16 + 1024);
+    double *rsum = reinterpret_cast<double *>(sm + USm<NS>::OFF_MISC + 16 + 2048);
     const Item it = a.items[blockIdx.y];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = warp >> 2;
-    const int row = 32 * (warp & 3) + lane, c0 = 32 * ch;
+    const int row = 32 * (warp & 3) + lane, c0 = NCOL * ch;
     const size_t npad = a.npad;
     const size_t h0 = (size_t)blockIdx.x * 128, h = h0 + row;
 
@@ -194,10 +197,10 @@ __global__ void __launch_bounds__(256, 1) prune_umma_kernel(FastFwdArgs a) {
     const uint32_t tmem = internal ? *tslot : 0u;
     uint32_t phase = 0;
     bool ok = true;
-    float2 prod[32];
+    float2 prod[NCOL];
     int expo = 0;
     for (int ci = 0; ci < it.nchild && ok; ci++) {
-        float2 E[32];
+        float2 E[NCOL];
         const int cs = it.cslot[ci];
         if (cs < 0) {
             const int zc = a.z[(size_t)it.child[ci] * npad + h];
@@ -212,26 +215,26 @@ __global__ void __launch_bounds__(256, 1) prune_umma_kernel(FastFwdArgs a) {
         }
         if (a.E) store_row32(a.E + ((size_t)(it.eslot + ci) * npad + h) * 64 + c0, E);
 #pragma unroll
-        for (int c = 0; c < 32; c++) prod[c] = ci == 0 ? E[c] : df_mul(prod[c], E[c]);
+        for (int c = 0; c < NCOL; c++) prod[c] = ci == 0 ? E[c] : df_mul(prod[c], E[c]);
     }
     if (ok) {
         const float m = row_max(prod, c0, rmax, row, ch);
         const int sh = m > 0.f ? ilogbf(m) + 1 : 0;
         expo += sh;
 #pragma unroll
-        for (int c = 0; c < 32; c++) prod[c] = df_scale(prod[c], -sh);
+        for (int c = 0; c < NCOL; c++) prod[c] = df_scale(prod[c], -sh);
         if (!it.is_root) {
             store_row32(a.conP + ((size_t)it.slot * npad + h) * 64 + c0, prod);
             if (ch == 0) a.expo[(size_t)it.slot * npad + h] = expo;
         } else {
             double f = 0.0;
 #pragma unroll
-            for (int c = 0; c < 32; c++)
+            for (int c = 0; c < NCOL; c++)
                 if (c0 + c < NC) f = fma(a.pi[c0 + c], (double)prod[c].x + (double)prod[c].y, f);
             rsum[ch * 128 + row] = f;
             __syncthreads();
             if (ch == 0) {
-                f = rsum[row] + rsum[128 + row];
+                f = (rsum[row] + rsum[128 + row]) + (rsum[256 + row] + rsum[384 + row]);
                 if (f <= 0.0) f = 1e-300;
                 const double sl = (double)expo * 0.69314718055994530942;
                 a.fbar[(size_t)it.cls * npad + h] = f;
@@ -252,7 +255,7 @@ __global__ void __launch_bounds__(256, 1) prune_umma_kernel(FastFwdArgs a) {
 }
 
 template <int NS>
-__global__ void __launch_bounds__(256, 1) bwd_umma_kernel(FastBwdArgs a) {
+__global__ void __launch_bounds__(NT, 1) bwd_umma_kernel(FastBwdArgs a) {
     extern __shared__ __align__(1024) unsigned char sm[];
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + USm<NS>::OFF_MISC);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + USm<NS>::OFF_MISC + 8);
@@ -260,7 +263,7 @@ __global__ void __launch_bounds__(256, 1) bwd_umma_kernel(FastBwdArgs a) {
     const BItem it = a.bitems[blockIdx.y];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = warp >> 2;
-    const int row = 32 * (warp & 3) + lane, c0 = 32 * ch;
+    const int row = 32 * (warp & 3) + lane, c0 = NCOL * ch;
     const size_t npad = a.npad;
     const size_t h0 = (size_t)blockIdx.x * 128, h = h0 + row;
 
@@ -293,12 +296,12 @@ __global__ void __launch_bounds__(256, 1) bwd_umma_kernel(FastBwdArgs a) {
     for (int i = 0; i < it.nchild && ok; i++) {
         for (int k = 0; k < it.ncls; k++) {
             const int c = it.cls[k];
-            float2 X[32];
+            float2 X[NCOL];
             int eX;
             if (it.is_root) {
                 const double g = a.fpatt[h] * a.post[(size_t)c * npad + h] / a.fbar[(size_t)c * npad + h];
 #pragma unroll
-                for (int q = 0; q < 32; q++) {
+                for (int q = 0; q < NCOL; q++) {
                     const double v = (c0 + q < NC) ? g * a.pi[c0 + q] : 0.0;
                     const float hi = (float)v;
                     X[q] = make_float2(hi, (float)(v - (double)hi));
@@ -311,15 +314,15 @@ __global__ void __launch_bounds__(256, 1) bwd_umma_kernel(FastBwdArgs a) {
             }
             for (int i2 = 0; i2 < it.nchild; i2++) {
                 if (i2 == i) continue;
-                float2 Ev[32];
+                float2 Ev[NCOL];
                 load_row32(a.E + ((size_t)(it.pslot[k] * MAXC + i2) * npad + h) * 64 + c0, Ev);
 #pragma unroll
-                for (int q = 0; q < 32; q++) X[q] = df_mul(X[q], Ev[q]);
+                for (int q = 0; q < NCOL; q++) X[q] = df_mul(X[q], Ev[q]);
             }
             const float m = row_max(X, c0, rmax, row, ch);
             const int sh = m > 0.f ? ilogbf(m) + 1 : 0;
 #pragma unroll
-            for (int q = 0; q < 32; q++) X[q] = df_scale(X[q], -sh);
+            for (int q = 0; q < NCOL; q++) X[q] = df_scale(X[q], -sh);
             const size_t eb = (size_t)(it.pslot[k] * MAXC + i);
             store_row32(a.Ebar + (eb * npad + h) * 64 + c0, X);
             if (ch == 0) a.ebexp[eb * npad + h] = (!(m > 0.f) || eX == ZERO_EXP) ? ZERO_EXP : eX + sh;
@@ -328,7 +331,7 @@ __global__ void __launch_bounds__(256, 1) bwd_umma_kernel(FastBwdArgs a) {
         const bool shared = it.ncls == 1 || it.tslot[i][0] == it.tslot[i][1];
         const int ntarget = shared ? 1 : 2;
         for (int tg = 0; tg < ntarget && ok; tg++) {
-            float2 acc[32];
+            float2 acc[NCOL];
             int eacc = ZERO_EXP;
             const int kbeg = shared ? 0 : tg, kend = shared ? it.ncls : tg + 1;
             for (int k = kbeg; k < kend; k++) {
@@ -336,19 +339,19 @@ __global__ void __launch_bounds__(256, 1) bwd_umma_kernel(FastBwdArgs a) {
                 __syncthreads();        // this tile's Ebar rows are written and visible
                 slice_A_cm<NS>(a.Ebar + (eb * npad + h0) * 64, sm);
                 load_B_cm<NS>(a.Bb + (size_t)it.pidx[i][k] * a.nsP * 4096, sm + USm<NS>::OFF_B);
-                float2 C[32];
+                float2 C[NCOL];
                 ok = contract<NS>(sm, tmem, mbar, phase, C);
                 if (!ok) break;
                 const int eC = a.ebexp[eb * npad + h];
                 if (k == kbeg) {
 #pragma unroll
-                    for (int q = 0; q < 32; q++) acc[q] = C[q];
+                    for (int q = 0; q < NCOL; q++) acc[q] = C[q];
                     eacc = eC;
                 } else {
                     const int e = max(eacc, eC);
                     const int da = max(eacc - e, -1000), dc = max(eC - e, -1000);
 #pragma unroll
-                    for (int q = 0; q < 32; q++) acc[q] = df_add(df_scale(acc[q], da), df_scale(C[q], dc));
+                    for (int q = 0; q < NCOL; q++) acc[q] = df_add(df_scale(acc[q], da), df_scale(C[q], dc));
                     eacc = e;
                 }
             }
@@ -356,7 +359,7 @@ __global__ void __launch_bounds__(256, 1) bwd_umma_kernel(FastBwdArgs a) {
             const float m = row_max(acc, c0, rmax, row, ch);
             const int sh = m > 0.f ? ilogbf(m) + 1 : 0;
 #pragma unroll
-            for (int q = 0; q < 32; q++) acc[q] = df_scale(acc[q], -sh);
+            for (int q = 0; q < NCOL; q++) acc[q] = df_scale(acc[q], -sh);
             const int ts = it.tslot[i][tg];
             store_row32(a.Abar + ((size_t)ts * npad + h) * 64 + c0, acc);
             if (ch == 0) a.aexp[(size_t)ts * npad + h] = (!(m > 0.f) || eacc == ZERO_EXP) ? ZERO_EXP : eacc + sh;
@@ -381,10 +384,10 @@ __global__ void __launch_bounds__(256, 1) bwd_umma_kernel(FastBwdArgs a) {
 // planes with K = patterns; tcgen05 with M = 128 of which rows 64..127 are
 // zero; the exact level sums are combined in double-float against a
 // reference exponent xr (the chunk's largest), with no FP64 arithmetic until
-// the final write.  Threads of TMEM lanes 0..63 (warps 0, 1, 4, 5) own
-// output rows j, 32 columns each.
+// the final write.  Threads of TMEM lanes 0..63 (warps w with w % 4 < 2) own
+// output rows j, 16 columns each.
 template <int NB>
-__global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
+__global__ void __launch_bounds__(NT, 1) gradP_umma_kernel(FastBwdArgs a) {
     extern __shared__ __align__(1024) unsigned char sm[];
     uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + GSm<NB>::OFF_MISC);
     uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + GSm<NB>::OFF_MISC + 8);
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
     int *red = reinterpret_cast<int *>(sm + GSm<NB>::OFF_MISC + 16 + 256);   // [2]
     const int p = blockIdx.x, chunk = blockIdx.y;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int row = 32 * (warp & 3) + lane, c0 = 32 * (warp >> 2);
+    const int row = 32 * (warp & 3) + lane, c0 = NCOL * (warp >> 2);
     const size_t npad = a.npad;
     const int hbeg = chunk * a.gchunk, hend = min(a.npatt, hbeg + a.gchunk);
     const int cbeg = a.coff[p], cend = a.coff[p + 1];
@@ -403,14 +406,14 @@ __global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
     int xl = ZERO_EXP;
     for (int ci = cbeg; ci < cend; ci++) {
         const int eb = a.contrib[ci].ebar;
-        for (int h = hbeg + tid; h < hend; h += 256) xl = max(xl, a.ebexp[(size_t)eb * npad + h]);
+        for (int h = hbeg + tid; h < hend; h += NT) xl = max(xl, a.ebexp[(size_t)eb * npad + h]);
     }
     atomicMax(&red[0], xl);
     __syncthreads();
     const int xr = red[0];
     double *out = a.Gpart + ((size_t)p * a.nchunk + chunk) * 64 * 64;
     if (xr == ZERO_EXP) {
-        for (int i = tid; i < 4096; i += 256) out[i] = 0.0;
+        for (int i = tid; i < 4096; i += NT) out[i] = 0.0;
         return;
     }
     if (warp == 0) {
@@ -419,7 +422,7 @@ __global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
     }
     if (tid == 0) umma::mbar_init(mbar, 1);
     // A rows 64..127 of every plane stay zero
-    for (int i = tid; i < NB * (A_PLANE / 2) / 16; i += 256) {
+    for (int i = tid; i < NB * (A_PLANE / 2) / 16; i += NT) {
         const int s = i / (A_PLANE / 2 / 16), r = i % (A_PLANE / 2 / 16);
         reinterpret_cast<uint4 *>(sm + s * A_PLANE + A_PLANE / 2)[r] = make_uint4(0, 0, 0, 0);
     }
@@ -429,9 +432,9 @@ __global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
     const uint32_t tmem = *tslot;
     uint32_t phase = 0;
     bool ok = true;
-    float2 acc[32];
+    float2 acc[NCOL];
 #pragma unroll
-    for (int c = 0; c < 32; c++) acc[c] = make_float2(0.f, 0.f);
+    for (int c = 0; c < NCOL; c++) acc[c] = make_float2(0.f, 0.f);
     const int rr = lane >> 2, kp = lane & 3;
     bool any_tip = false;
     for (int ci = cbeg; ci < cend && ok; ci++) {
@@ -452,8 +455,8 @@ __global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
             const int xmax = red[1];
             if (xmax == ZERO_EXP) continue;
             // transposed digit planes: warp writes core matrices (j group, h group)
-            for (int q = 0; q < 8; q++) {
-                const int cmi = warp * 8 + q;                  // 64 core matrices: jg = cmi / 8, hg = cmi % 8
+            for (int q = 0; q < 4; q++) {
+                const int cmi = warp * 4 + q;                  // 64 core matrices: jg = cmi / 8, hg = cmi % 8
                 const int j = (cmi >> 3) * 8 + rr, hh = (cmi & 7) * 8 + 2 * kp;
                 const int off = cmi * 128 + rr * 16 + kp * 4;
                 int d0[NB], d1[NB];
@@ -479,12 +482,12 @@ __global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
                     for (int s = 0; s < NB; s++) *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16_pair(d0[s], d1[s]);
                 }
             }
-            float2 C[32];
+            float2 C[NCOL];
             ok = contract<NB>(sm, tmem, mbar, phase, C, GSm<NB>::OFF_B, tip);
             if (!ok) break;
             const int sc = max(xmax - xr, -1000);
 #pragma unroll
-            for (int c = 0; c < 32; c++) acc[c] = df_add(acc[c], df_scale(C[c], sc));
+            for (int c = 0; c < NCOL; c++) acc[c] = df_add(acc[c], df_scale(C[c], sc));
         }
     }
     if (ok && any_tip) {
@@ -492,10 +495,10 @@ __global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
         // double-float partial sums in shared memory, 4 pattern partitions x 64 x 64
         __syncthreads();
         float2 *Gt = reinterpret_cast<float2 *>(sm);
-        for (int i = tid; i < 4 * 4096; i += 256) Gt[i] = make_float2(0.f, 0.f);
+        for (int i = tid; i < 4 * 4096; i += NT) Gt[i] = make_float2(0.f, 0.f);
         __syncthreads();
         const int j = tid & 63, part = tid >> 6;
-        for (int ci = cbeg; ci < cend; ci++) {
+        for (int ci = cbeg; ci < cend && tid < 256; ci++) {
             const Contrib cb = a.contrib[ci];
             if (cb.tslot >= 0) continue;
             const unsigned char *zz = a.z + (size_t)cb.tip * npad;
@@ -513,13 +516,13 @@ __global__ void __launch_bounds__(256, 1) gradP_umma_kernel(FastBwdArgs a) {
         __syncthreads();
         if (row < 64)
 #pragma unroll 4
-            for (int c = 0; c < 32; c++)
+            for (int c = 0; c < NCOL; c++)
                 for (int pp = 0; pp < 4; pp++) acc[c] = df_add(acc[c], Gt[(pp * 64 + c0 + c) * 64 + row]);
     }
     if (ok) {
         if (row < 64)
 #pragma unroll
-            for (int c = 0; c < 32; c++) out[row * 64 + c0 + c] = ldexp((double)acc[c].x + (double)acc[c].y, xr);
+            for (int c = 0; c < NCOL; c++) out[row * 64 + c0 + c] = ldexp((double)acc[c].x + (double)acc[c].y, xr);
     } else if (tid == 0) {
         atomicExch(a.err, 1);
         umma::mbar_wait(mbar, phase ^ 1u, 1000000000ull);
@@ -554,33 +557,33 @@ cudaError_t init_umma_kernels(int ns) {
 void launch_prune_umma(const FastFwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st) {
     dim3 grid(ntile, nitems);
     switch (ns) {
-        case 4: prune_umma_kernel<4><<<grid, 256, USm<4>::BYTES, st>>>(a); break;
-        case 5: prune_umma_kernel<5><<<grid, 256, USm<5>::BYTES, st>>>(a); break;
-        case 6: prune_umma_kernel<6><<<grid, 256, USm<6>::BYTES, st>>>(a); break;
-        case 7: prune_umma_kernel<7><<<grid, 256, USm<7>::BYTES, st>>>(a); break;
-        case 8: prune_umma_kernel<8><<<grid, 256, USm<8>::BYTES, st>>>(a); break;
+        case 4: prune_umma_kernel<4><<<grid, NT, USm<4>::BYTES, st>>>(a); break;
+        case 5: prune_umma_kernel<5><<<grid, NT, USm<5>::BYTES, st>>>(a); break;
+        case 6: prune_umma_kernel<6><<<grid, NT, USm<6>::BYTES, st>>>(a); break;
+        case 7: prune_umma_kernel<7><<<grid, NT, USm<7>::BYTES, st>>>(a); break;
+        case 8: prune_umma_kernel<8><<<grid, NT, USm<8>::BYTES, st>>>(a); break;
     }
 }
 
 void launch_bwd_umma(const FastBwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st) {
     dim3 grid(ntile, nitems);
     switch (ns) {
-        case 4: bwd_umma_kernel<4><<<grid, 256, USm<4>::BYTES, st>>>(a); break;
-        case 5: bwd_umma_kernel<5><<<grid, 256, USm<5>::BYTES, st>>>(a); break;
-        case 6: bwd_umma_kernel<6><<<grid, 256, USm<6>::BYTES, st>>>(a); break;
-        case 7: bwd_umma_kernel<7><<<grid, 256, USm<7>::BYTES, st>>>(a); break;
-        case 8: bwd_umma_kernel<8><<<grid, 256, USm<8>::BYTES, st>>>(a); break;
+        case 4: bwd_umma_kernel<4><<<grid, NT, USm<4>::BYTES, st>>>(a); break;
+        case 5: bwd_umma_kernel<5><<<grid, NT, USm<5>::BYTES, st>>>(a); break;
+        case 6: bwd_umma_kernel<6><<<grid, NT, USm<6>::BYTES, st>>>(a); break;
+        case 7: bwd_umma_kernel<7><<<grid, NT, USm<7>::BYTES, st>>>(a); break;
+        case 8: bwd_umma_kernel<8><<<grid, NT, USm<8>::BYTES, st>>>(a); break;
     }
 }
 
 void launch_gradP_umma(const FastBwdArgs &a, int ns, int npair, cudaStream_t st) {
     dim3 grid(npair, a.nchunk);
     switch (ns) {
-        case 4: gradP_umma_kernel<4><<<grid, 256, GSm<4>::BYTES, st>>>(a); break;
-        case 5: gradP_umma_kernel<5><<<grid, 256, GSm<5>::BYTES, st>>>(a); break;
-        case 6: gradP_umma_kernel<6><<<grid, 256, GSm<6>::BYTES, st>>>(a); break;
-        case 7: gradP_umma_kernel<7><<<grid, 256, GSm<7>::BYTES, st>>>(a); break;
-        case 8: gradP_umma_kernel<8><<<grid, 256, GSm<8>::BYTES, st>>>(a); break;
+        case 4: gradP_umma_kernel<4><<<grid, NT, GSm<4>::BYTES, st>>>(a); break;
+        case 5: gradP_umma_kernel<5><<<grid, NT, GSm<5>::BYTES, st>>>(a); break;
+        case 6: gradP_umma_kernel<6><<<grid, NT, GSm<6>::BYTES, st>>>(a); break;
+        case 7: gradP_umma_kernel<7><<<grid, NT, GSm<7>::BYTES, st>>>(a); break;
+        case 8: gradP_umma_kernel<8><<<grid, NT, GSm<8>::BYTES, st>>>(a); break;
     }
 }
 

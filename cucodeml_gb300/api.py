@@ -166,6 +166,20 @@ class Likelihood:
                                       n.ctypes.data_as(C.POINTER(C.c_int))))
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_lib.KCLASS)}
 
+    def task_trace(self, kernel: int) -> np.ndarray:
+        """[ntask, 8] uint64 trace of the last evaluation's persistent kernel
+        (0 pruning, 1 adjoint propagation, 2 dlnL/dP): gene, item, tile, 0,
+        claim ns, dependencies-met ns, end ns, SM.  Needs GBCODEML_TRACE=1 in
+        the environment before the first evaluation of this handle."""
+        n = self._L.gb_task_trace(self._h, int(kernel), None, 0)
+        if n < 0:
+            _lib.check(n)
+        out = np.zeros((n, 8), dtype=np.uint64)
+        r = self._L.gb_task_trace(self._h, int(kernel), out.ctypes.data_as(C.POINTER(C.c_ulonglong)), n)
+        if r < 0:
+            _lib.check(r)
+        return out
+
     def evaluate_x(self, x, lastround: bool = True, grad: bool = False) -> EvalResult:
         """-lnL (and gradient in node order) from codeml's x vector."""
         x = np.asarray(x, dtype=np.float64)

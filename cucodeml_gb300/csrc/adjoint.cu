@@ -365,6 +365,7 @@ int adjoint_init(gb_handle *h) {
                 }
                 for (int i = 0; i < MAXC; i++)
                     for (int k = 0; k < 2; k++) { b.pidx[i][k] = -1; b.tslot[i][k] = -1; }
+                for (int i = 0; i < MAXC; i++) b.child[i] = i < b.nchild ? h->sons[n * MAXC + i] : -1;
                 for (int i = 0; i < b.nchild; i++) {
                     int s = h->sons[n * MAXC + i];
                     for (int k = 0; k < b.ncls; k++) {

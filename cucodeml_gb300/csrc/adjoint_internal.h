@@ -21,6 +21,7 @@ struct BItem {                // backward work: (node, class family) of one leve
     int cls[2], pslot[2], sslot[2];
     int pidx[MAXC][2];        // pair of edge i under parent class k
     int tslot[MAXC][2];       // child slot receiving the adjoint (-1: tip)
+    int child[MAXC];          // child node of edge i
 };
 
 struct Contrib {              // one (parent slot, child) term of dlnL/dP for a pair

@@ -1,9 +1,13 @@
 // Batched evaluation of many independent alignments (genes): one handle per
-// gene, and ONE CUDA graph per batch evaluation in which every gene's device
-// work (parameter upload, forward levels, adjoint levels, result download) is
-// an independent branch, so the GPU runs the genes' small launches side by
-// side.  The host side (eigen solutions, Qfactors, chain rule of the
-// gradient) runs on a pool of host threads, one slice of genes per thread.
+// gene, and ONE CUDA graph per batch evaluation.  Split precision with the
+// persistent kernels: the pruning recursion, the adjoint propagation and
+// dlnL/dP of ALL genes are one persistent launch each over a task list that
+// mixes the genes (tasks ordered by tree level, dependencies tracked per
+// (slot, tile) on the device); the small per-gene steps (P matrices and their
+// digit planes, the mixture, dP/dt, per-pair sums, copies) are independent
+// graph branches between them.  Otherwise every gene's whole evaluation is an
+// independent branch.  The host side (eigen solutions, Qfactors, chain rule of
+// the gradient) runs on a pool of host threads, one slice of genes per thread.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -13,6 +17,7 @@
 #include <vector>
 
 #include "adjoint_internal.h"
+#include "fast_internal.h"
 #include "handle.h"
 
 struct gb_batch {
@@ -24,6 +29,7 @@ struct gb_batch {
     std::vector<cudaEvent_t> join;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int kernels[2] = {0, 0};
+    gb::PersistPlan plan;
 };
 
 namespace {
@@ -56,10 +62,59 @@ void batch_free(gb_batch *b) {
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
     if (b->origin) cudaStreamDestroy(b->origin);
+    gb::persist_free(&b->plan);
     for (auto h : b->h)
         if (h) gb_destroy(h);
     for (auto d : b->D) delete d;
     delete b;
+}
+
+// every gene's branch: origin -> gene stream -> fn(h) -> origin
+template <class F>
+int fork_join(gb_batch *b, F fn) {
+    CK(cudaEventRecord(b->fork, b->origin));
+    int nk = 0;
+    for (int i = 0; i < b->n; i++) {
+        gb_handle *h = b->h[i];
+        CK(cudaStreamWaitEvent(h->stream, b->fork, 0));
+        const int r = fn(h);
+        if (r < 0) return r;
+        nk += r;
+        CK(cudaEventRecord(b->join[i], h->stream));
+        CK(cudaStreamWaitEvent(b->origin, b->join[i], 0));
+    }
+    return nk;
+}
+
+bool batch_persistent(const gb_batch *b) {
+    for (auto h : b->h)
+        if (h->precision != GB_PREC_FAST || !fast_persistent(h) || fast_ns(h, false) != fast_ns(b->h[0], false) ||
+            fast_ns(h, true) != fast_ns(b->h[0], true))
+            return false;
+    return true;
+}
+
+int record_persistent(gb_batch *b, bool grad) {
+    const int ns = fast_ns(b->h[0], false), nsb = fast_ns(b->h[0], true);
+    launch_bump(b->plan.ctl, b->origin);
+    int nk = 1, r;
+    if ((r = fork_join(b, [&](gb_handle *h) {
+             const int rc = fast_rec_copies_in(h, grad);
+             return rc ? rc : fast_rec_pmat(h);
+         })) < 0)
+        return r;
+    nk += r + persist_record_fwd(&b->plan, grad, ns, b->origin, nullptr);
+    if ((r = fork_join(b, [&](gb_handle *h) { return fast_rec_mix(h) + (grad ? fast_rec_dmat(h) : 0); })) < 0)
+        return r;
+    nk += r;
+    if (grad) nk += persist_record_bwd(&b->plan, nsb, b->origin, nullptr);
+    if ((r = fork_join(b, [&](gb_handle *h) {
+             const int n = grad ? fast_rec_tail(h) : 0;
+             const int rc = fast_rec_copies_out(h, grad);
+             return rc ? rc : n;
+         })) < 0)
+        return r;
+    return nk + r;
 }
 
 int build_graph(gb_batch *b, bool grad) {
@@ -69,21 +124,25 @@ int build_graph(gb_batch *b, bool grad) {
         int rc = h->precision == GB_PREC_FAST ? fast_prepare(h, grad) : fp64_prepare(h, grad);
         if (rc) return rc;
     }
+    const bool persist = batch_persistent(b);
+    if (persist) {
+        int rc = persist_build(&b->plan, b->h.data(), b->n, grad);
+        if (rc) return rc;
+    }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
-    CK(cudaEventRecord(b->fork, b->origin));
-    int nk = 0;
-    for (int i = 0; i < b->n; i++) {
-        gb_handle *h = b->h[i];
-        CK(cudaStreamWaitEvent(h->stream, b->fork, 0));
-        int r = h->precision == GB_PREC_FAST ? fast_record_eval(h, grad) : fp64_record_eval(h, grad);
-        if (r < 0) {
-            cudaStreamEndCapture(b->origin, &g);
-            return r;
-        }
-        nk += r;
-        CK(cudaEventRecord(b->join[i], h->stream));
-        CK(cudaStreamWaitEvent(b->origin, b->join[i], 0));
+    int nk;
+    if (persist) {
+        nk = record_persistent(b, grad);
+    } else {
+        nk = fork_join(b, [&](gb_handle *h) {
+            return h->precision == GB_PREC_FAST ? fast_record_eval(h, grad) : fp64_record_eval(h, grad);
+        });
+    }
+    if (nk < 0) {
+        cudaStreamEndCapture(b->origin, &g);
+        if (g) cudaGraphDestroy(g);
+        return nk;
     }
     CK(cudaStreamEndCapture(b->origin, &g));
     cudaError_t e = cudaGraphInstantiate(&ge, g, 0);

@@ -2,11 +2,14 @@
 // and launches.  Kernels: k_umma.cu (tcgen05 contractions, the default),
 // k_fast.cu / k_fast_bwd.cu (mma.sync contractions, P digit planes, dlnL/dP).
 // GBCODEML_MMA=sync in the environment selects the mma.sync contraction
-// kernels for the forward and adjoint levels.
+// kernels for the forward and adjoint levels; GBCODEML_PERSIST=0 selects one
+// tcgen05 launch per tree level instead of the persistent task-list kernels.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "adjoint_internal.h"
 #include "fast_internal.h"
@@ -22,7 +25,10 @@ struct FastState {
     int *ebexp = nullptr, *aexp = nullptr;     // adjoint exponents
     int *err = nullptr, *h_err = nullptr;      // bounded-wait failure flag (device, pinned host)
     bool umma = true;                          // tcgen05 contractions (else mma.sync)
+    bool persist = true;                       // persistent task-list kernels (tcgen05 only)
     int nsb = 7;                               // digit planes in the adjoint contractions
+    unsigned *ready_f = nullptr, *ready_b = nullptr;   // [nslot][ntile] forward / adjoint ready flags
+    PersistPlan plan;                          // this handle's own persistent launches
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     cudaGraphExec_t bwd_graph = nullptr;
     int graph_kernels = 0, bwd_kernels = 0;
@@ -34,7 +40,9 @@ void fast_free(FastState *f) {
         if (g) cudaGraphExecDestroy(g);
     if (f->bwd_graph) cudaGraphExecDestroy(f->bwd_graph);
     if (f->h_err) cudaFreeHost(f->h_err);
-    void *p[] = {f->Pdf, f->conP, f->E, f->Bf, f->Bb, f->expo, f->expo_root, f->ebexp, f->aexp, f->err};
+    persist_free(&f->plan);
+    void *p[] = {f->Pdf, f->conP, f->E, f->Bf, f->Bb, f->expo, f->expo_root, f->ebexp, f->aexp, f->err,
+                 f->ready_f, f->ready_b};
     for (void *q : p)
         if (q) cudaFree(q);
     delete f;
@@ -58,6 +66,12 @@ int fast_init(gb_handle *h) {
     f->nsb = nb ? std::atoi(nb) : 7;
     if (f->nsb < 4 || f->nsb > f->ns) f->nsb = f->ns < 7 ? f->ns : 7;
     f->umma = !(mode && std::strcmp(mode, "sync") == 0) && f->ns >= 6;
+    const char *ps = std::getenv("GBCODEML_PERSIST");
+    f->persist = f->umma && !(ps && std::strcmp(ps, "0") == 0);
+    const size_t nflag = (size_t)h->nslot * (npad / FAST_MT);
+    if ((rc = dalloc(&f->ready_f, nflag)) || (rc = dalloc(&f->ready_b, nflag))) return rc;
+    CK(cudaMemset(f->ready_f, 0, sizeof(unsigned) * std::max<size_t>(nflag, 1)));
+    CK(cudaMemset(f->ready_b, 0, sizeof(unsigned) * std::max<size_t>(nflag, 1)));
     if ((rc = dalloc(&f->err, 1))) return rc;
     CK(cudaMemset(f->err, 0, sizeof(int)));
     CK(cudaMallocHost((void **)&f->h_err, sizeof(int)));
@@ -88,21 +102,17 @@ FastFwdArgs fwd_args(gb_handle *h, bool keepE) {
     a.fhK = h->d_fhK;
     a.expo_root = f->expo_root;
     a.err = f->err;
+    a.ready = f->ready_f;
+    a.ntile = h->npad / FAST_MT;
     return a;
 }
 
-int record_forward_fast(gb_handle *h, bool keepE) {
+int rec_levels_fwd(gb_handle *h, bool keepE) {
     FastState *f = h->fast;
-    int nk = 0;
-    launch_pmat_fp64(h->d_pairs, (int)h->pairs.size(), h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->stream);
-    prof_mark(h, GB_K_PMAT);
-    nk++;
     FastFwdArgs a = fwd_args(h, keepE);
-    launch_pslice(a, f->ns, (int)h->pairs.size(), h->stream);
-    prof_mark(h, GB_K_PMAT);
-    nk++;
     const int ntile = h->npad / FAST_MT;
     const int H = (int)h->level_off.size() - 1;
+    int nk = 0;
     for (int L = 0; L < H; L++) {
         const int n = h->level_off[L + 1] - h->level_off[L];
         if (!n) continue;
@@ -113,11 +123,21 @@ int record_forward_fast(gb_handle *h, bool keepE) {
         prof_mark(h, GB_K_PRUNE);
         nk++;
     }
-    // every node is renormalised, so fhK is always in log form
-    launch_mix(h->d_fhK, h->d_fpatt, h->d_prm, h->npatt, h->npad, 1, h->d_lnf, h->d_post, h->d_partial,
-               h->d_ticket, h->d_out, h->stream);
-    prof_mark(h, GB_K_MIX);
-    nk++;
+    return nk;
+}
+
+int record_forward_fast(gb_handle *h, bool keepE) {
+    FastState *f = h->fast;
+    int nk = 0;
+    if (f->persist) {
+        launch_bump(f->plan.ctl, h->stream);
+        prof_mark(h, GB_K_OTHER);
+        nk++;
+    }
+    nk += fast_rec_pmat(h);
+    if (f->persist) nk += persist_record_fwd(&f->plan, keepE, f->ns, h->stream, h);
+    else nk += rec_levels_fwd(h, keepE);
+    nk += fast_rec_mix(h);
     return nk;
 }
 
@@ -150,16 +170,16 @@ FastBwdArgs bwd_args(gb_handle *h) {
     b.err = f->err;
     b.nsP = f->ns;
     b.gchunk = GCHUNK;
+    b.ready = f->ready_b;
+    b.ntile = h->npad / FAST_MT;
+    b.Pdf = f->Pdf;
     return b;
 }
 
-int record_backward_fast(gb_handle *h) {
+int rec_levels_bwd(gb_handle *h) {
     FastState *f = h->fast;
     AdjointState *ad = h->adj;
     int nk = 0;
-    launch_dmat(h);
-    prof_mark(h, GB_K_OTHER);
-    nk++;
     FastBwdArgs b = bwd_args(h);
     const int ntile = h->npad / FAST_MT;
     for (size_t L = 0; L + 1 < ad->blevel_off.size(); L++) {
@@ -176,27 +196,48 @@ int record_backward_fast(gb_handle *h) {
     else launch_gradP_fast(b, f->ns, (int)h->pairs.size(), h->stream);
     prof_mark(h, GB_K_GRADP);
     nk++;
-    launch_gradH(h);
-    prof_mark(h, GB_K_GRADH);
-    nk++;
-    launch_freq(h, 1);
-    prof_mark(h, GB_K_OTHER);
-    nk++;
     return nk;
 }
 
-int ensure_bwd_graph(gb_handle *h) {
+int record_backward_fast(gb_handle *h) {
     FastState *f = h->fast;
-    if (f->bwd_graph) return 0;
-    int rc = adjoint_init(h);
-    if (rc) return rc;
+    int nk = fast_rec_dmat(h);
+    if (f->persist) nk += persist_record_bwd(&f->plan, f->nsb, h->stream, h);
+    else nk += rec_levels_bwd(h);
+    nk += fast_rec_tail(h);
+    return nk;
+}
+
+// buffers of an evaluation with (grad) or without the adjoint; no graph
+int fast_alloc(gb_handle *h, bool grad) {
+    if (!h->fast) {
+        int rc = fast_init(h);
+        if (rc) return rc;
+    }
+    FastState *f = h->fast;
+    if (!grad) return 0;
+    int rc;
+    if (!f->E && (rc = dalloc(&f->E, (size_t)h->nslot * MAXC * h->npad * 64))) return rc;
+    if ((rc = adjoint_init(h))) return rc;
     if (!f->ebexp) {
         if ((rc = dalloc(&f->ebexp, (size_t)h->nslot * MAXC * h->npad)) ||
             (rc = dalloc(&f->aexp, (size_t)h->nslot * h->npad)))
             return rc;
         CK(cudaMemset(f->aexp, 0, sizeof(int) * h->nslot * h->npad));
+        CK(init_fast_bwd_kernels(f->ns));
     }
-    CK(init_fast_bwd_kernels(f->ns));
+    return 0;
+}
+
+int ensure_bwd_graph(gb_handle *h) {
+    FastState *f = h->fast;
+    if (f->bwd_graph) return 0;
+    int rc = fast_alloc(h, true);
+    if (rc) return rc;
+    if (f->persist) {
+        gb_handle *one[1] = {h};
+        if ((rc = persist_build(&f->plan, one, 1, true))) return rc;
+    }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     f->bwd_kernels = record_backward_fast(h);
@@ -211,9 +252,11 @@ int ensure_fast_graph(gb_handle *h, bool keepE) {
     FastState *f = h->fast;
     cudaGraphExec_t &ge = f->graph[keepE ? 1 : 0];
     if (ge) return 0;
-    if (keepE && !f->E) {
-        int rc = dalloc(&f->E, (size_t)h->nslot * MAXC * h->npad * 64);
-        if (rc) return rc;
+    int rc = fast_alloc(h, keepE);
+    if (rc) return rc;
+    if (f->persist) {
+        gb_handle *one[1] = {h};
+        if ((rc = persist_build(&f->plan, one, 1, keepE))) return rc;
     }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -227,30 +270,212 @@ int ensure_fast_graph(gb_handle *h, bool keepE) {
 
 }  // namespace
 
-int fast_prepare(gb_handle *h, bool grad) {
-    CK(cudaSetDevice(h->device));
-    if (!h->fast) {
-        int rc = fast_init(h);
-        if (rc) return rc;
-    }
-    int rc = ensure_fast_graph(h, grad);
-    if (!rc && grad) rc = ensure_bwd_graph(h);
-    return rc;
+// ---------------------------------------------------------------- persistent plans
+
+void persist_free(PersistPlan *pp) {
+    void *p[] = {pp->ctl,     pp->d_fargs[0], pp->d_fargs[1], pp->d_bargs, pp->d_ftask,
+                 pp->d_btask, pp->d_gtask,    pp->trace[0],   pp->trace[1], pp->trace[2]};
+    for (void *q : p)
+        if (q) cudaFree(q);
+    *pp = PersistPlan();
 }
 
-int fast_record_eval(gb_handle *h, bool grad) {
-    FastState *f = h->fast;
+int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd) {
+    int rc;
+    if (!pp->ctl) {
+        if ((rc = dalloc(&pp->ctl, CTL_WORDS))) return rc;
+        CK(cudaMemset(pp->ctl, 0, sizeof(unsigned) * CTL_WORDS));
+        int dev = 0;
+        CK(cudaGetDevice(&dev));
+        CK(cudaDeviceGetAttribute(&pp->nblock, cudaDevAttrMultiProcessorCount, dev));
+        pp->ngene = n;
+    }
+    if (pp->ngene != n) return fail(GB_ERR_STATE, "persistent plan: gene count changed");
+    // argument blocks (re-uploaded: buffers such as E may have been allocated since)
+    std::vector<FastFwdArgs> fa(n);
+    for (int k = 0; k < 2; k++) {
+        for (int g = 0; g < n; g++) fa[g] = fwd_args(hs[g], k == 1);
+        if (!pp->d_fargs[k] && (rc = dalloc(&pp->d_fargs[k], n))) return rc;
+        CK(cudaMemcpy(pp->d_fargs[k], fa.data(), sizeof(FastFwdArgs) * n, cudaMemcpyHostToDevice));
+    }
+    if (!pp->d_ftask) {
+        // children before parents: level by level (tree height), all genes per level
+        std::vector<Task> t;
+        int maxH = 0;
+        for (int g = 0; g < n; g++) maxH = std::max(maxH, (int)hs[g]->level_off.size() - 1);
+        for (int L = 0; L < maxH; L++)
+            for (int g = 0; g < n; g++) {
+                const gb_handle *h = hs[g];
+                if (L + 1 >= (int)h->level_off.size()) continue;
+                const int nt = h->npad / FAST_MT;
+                for (int i = h->level_off[L]; i < h->level_off[L + 1]; i++)
+                    for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, 0});
+            }
+        pp->nftask = (int)t.size();
+        const char *tr = std::getenv("GBCODEML_TRACE");
+        pp->tracing = tr && std::strcmp(tr, "1") == 0;
+        if (pp->tracing && (rc = dalloc(&pp->trace[0], 4 * t.size()))) return rc;
+        if ((rc = dalloc(&pp->d_ftask, t.size()))) return rc;
+        CK(cudaMemcpy(pp->d_ftask, t.data(), sizeof(Task) * t.size(), cudaMemcpyHostToDevice));
+    }
+    if (!bwd) return 0;
+    std::vector<FastBwdArgs> ba(n);
+    for (int g = 0; g < n; g++) {
+        if (!hs[g]->adj || !hs[g]->fast->ebexp) return fail(GB_ERR_STATE, "persistent plan: adjoint buffers missing");
+        ba[g] = bwd_args(hs[g]);
+    }
+    if (!pp->d_bargs && (rc = dalloc(&pp->d_bargs, n))) return rc;
+    CK(cudaMemcpy(pp->d_bargs, ba.data(), sizeof(FastBwdArgs) * n, cudaMemcpyHostToDevice));
+    if (!pp->d_btask) {
+        // parents before children: backward levels from each gene's root down
+        std::vector<Task> t;
+        int maxB = 0;
+        for (int g = 0; g < n; g++) maxB = std::max(maxB, (int)hs[g]->adj->blevel_off.size() - 1);
+        for (int d = 0; d < maxB; d++)
+            for (int g = 0; g < n; g++) {
+                const AdjointState *ad = hs[g]->adj;
+                if (d + 1 >= (int)ad->blevel_off.size()) continue;
+                const int nt = hs[g]->npad / FAST_MT;
+                for (int i = ad->blevel_off[d]; i < ad->blevel_off[d + 1]; i++)
+                    for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, 0});
+            }
+        pp->nbtask = (int)t.size();
+        if (pp->tracing && (rc = dalloc(&pp->trace[1], 4 * t.size()))) return rc;
+        if ((rc = dalloc(&pp->d_btask, t.size()))) return rc;
+        CK(cudaMemcpy(pp->d_btask, t.data(), sizeof(Task) * t.size(), cudaMemcpyHostToDevice));
+        // dlnL/dP: independent (gene, pair, chunk) tasks, heaviest first
+        std::vector<std::pair<long, Task>> gt;
+        for (int g = 0; g < n; g++) {
+            const gb_handle *h = hs[g];
+            const AdjointState *ad = h->adj;
+            for (int p = 0; p < (int)h->pairs.size(); p++)
+                for (int c = 0; c < ad->nchunk; c++) {
+                    const long np = std::min(h->npatt, (c + 1) * GCHUNK) - c * GCHUNK;
+                    gt.push_back({(long)(ad->coff[p + 1] - ad->coff[p]) * np, Task{g, p, c, 0}});
+                }
+        }
+        std::stable_sort(gt.begin(), gt.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+        t.clear();
+        for (auto &x : gt) t.push_back(x.second);
+        pp->ngtask = (int)t.size();
+        if (pp->tracing && (rc = dalloc(&pp->trace[2], 4 * t.size()))) return rc;
+        if ((rc = dalloc(&pp->d_gtask, t.size()))) return rc;
+        CK(cudaMemcpy(pp->d_gtask, t.data(), sizeof(Task) * t.size(), cudaMemcpyHostToDevice));
+    }
+    pp->has_bwd = true;
+    return 0;
+}
+
+int persist_record_fwd(PersistPlan *pp, bool keepE, int ns, cudaStream_t st, gb_handle *prof) {
+    launch_prune_persist(pp->d_fargs[keepE ? 1 : 0], pp->d_ftask, pp->nftask, pp->ctl, ns, pp->nblock,
+                         pp->trace[0], st);
+    if (prof) prof_mark(prof, GB_K_PRUNE);
+    return 1;
+}
+
+int persist_record_bwd(PersistPlan *pp, int nsb, cudaStream_t st, gb_handle *prof) {
+    launch_bwd_persist(pp->d_bargs, pp->d_btask, pp->nbtask, pp->ctl, nsb, pp->nblock, pp->trace[1], st);
+    if (prof) prof_mark(prof, GB_K_BWD);
+    launch_gradP_persist(pp->d_bargs, pp->d_gtask, pp->ngtask, pp->ctl, nsb, pp->nblock, pp->trace[2], st);
+    if (prof) prof_mark(prof, GB_K_GRADP);
+    return 2;
+}
+
+// ---------------------------------------------------------------- per-gene pieces
+
+int fast_rec_pmat(gb_handle *h) {
+    launch_pmat_fp64(h->d_pairs, (int)h->pairs.size(), h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->stream);
+    prof_mark(h, GB_K_PMAT);
+    FastFwdArgs a = fwd_args(h, false);
+    launch_pslice(a, h->fast->ns, (int)h->pairs.size(), h->fast->umma, h->stream);
+    prof_mark(h, GB_K_PMAT);
+    return 2;
+}
+
+int fast_rec_mix(gb_handle *h) {
+    // every node is renormalised, so fhK is always in log form
+    launch_mix(h->d_fhK, h->d_fpatt, h->d_prm, h->npatt, h->npad, 1, h->d_lnf, h->d_post, h->d_partial,
+               h->d_ticket, h->d_out, h->stream);
+    prof_mark(h, GB_K_MIX);
+    return 1;
+}
+
+int fast_rec_dmat(gb_handle *h) {
+    launch_dmat(h);
+    prof_mark(h, GB_K_OTHER);
+    return 1;
+}
+
+int fast_rec_tail(gb_handle *h) {
+    launch_gradH(h);
+    prof_mark(h, GB_K_GRADH);
+    launch_freq(h, 1);
+    prof_mark(h, GB_K_OTHER);
+    return 2;
+}
+
+int fast_rec_copies_in(gb_handle *h, bool grad) {
     CK(cudaMemcpyAsync(h->d_prm, h->h_prm, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemcpyAsync(h->d_tnode, h->h_tnode, sizeof(double) * h->nnode, cudaMemcpyHostToDevice, h->stream));
     if (grad) CK(cudaMemcpyAsync(h->adj->d_gp, h->adj->h_gp, sizeof(GradParams), cudaMemcpyHostToDevice, h->stream));
-    int nk = record_forward_fast(h, grad);
+    return 0;
+}
+
+int fast_rec_copies_out(gb_handle *h, bool grad) {
     if (grad) {
-        nk += record_backward_fast(h);
         int rc = adjoint_fetch(h);
-        if (rc) return -rc;
+        if (rc) return rc;
     }
     CK(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    CK(cudaMemcpyAsync(f->h_err, f->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    CK(cudaMemcpyAsync(h->fast->h_err, h->fast->err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    return 0;
+}
+
+int fast_prepare(gb_handle *h, bool grad) {
+    CK(cudaSetDevice(h->device));
+    return fast_alloc(h, grad);
+}
+
+bool fast_persistent(const gb_handle *h) { return h->fast && h->fast->persist; }
+
+// the last evaluation's task trace of one persistent kernel of this handle:
+// 8 words per task (gene, item, tile, 0, claim ns, dependencies met ns, end ns, SM)
+int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap) {
+    if (!h->fast || !h->fast->persist) return fail(GB_ERR_STATE, "gb_task_trace: no persistent kernels on this handle");
+    PersistPlan *pp = &h->fast->plan;
+    if (kernel < 0 || kernel > 2) return fail(GB_ERR_ARG, "gb_task_trace: kernel must be 0, 1 or 2");
+    const Task *dt[3] = {pp->d_ftask, pp->d_btask, pp->d_gtask};
+    const int nt[3] = {pp->nftask, pp->nbtask, pp->ngtask};
+    if (!pp->tracing || !pp->trace[kernel] || !dt[kernel])
+        return fail(GB_ERR_STATE, "gb_task_trace: tracing off (GBCODEML_TRACE=1 at creation) or kernel not run");
+    const int n = std::min(cap, nt[kernel]);
+    if (out && n > 0) {
+        CK(cudaSetDevice(h->device));
+        CK(cudaStreamSynchronize(h->stream));
+        std::vector<Task> t(n);
+        std::vector<unsigned long long> tr(4 * (size_t)n);
+        CK(cudaMemcpy(t.data(), dt[kernel], sizeof(Task) * n, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(tr.data(), pp->trace[kernel], sizeof(unsigned long long) * 4 * n, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < n; i++) {
+            out[8 * i + 0] = (unsigned long long)t[i].gene;
+            out[8 * i + 1] = (unsigned long long)t[i].item;
+            out[8 * i + 2] = (unsigned long long)t[i].tile;
+            out[8 * i + 3] = 0;
+            for (int q = 0; q < 4; q++) out[8 * i + 4 + q] = tr[4 * i + q];
+        }
+    }
+    return nt[kernel];
+}
+int fast_ns(const gb_handle *h, bool adjoint) { return adjoint ? h->fast->nsb : h->fast->ns; }
+
+// one gene's whole evaluation with one launch per tree level (batches whose
+// genes do not share a persistent plan)
+int fast_record_eval(gb_handle *h, bool grad) {
+    int rc = fast_rec_copies_in(h, grad);
+    if (rc) return rc;
+    int nk = fast_rec_pmat(h) + rec_levels_fwd(h, grad) + fast_rec_mix(h);
+    if (grad) nk += fast_rec_dmat(h) + rec_levels_bwd(h) + fast_rec_tail(h);
+    if ((rc = fast_rec_copies_out(h, grad))) return rc;
     return nk;
 }
 

@@ -60,23 +60,50 @@ __device__ __forceinline__ int small_float_to_int(float c) {   // exact for 0 <=
     return __float_as_int(__fadd_rn(c, 8388608.0f)) - 0x4B000000;
 }
 
+// floor(|x| * 2^B) from the bit fields of x (|x| = m 2^(e-150), m the 24-bit
+// significand), and whether the product had a fractional part
+template <int B>
+__device__ __forceinline__ unsigned long long fixed_of(float x, bool &inexact) {
+    const unsigned u = __float_as_uint(x) & 0x7fffffffu;
+    const int e = (int)(u >> 23);
+    inexact = false;
+    if (e == 0) {                                   // zero (a denormal is below 2^-126: no digit)
+        inexact = u != 0u;
+        return 0ull;
+    }
+    const unsigned m = (u & 0x7fffffu) | 0x800000u;
+    const int sh = e - 150 + B;
+    if (sh >= 0) return (unsigned long long)m << sh;
+    if (sh <= -24) {
+        inexact = true;
+        return 0ull;
+    }
+    inexact = (m & ((1u << -sh) - 1u)) != 0u;
+    return (unsigned long long)(m >> -sh);
+}
+
+// Digits of v = hi + lo (a double-float in [0, 1]): q = floor(v 2^(7 NS))
+// exactly (hi 2^(7NS) is an integer or truncates to one, lo is added as
+// floor(lo 2^(7NS)) with its sign), then d_s = bits 7(NS-1-s) .. +6 of q;
+// the first digit is 128 only for v = 1.
 template <int NS>
 __device__ __forceinline__ void digits_of(float hi, float lo, int (&d)[NS]) {
-    float x = hi, y = lo;
-#pragma unroll
-    for (int g0 = 0; g0 < NS; g0 += 3) {
-        const int nd = NS - g0 < 3 ? NS - g0 : 3;
-        x = scalbnf(x, 7 * nd);
-        y = scalbnf(y, 7 * nd);
-        float c;
-        df_floor_step(x, y, c);
-        int ci = small_float_to_int(c < 0.f ? 0.f : c);
-#pragma unroll
-        for (int q = 0; q < nd; q++) {
-            const int sh = 7 * (nd - 1 - q);
-            d[g0 + q] = (g0 == 0 && q == 0) ? (ci >> sh) : ((ci >> sh) & 127);   // first may be 128
-        }
+    constexpr int B = 7 * NS;
+    bool ih, il;
+    const unsigned long long qh = fixed_of<B>(hi, ih);
+    const unsigned long long ql = fixed_of<B>(lo, il);
+    // a fractional hi 2^B is a multiple of 2^(-k) above |lo| 2^B <= 2^(-k-1)
+    // (|lo| <= ulp(hi) / 2), so lo cannot move the floor then
+    long long q = (long long)qh;
+    if (!ih) {
+        if (lo < 0.f) q -= (long long)ql + (il ? 1 : 0);
+        else q += (long long)ql;
     }
+    if (q < 0) q = 0;
+    const unsigned long long uq = (unsigned long long)q;
+    d[0] = (int)(uq >> (B - 7));
+#pragma unroll
+    for (int s = 1; s < NS; s++) d[s] = (int)((uq >> (B - 7 * (s + 1))) & 127ull);
 }
 
 __device__ __forceinline__ float small_int_to_float(int d) {   // exact for 0 <= d < 2^23

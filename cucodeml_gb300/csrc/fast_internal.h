@@ -12,6 +12,35 @@ namespace gb {
 
 constexpr int FAST_MT = 128;   // patterns per CTA tile in the split-precision kernels
 
+// one unit of work of a persistent kernel: (gene, item, tile); for dlnL/dP
+// item = pair and tile = pattern chunk
+struct Task {
+    int gene, item, tile, pad;
+};
+
+// control words of a persistent executor (device memory): the evaluation
+// epoch (ready flags hold the epoch of the evaluation that wrote them) and
+// the task counters of the three persistent kernels
+enum { CTL_EPOCH = 0, CTL_FWD = 1, CTL_BWD = 2, CTL_GRADP = 3, CTL_WORDS = 4 };
+
+struct FastFwdArgs;
+struct FastBwdArgs;
+
+// the persistent launches of one executor (a handle, or a batch of genes):
+// per-gene argument blocks, task lists and control words, all in device memory
+struct PersistPlan {
+    unsigned *ctl = nullptr;                         // [CTL_WORDS]
+    FastFwdArgs *d_fargs[2] = {nullptr, nullptr};    // per gene, without / with edge messages
+    FastBwdArgs *d_bargs = nullptr;                  // per gene
+    Task *d_ftask = nullptr, *d_btask = nullptr, *d_gtask = nullptr;
+    int nftask = 0, nbtask = 0, ngtask = 0;
+    int nblock = 0;                                  // CTAs per persistent launch (one per SM)
+    int ngene = 0;
+    bool has_bwd = false;
+    unsigned long long *trace[3] = {nullptr, nullptr, nullptr};   // per kernel, when tracing
+    bool tracing = false;
+};
+
 struct FastFwdArgs {
     const Item *items;
     int npad;
@@ -27,6 +56,8 @@ struct FastFwdArgs {
     double *fbar, *ssum, *fhK;   // [4][npad]
     int *expo_root;              // [4][npad]
     int *err;                    // set to 1 by a CTA whose bounded wait gave up
+    unsigned *ready;             // [nslot][ntile] epoch of the last write of (slot, tile)
+    int ntile;
 };
 
 struct FastBwdArgs {
@@ -48,6 +79,9 @@ struct FastBwdArgs {
     int *err;
     int nsP;                     // digit planes stored per pair in Bb
     int gchunk;                  // patterns per dlnL/dP partial
+    unsigned *ready;             // [nslot][ntile] epoch of the last Abar write of (slot, tile)
+    int ntile;
+    const float2 *Pdf;           // P as double-float (a tip's edge message is a row of it)
 };
 
 cudaError_t init_fast_kernels(int ns);
@@ -58,7 +92,15 @@ void launch_bwd_umma(const FastBwdArgs &a, int ns, int nitems, int ntile, cudaSt
 void launch_gradP_umma(const FastBwdArgs &a, int ns, int npair, cudaStream_t st);
 void launch_bwd_fast(const FastBwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st);
 void launch_gradP_fast(const FastBwdArgs &a, int ns, int npair, cudaStream_t st);
-void launch_pslice(const FastFwdArgs &a, int ns, int npair, cudaStream_t st);
+void launch_pslice(const FastFwdArgs &a, int ns, int npair, bool cm, cudaStream_t st);
 void launch_prune_fast(const FastFwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st);
+void launch_bump(unsigned *ctl, cudaStream_t st);
+// trace: nullable, 4 words per task (claim ns, dependencies met ns, end ns, SM)
+void launch_prune_persist(const FastFwdArgs *genes, const Task *tasks, int ntask, unsigned *ctl, int ns,
+                          int nblock, unsigned long long *trace, cudaStream_t st);
+void launch_bwd_persist(const FastBwdArgs *genes, const Task *tasks, int ntask, unsigned *ctl, int ns,
+                        int nblock, unsigned long long *trace, cudaStream_t st);
+void launch_gradP_persist(const FastBwdArgs *genes, const Task *tasks, int ntask, unsigned *ctl, int ns,
+                          int nblock, unsigned long long *trace, cudaStream_t st);
 
 }  // namespace gb

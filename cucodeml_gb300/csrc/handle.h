@@ -16,6 +16,7 @@ namespace gb {
 
 struct AdjointState;
 struct FastState;
+struct PersistPlan;
 
 int fail(int code, const std::string &msg);
 double now_ms();
@@ -116,6 +117,22 @@ int fast_record_eval(gb_handle *h, bool grad);
 int fast_prepare(gb_handle *h, bool grad);     // allocations / kernel attributes before a capture
 int fp64_prepare(gb_handle *h, bool grad);
 int fast_check_error(gb_handle *h);
+// split-precision pieces (fast.cu), each recorded on h->stream; they return
+// the number of kernels (copies: 0 or a GB_ERR_*)
+int fast_rec_copies_in(gb_handle *h, bool grad);
+int fast_rec_pmat(gb_handle *h);      // P (FP64) and its digit planes
+int fast_rec_mix(gb_handle *h);       // site-class mixture, lnL
+int fast_rec_dmat(gb_handle *h);      // dP/dt terms of the adjoint
+int fast_rec_tail(gb_handle *h);      // per-pair and class-weight gradient sums
+int fast_rec_copies_out(gb_handle *h, bool grad);
+bool fast_persistent(const gb_handle *h);
+int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);
+int fast_ns(const gb_handle *h, bool adjoint);
+// persistent executors over one or many genes (fast.cu)
+void persist_free(PersistPlan *pp);
+int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd);
+int persist_record_fwd(PersistPlan *pp, bool keepE, int ns, cudaStream_t st, gb_handle *prof);
+int persist_record_bwd(PersistPlan *pp, int nsb, cudaStream_t st, gb_handle *prof);
 // forward pass on the handle's stream (runtime.cu); keepE keeps the edge
 // messages for the adjoint
 int run_forward(gb_handle *h, const Derived *D, const double *blength, bool keepE, double *neg_lnL,

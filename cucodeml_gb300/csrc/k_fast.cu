@@ -37,13 +37,22 @@ constexpr int NC = 61;
 
 // ---------------------------------------------------------------- P slices
 
+// element (n, k) of a 64 x 64 plane in the K-major core-matrix layout of the
+// tcgen05 operands: 8 x 8 blocks of 128 contiguous bytes, block (n/8, k/8) at
+// block index 8 (n/8) + k/8
+__device__ __forceinline__ int cm_index(int n, int k) {
+    return (((n >> 3) << 3) + (k >> 3)) * 64 + (n & 7) * 8 + (k & 7);
+}
+
 // Per pair: Pdf[k][j] = Pt[k][j] as double-float, and the NS digit planes of
 //   Bf[s][j][k] = digit s of P[j][k] = Pt[k][j]   (forward:  out[h][j] = sum_k L[h][k] P[j][k])
 //   Bb[s][k][j] = digit s of Pt[k][j]            (adjoint:  out[h][k] = sum_j E[h][j] P[j][k])
+// row-major planes (cm = 0, mma.sync kernels) or core-matrix planes (cm = 1,
+// tcgen05 kernels, copied to shared memory as they are)
 template <int NS>
 __global__ void __launch_bounds__(256) pslice_kernel(const double *__restrict__ Pt, float2 *__restrict__ Pdf,
                                                      __nv_bfloat16 *__restrict__ Bf,
-                                                     __nv_bfloat16 *__restrict__ Bb) {
+                                                     __nv_bfloat16 *__restrict__ Bb, int cm) {
     const int p = blockIdx.x;
     const double *P = Pt + (size_t)p * 4096;
     float2 *D = Pdf + (size_t)p * 4096;
@@ -60,8 +69,8 @@ __global__ void __launch_bounds__(256) pslice_kernel(const double *__restrict__ 
             const int sh = 7 * (NS - 1 - s);
             const int dgt = s == 0 ? (int)(q >> sh) : (int)((q >> sh) & 127);
             const __nv_bfloat16 b = __float2bfloat16_rn((float)dgt);
-            bf[(size_t)s * 4096 + j * 64 + k] = b;
-            bb[(size_t)s * 4096 + k * 64 + j] = b;
+            bf[(size_t)s * 4096 + (cm ? cm_index(j, k) : j * 64 + k)] = b;
+            bb[(size_t)s * 4096 + (cm ? cm_index(k, j) : k * 64 + j)] = b;
         }
     }
 }
@@ -203,22 +212,23 @@ cudaError_t init_fast_kernels(int ns) {
 }
 
 template <int NS>
-static void launch_fwd_ns(const FastFwdArgs &a, int nitems, int ntile, bool slice, int npair, cudaStream_t st) {
+static void launch_fwd_ns(const FastFwdArgs &a, int nitems, int ntile, bool slice, int npair, cudaStream_t st,
+                          int cm = 0) {
     if (slice) {
         pslice_kernel<NS><<<npair, 256, 0, st>>>(a.Pt64, const_cast<float2 *>(a.Pdf),
-                                                 const_cast<__nv_bfloat16 *>(a.Bf), a.Bb);
+                                                 const_cast<__nv_bfloat16 *>(a.Bf), a.Bb, cm);
         return;
     }
     dim3 grid(ntile, nitems);
     prune_fast_kernel<NS><<<grid, 256, Smem<NS>::BYTES, st>>>(a);
 }
 
-void launch_pslice(const FastFwdArgs &a, int ns, int npair, cudaStream_t st) {
+void launch_pslice(const FastFwdArgs &a, int ns, int npair, bool cm, cudaStream_t st) {
     switch (ns) {
-        case 5: launch_fwd_ns<5>(a, 0, 0, true, npair, st); break;
-        case 6: launch_fwd_ns<6>(a, 0, 0, true, npair, st); break;
-        case 7: launch_fwd_ns<7>(a, 0, 0, true, npair, st); break;
-        case 8: launch_fwd_ns<8>(a, 0, 0, true, npair, st); break;
+        case 5: launch_fwd_ns<5>(a, 0, 0, true, npair, st, cm); break;
+        case 6: launch_fwd_ns<6>(a, 0, 0, true, npair, st, cm); break;
+        case 7: launch_fwd_ns<7>(a, 0, 0, true, npair, st, cm); break;
+        case 8: launch_fwd_ns<8>(a, 0, 0, true, npair, st, cm); break;
     }
 }
 

@@ -1,14 +1,18 @@
 // tcgen05 versions of the split-precision forward and adjoint-propagation
 // kernels (same numerics as k_fast.cu / k_fast_bwd.cu, see there).
 //
-// Per (128-pattern tile, node, class) CTA and per internal child: the SIMT
-// threads cut the child's 128 x 64 double-float tile into NS digit planes
-// (K-major core-matrix layout) and copy the NS planes of P; one thread then
-// issues, for every significance level L = 2..NS+1, the tcgen05.mma
-// (M = 128, N = 64, K = 16, bf16 x bf16 -> FP32) of every digit pair (i, j)
-// with i + j = L into that level's 64 TMEM columns (NS = 8: 8 levels = all
-// 512 columns), and commits to an mbarrier.  The level sums are exact integers
-// in FP32; each thread reads one row (TMEM lane) x 16 columns per level with
+// Per (128-pattern tile, node, class) task and per internal child: one thread
+// starts a bulk copy (cp.async.bulk, completion on an mbarrier) of the NS
+// digit planes of P, stored in global memory already in the K-major
+// core-matrix layout; meanwhile the SIMT threads cut the child's 128 x 64
+// double-float tile into NS digit planes in shared memory.  Warp 0 then
+// issues (one elected lane; descriptors computed warp-uniformly from
+// compile-time offsets), for every significance level L = 2..NS+1, the
+// tcgen05.mma (M = 128, N = 64, K = 16, bf16 x bf16 -> FP32) of every digit
+// pair (i, j) with i + j = L into that level's 64 TMEM columns (NS = 8:
+// 8 levels = all 512 columns), and commits to an mbarrier.  The level sums
+// are exact integers in FP32;
+// each thread reads one row (TMEM lane) x 16 columns per level with
 // tcgen05.ld and combines the levels in double-float.
 // 16 warps (512 threads) per CTA: warp w reads TMEM lanes 32 (w % 4) .. + 31 and
 // columns 16 (w / 4) .. + 15, so thread (w, lane) owns pattern row
@@ -34,11 +38,25 @@ constexpr int NCOL = 16;           // states per thread in the epilogues
 constexpr int A_PLANE = 128 * 64 * 2;
 constexpr int B_PLANE = 64 * 64 * 2;
 
+// misc block after the planes (struct Misc, 64 B), then the kernel's own
+// scratch, the staged argument struct and the staged work item
+constexpr int ARGS_BYTES = 256;
+constexpr int ITEM_BYTES = 128;
+static_assert(sizeof(FastFwdArgs) <= ARGS_BYTES && sizeof(FastBwdArgs) <= ARGS_BYTES, "argument staging");
+static_assert(sizeof(Item) <= ITEM_BYTES && sizeof(BItem) <= ITEM_BYTES, "item staging");
+// at most one CTA per SM, so that a CTA's 512-column TMEM allocation never waits
+constexpr int MIN_SMEM = 120 * 1024;
+
 template <int NS>
 struct USm {
     static constexpr int OFF_B = NS * A_PLANE;
     static constexpr int OFF_MISC = OFF_B + NS * B_PLANE;
-    static constexpr int BYTES = OFF_MISC + 16 + 2048 + 4096;   // mbar, tmem slot, row max [4][128], row sums [4][128]
+    static constexpr int OFF_RMAX = OFF_MISC + 64;            // float [4][128]
+    static constexpr int OFF_RSUM = OFF_RMAX + 2048;          // double [4][128]
+    static constexpr int OFF_ARGS = OFF_RSUM + 4096;
+    static constexpr int OFF_ITEM = OFF_ARGS + ARGS_BYTES;
+    static constexpr int NEED = OFF_ITEM + ITEM_BYTES;
+    static constexpr int BYTES = NEED > MIN_SMEM ? NEED : MIN_SMEM;
 };
 
 // dlnL/dP kernel: A planes of 128 rows (rows 64..127 stay zero), B planes of 64 rows
@@ -47,103 +65,182 @@ struct GSm {
     static constexpr int OFF_B = NB * A_PLANE;
     static constexpr int PLANES = NB * (A_PLANE + B_PLANE);
     static constexpr int OFF_MISC = PLANES > 4 * 4096 * 8 ? PLANES : 4 * 4096 * 8;   // also holds the tip partials
-    static constexpr int BYTES = OFF_MISC + 16 + 256 + 64 * 4;  // mbar, tmem slot, exponents, reductions
+    static constexpr int OFF_XS = OFF_MISC + 64;              // int [64] exponents
+    static constexpr int OFF_RED = OFF_XS + 256;              // int [16] reductions
+    static constexpr int OFF_ARGS = OFF_RED + 64;
+    static constexpr int NEED = OFF_ARGS + ARGS_BYTES;
+    static constexpr int BYTES = NEED > MIN_SMEM ? NEED : MIN_SMEM;
 };
+
+struct Misc {
+    uint64_t mbar;          // MMA completion
+    uint64_t mbar_b;        // bulk copy of the P planes
+    uint32_t tmem;
+    int task;
+    int okb;                // the P planes arrived (set by the issuing thread)
+};
+static_assert(sizeof(Misc) <= 64, "misc block");
+
+// cooperative copy of a 4-byte-granular struct into shared memory
+template <class T>
+__device__ __forceinline__ void stage(T *dst, const T *src) {
+    static_assert(sizeof(T) % 4 == 0, "staging granularity");
+    for (int i = threadIdx.x; i < (int)(sizeof(T) / 4); i += blockDim.x)
+        reinterpret_cast<int *>(dst)[i] = reinterpret_cast<const int *>(src)[i];
+}
+
+// ---------------------------------------------------------------- cross-CTA flags
+
+// Wait until *flag == epoch (acquire).  Bounded: gives up after 2 s, or at
+// once when *err is set by another CTA.
+__device__ __forceinline__ bool wait_flag(const unsigned *flag, unsigned epoch, const int *err) {
+    const uint64_t t0 = umma::global_ns();
+    for (int i = 0; i < (1 << 26); i++) {
+        unsigned v;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(flag) : "memory");
+        if (v == epoch) return true;
+        if (*reinterpret_cast<const volatile int *>(err)) return false;
+        if (umma::global_ns() - t0 > 2000000000ull) return false;
+        __nanosleep(100);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void set_flag(unsigned *flag, unsigned epoch) {
+    __threadfence();
+    asm volatile("st.release.gpu.global.u32 [%0], %1;\n" ::"l"(flag), "r"(epoch) : "memory");
+}
+
+__device__ __forceinline__ unsigned smid() {
+    unsigned s;
+    asm volatile("mov.u32 %0, %%smid;\n" : "=r"(s));
+    return s;
+}
+
+// optional task trace: per task (claim time, dependencies met, end time, SM)
+__device__ __forceinline__ void trace_put(unsigned long long *trace, int idx, int slot, unsigned long long v) {
+    if (trace && threadIdx.x == 0) trace[(size_t)idx * 4 + slot] = v;
+}
+
+// claim the next task index (block-uniform)
+__device__ __forceinline__ int claim(unsigned *counter, Misc *m) {
+    if (threadIdx.x == 0) m->task = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    return m->task;
+}
 
 template <int NS>
 __device__ __forceinline__ void slice_A_cm(const float2 *__restrict__ src, unsigned char *A) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = lane >> 2, kp = lane & 3;
-#pragma unroll 2
-    for (int q = 0; q < 8; q++) {
+    float4 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {                        // all loads in flight first
         const int cmi = warp * 8 + q;                    // core matrix: row group cmi/8, k group cmi%8
         const int row = (cmi >> 3) * 8 + rr, k = (cmi & 7) * 8 + 2 * kp;
-        const float4 v = *reinterpret_cast<const float4 *>(src + (size_t)row * 64 + k);
+        v[q] = __ldcg(reinterpret_cast<const float4 *>(src + (size_t)row * 64 + k));
+    }
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+        const int cmi = warp * 8 + q;
         int d0[NS], d1[NS];
-        digits_of<NS>(v.x, v.y, d0);
-        digits_of<NS>(v.z, v.w, d1);
+        digits_of<NS>(v[q].x, v[q].y, d0);
+        digits_of<NS>(v[q].z, v[q].w, d1);
         const int off = cmi * 128 + rr * 16 + kp * 4;
 #pragma unroll
         for (int s = 0; s < NS; s++) *reinterpret_cast<unsigned *>(A + s * A_PLANE + off) = bf16_pair(d0[s], d1[s]);
     }
 }
 
-// the first NS digit planes of P from global [planes][64][64] (row-major) into core matrices
+// thread 0: bulk copy of the first NS digit planes of P (global, core-matrix
+// layout, 8 KB per plane) into shared memory, completing on m->mbar_b
 template <int NS>
-__device__ __forceinline__ void load_B_cm(const __nv_bfloat16 *__restrict__ B, unsigned char *Bs) {
-    for (int c = threadIdx.x; c < NS * 512; c += blockDim.x) {
-        const int s = c >> 9, rem = c & 511, n = rem >> 3, kg = rem & 7;
-        const uint4 v = *reinterpret_cast<const uint4 *>(B + (size_t)s * 4096 + n * 64 + kg * 8);
-        *reinterpret_cast<uint4 *>(Bs + s * B_PLANE + ((n >> 3) * 8 + kg) * 128 + (n & 7) * 16) = v;
+__device__ __forceinline__ void start_B(const __nv_bfloat16 *__restrict__ B, unsigned char *Bs, uint64_t *mbar_b) {
+    if (threadIdx.x == 0) {
+        umma::mbar_expect_tx(mbar_b, NS * B_PLANE);
+#pragma unroll
+        for (int s = 0; s < NS; s++) umma::bulk_g2s(Bs + s * B_PLANE, B + (size_t)s * 4096, B_PLANE, mbar_b);
     }
 }
 
-// b_top_only: B has a single non-zero digit plane (the first), so only the
-// pairs (i, 1) are issued
+// All MMAs of a contraction, issued by the calling warp (all lanes; the
+// instruction executes in the leader lane): level L = 2..NS+1 accumulates the
+// pairs (i, L - i) over K = 64 (4 steps of 16) into TMEM columns 64 (L - 2).
+// Shared-memory descriptor start addresses are in 16-byte units in the low
+// 14 bits, so plane and K-step offsets are added to the base descriptors.
 template <int NS>
-__device__ __forceinline__ void issue_levels(uint32_t tmem, uint32_t a_base, uint32_t b_base,
-                                             bool b_top_only = false) {
+__device__ __forceinline__ void issue_levels(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t leader) {
     constexpr uint32_t idesc = umma::make_idesc(128, 64);
-#pragma unroll 1
+#pragma unroll
     for (int L = 2; L <= NS + 1; L++) {
-        uint32_t acc = 0;
-        const int ilo = L - NS > 1 ? L - NS : 1, ihi = L - 1 < NS ? L - 1 : NS;
-#pragma unroll 1
-        for (int i = ilo; i <= ihi; i++) {
+        const int ilo = L - NS > 1 ? L - NS : 1;
+#pragma unroll
+        for (int i = 1; i <= NS; i++) {
             const int j = L - i;
-            if (b_top_only && j != 1) continue;
+            if (i < ilo || j < 1) continue;
 #pragma unroll
             for (int ks = 0; ks < 4; ks++) {
-                const uint64_t ad = umma::make_desc(a_base + (i - 1) * A_PLANE + ks * 256);
-                const uint64_t bd = umma::make_desc(b_base + (j - 1) * B_PLANE + ks * 256);
-                umma::mma_bf16(tmem + (L - 2) * 64, ad, bd, idesc, acc);
-                acc = 1;
+                const uint64_t ad = adesc + (uint64_t)(((i - 1) * A_PLANE + ks * 256) >> 4);
+                const uint64_t bd = bdesc + (uint64_t)(((j - 1) * B_PLANE + ks * 256) >> 4);
+                umma::mma_bf16_leader(tmem + (L - 2) * 64, ad, bd, idesc, (i == ilo && ks == 0) ? 0u : 1u, leader);
             }
         }
     }
 }
 
-// All threads: the planes in shared memory are complete (generic-proxy
-// stores).  Issue, wait (bounded), read the levels.  Returns a block-uniform
+// All threads: the A planes in shared memory are complete (generic-proxy
+// stores); the B planes are complete or, with wait_b, arriving by bulk copy.
+// Warp 0 issues the MMAs and commits; every thread waits (bounded) and reads
+// its row's 16 columns of every level, accumulating
+//   C = (init ? 0 : C 2^sc_in) + 2^sc_new sum_L S_L 2^(-7L)
+// in double-float (exact power-of-two scalings).  Returns a block-uniform
 // success flag.
 template <int NS>
-__device__ __forceinline__ bool contract(unsigned char *sm, uint32_t tmem, uint64_t *mbar, uint32_t &phase,
-                                         float2 (&C)[NCOL], int off_b = USm<NS>::OFF_B, bool b_top_only = false) {
+__device__ __forceinline__ bool contract(unsigned char *sm, Misc *m, uint32_t &phase, float2 (&C)[NCOL],
+                                         int off_b, bool wait_b, bool init = true, int sc_in = 0,
+                                         int sc_new = 0) {
     umma::fence_proxy_async();
     umma::fence_before();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    const int warp = threadIdx.x >> 5;
+    if (warp == 0) {
         umma::fence_after();
-        issue_levels<NS>(tmem, umma::smem_u32(sm), umma::smem_u32(sm + off_b), b_top_only);
-        umma::commit(mbar);
+        const bool okb = !wait_b || umma::mbar_wait(&m->mbar_b, phase);
+        const uint32_t leader = umma::elect_one();
+        if (okb)
+            issue_levels<NS>(m->tmem, umma::make_desc(umma::smem_u32(sm)), umma::make_desc(umma::smem_u32(sm + off_b)),
+                             leader);
+        if (leader) {
+            umma::commit(&m->mbar);
+            m->okb = okb;
+        }
     }
-    bool ok = umma::mbar_wait(mbar, phase);
-    phase ^= 1u;
-    ok = __syncthreads_and(ok);
+    const int col = NCOL * (warp >> 2);
+    bool ok = umma::mbar_wait(&m->mbar, phase);
     umma::fence_after();
     if (ok) {
-        const int warp = threadIdx.x >> 5;
         const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-        const int col = NCOL * (warp >> 2);
 #pragma unroll
-        for (int c = 0; c < NCOL; c++) C[c] = make_float2(0.f, 0.f);
+        for (int c = 0; c < NCOL; c++) C[c] = init ? make_float2(0.f, 0.f) : df_scale(C[c], sc_in);
 #pragma unroll 1
         for (int L = NS + 1; L >= 2; L--) {
             float v[NCOL];
-            umma::tmem_ld16(tmem + lane_base + (L - 2) * 64 + col, v);
-            const float w = scalbnf(1.0f, -7 * L);
+            umma::tmem_ld16(m->tmem + lane_base + (L - 2) * 64 + col, v);
+            const float w = scalbnf(1.0f, -7 * L + sc_new);
 #pragma unroll
             for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(v[c] * w, 0.f));
         }
     }
+    phase ^= 1u;
     umma::fence_before();
+    ok = __syncthreads_and(ok) && m->okb;
     return ok;
 }
 
 __device__ __forceinline__ void load_row32(const float2 *p, float2 (&v)[NCOL]) {
 #pragma unroll
     for (int c = 0; c < NCOL / 2; c++) {
-        const float4 x = reinterpret_cast<const float4 *>(p)[c];
+        const float4 x = __ldcg(reinterpret_cast<const float4 *>(p) + c);
         v[2 * c] = make_float2(x.x, x.y);
         v[2 * c + 1] = make_float2(x.z, x.w);
     }
@@ -168,34 +265,50 @@ __device__ __forceinline__ float row_max(const float2 (&v)[NCOL], int col0, floa
     return m;
 }
 
+// ---------------------------------------------------------------- forward
+
+__device__ __forceinline__ void tmem_setup(Misc *m) {
+    if ((threadIdx.x >> 5) == 0) {
+        umma::tmem_alloc(&m->tmem, 512);
+        umma::tmem_relinquish();
+    }
+    if (threadIdx.x == 0) {
+        umma::mbar_init(&m->mbar, 1);
+        umma::mbar_init(&m->mbar_b, 1);
+    }
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+}
+
+__device__ __forceinline__ void tmem_teardown(Misc *m) {
+    umma::fence_before();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0) umma::tmem_dealloc(m->tmem, 512);
+}
+
+// after a failed wait: flag the error and let in-flight MMAs (and, with
+// drain_b, the last bulk copy) drain, each wait bounded
+__device__ __forceinline__ void on_failure(int *err, Misc *m, uint32_t phase, bool drain_b) {
+    if (threadIdx.x == 0) {
+        atomicExch(err, 1);
+        umma::mbar_wait(&m->mbar, phase ^ 1u, 1000000000ull);
+        if (drain_b) umma::mbar_wait(&m->mbar_b, phase ^ 1u, 1000000000ull);
+    }
+}
+
+// One (node, class) item on one 128-pattern tile.  Needs TMEM when the item
+// has an internal child.  Returns the block-uniform success flag.
 template <int NS>
-__global__ void __launch_bounds__(NT, 1) prune_umma_kernel(FastFwdArgs a) {
-    extern __shared__ __align__(1024) unsigned char sm[];
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + USm<NS>::OFF_MISC);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + USm<NS>::OFF_MISC + 8);
-    float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_MISC + 16);
-    double *rsum = reinterpret_cast<double *>(sm + USm<NS>::OFF_MISC + 16 + 2048);
-    const Item it = a.items[blockIdx.y];
+__device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsigned char *sm, Misc *m,
+                           uint32_t &phase) {
+    float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_RMAX);
+    double *rsum = reinterpret_cast<double *>(sm + USm<NS>::OFF_RSUM);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = warp >> 2;
     const int row = 32 * (warp & 3) + lane, c0 = NCOL * ch;
     const size_t npad = a.npad;
-    const size_t h0 = (size_t)blockIdx.x * 128, h = h0 + row;
-
-    bool internal = false;
-    for (int ci = 0; ci < it.nchild; ci++) internal |= it.cslot[ci] >= 0;
-    if (internal) {
-        if (warp == 0) {
-            umma::tmem_alloc(tslot, 512);
-            umma::tmem_relinquish();
-        }
-        if (threadIdx.x == 0) umma::mbar_init(mbar, 1);
-        umma::fence_before();
-        __syncthreads();
-        umma::fence_after();
-    }
-    const uint32_t tmem = internal ? *tslot : 0u;
-    uint32_t phase = 0;
+    const size_t h0 = (size_t)tile * 128, h = h0 + row;
     bool ok = true;
     float2 prod[NCOL];
     int expo = 0;
@@ -206,81 +319,124 @@ __global__ void __launch_bounds__(NT, 1) prune_umma_kernel(FastFwdArgs a) {
             const int zc = a.z[(size_t)it.child[ci] * npad + h];
             load_row32(a.Pdf + (size_t)it.pidx[ci] * 4096 + zc * 64 + c0, E);
         } else {
-            __syncthreads();
+            __syncthreads();                               // the previous contraction's planes are free
+            start_B<NS>(a.Bf + (size_t)it.pidx[ci] * NS * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
             slice_A_cm<NS>(a.conP + ((size_t)cs * npad + h0) * 64, sm);
-            load_B_cm<NS>(a.Bf + (size_t)it.pidx[ci] * NS * 4096, sm + USm<NS>::OFF_B);
-            ok = contract<NS>(sm, tmem, mbar, phase, E);
+            ok = contract<NS>(sm, m, phase, E, USm<NS>::OFF_B, true);
             if (!ok) break;
-            expo += a.expo[(size_t)cs * npad + h];
+            expo += __ldcg(a.expo + (size_t)cs * npad + h);
         }
-        if (a.E) store_row32(a.E + ((size_t)(it.eslot + ci) * npad + h) * 64 + c0, E);
+        // edge messages of internal children are kept for the adjoint; a tip's
+        // message is a row of P, gathered again there
+        if (a.E && cs >= 0) store_row32(a.E + ((size_t)(it.eslot + ci) * npad + h) * 64 + c0, E);
 #pragma unroll
         for (int c = 0; c < NCOL; c++) prod[c] = ci == 0 ? E[c] : df_mul(prod[c], E[c]);
     }
-    if (ok) {
-        const float m = row_max(prod, c0, rmax, row, ch);
-        const int sh = m > 0.f ? ilogbf(m) + 1 : 0;
-        expo += sh;
-#pragma unroll
-        for (int c = 0; c < NCOL; c++) prod[c] = df_scale(prod[c], -sh);
-        if (!it.is_root) {
-            store_row32(a.conP + ((size_t)it.slot * npad + h) * 64 + c0, prod);
-            if (ch == 0) a.expo[(size_t)it.slot * npad + h] = expo;
-        } else {
-            double f = 0.0;
-#pragma unroll
-            for (int c = 0; c < NCOL; c++)
-                if (c0 + c < NC) f = fma(a.pi[c0 + c], (double)prod[c].x + (double)prod[c].y, f);
-            rsum[ch * 128 + row] = f;
-            __syncthreads();
-            if (ch == 0) {
-                f = (rsum[row] + rsum[128 + row]) + (rsum[256 + row] + rsum[384 + row]);
-                if (f <= 0.0) f = 1e-300;
-                const double sl = (double)expo * 0.69314718055994530942;
-                a.fbar[(size_t)it.cls * npad + h] = f;
-                a.ssum[(size_t)it.cls * npad + h] = sl;
-                a.fhK[(size_t)it.cls * npad + h] = log(f) + sl;
-                a.expo_root[(size_t)it.cls * npad + h] = expo;
-            }
-        }
-    } else if (threadIdx.x == 0) {
-        atomicExch(a.err, 1);
-        umma::mbar_wait(mbar, phase ^ 1u, 1000000000ull);   // let in-flight MMAs drain (bounded)
+    if (!ok) {
+        on_failure(a.err, m, phase, true);
+        return false;
     }
-    if (internal) {
-        umma::fence_before();
+    const float mx = row_max(prod, c0, rmax, row, ch);
+    const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
+    expo += sh;
+#pragma unroll
+    for (int c = 0; c < NCOL; c++) prod[c] = df_scale(prod[c], -sh);
+    if (!it.is_root) {
+        store_row32(a.conP + ((size_t)it.slot * npad + h) * 64 + c0, prod);
+        if (ch == 0) a.expo[(size_t)it.slot * npad + h] = expo;
+    } else {
+        double f = 0.0;
+#pragma unroll
+        for (int c = 0; c < NCOL; c++)
+            if (c0 + c < NC) f = fma(a.pi[c0 + c], (double)prod[c].x + (double)prod[c].y, f);
+        rsum[ch * 128 + row] = f;
         __syncthreads();
-        if (warp == 0) umma::tmem_dealloc(tmem, 512);
+        if (ch == 0) {
+            f = (rsum[row] + rsum[128 + row]) + (rsum[256 + row] + rsum[384 + row]);
+            if (f <= 0.0) f = 1e-300;
+            const double sl = (double)expo * 0.69314718055994530942;
+            a.fbar[(size_t)it.cls * npad + h] = f;
+            a.ssum[(size_t)it.cls * npad + h] = sl;
+            a.fhK[(size_t)it.cls * npad + h] = log(f) + sl;
+            a.expo_root[(size_t)it.cls * npad + h] = expo;
+        }
     }
+    return true;
 }
 
+// one launch per level: blockIdx.y = item of the level, blockIdx.x = tile
 template <int NS>
-__global__ void __launch_bounds__(NT, 1) bwd_umma_kernel(FastBwdArgs a) {
+__global__ void __launch_bounds__(NT, 1) prune_umma_kernel(FastFwdArgs args) {
     extern __shared__ __align__(1024) unsigned char sm[];
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + USm<NS>::OFF_MISC);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + USm<NS>::OFF_MISC + 8);
-    float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_MISC + 16);
-    const BItem it = a.bitems[blockIdx.y];
+    Misc *m = reinterpret_cast<Misc *>(sm + USm<NS>::OFF_MISC);
+    FastFwdArgs *a = reinterpret_cast<FastFwdArgs *>(sm + USm<NS>::OFF_ARGS);
+    Item *it = reinterpret_cast<Item *>(sm + USm<NS>::OFF_ITEM);
+    stage(a, &args);
+    stage(it, args.items + blockIdx.y);
+    __syncthreads();
+    bool internal = false;
+    for (int ci = 0; ci < it->nchild; ci++) internal |= it->cslot[ci] >= 0;
+    if (internal) tmem_setup(m);
+    uint32_t phase = 0;
+    prune_tile<NS>(*a, *it, blockIdx.x, sm, m, phase);
+    if (internal) tmem_teardown(m);
+}
+
+// Persistent forward over a task list (gene, item, tile) in dependency order
+// (children before parents).  Each CTA claims tasks from an atomic counter;
+// before a task it waits (bounded) for the ready flags of its internal
+// children's (slot, tile), and after it publishes its own.  Every dependency
+// of a claimed task was claimed earlier by a running CTA, so the waits end.
+template <int NS>
+__global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs *__restrict__ genes,
+                                                              const Task *__restrict__ tasks, int ntask,
+                                                              unsigned *ctl, unsigned long long *trace) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    Misc *m = reinterpret_cast<Misc *>(sm + USm<NS>::OFF_MISC);
+    FastFwdArgs *a = reinterpret_cast<FastFwdArgs *>(sm + USm<NS>::OFF_ARGS);
+    Item *it = reinterpret_cast<Item *>(sm + USm<NS>::OFF_ITEM);
+    const unsigned epoch = ctl[CTL_EPOCH];
+    tmem_setup(m);
+    uint32_t phase = 0;
+    for (;;) {
+        const int idx = claim(ctl + CTL_FWD, m);
+        if (idx >= ntask) break;
+        trace_put(trace, idx, 0, umma::global_ns());
+        const Task t = tasks[idx];
+        stage(a, genes + t.gene);
+        __syncthreads();
+        stage(it, a->items + t.item);
+        __syncthreads();
+        int good = 1;
+        if (threadIdx.x == 0)
+            for (int ci = 0; ci < it->nchild && good; ci++)
+                if (it->cslot[ci] >= 0)
+                    good = wait_flag(a->ready + (size_t)it->cslot[ci] * a->ntile + t.tile, epoch, a->err);
+        if (!__syncthreads_and(good)) {
+            if (threadIdx.x == 0) atomicExch(a->err, 1);
+            break;
+        }
+        trace_put(trace, idx, 1, umma::global_ns());
+        if (!prune_tile<NS>(*a, *it, t.tile, sm, m, phase)) break;
+        __syncthreads();                                   // the tile's rows are written
+        trace_put(trace, idx, 2, umma::global_ns());
+        trace_put(trace, idx, 3, smid());
+        if (threadIdx.x == 0 && !it->is_root) set_flag(a->ready + (size_t)it->slot * a->ntile + t.tile, epoch);
+    }
+    tmem_teardown(m);
+}
+
+// ---------------------------------------------------------------- adjoint propagation
+
+template <int NS>
+__device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsigned char *sm, Misc *m,
+                         uint32_t &phase) {
+    float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_RMAX);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = warp >> 2;
     const int row = 32 * (warp & 3) + lane, c0 = NCOL * ch;
     const size_t npad = a.npad;
-    const size_t h0 = (size_t)blockIdx.x * 128, h = h0 + row;
-
-    bool internal = false;
-    for (int i = 0; i < it.nchild; i++) internal |= it.tslot[i][0] >= 0;
-    if (internal) {
-        if (warp == 0) {
-            umma::tmem_alloc(tslot, 512);
-            umma::tmem_relinquish();
-        }
-        if (threadIdx.x == 0) umma::mbar_init(mbar, 1);
-        umma::fence_before();
-        __syncthreads();
-        umma::fence_after();
-    }
-    const uint32_t tmem = internal ? *tslot : 0u;
-    uint32_t phase = 0;
+    const size_t h0 = (size_t)tile * 128, h = h0 + row;
     bool ok = true;
 
     int eAs[2] = {0, 0};   // exponent of A_a 2^{-sh_a} per class for this row
@@ -309,23 +465,28 @@ __global__ void __launch_bounds__(NT, 1) bwd_umma_kernel(FastBwdArgs a) {
                 eX = eAs[k];
             } else {
                 load_row32(a.Abar + ((size_t)it.pslot[k] * npad + h) * 64 + c0, X);
-                const int ea = a.aexp[(size_t)it.pslot[k] * npad + h];
+                const int ea = __ldcg(a.aexp + (size_t)it.pslot[k] * npad + h);
                 eX = ea == ZERO_EXP ? ZERO_EXP : ea + eAs[k];
             }
             for (int i2 = 0; i2 < it.nchild; i2++) {
                 if (i2 == i) continue;
                 float2 Ev[NCOL];
-                load_row32(a.E + ((size_t)(it.pslot[k] * MAXC + i2) * npad + h) * 64 + c0, Ev);
+                if (it.tslot[i2][k] < 0) {
+                    const int zc = a.z[(size_t)it.child[i2] * npad + h];
+                    load_row32(a.Pdf + (size_t)it.pidx[i2][k] * 4096 + zc * 64 + c0, Ev);
+                } else {
+                    load_row32(a.E + ((size_t)(it.pslot[k] * MAXC + i2) * npad + h) * 64 + c0, Ev);
+                }
 #pragma unroll
                 for (int q = 0; q < NCOL; q++) X[q] = df_mul(X[q], Ev[q]);
             }
-            const float m = row_max(X, c0, rmax, row, ch);
-            const int sh = m > 0.f ? ilogbf(m) + 1 : 0;
+            const float mx = row_max(X, c0, rmax, row, ch);
+            const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
 #pragma unroll
             for (int q = 0; q < NCOL; q++) X[q] = df_scale(X[q], -sh);
             const size_t eb = (size_t)(it.pslot[k] * MAXC + i);
             store_row32(a.Ebar + (eb * npad + h) * 64 + c0, X);
-            if (ch == 0) a.ebexp[eb * npad + h] = (!(m > 0.f) || eX == ZERO_EXP) ? ZERO_EXP : eX + sh;
+            if (ch == 0) a.ebexp[eb * npad + h] = (!(mx > 0.f) || eX == ZERO_EXP) ? ZERO_EXP : eX + sh;
         }
         if (it.tslot[i][0] < 0) continue;
         const bool shared = it.ncls == 1 || it.tslot[i][0] == it.tslot[i][1];
@@ -337,63 +498,119 @@ __global__ void __launch_bounds__(NT, 1) bwd_umma_kernel(FastBwdArgs a) {
             for (int k = kbeg; k < kend; k++) {
                 const size_t eb = (size_t)(it.pslot[k] * MAXC + i);
                 __syncthreads();        // this tile's Ebar rows are written and visible
+                start_B<NS>(a.Bb + (size_t)it.pidx[i][k] * a.nsP * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
                 slice_A_cm<NS>(a.Ebar + (eb * npad + h0) * 64, sm);
-                load_B_cm<NS>(a.Bb + (size_t)it.pidx[i][k] * a.nsP * 4096, sm + USm<NS>::OFF_B);
-                float2 C[NCOL];
-                ok = contract<NS>(sm, tmem, mbar, phase, C);
-                if (!ok) break;
                 const int eC = a.ebexp[eb * npad + h];
                 if (k == kbeg) {
-#pragma unroll
-                    for (int q = 0; q < NCOL; q++) acc[q] = C[q];
+                    ok = contract<NS>(sm, m, phase, acc, USm<NS>::OFF_B, true);
                     eacc = eC;
-                } else {
+                } else {                                   // acc 2^eacc + C 2^eC on the larger exponent
                     const int e = max(eacc, eC);
-                    const int da = max(eacc - e, -1000), dc = max(eC - e, -1000);
-#pragma unroll
-                    for (int q = 0; q < NCOL; q++) acc[q] = df_add(df_scale(acc[q], da), df_scale(C[q], dc));
+                    ok = contract<NS>(sm, m, phase, acc, USm<NS>::OFF_B, true, false, max(eacc - e, -1000),
+                                      max(eC - e, -1000));
                     eacc = e;
                 }
+                if (!ok) break;
             }
             if (!ok) break;
-            const float m = row_max(acc, c0, rmax, row, ch);
-            const int sh = m > 0.f ? ilogbf(m) + 1 : 0;
+            const float mx = row_max(acc, c0, rmax, row, ch);
+            const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
 #pragma unroll
             for (int q = 0; q < NCOL; q++) acc[q] = df_scale(acc[q], -sh);
             const int ts = it.tslot[i][tg];
             store_row32(a.Abar + ((size_t)ts * npad + h) * 64 + c0, acc);
-            if (ch == 0) a.aexp[(size_t)ts * npad + h] = (!(m > 0.f) || eacc == ZERO_EXP) ? ZERO_EXP : eacc + sh;
+            if (ch == 0) a.aexp[(size_t)ts * npad + h] = (!(mx > 0.f) || eacc == ZERO_EXP) ? ZERO_EXP : eacc + sh;
         }
     }
-    if (!ok && threadIdx.x == 0) {
-        atomicExch(a.err, 1);
-        umma::mbar_wait(mbar, phase ^ 1u, 1000000000ull);   // let in-flight MMAs drain (bounded)
+    if (!ok) {
+        on_failure(a.err, m, phase, true);
+        return false;
     }
-    if (internal) {
-        umma::fence_before();
-        __syncthreads();
-        if (warp == 0) umma::tmem_dealloc(tmem, 512);
-    }
+    return true;
 }
 
+template <int NS>
+__global__ void __launch_bounds__(NT, 1) bwd_umma_kernel(FastBwdArgs args) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    Misc *m = reinterpret_cast<Misc *>(sm + USm<NS>::OFF_MISC);
+    FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + USm<NS>::OFF_ARGS);
+    BItem *it = reinterpret_cast<BItem *>(sm + USm<NS>::OFF_ITEM);
+    stage(a, &args);
+    stage(it, args.bitems + blockIdx.y);
+    __syncthreads();
+    bool internal = false;
+    for (int i = 0; i < it->nchild; i++) internal |= it->tslot[i][0] >= 0;
+    if (internal) tmem_setup(m);
+    uint32_t phase = 0;
+    bwd_tile<NS>(*a, *it, blockIdx.x, sm, m, phase);
+    if (internal) tmem_teardown(m);
+}
+
+// Persistent adjoint propagation over (gene, backward item, tile) tasks in
+// root-first order: a task waits for the upper partials (Abar) of its own
+// slots, published by its parent's task, and publishes its children's.
+template <int NS>
+__global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *__restrict__ genes,
+                                                            const Task *__restrict__ tasks, int ntask,
+                                                            unsigned *ctl, unsigned long long *trace) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    Misc *m = reinterpret_cast<Misc *>(sm + USm<NS>::OFF_MISC);
+    FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + USm<NS>::OFF_ARGS);
+    BItem *it = reinterpret_cast<BItem *>(sm + USm<NS>::OFF_ITEM);
+    const unsigned epoch = ctl[CTL_EPOCH];
+    tmem_setup(m);
+    uint32_t phase = 0;
+    for (;;) {
+        const int idx = claim(ctl + CTL_BWD, m);
+        if (idx >= ntask) break;
+        trace_put(trace, idx, 0, umma::global_ns());
+        const Task t = tasks[idx];
+        stage(a, genes + t.gene);
+        __syncthreads();
+        stage(it, a->bitems + t.item);
+        __syncthreads();
+        int good = 1;
+        if (threadIdx.x == 0 && !it->is_root)
+            for (int k = 0; k < it->ncls && good; k++)
+                good = wait_flag(a->ready + (size_t)it->pslot[k] * a->ntile + t.tile, epoch, a->err);
+        if (!__syncthreads_and(good)) {
+            if (threadIdx.x == 0) atomicExch(a->err, 1);
+            break;
+        }
+        trace_put(trace, idx, 1, umma::global_ns());
+        if (!bwd_tile<NS>(*a, *it, t.tile, sm, m, phase)) break;
+        __syncthreads();
+        trace_put(trace, idx, 2, umma::global_ns());
+        trace_put(trace, idx, 3, smid());
+        // publish the children's slots that received an upper partial; the
+        // staged item and arguments are not rewritten before the next claim's
+        // barrier, which thread 0 reaches only after this
+        if (threadIdx.x == 0)
+            for (int i = 0; i < it->nchild; i++) {
+                if (it->tslot[i][0] < 0) continue;
+                set_flag(a->ready + (size_t)it->tslot[i][0] * a->ntile + t.tile, epoch);
+                if (it->ncls == 2 && it->tslot[i][1] != it->tslot[i][0])
+                    set_flag(a->ready + (size_t)it->tslot[i][1] * a->ntile + t.tile, epoch);
+            }
+    }
+    tmem_teardown(m);
+}
+
+// ---------------------------------------------------------------- dlnL/dP
 
 // Partial dlnL/dP of one (branch, omega) pair over a chunk of patterns (see
 // k_fast_bwd.cu for the sums).  Per 64-pattern sub-chunk: A[j][h] =
-// Ebar[h][j] 2^{x_h - xmax} and B[k][h] = L~[h][k] (a tip: one-hot at the
-// pattern's codon, whose only non-zero digit plane is the first) as digit
-// planes with K = patterns; tcgen05 with M = 128 of which rows 64..127 are
-// zero; the exact level sums are combined in double-float against a
-// reference exponent xr (the chunk's largest), with no FP64 arithmetic until
-// the final write.  Threads of TMEM lanes 0..63 (warps w with w % 4 < 2) own
-// output rows j, 16 columns each.
+// Ebar[h][j] 2^{x_h - xmax} and B[k][h] = L~[h][k] as digit planes with
+// K = patterns; tcgen05 with M = 128 of which rows 64..127 are zero; the
+// exact level sums are combined in double-float against a reference exponent
+// xr (the chunk's largest), with no FP64 arithmetic until the final write.
+// Children that are tips (one-hot rows) are summed by a segmented scatter in
+// shared memory instead.  Threads of TMEM lanes 0..63 (warps w with
+// w % 4 < 2) own output rows j, 16 columns each.
 template <int NB>
-__global__ void __launch_bounds__(NT, 1) gradP_umma_kernel(FastBwdArgs a) {
-    extern __shared__ __align__(1024) unsigned char sm[];
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + GSm<NB>::OFF_MISC);
-    uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + GSm<NB>::OFF_MISC + 8);
-    int *xs = reinterpret_cast<int *>(sm + GSm<NB>::OFF_MISC + 16);          // [64]
-    int *red = reinterpret_cast<int *>(sm + GSm<NB>::OFF_MISC + 16 + 256);   // [2]
-    const int p = blockIdx.x, chunk = blockIdx.y;
+__device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char *sm, Misc *m, uint32_t &phase) {
+    int *xs = reinterpret_cast<int *>(sm + GSm<NB>::OFF_XS);
+    int *red = reinterpret_cast<int *>(sm + GSm<NB>::OFF_RED);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int row = 32 * (warp & 3) + lane, c0 = NCOL * (warp >> 2);
     const size_t npad = a.npad;
@@ -414,23 +631,13 @@ __global__ void __launch_bounds__(NT, 1) gradP_umma_kernel(FastBwdArgs a) {
     double *out = a.Gpart + ((size_t)p * a.nchunk + chunk) * 64 * 64;
     if (xr == ZERO_EXP) {
         for (int i = tid; i < 4096; i += NT) out[i] = 0.0;
-        return;
+        return true;
     }
-    if (warp == 0) {
-        umma::tmem_alloc(tslot, 512);
-        umma::tmem_relinquish();
-    }
-    if (tid == 0) umma::mbar_init(mbar, 1);
-    // A rows 64..127 of every plane stay zero
+    // A rows 64..127 of every plane are zero (the tip partials below overwrite them)
     for (int i = tid; i < NB * (A_PLANE / 2) / 16; i += NT) {
         const int s = i / (A_PLANE / 2 / 16), r = i % (A_PLANE / 2 / 16);
         reinterpret_cast<uint4 *>(sm + s * A_PLANE + A_PLANE / 2)[r] = make_uint4(0, 0, 0, 0);
     }
-    umma::fence_before();
-    __syncthreads();
-    umma::fence_after();
-    const uint32_t tmem = *tslot;
-    uint32_t phase = 0;
     bool ok = true;
     float2 acc[NCOL];
 #pragma unroll
@@ -439,8 +646,7 @@ __global__ void __launch_bounds__(NT, 1) gradP_umma_kernel(FastBwdArgs a) {
     bool any_tip = false;
     for (int ci = cbeg; ci < cend && ok; ci++) {
         const Contrib cb = a.contrib[ci];
-        const bool tip = cb.tslot < 0;
-        if (tip) {          // one-hot children: segmented scatter below, no digit planes
+        if (cb.tslot < 0) {          // one-hot children: segmented scatter below, no digit planes
             any_tip = true;
             continue;
         }
@@ -454,40 +660,41 @@ __global__ void __launch_bounds__(NT, 1) gradP_umma_kernel(FastBwdArgs a) {
             __syncthreads();
             const int xmax = red[1];
             if (xmax == ZERO_EXP) continue;
-            // transposed digit planes: warp writes core matrices (j group, h group)
+            // transposed digit planes: warp writes core matrices (j group, h group);
+            // all loads in flight first
+            float2 xe[4][2], yl[4][2];
+#pragma unroll
             for (int q = 0; q < 4; q++) {
                 const int cmi = warp * 4 + q;                  // 64 core matrices: jg = cmi / 8, hg = cmi % 8
                 const int j = (cmi >> 3) * 8 + rr, hh = (cmi & 7) * 8 + 2 * kp;
+                const float2 *eb = a.Ebar + ((size_t)cb.ebar * npad + hb + hh) * 64 + j;
+                const float2 *lb = a.conP + ((size_t)cb.tslot * npad + hb + hh) * 64 + j;
+                const float2 z = make_float2(0.f, 0.f);
+                xe[q][0] = hh < nh ? eb[0] : z;
+                xe[q][1] = hh + 1 < nh ? eb[64] : z;
+                yl[q][0] = hh < nh ? lb[0] : z;
+                yl[q][1] = hh + 1 < nh ? lb[64] : z;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const int cmi = warp * 4 + q;
+                const int hh = (cmi & 7) * 8 + 2 * kp;
                 const int off = cmi * 128 + rr * 16 + kp * 4;
                 int d0[NB], d1[NB];
-                const float2 *eb = a.Ebar + ((size_t)cb.ebar * npad + hb + hh) * 64 + j;
-                const float2 x0 = hh < nh ? df_scale(eb[0], max(xs[hh] - xmax, -1000)) : make_float2(0.f, 0.f);
-                const float2 x1 = hh + 1 < nh ? df_scale(eb[64], max(xs[hh + 1] - xmax, -1000)) : make_float2(0.f, 0.f);
+                const float2 x0 = hh < nh ? df_scale(xe[q][0], max(xs[hh] - xmax, -1000)) : xe[q][0];
+                const float2 x1 = hh + 1 < nh ? df_scale(xe[q][1], max(xs[hh + 1] - xmax, -1000)) : xe[q][1];
                 digits_of<NB>(x0.x, x0.y, d0);
                 digits_of<NB>(x1.x, x1.y, d1);
 #pragma unroll
                 for (int s = 0; s < NB; s++) *reinterpret_cast<unsigned *>(sm + s * A_PLANE + off) = bf16_pair(d0[s], d1[s]);
                 unsigned char *Bp = sm + GSm<NB>::OFF_B + off;
-                if (tip) {
-                    const unsigned char *zz = a.z + (size_t)cb.tip * npad + hb;
-                    const int z0 = hh < nh ? zz[hh] : -1, z1 = hh + 1 < nh ? zz[hh + 1] : -1;
-                    *reinterpret_cast<unsigned *>(Bp) = bf16_pair(z0 == j ? 128 : 0, z1 == j ? 128 : 0);
-                } else {
-                    const float2 *lb = a.conP + ((size_t)cb.tslot * npad + hb + hh) * 64 + j;
-                    const float2 y0 = hh < nh ? lb[0] : make_float2(0.f, 0.f);
-                    const float2 y1 = hh + 1 < nh ? lb[64] : make_float2(0.f, 0.f);
-                    digits_of<NB>(y0.x, y0.y, d0);
-                    digits_of<NB>(y1.x, y1.y, d1);
+                digits_of<NB>(yl[q][0].x, yl[q][0].y, d0);
+                digits_of<NB>(yl[q][1].x, yl[q][1].y, d1);
 #pragma unroll
-                    for (int s = 0; s < NB; s++) *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16_pair(d0[s], d1[s]);
-                }
+                for (int s = 0; s < NB; s++) *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16_pair(d0[s], d1[s]);
             }
-            float2 C[NCOL];
-            ok = contract<NB>(sm, tmem, mbar, phase, C, GSm<NB>::OFF_B, tip);
+            ok = contract<NB>(sm, m, phase, acc, GSm<NB>::OFF_B, false, false, 0, max(xmax - xr, -1000));
             if (!ok) break;
-            const int sc = max(xmax - xr, -1000);
-#pragma unroll
-            for (int c = 0; c < NCOL; c++) acc[c] = df_add(acc[c], df_scale(C[c], sc));
         }
     }
     if (ok && any_tip) {
@@ -518,27 +725,70 @@ __global__ void __launch_bounds__(NT, 1) gradP_umma_kernel(FastBwdArgs a) {
 #pragma unroll 4
             for (int c = 0; c < NCOL; c++)
                 for (int pp = 0; pp < 4; pp++) acc[c] = df_add(acc[c], Gt[(pp * 64 + c0 + c) * 64 + row]);
+        __syncthreads();                                       // partials read before the planes are reused
     }
-    if (ok) {
-        if (row < 64)
+    if (!ok) {
+        on_failure(a.err, m, phase, false);
+        return false;
+    }
+    if (row < 64)
 #pragma unroll
-            for (int c = 0; c < NCOL; c++) out[row * 64 + c0 + c] = ldexp((double)acc[c].x + (double)acc[c].y, xr);
-    } else if (tid == 0) {
-        atomicExch(a.err, 1);
-        umma::mbar_wait(mbar, phase ^ 1u, 1000000000ull);
+        for (int c = 0; c < NCOL; c++) out[row * 64 + c0 + c] = ldexp((double)acc[c].x + (double)acc[c].y, xr);
+    return true;
+}
+
+template <int NB>
+__global__ void __launch_bounds__(NT, 1) gradP_umma_kernel(FastBwdArgs args) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    Misc *m = reinterpret_cast<Misc *>(sm + GSm<NB>::OFF_MISC);
+    FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + GSm<NB>::OFF_ARGS);
+    stage(a, &args);
+    tmem_setup(m);
+    uint32_t phase = 0;
+    gradP_task<NB>(*a, blockIdx.x, blockIdx.y, sm, m, phase);
+    tmem_teardown(m);
+}
+
+// persistent dlnL/dP over (gene, pair, chunk) tasks (independent; heaviest first)
+template <int NB>
+__global__ void __launch_bounds__(NT, 1) gradP_persist_kernel(const FastBwdArgs *__restrict__ genes,
+                                                              const Task *__restrict__ tasks, int ntask,
+                                                              unsigned *ctl, unsigned long long *trace) {
+    extern __shared__ __align__(1024) unsigned char sm[];
+    Misc *m = reinterpret_cast<Misc *>(sm + GSm<NB>::OFF_MISC);
+    FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + GSm<NB>::OFF_ARGS);
+    tmem_setup(m);
+    uint32_t phase = 0;
+    for (;;) {
+        const int idx = claim(ctl + CTL_GRADP, m);
+        if (idx >= ntask) break;
+        trace_put(trace, idx, 0, umma::global_ns());
+        const Task t = tasks[idx];
+        stage(a, genes + t.gene);
+        __syncthreads();
+        trace_put(trace, idx, 1, umma::global_ns());
+        if (!gradP_task<NB>(*a, t.item, t.tile, sm, m, phase)) break;
+        __syncthreads();
+        trace_put(trace, idx, 2, umma::global_ns());
+        trace_put(trace, idx, 3, smid());
     }
-    umma::fence_before();
-    __syncthreads();
-    if (warp == 0) umma::tmem_dealloc(tmem, 512);
+    tmem_teardown(m);
 }
 
 template <int NS>
 cudaError_t init_umma_ns() {
-    cudaError_t e = cudaFuncSetAttribute(prune_umma_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, USm<NS>::BYTES);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(bwd_umma_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, USm<NS>::BYTES);
-    if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(gradP_umma_kernel<NS>, cudaFuncAttributeMaxDynamicSharedMemorySize, GSm<NS>::BYTES);
+    const void *fu[] = {(const void *)prune_umma_kernel<NS>, (const void *)bwd_umma_kernel<NS>,
+                        (const void *)prune_persist_kernel<NS>, (const void *)bwd_persist_kernel<NS>};
+    for (const void *f : fu) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, USm<NS>::BYTES);
+        if (e != cudaSuccess) return e;
+    }
+    const void *fg[] = {(const void *)gradP_umma_kernel<NS>, (const void *)gradP_persist_kernel<NS>};
+    for (const void *f : fg) {
+        cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, GSm<NS>::BYTES);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -554,37 +804,72 @@ cudaError_t init_umma_kernels(int ns) {
     }
 }
 
+#define GB_NS_SWITCH(ns, CALL)          \
+    switch (ns) {                       \
+        case 4: CALL(4); break;         \
+        case 5: CALL(5); break;         \
+        case 6: CALL(6); break;         \
+        case 7: CALL(7); break;         \
+        case 8: CALL(8); break;         \
+    }
+
 void launch_prune_umma(const FastFwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st) {
     dim3 grid(ntile, nitems);
-    switch (ns) {
-        case 4: prune_umma_kernel<4><<<grid, NT, USm<4>::BYTES, st>>>(a); break;
-        case 5: prune_umma_kernel<5><<<grid, NT, USm<5>::BYTES, st>>>(a); break;
-        case 6: prune_umma_kernel<6><<<grid, NT, USm<6>::BYTES, st>>>(a); break;
-        case 7: prune_umma_kernel<7><<<grid, NT, USm<7>::BYTES, st>>>(a); break;
-        case 8: prune_umma_kernel<8><<<grid, NT, USm<8>::BYTES, st>>>(a); break;
-    }
+#define L_(n) prune_umma_kernel<n><<<grid, NT, USm<n>::BYTES, st>>>(a)
+    GB_NS_SWITCH(ns, L_)
+#undef L_
 }
 
 void launch_bwd_umma(const FastBwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st) {
     dim3 grid(ntile, nitems);
-    switch (ns) {
-        case 4: bwd_umma_kernel<4><<<grid, NT, USm<4>::BYTES, st>>>(a); break;
-        case 5: bwd_umma_kernel<5><<<grid, NT, USm<5>::BYTES, st>>>(a); break;
-        case 6: bwd_umma_kernel<6><<<grid, NT, USm<6>::BYTES, st>>>(a); break;
-        case 7: bwd_umma_kernel<7><<<grid, NT, USm<7>::BYTES, st>>>(a); break;
-        case 8: bwd_umma_kernel<8><<<grid, NT, USm<8>::BYTES, st>>>(a); break;
-    }
+#define L_(n) bwd_umma_kernel<n><<<grid, NT, USm<n>::BYTES, st>>>(a)
+    GB_NS_SWITCH(ns, L_)
+#undef L_
 }
 
 void launch_gradP_umma(const FastBwdArgs &a, int ns, int npair, cudaStream_t st) {
     dim3 grid(npair, a.nchunk);
-    switch (ns) {
-        case 4: gradP_umma_kernel<4><<<grid, NT, GSm<4>::BYTES, st>>>(a); break;
-        case 5: gradP_umma_kernel<5><<<grid, NT, GSm<5>::BYTES, st>>>(a); break;
-        case 6: gradP_umma_kernel<6><<<grid, NT, GSm<6>::BYTES, st>>>(a); break;
-        case 7: gradP_umma_kernel<7><<<grid, NT, GSm<7>::BYTES, st>>>(a); break;
-        case 8: gradP_umma_kernel<8><<<grid, NT, GSm<8>::BYTES, st>>>(a); break;
-    }
+#define L_(n) gradP_umma_kernel<n><<<grid, NT, GSm<n>::BYTES, st>>>(a)
+    GB_NS_SWITCH(ns, L_)
+#undef L_
 }
+
+void launch_prune_persist(const FastFwdArgs *genes, const Task *tasks, int ntask, unsigned *ctl, int ns,
+                          int nblock, unsigned long long *trace, cudaStream_t st) {
+    if (ntask <= 0) return;
+    const int g = ntask < nblock ? ntask : nblock;
+#define L_(n) prune_persist_kernel<n><<<g, NT, USm<n>::BYTES, st>>>(genes, tasks, ntask, ctl, trace)
+    GB_NS_SWITCH(ns, L_)
+#undef L_
+}
+
+void launch_bwd_persist(const FastBwdArgs *genes, const Task *tasks, int ntask, unsigned *ctl, int ns,
+                        int nblock, unsigned long long *trace, cudaStream_t st) {
+    if (ntask <= 0) return;
+    const int g = ntask < nblock ? ntask : nblock;
+#define L_(n) bwd_persist_kernel<n><<<g, NT, USm<n>::BYTES, st>>>(genes, tasks, ntask, ctl, trace)
+    GB_NS_SWITCH(ns, L_)
+#undef L_
+}
+
+void launch_gradP_persist(const FastBwdArgs *genes, const Task *tasks, int ntask, unsigned *ctl, int ns,
+                          int nblock, unsigned long long *trace, cudaStream_t st) {
+    if (ntask <= 0) return;
+    const int g = ntask < nblock ? ntask : nblock;
+#define L_(n) gradP_persist_kernel<n><<<g, NT, GSm<n>::BYTES, st>>>(genes, tasks, ntask, ctl, trace)
+    GB_NS_SWITCH(ns, L_)
+#undef L_
+}
+
+namespace {
+__global__ void bump_kernel(unsigned *ctl) {
+    ctl[CTL_EPOCH] += 1u;
+    ctl[CTL_FWD] = 0u;
+    ctl[CTL_BWD] = 0u;
+    ctl[CTL_GRADP] = 0u;
+}
+}  // namespace
+
+void launch_bump(unsigned *ctl, cudaStream_t st) { bump_kernel<<<1, 1, 0, st>>>(ctl); }
 
 }  // namespace gb

@@ -318,7 +318,7 @@ int fp64_record_eval(gb_handle *h, bool grad) {
         CK(cudaMemcpyAsync(h->adj->d_gp, h->adj->h_gp, sizeof(GradParams), cudaMemcpyHostToDevice, h->stream));
         nk += adjoint_record(h);
         int rc = adjoint_fetch(h);
-        if (rc) return -rc;
+        if (rc) return rc;
     }
     CK(cudaMemcpyAsync(h->h_out, h->d_out, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     return nk;
@@ -556,6 +556,11 @@ int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches
     for (auto ev : rec.ev) cudaEventDestroy(ev);
     if (e != cudaSuccess) return cuda_fail(e, "gb_profile");
     return GB_OK;
+}
+
+int gb_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap) {
+    if (!h || cap < 0) return fail(GB_ERR_ARG, "gb_task_trace: bad arguments");
+    return fast_task_trace(h, kernel, out, cap);
 }
 
 int gb_model_setup(const double *pi, double kappa, double omega0, double omega2, double p0, double p1,

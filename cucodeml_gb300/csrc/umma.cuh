@@ -63,6 +63,33 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
         "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
 }
 
+// the same MMA issued by the whole warp, executed only by the lane with
+// leader != 0 (the operands are computed warp-uniformly)
+__device__ __forceinline__ void mma_bf16_leader(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                                uint32_t accumulate, uint32_t leader) {
+    asm volatile(
+        "{\n"
+        ".reg .pred p, q;\n"
+        "setp.ne.b32 p, %4, 0;\n"
+        "setp.ne.b32 q, %5, 0;\n"
+        "@q tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate), "r"(leader));
+}
+
+// 1 in exactly one lane of the (fully active) warp
+__device__ __forceinline__ uint32_t elect_one() {
+    uint32_t p;
+    asm volatile(
+        "{\n"
+        ".reg .pred e;\n"
+        "elect.sync _|e, 0xffffffff;\n"
+        "selp.u32 %0, 1, 0, e;\n"
+        "}\n"
+        : "=r"(p));
+    return p;
+}
+
 __device__ __forceinline__ void commit(uint64_t *mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(smem_u32(mbar)));
 }
@@ -87,6 +114,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *mbar, uint32_t parity) {
         : "=r"(ok)
         : "r"(smem_u32(mbar)), "r"(parity));
     return ok != 0;
+}
+
+// arrive on the mbarrier and add the expected transaction bytes of the bulk
+// copies that complete this phase
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// bulk copy global -> shared (16-byte aligned addresses, size a multiple of
+// 16), completion counted in bytes on the mbarrier
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
 }
 
 __device__ __forceinline__ uint64_t global_ns() {

@@ -210,6 +210,18 @@ int gb_replay(gb_handle *h, int iters, int with_grad, double *ms);
 int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches);
 
 /*
+ * Task trace of the persistent split-precision kernels (no counterpart in the
+ * reference): with GBCODEML_TRACE=1 in the environment when the handle's
+ * kernels are first set up, every task of the last evaluation records, from
+ * the device's global timer, when it was claimed, when its dependencies were
+ * met and when it ended, and the SM that ran it.  kernel: 0 pruning, 1 adjoint
+ * propagation, 2 dlnL/dP.  Writes up to cap tasks, 8 words each (gene, item,
+ * tile, 0, claim ns, ready ns, end ns, SM), and returns the kernel's task
+ * count (GB_ERR_STATE when tracing is off or the kernel has not run).
+ */
+int gb_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);
+
+/*
  * Host-only model set-up (no GPU needed): for codon frequencies pi[61] and
  * model-A parameters, the three eigen solutions U[i], V[i] (61x61 row-major),
  * Root[i] for w0, w1 = 1, w2, the Qfactors qf[2] and class proportions

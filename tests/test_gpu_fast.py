@@ -96,3 +96,35 @@ def test_fast_gradient_64x5000():
           f"fp64 {a.ms_device:.2f} ms fast {b.ms_device:.2f} ms")
     assert abs(a.neg_lnL - b.neg_lnL) <= 1e-6
     assert err <= 1e-5
+
+
+@pytest.mark.parametrize("case", ["c24x400_s3", "c40x200_s4", "64x5000"])
+def test_persistent_equals_levels(case, monkeypatch):
+    """The persistent task-list kernels do the same arithmetic per (item, tile)
+    as the one-launch-per-level kernels: results must be bit-identical, also
+    when lnL-only and lnL+gradient evaluations alternate on one handle."""
+    if case == "64x5000":
+        aln = simulate(64, 5000, seed=2024)
+        z, fpatt, pi = api.patterns(aln.codons)
+        tree = aln.tree
+        args = (tree.branch, 2.0, 0.3, 3.0, 0.5, 0.3)
+    else:
+        fx, tree, codons = load_golden(case)
+        z, fpatt, pi = O.patterns(codons)
+        x = np.array(fx["x"])
+        nb = tree.nbranch
+        args = (node_blength(tree, x), x[nb], x[nb + 3], x[nb + 4], x[nb + 1], x[nb + 2])
+    res = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("GBCODEML_PERSIST", mode)
+        lk = api.Likelihood(tree, z, fpatt, pi, precision="fast")
+        r0 = lk.evaluate(*args, want_site=True)
+        r1 = lk.evaluate(*args, grad=True)
+        r2 = lk.evaluate(*args)
+        res[mode] = (r0, r1, r2)
+        lk.close()
+    p, l = res["1"], res["0"]
+    assert p[0].neg_lnL == l[0].neg_lnL and np.array_equal(p[0].lnf, l[0].lnf)
+    assert p[1].neg_lnL == l[1].neg_lnL and p[2].neg_lnL == l[0].neg_lnL
+    assert np.array_equal(grad_vec(p[1]), grad_vec(l[1]))
+    print(f"{case}: persistent == per-level; device ms (lnL+grad) {p[1].ms_device:.2f} vs {l[1].ms_device:.2f}")

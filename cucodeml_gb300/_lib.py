@@ -73,6 +73,7 @@ SIGNATURES = {
     "gb_batch_destroy": (C.c_int, [C.c_void_p]),
     "gb_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),
     "gb_task_trace": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_ulonglong), C.c_int]),
+    "gb_batch_task_trace": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_ulonglong), C.c_int]),
     "gb_lnL_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, C.c_char_p, C.c_int, C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_void_p]),

@@ -206,7 +206,8 @@ class Likelihood:
 
 class Batch:
     """Many independent alignments evaluated together (gb_batch_*): one CUDA
-    graph launch per evaluation, each gene an independent branch."""
+    graph launch per evaluation (split precision: one persistent launch per
+    phase over all genes; FP64: each gene an independent branch)."""
 
     def __init__(self, genes, precision: str = "fast", device: int = 0):
         """genes: list of (tree, z, fpatt, pi)."""
@@ -277,3 +278,14 @@ class Batch:
         ms = C.c_double(0)
         _lib.check(self._L.gb_batch_replay(self._h, int(iters), int(with_grad), C.byref(ms)))
         return ms.value
+
+    def task_trace(self, kernel: int) -> np.ndarray:
+        """As Likelihood.task_trace, for the batch's persistent kernels."""
+        n = self._L.gb_batch_task_trace(self._h, int(kernel), None, 0)
+        if n < 0:
+            _lib.check(n)
+        out = np.zeros((n, 8), dtype=np.uint64)
+        r = self._L.gb_batch_task_trace(self._h, int(kernel), out.ctypes.data_as(C.POINTER(C.c_ulonglong)), n)
+        if r < 0:
+            _lib.check(r)
+        return out

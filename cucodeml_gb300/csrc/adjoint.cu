@@ -36,17 +36,29 @@ namespace gb {
 namespace {
 
 constexpr int NCd = 61;
+constexpr int DM_BLOCKS = 8;   // Dm: 5 derivative matrices + 3 inverse-difference tables
 constexpr int kGradPSmem = (2 * TILE64 * 65 + 64 * 65) * sizeof(double);
-constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256) * sizeof(double);
+constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256 + 64) * sizeof(double);
 
 // ---------------------------------------------------------------- kernels
 
-// D matrices V dQ U for (kappa: w=0,1,2) and (omega: w=0,2), 64-padded
+// D matrices V dQ U for (kappa: w=0,1,2) and (omega: w=0,2), 64-padded, and
+// the inverse eigenvalue differences of each w (for Phi)
 __global__ void __launch_bounds__(256) dmat_kernel(const DevParams *__restrict__ prm,
                                                    const GradParams *__restrict__ gp,
                                                    double *__restrict__ Dm) {
     __shared__ double T[61 * 62];
-    const int which = blockIdx.x;   // 0,1,2: kappa for w; 3: omega w0; 4: omega w2
+    const int which = blockIdx.x;   // 0,1,2: kappa for w; 3: omega w0; 4: omega w2; 5,6,7: 1/(Root_m - Root_n) for w
+    if (which >= 5) {
+        const double *R = prm->Root[which - 5];
+        double *out = Dm + (size_t)which * 64 * 64;
+        for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
+            const int r = i / 64, c = i % 64;
+            const double d = (r < 61 && c < 61) ? R[r] - R[c] : 0.0;
+            out[i] = d != 0.0 ? 1.0 / d : 0.0;
+        }
+        return;
+    }
     const int w = which < 3 ? which : (which == 3 ? 0 : 2);
     const double *dQ = which < 3 ? gp->dQk[w] : gp->dQw[w];
     const double *U = prm->U[w];
@@ -231,6 +243,19 @@ __global__ void __launch_bounds__(128) gradP_kernel(const Contrib *__restrict__ 
         for (int u = 0; u < 4; u++) out[(j0 + q) * 64 + k0 + u] = g[q][u] + Gs[(j0 + q) * 65 + k0 + u];
 }
 
+// Phi_mn = (e^{a_m} - e^{a_n}) / (a_m - a_n), a = t' Root, from em = e^{a_m},
+// en = e^{a_n} and inv = 1 / (Root_m - Root_n): the divided difference when
+// |a_m - a_n| >= 1e-3 (relative error <= eps / 1e-3), else the series
+// e^{(a_m + a_n)/2} (1 + d^2/24 + d^4/1920)
+__device__ __forceinline__ double phi_of(double am, double an, double em, double en, double inv, double rtp) {
+    const double d = am - an;
+    if (fabs(d) < 1e-3) {
+        const double d2 = d * d;
+        return sqrt(em * en) * (1.0 + d2 * (1.0 / 24.0 + d2 * (1.0 / 1920.0)));
+    }
+    return (em - en) * inv * rtp;
+}
+
 // per pair: G = sum of chunk partials; H = U^T G V^T; contributions to dlnL/dt',
 // dlnL/dkappa and dlnL/domega (out[pair][3])
 __global__ void __launch_bounds__(256) gradH_kernel(const PairDesc *__restrict__ pairs,
@@ -244,6 +269,7 @@ __global__ void __launch_bounds__(256) gradH_kernel(const PairDesc *__restrict__
     double *Gs = smh;                    // [61][62]
     double *Ts = smh + 61 * 62;          // [61][62]
     double (*red)[256] = reinterpret_cast<double (*)[256]>(smh + 2 * 61 * 62);
+    double *ex = smh + 2 * 61 * 62 + 3 * 256;   // [64] e^{t' Root_m}
     const int p = blockIdx.x;
     const PairDesc pd = pairs[p];
     const int w = pd.w;
@@ -251,6 +277,7 @@ __global__ void __launch_bounds__(256) gradH_kernel(const PairDesc *__restrict__
     const double *U = prm->U[w];
     const double *V = prm->V[w];
     const double *R = prm->Root[w];
+    if (threadIdx.x < 61) ex[threadIdx.x] = exp(tp * R[threadIdx.x]);
     for (int i = threadIdx.x; i < 61 * 61; i += blockDim.x) {
         int j = i / 61, k = i % 61;
         double s = 0;
@@ -270,16 +297,14 @@ __global__ void __launch_bounds__(256) gradH_kernel(const PairDesc *__restrict__
     double sdt = 0, sk = 0, sw = 0;
     const double *Dk = Dm + (size_t)w * 64 * 64;
     const double *Dw = w == 0 ? Dm + 3 * 64 * 64 : (w == 2 ? Dm + 4 * 64 * 64 : nullptr);
+    const double *inv = Dm + (size_t)(5 + w) * 64 * 64;
+    const double rtp = tp > 0.0 ? 1.0 / tp : 0.0;
     for (int i = threadIdx.x; i < 61 * 61; i += blockDim.x) {
         int m = i / 61, n = i % 61;
         double hmn = 0;
         for (int j = 0; j < 61; j++) hmn = fma(U[j * 61 + m], Ts[j * 62 + n], hmn);
-        const double am = tp * R[m], an = tp * R[n];
-        double phi;
-        const double d = am - an;
-        if (fabs(d) < 1e-8) phi = exp(0.5 * (am + an)) * (1.0 + d * d / 24.0);
-        else phi = exp(an) * expm1(d) / d;
-        if (m == n) sdt += R[m] * exp(am) * hmn;
+        const double phi = phi_of(tp * R[m], tp * R[n], ex[m], ex[n], inv[m * 64 + n], rtp);
+        if (m == n) sdt += R[m] * ex[m] * hmn;
         const double hp = hmn * phi * tp;
         sk = fma(hp, Dk[m * 64 + n], sk);
         if (Dw) sw = fma(hp, Dw[m * 64 + n], sw);
@@ -294,6 +319,120 @@ __global__ void __launch_bounds__(256) gradH_kernel(const PairDesc *__restrict__
         __syncthreads();
     }
     if (threadIdx.x < 3) out[p * 3 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// The same per-pair sums for the split-precision path, with the two 61^3
+// products in double-float on the FP32 pipe (no FP64 arithmetic in the
+// contractions): every term's product error is recovered exactly with an FMA
+// and the sums are compensated (TwoSum of the high parts, errors summed
+// apart), then H is rounded to FP64 for the Phi-weighted sums.
+// Thread (r = tid / 4, c0 = 16 (tid % 4)) owns row r, columns c0..c0+15.
+__device__ __forceinline__ void dot2_step(float &s, float &c, float2 a, float2 b) {
+    const float p = a.x * b.x;
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, e);
+    e = fmaf(a.y, b.x, e);
+    const float t = s + p;
+    const float z = t - s;
+    c += ((s - (t - z)) + (p - z)) + e;
+    s = t;
+}
+
+__device__ __forceinline__ float2 df_of(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+
+constexpr int kGradHdfSmem = 3 * 61 * 64 * 8 + (64 + 3 * 256) * 8;
+
+__global__ void __launch_bounds__(256) gradH_df_kernel(const PairDesc *__restrict__ pairs,
+                                                       const int *__restrict__ label,
+                                                       const double *__restrict__ tnode,
+                                                       const DevParams *__restrict__ prm,
+                                                       const double *__restrict__ Gpart, int nchunk,
+                                                       const double *__restrict__ Dm,
+                                                       double *__restrict__ out) {
+    extern __shared__ __align__(16) unsigned char smr[];
+    float2 *GT = reinterpret_cast<float2 *>(smr);          // [61][64] G, then T
+    float2 *Vt = GT + 61 * 64;                              // [61][64] Vt[k][n] = V[n][k]
+    float2 *Us = Vt + 61 * 64;                              // [61][64] U[j][m]
+    double *ex = reinterpret_cast<double *>(Us + 61 * 64);  // [64]
+    double (*red)[256] = reinterpret_cast<double (*)[256]>(ex + 64);
+    const int p = blockIdx.x, tid = threadIdx.x;
+    const PairDesc pd = pairs[p];
+    const int w = pd.w;
+    const double tp = tnode[pd.node] * prm->qf[label[pd.node]];
+    const double *U = prm->U[w];
+    const double *V = prm->V[w];
+    const double *R = prm->Root[w];
+    if (tid < 61) ex[tid] = exp(tp * R[tid]);
+    for (int i = tid; i < 61 * 64; i += blockDim.x) {
+        const int r = i / 64, c = i % 64;
+        double g = 0.0;
+        if (c < 61)
+            for (int q = 0; q < nchunk; q++) g += Gpart[((size_t)p * nchunk + q) * 64 * 64 + r * 64 + c];
+        GT[i] = df_of(g);
+        Vt[i] = c < 61 ? df_of(V[c * 61 + r]) : make_float2(0.f, 0.f);
+        Us[i] = c < 61 ? df_of(U[r * 61 + c]) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int r = tid >> 2, c0 = (tid & 3) * 16;
+    float s[16], e[16];
+    // T[r][n] = sum_k G[r][k] Vt[k][n]
+#pragma unroll
+    for (int i = 0; i < 16; i++) s[i] = e[i] = 0.f;
+    if (r < 61)
+        for (int k = 0; k < 61; k++) {
+            const float2 g = GT[r * 64 + k];
+#pragma unroll
+            for (int i = 0; i < 16; i++) dot2_step(s[i], e[i], g, Vt[k * 64 + c0 + i]);
+        }
+    __syncthreads();                                        // every read of G is done
+    if (r < 61)
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const float hi = s[i] + e[i];
+            GT[r * 64 + c0 + i] = make_float2(hi, e[i] - (hi - s[i]));
+        }
+    __syncthreads();
+    // H[r][n] = sum_j U[j][r] T[j][n]
+#pragma unroll
+    for (int i = 0; i < 16; i++) s[i] = e[i] = 0.f;
+    if (r < 61)
+        for (int j = 0; j < 61; j++) {
+            const float2 u = Us[j * 64 + r];
+#pragma unroll
+            for (int i = 0; i < 16; i++) dot2_step(s[i], e[i], u, GT[j * 64 + c0 + i]);
+        }
+    double sdt = 0, sk = 0, sw = 0;
+    const double *Dk = Dm + (size_t)w * 64 * 64;
+    const double *Dw = w == 0 ? Dm + 3 * 64 * 64 : (w == 2 ? Dm + 4 * 64 * 64 : nullptr);
+    const double *inv = Dm + (size_t)(5 + w) * 64 * 64;
+    const double rtp = tp > 0.0 ? 1.0 / tp : 0.0;
+    if (r < 61) {
+        const double am = tp * R[r], em = ex[r];
+#pragma unroll
+        for (int i = 0; i < 16; i++) {
+            const int n = c0 + i;
+            if (n >= 61) continue;
+            const double hmn = (double)s[i] + (double)e[i];
+            const double phi = phi_of(am, tp * R[n], em, ex[n], inv[r * 64 + n], rtp);
+            if (r == n) sdt += R[r] * em * hmn;
+            const double hp = hmn * phi * tp;
+            sk = fma(hp, Dk[r * 64 + n], sk);
+            if (Dw) sw = fma(hp, Dw[r * 64 + n], sw);
+        }
+    }
+    red[0][tid] = sdt;
+    red[1][tid] = sk;
+    red[2][tid] = sw;
+    __syncthreads();
+    for (int st = 128; st > 0; st >>= 1) {
+        if (tid < st)
+            for (int q = 0; q < 3; q++) red[q][tid] += red[q][tid + st];
+        __syncthreads();
+    }
+    if (tid < 3) out[p * 3 + tid] = red[tid][0];
 }
 
 // dlnL/dfreqK_c (up to the 1/freqK_c factor) : sum_h fpatt_h f_c / R_h
@@ -402,7 +541,7 @@ int adjoint_init(gb_handle *h) {
         (rc = dalloc(&a->d_Ebar, (size_t)h->nslot * MAXC * npad * 64)) ||
         (rc = dalloc(&a->d_Abar, (size_t)h->nslot * npad * 64)) ||
         (rc = dalloc(&a->d_Gpart, h->pairs.size() * a->nchunk * 64 * 64)) ||
-        (rc = dalloc(&a->d_Dm, 5 * 64 * 64)) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
+        (rc = dalloc(&a->d_Dm, DM_BLOCKS * 64 * 64)) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
         (rc = dalloc(&a->d_fpart, a->nfreq_blocks * 4)) || (rc = dalloc(&a->d_gp, 1)))
         return rc;
     if (cudaMallocHost((void **)&a->h_gp, sizeof(GradParams)) ||
@@ -417,11 +556,12 @@ int adjoint_init(gb_handle *h) {
     CK(cudaMemset(a->d_Abar, 0, sizeof(double) * (size_t)h->nslot * npad * 64));
     CK(cudaFuncSetAttribute(gradP_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradPSmem));
     CK(cudaFuncSetAttribute(gradH_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHSmem));
+    CK(cudaFuncSetAttribute(gradH_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHdfSmem));
     return 0;
 }
 
 void launch_dmat(gb_handle *h) {
-    dmat_kernel<<<5, 256, 0, h->stream>>>(h->d_prm, h->adj->d_gp, h->adj->d_Dm);
+    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, h->adj->d_gp, h->adj->d_Dm);
 }
 
 void launch_gradH(gb_handle *h) {
@@ -429,6 +569,12 @@ void launch_gradH(gb_handle *h) {
     gradH_kernel<<<(unsigned)h->pairs.size(), 256, kGradHSmem, h->stream>>>(h->d_pairs, h->d_label, h->d_tnode,
                                                                            h->d_prm, a->d_Gpart, a->nchunk,
                                                                            a->d_Dm, a->d_pout);
+}
+
+void launch_gradH_df(gb_handle *h) {
+    AdjointState *a = h->adj;
+    gradH_df_kernel<<<(unsigned)h->pairs.size(), 256, kGradHdfSmem, h->stream>>>(
+        h->d_pairs, h->d_label, h->d_tnode, h->d_prm, a->d_Gpart, a->nchunk, a->d_Dm, a->d_pout);
 }
 
 void launch_freq(gb_handle *h, int nscale) {
@@ -442,7 +588,7 @@ namespace {
 int record_backward(gb_handle *h) {
     AdjointState *a = h->adj;
     int nk = 0;
-    dmat_kernel<<<5, 256, 0, h->stream>>>(h->d_prm, a->d_gp, a->d_Dm);
+    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, a->d_gp, a->d_Dm);
     prof_mark(h, GB_K_OTHER);
     nk++;
     for (size_t L = 0; L + 1 < a->blevel_off.size(); L++) {

@@ -55,6 +55,7 @@ struct AdjointState {
 int adjoint_init(gb_handle *h);               // host structures and device buffers
 void launch_dmat(gb_handle *h);
 void launch_gradH(gb_handle *h);
+void launch_gradH_df(gb_handle *h);      // split-precision path: double-float products
 void launch_freq(gb_handle *h, int nscale);
 void adjoint_chain(gb_handle *h, const Derived *D, const double *blength, gb_grad *grad);
 int adjoint_fetch(gb_handle *h);              // D2H of per-pair and class-weight sums (async)

@@ -252,6 +252,13 @@ int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *g
     return GB_OK;
 }
 
+int gb_batch_task_trace(gb_batch *b, int kernel, unsigned long long *out, int cap) {
+    if (!b || cap < 0) return fail(GB_ERR_ARG, "gb_batch_task_trace: bad arguments");
+    if (!b->plan.ctl) return fail(GB_ERR_STATE, "gb_batch_task_trace: the batch has no persistent kernels");
+    CK(cudaSetDevice(b->device));
+    return persist_task_trace(&b->plan, kernel, out, cap);
+}
+
 int gb_batch_replay(gb_batch *b, int iters, int with_grad, double *ms) {
     if (!b || !ms || iters < 1) return fail(GB_ERR_ARG, "gb_batch_replay: bad arguments");
     cudaGraphExec_t g = b->graph[with_grad ? 1 : 0];

@@ -407,7 +407,7 @@ int fast_rec_dmat(gb_handle *h) {
 }
 
 int fast_rec_tail(gb_handle *h) {
-    launch_gradH(h);
+    launch_gradH_df(h);
     prof_mark(h, GB_K_GRADH);
     launch_freq(h, 1);
     prof_mark(h, GB_K_OTHER);
@@ -438,20 +438,17 @@ int fast_prepare(gb_handle *h, bool grad) {
 
 bool fast_persistent(const gb_handle *h) { return h->fast && h->fast->persist; }
 
-// the last evaluation's task trace of one persistent kernel of this handle:
+// the last evaluation's task trace of one persistent kernel of a plan:
 // 8 words per task (gene, item, tile, 0, claim ns, dependencies met ns, end ns, SM)
-int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap) {
-    if (!h->fast || !h->fast->persist) return fail(GB_ERR_STATE, "gb_task_trace: no persistent kernels on this handle");
-    PersistPlan *pp = &h->fast->plan;
-    if (kernel < 0 || kernel > 2) return fail(GB_ERR_ARG, "gb_task_trace: kernel must be 0, 1 or 2");
+int persist_task_trace(PersistPlan *pp, int kernel, unsigned long long *out, int cap) {
+    if (kernel < 0 || kernel > 2) return fail(GB_ERR_ARG, "task trace: kernel must be 0, 1 or 2");
     const Task *dt[3] = {pp->d_ftask, pp->d_btask, pp->d_gtask};
     const int nt[3] = {pp->nftask, pp->nbtask, pp->ngtask};
     if (!pp->tracing || !pp->trace[kernel] || !dt[kernel])
-        return fail(GB_ERR_STATE, "gb_task_trace: tracing off (GBCODEML_TRACE=1 at creation) or kernel not run");
+        return fail(GB_ERR_STATE, "task trace: tracing off (GBCODEML_TRACE=1 at creation) or kernel not run");
     const int n = std::min(cap, nt[kernel]);
     if (out && n > 0) {
-        CK(cudaSetDevice(h->device));
-        CK(cudaStreamSynchronize(h->stream));
+        CK(cudaDeviceSynchronize());
         std::vector<Task> t(n);
         std::vector<unsigned long long> tr(4 * (size_t)n);
         CK(cudaMemcpy(t.data(), dt[kernel], sizeof(Task) * n, cudaMemcpyDeviceToHost));
@@ -465,6 +462,12 @@ int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap) 
         }
     }
     return nt[kernel];
+}
+
+int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap) {
+    if (!h->fast || !h->fast->persist) return fail(GB_ERR_STATE, "gb_task_trace: no persistent kernels on this handle");
+    CK(cudaSetDevice(h->device));
+    return persist_task_trace(&h->fast->plan, kernel, out, cap);
 }
 int fast_ns(const gb_handle *h, bool adjoint) { return adjoint ? h->fast->nsb : h->fast->ns; }
 

@@ -127,6 +127,7 @@ int fast_rec_tail(gb_handle *h);      // per-pair and class-weight gradient sums
 int fast_rec_copies_out(gb_handle *h, bool grad);
 bool fast_persistent(const gb_handle *h);
 int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);
+int persist_task_trace(PersistPlan *pp, int kernel, unsigned long long *out, int cap);
 int fast_ns(const gb_handle *h, bool adjoint);
 // persistent executors over one or many genes (fast.cu)
 void persist_free(PersistPlan *pp);

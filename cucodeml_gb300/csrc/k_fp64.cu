@@ -44,9 +44,12 @@ __global__ void __launch_bounds__(256) pmat_fp64_kernel(const PairDesc *__restri
     }
     const double *U = prm->U[w];
     const double *V = prm->V[w];
+    __shared__ double ex[64];
+    if (tid < NC) ex[tid] = exp(t * prm->Root[w][tid]);
+    __syncthreads();
     for (int i = tid; i < NC * 64; i += blockDim.x) {
         int m = i / 64, c = i % 64;
-        UeT[i] = c < NC ? U[c * NC + m] * exp(t * prm->Root[w][m]) : 0.0;
+        UeT[i] = c < NC ? U[c * NC + m] * ex[m] : 0.0;
         Vs[i] = c < NC ? V[m * NC + c] : 0.0;
     }
     __syncthreads();

@@ -220,6 +220,8 @@ int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches
  * count (GB_ERR_STATE when tracing is off or the kernel has not run).
  */
 int gb_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);
+/* the same for a batch's persistent kernels (gene = index in the batch) */
+int gb_batch_task_trace(gb_batch *b, int kernel, unsigned long long *out, int cap);
 
 /*
  * Host-only model set-up (no GPU needed): for codon frequencies pi[61] and

@@ -176,8 +176,17 @@ def batched_leg(args, dev):
     out = {"genes": args.batch, "patterns": int(sum(len(g[2]) for g in genes)),
            "workload": f"{args.batch} genes, taxa U{{12..48}}, codons log-uniform [100, 3000], lnL+gradient"}
     res = {}
+    tuning = None
+    if not args.no_tune:
+        from cucodeml_gb300 import autotune
+        t0 = time.perf_counter()
+        tr = autotune.tune_batch(genes, prm, use_cache=False)
+        tuning = tr["config"]
+        out["autotune"] = {"chosen": tuning, "seconds": round(time.perf_counter() - t0, 1),
+                           "candidates": [{"config": t["config"], "ms_per_batch": t.get("ms"),
+                                           "agrees": t.get("agrees")} for t in tr["table"]]}
     for prec in ("fast", "fp64"):
-        b = api.Batch(genes, precision=prec, device=dev)
+        b = api.Batch(genes, precision=prec, device=dev, tuning=tuning if prec == "fast" else None)
         f, g, st = b.evaluate(prm, grad=True)
         f, g, st = b.evaluate(prm, grad=True)
         res[prec] = (f, g)
@@ -272,6 +281,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--batch", type=int, default=512, help="genes in the batched leg (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=3)
+    ap.add_argument("--no-tune", action="store_true", help="batched leg: skip the autotuner (library defaults)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":

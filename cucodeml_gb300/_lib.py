@@ -16,6 +16,8 @@ _ip = C.POINTER(C.c_int)
 GB_OK = 0
 GB_PREC_FP64 = 0
 GB_PREC_FAST = 1
+# gb_tune knobs (include/gbcodeml.h)
+TUNE = {"mma": 1, "persist": 2, "gchunk": 3, "order": 4, "grid": 5}
 ERRORS = {-1: "GB_ERR_ARG", -2: "GB_ERR_CUDA", -3: "GB_ERR_OOM", -4: "GB_ERR_PARAM",
           -5: "GB_ERR_TIMEOUT", -6: "GB_ERR_STATE", -7: "GB_ERR_NODEVICE"}
 
@@ -73,6 +75,8 @@ SIGNATURES = {
     "gb_batch_destroy": (C.c_int, [C.c_void_p]),
     "gb_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),
     "gb_task_trace": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_ulonglong), C.c_int]),
+    "gb_tune": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "gb_batch_tune": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "gb_batch_task_trace": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_ulonglong), C.c_int]),
     "gb_lnL_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, _ip, _ip, C.c_char_p, C.c_int, C.c_void_p,
                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -71,7 +71,7 @@ class EvalResult:
 
 class Likelihood:
     def __init__(self, tree: Tree, z: np.ndarray, fpatt: np.ndarray, pi: np.ndarray,
-                 precision: str = "fp64", device: int = 0, node_scale=None):
+                 precision: str = "fp64", device: int = 0, node_scale=None, tuning: dict | None = None):
         self._L = _lib.load()
         self.tree = tree
         self.ns, self.nnode = tree.ns, tree.nnode
@@ -94,6 +94,8 @@ class Likelihood:
         h = C.c_void_p()
         _lib.check(self._L.gb_create(C.byref(self._prob), C.byref(h)))
         self._h = h
+        for knob, value in (tuning or {}).items():
+            _lib.check(self._L.gb_tune(self._h, _lib.TUNE[knob], int(value)))
         self.bnode = np.ascontiguousarray(tree.branch_nodes(), dtype=np.int32)
 
     @property
@@ -209,7 +211,7 @@ class Batch:
     graph launch per evaluation (split precision: one persistent launch per
     phase over all genes; FP64: each gene an independent branch)."""
 
-    def __init__(self, genes, precision: str = "fast", device: int = 0):
+    def __init__(self, genes, precision: str = "fast", device: int = 0, tuning: dict | None = None):
         """genes: list of (tree, z, fpatt, pi)."""
         self._L = _lib.load()
         prec = precision if isinstance(precision, int) else \
@@ -233,6 +235,8 @@ class Batch:
         h = C.c_void_p()
         _lib.check(self._L.gb_batch_create(len(genes), probs, C.byref(h)))
         self._h = h
+        for knob, value in (tuning or {}).items():
+            _lib.check(self._L.gb_batch_tune(self._h, _lib.TUNE[knob], int(value)))
         self.n = len(genes)
 
     def close(self):

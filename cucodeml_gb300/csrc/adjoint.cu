@@ -532,7 +532,9 @@ int adjoint_init(gb_handle *h) {
         a->coff[p + 1] = a->coff[p] + (int)per[p].size();
         for (auto &c : per[p]) a->contrib.push_back(c);
     }
-    a->nchunk = (h->npatt + GCHUNK - 1) / GCHUNK;
+    // the FP64 kernel works in chunks of GCHUNK; the split-precision ones as tuned
+    a->gchunk = (h->precision != GB_PREC_FP64 && h->tune.gchunk > 0) ? h->tune.gchunk : GCHUNK;
+    a->nchunk = (h->npatt + a->gchunk - 1) / a->gchunk;
     a->nfreq_blocks = (h->npatt + 255) / 256;
     const size_t npad = h->npad;
     int rc;

@@ -41,6 +41,7 @@ struct AdjointState {
     std::vector<Contrib> contrib;
     std::vector<int> coff;
     int nchunk = 1, nfreq_blocks = 1;
+    int gchunk = GCHUNK;             // patterns per dlnL/dP partial
     BItem *d_bitems = nullptr;
     Contrib *d_contrib = nullptr;
     int *d_coff = nullptr;

@@ -30,6 +30,7 @@ struct gb_batch {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int kernels[2] = {0, 0};
     gb::PersistPlan plan;
+    gb::Tuning tune;
 };
 
 namespace {
@@ -126,7 +127,7 @@ int build_graph(gb_batch *b, bool grad) {
     }
     const bool persist = batch_persistent(b);
     if (persist) {
-        int rc = persist_build(&b->plan, b->h.data(), b->n, grad);
+        int rc = persist_build(&b->plan, b->h.data(), b->n, grad, b->tune);
         if (rc) return rc;
     }
     cudaGraph_t g;
@@ -249,6 +250,22 @@ int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *g
         stats->h2d_bytes = h2d;
         stats->d2h_bytes = d2h;
     }
+    return GB_OK;
+}
+
+int gb_batch_tune(gb_batch *b, int knob, int value) {
+    if (!b) return fail(GB_ERR_ARG, "gb_batch_tune: null batch");
+    if (b->graph[0] || b->graph[1] || b->plan.ctl) return fail(GB_ERR_STATE, "gb_batch_tune: batch already evaluated");
+    if (knob == GB_TUNE_ORDER) {
+        if (value != 0 && value != 1) return fail(GB_ERR_ARG, "gb_batch_tune: order must be 0 or 1");
+        b->tune.order = value;
+        return GB_OK;
+    }
+    for (auto h : b->h) {
+        const int rc = gb_tune(h, knob, value);
+        if (rc) return rc;
+    }
+    if (knob == GB_TUNE_GRID) b->tune.grid = value;
     return GB_OK;
 }
 

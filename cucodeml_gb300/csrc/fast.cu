@@ -67,7 +67,10 @@ int fast_init(gb_handle *h) {
     if (f->nsb < 4 || f->nsb > f->ns) f->nsb = f->ns < 7 ? f->ns : 7;
     f->umma = !(mode && std::strcmp(mode, "sync") == 0) && f->ns >= 6;
     const char *ps = std::getenv("GBCODEML_PERSIST");
-    f->persist = f->umma && !(ps && std::strcmp(ps, "0") == 0);
+    f->persist = !(ps && std::strcmp(ps, "0") == 0);
+    if (h->tune.mma >= 0) f->umma = h->tune.mma != 0 && f->ns >= 6;
+    if (h->tune.persist >= 0) f->persist = h->tune.persist != 0;
+    f->persist = f->persist && f->umma;
     const size_t nflag = (size_t)h->nslot * (npad / FAST_MT);
     if ((rc = dalloc(&f->ready_f, nflag)) || (rc = dalloc(&f->ready_b, nflag))) return rc;
     CK(cudaMemset(f->ready_f, 0, sizeof(unsigned) * std::max<size_t>(nflag, 1)));
@@ -169,7 +172,7 @@ FastBwdArgs bwd_args(gb_handle *h) {
     b.Gpart = ad->d_Gpart;
     b.err = f->err;
     b.nsP = f->ns;
-    b.gchunk = GCHUNK;
+    b.gchunk = ad->gchunk;
     b.ready = f->ready_b;
     b.ntile = h->npad / FAST_MT;
     b.Pdf = f->Pdf;
@@ -236,7 +239,7 @@ int ensure_bwd_graph(gb_handle *h) {
     if (rc) return rc;
     if (f->persist) {
         gb_handle *one[1] = {h};
-        if ((rc = persist_build(&f->plan, one, 1, true))) return rc;
+        if ((rc = persist_build(&f->plan, one, 1, true, h->tune))) return rc;
     }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -256,7 +259,7 @@ int ensure_fast_graph(gb_handle *h, bool keepE) {
     if (rc) return rc;
     if (f->persist) {
         gb_handle *one[1] = {h};
-        if ((rc = persist_build(&f->plan, one, 1, keepE))) return rc;
+        if ((rc = persist_build(&f->plan, one, 1, keepE, h->tune))) return rc;
     }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
@@ -280,14 +283,16 @@ void persist_free(PersistPlan *pp) {
     *pp = PersistPlan();
 }
 
-int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd) {
+int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const Tuning &tune) {
     int rc;
     if (!pp->ctl) {
         if ((rc = dalloc(&pp->ctl, CTL_WORDS))) return rc;
         CK(cudaMemset(pp->ctl, 0, sizeof(unsigned) * CTL_WORDS));
-        int dev = 0;
+        int dev = 0, nsm = 1;
         CK(cudaGetDevice(&dev));
-        CK(cudaDeviceGetAttribute(&pp->nblock, cudaDevAttrMultiProcessorCount, dev));
+        CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+        // one CTA per SM at most (the kernels' shared memory allows no more)
+        pp->nblock = tune.grid > 0 ? std::min(tune.grid, nsm) : nsm;
         pp->ngene = n;
     }
     if (pp->ngene != n) return fail(GB_ERR_STATE, "persistent plan: gene count changed");
@@ -299,18 +304,24 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd) {
         CK(cudaMemcpy(pp->d_fargs[k], fa.data(), sizeof(FastFwdArgs) * n, cudaMemcpyHostToDevice));
     }
     if (!pp->d_ftask) {
-        // children before parents: level by level (tree height), all genes per level
+        // children before parents: level by level (tree height), all genes per
+        // level (order 0) or gene by gene (order 1)
         std::vector<Task> t;
+        auto push_level = [&](int g, int L) {
+            const gb_handle *h = hs[g];
+            if (L + 1 >= (int)h->level_off.size()) return;
+            const int nt = h->npad / FAST_MT;
+            for (int i = h->level_off[L]; i < h->level_off[L + 1]; i++)
+                for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, 0});
+        };
         int maxH = 0;
         for (int g = 0; g < n; g++) maxH = std::max(maxH, (int)hs[g]->level_off.size() - 1);
-        for (int L = 0; L < maxH; L++)
-            for (int g = 0; g < n; g++) {
-                const gb_handle *h = hs[g];
-                if (L + 1 >= (int)h->level_off.size()) continue;
-                const int nt = h->npad / FAST_MT;
-                for (int i = h->level_off[L]; i < h->level_off[L + 1]; i++)
-                    for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, 0});
-            }
+        if (tune.order == 1)
+            for (int g = 0; g < n; g++)
+                for (int L = 0; L < maxH; L++) push_level(g, L);
+        else
+            for (int L = 0; L < maxH; L++)
+                for (int g = 0; g < n; g++) push_level(g, L);
         pp->nftask = (int)t.size();
         const char *tr = std::getenv("GBCODEML_TRACE");
         pp->tracing = tr && std::strcmp(tr, "1") == 0;
@@ -329,16 +340,21 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd) {
     if (!pp->d_btask) {
         // parents before children: backward levels from each gene's root down
         std::vector<Task> t;
+        auto push_blevel = [&](int g, int d) {
+            const AdjointState *ad = hs[g]->adj;
+            if (d + 1 >= (int)ad->blevel_off.size()) return;
+            const int nt = hs[g]->npad / FAST_MT;
+            for (int i = ad->blevel_off[d]; i < ad->blevel_off[d + 1]; i++)
+                for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, 0});
+        };
         int maxB = 0;
         for (int g = 0; g < n; g++) maxB = std::max(maxB, (int)hs[g]->adj->blevel_off.size() - 1);
-        for (int d = 0; d < maxB; d++)
-            for (int g = 0; g < n; g++) {
-                const AdjointState *ad = hs[g]->adj;
-                if (d + 1 >= (int)ad->blevel_off.size()) continue;
-                const int nt = hs[g]->npad / FAST_MT;
-                for (int i = ad->blevel_off[d]; i < ad->blevel_off[d + 1]; i++)
-                    for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, 0});
-            }
+        if (tune.order == 1)
+            for (int g = 0; g < n; g++)
+                for (int d = 0; d < maxB; d++) push_blevel(g, d);
+        else
+            for (int d = 0; d < maxB; d++)
+                for (int g = 0; g < n; g++) push_blevel(g, d);
         pp->nbtask = (int)t.size();
         if (pp->tracing && (rc = dalloc(&pp->trace[1], 4 * t.size()))) return rc;
         if ((rc = dalloc(&pp->d_btask, t.size()))) return rc;
@@ -350,7 +366,7 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd) {
             const AdjointState *ad = h->adj;
             for (int p = 0; p < (int)h->pairs.size(); p++)
                 for (int c = 0; c < ad->nchunk; c++) {
-                    const long np = std::min(h->npatt, (c + 1) * GCHUNK) - c * GCHUNK;
+                    const long np = std::min(h->npatt, (c + 1) * ad->gchunk) - c * ad->gchunk;
                     gt.push_back({(long)(ad->coff[p + 1] - ad->coff[p]) * np, Task{g, p, c, 0}});
                 }
         }

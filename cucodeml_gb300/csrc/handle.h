@@ -60,8 +60,15 @@ void fast_free(FastState *f);
 
 }  // namespace gb
 
+namespace gb {
+struct Tuning {                     // gb_tune knobs; -1 / 0: default
+    int mma = -1, persist = -1, gchunk = 0, order = 0, grid = 0;
+};
+}  // namespace gb
+
 struct gb_handle {
     int device = 0;
+    gb::Tuning tune;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int ns = 0, nnode = 0, root = 0, npatt = 0, npad = 0, ntile = 0, precision = 0;
@@ -131,7 +138,7 @@ int persist_task_trace(PersistPlan *pp, int kernel, unsigned long long *out, int
 int fast_ns(const gb_handle *h, bool adjoint);
 // persistent executors over one or many genes (fast.cu)
 void persist_free(PersistPlan *pp);
-int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd);
+int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const Tuning &tune);
 int persist_record_fwd(PersistPlan *pp, bool keepE, int ns, cudaStream_t st, gb_handle *prof);
 int persist_record_bwd(PersistPlan *pp, int nsb, cudaStream_t st, gb_handle *prof);
 // forward pass on the handle's stream (runtime.cu); keepE keeps the edge

@@ -202,7 +202,7 @@ __global__ void __launch_bounds__(256, 1) gradP_fast_kernel(FastBwdArgs a) {
 #pragma unroll
         for (int q = 0; q < 4; q++) acc[nt][q] = 0.0;
     for (int i = tid; i < 64 * 65; i += 256) Gs[i] = 0.0;
-    const int hbeg = chunk * GCHUNK, hend = min(a.npatt, hbeg + GCHUNK);
+    const int hbeg = chunk * a.gchunk, hend = min(a.npatt, hbeg + a.gchunk);
     for (int ci = a.coff[p]; ci < a.coff[p + 1]; ci++) {
         const Contrib cb = a.contrib[ci];
         for (int hb = hbeg; hb < hend; hb += GSUB) {

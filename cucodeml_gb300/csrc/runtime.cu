@@ -558,6 +558,32 @@ int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches
     return GB_OK;
 }
 
+int gb_tune(gb_handle *h, int knob, int value) {
+    if (!h) return fail(GB_ERR_ARG, "gb_tune: null handle");
+    if (h->fast || h->adj) return fail(GB_ERR_STATE, "gb_tune: handle already evaluated");
+    switch (knob) {
+        case GB_TUNE_MMA:
+        case GB_TUNE_PERSIST:
+            if (value != 0 && value != 1) return fail(GB_ERR_ARG, "gb_tune: value must be 0 or 1");
+            (knob == GB_TUNE_MMA ? h->tune.mma : h->tune.persist) = value;
+            return GB_OK;
+        case GB_TUNE_GCHUNK:
+            if (value < 64 || value > 8192 || value % 64) return fail(GB_ERR_ARG, "gb_tune: chunk must be a multiple of 64 in [64, 8192]");
+            h->tune.gchunk = value;
+            return GB_OK;
+        case GB_TUNE_ORDER:
+            if (value != 0 && value != 1) return fail(GB_ERR_ARG, "gb_tune: order must be 0 or 1");
+            h->tune.order = value;
+            return GB_OK;
+        case GB_TUNE_GRID:
+            if (value < 0) return fail(GB_ERR_ARG, "gb_tune: grid must be >= 0");
+            h->tune.grid = value;
+            return GB_OK;
+        default:
+            return fail(GB_ERR_ARG, "gb_tune: unknown knob");
+    }
+}
+
 int gb_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap) {
     if (!h || cap < 0) return fail(GB_ERR_ARG, "gb_task_trace: bad arguments");
     return fast_task_trace(h, kernel, out, cap);

@@ -210,6 +210,27 @@ int gb_replay(gb_handle *h, int iters, int with_grad, double *ms);
 int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches);
 
 /*
+ * Tuning knobs of the split-precision path (no counterpart in the reference),
+ * set before the first evaluation of a handle or batch (GB_ERR_STATE after):
+ *   GB_TUNE_MMA      0: mma.sync contractions, 1: tcgen05 (default)
+ *   GB_TUNE_PERSIST  0: one launch per tree level, 1: persistent task-list
+ *                    kernels (default; tcgen05 only)
+ *   GB_TUNE_GCHUNK   patterns per partial sum of dlnL/dP (multiple of 64 in
+ *                    [64, 8192]; default 512)
+ *   GB_TUNE_ORDER    batches: 0 tasks ordered by tree level across genes
+ *                    (default), 1 gene by gene
+ *   GB_TUNE_GRID     CTAs per persistent launch (0: one per SM, the default)
+ * Environment defaults: GBCODEML_MMA=sync, GBCODEML_PERSIST=0.
+ */
+#define GB_TUNE_MMA     1
+#define GB_TUNE_PERSIST 2
+#define GB_TUNE_GCHUNK  3
+#define GB_TUNE_ORDER   4
+#define GB_TUNE_GRID    5
+int gb_tune(gb_handle *h, int knob, int value);
+int gb_batch_tune(gb_batch *b, int knob, int value);
+
+/*
  * Task trace of the persistent split-precision kernels (no counterpart in the
  * reference): with GBCODEML_TRACE=1 in the environment when the handle's
  * kernels are first set up, every task of the last evaluation records, from

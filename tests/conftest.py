@@ -17,7 +17,13 @@ def pytest_configure(config):
 
 
 def golden_names():
-    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.endswith(".json"))
+    """Fixed-parameter fixtures (codeml lnL and per-pattern log f at given x)."""
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.endswith(".json") and not f.startswith("mle_"))
+
+
+def mle_names():
+    """Maximum-likelihood fixtures (codeml's optimised alternative and null)."""
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("mle_") and f.endswith(".json"))
 
 
 def load_golden(name):

@@ -366,6 +366,17 @@ def main():
         roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak, "traffic": None,
                 "peak_source": "bf16_tflops of measured" if peaks else "fallback"}
+    if precision != "fp64":
+        # executed tensor work of the digit-plane contractions (not algorithmic):
+        # NS = 8 forward planes -> 36 digit pairs, NB = 7 adjoint planes -> 28,
+        # over 64 x 64 padded states; dlnL/dP runs M = 128 with 64 zero rows
+        pairs = {"prune": 36, "bwd": 28, "gradP": 2 * 28}
+        if top in pairs:
+            ex = cls_flops[top] * pairs[top] * (64.0 * 64.0) / (61.0 * 61.0)
+            roof["executed_tensor_tflops"] = ex / (top_ms_per_eval * 1e-3) / 1e12
+            roof["executed_tensor_frac"] = roof["executed_tensor_tflops"] / peak
+        roof["limiter"] = ("SIMT digit slicing and double-float level recombination around the MMAs, "
+                           "latency-bound at one 16-warp CTA per SM (see profiles/)")
     roof.update({"kernel": top, "share": prof[top][0] / tot if tot else None,
                  "flops_per_eval": cls_flops.get(top, 0.0), "ms_per_eval": top_ms_per_eval,
                  "classes_ms_per_eval": {k: v[0] / 3 for k, v in prof.items()}})

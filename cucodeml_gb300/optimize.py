@@ -129,13 +129,15 @@ def lrt(lnl_alt: float, lnl_null: float) -> dict:
 
 
 def alt_null(tree, z, fpatt, pi, precision: str = "fast", gradient: str = "adjoint", x0_alt=None,
-             gtol: float = 1e-6) -> dict:
-    """Fit the alternative (w2 free) and the null (w2 = 1) from the same start."""
+             gtol: float = 1e-6, x0_null=None) -> dict:
+    """Fit the alternative (w2 free) and the null (w2 = 1) from the same start
+    (or from x0_alt / x0_null, e.g. another precision's maxima)."""
     lk = api.Likelihood(tree, z, fpatt, pi, precision=precision)
     try:
         xa = initial_x(tree) if x0_alt is None else np.asarray(x0_alt, dtype=np.float64)
+        xn = xa[:-1] if x0_null is None else np.asarray(x0_null, dtype=np.float64)[:len(xa) - 1]
         alt = fit(lk, xa, False, gradient, gtol)
-        null = fit(lk, xa[:-1], True, gradient, gtol)
+        null = fit(lk, xn, True, gradient, gtol)
         # the null maximum is feasible for the alternative (w2 = 1): restart the
         # alternative there if it ended lower (a local optimum)
         if alt["lnL"] < null["lnL"]:
@@ -157,6 +159,8 @@ def main(argv=None):
     ap.add_argument("--precision", nargs="+", default=["fast", "fp64"])
     ap.add_argument("--gradient", default="adjoint", choices=["adjoint", "fd"])
     ap.add_argument("--gtol", type=float, default=1e-6)
+    ap.add_argument("--polish", action="store_true",
+                    help="after each non-FP64 fit, continue with the FP64 path from its maxima")
     ap.add_argument("--out", default=None, help="write the JSON result here as well")
     ap.add_argument("--fd-sample", type=int, default=24,
                     help="lnL evaluations timed per precision to cost codeml's finite-difference "
@@ -170,6 +174,13 @@ def main(argv=None):
            "patterns": int(len(fp)), "setup_seconds": time.perf_counter() - t0, "fits": []}
     for prec in a.precision:
         r = alt_null(aln.tree, z, fp, pi, precision=prec, gradient=a.gradient, gtol=a.gtol)
+        if a.polish and prec != "fp64":
+            # continue with the FP64 path from this precision's maxima
+            p = alt_null(aln.tree, z, fp, pi, precision="fp64", gradient=a.gradient, gtol=a.gtol,
+                         x0_alt=r["alt"]["x"], x0_null=r["null"]["x"])
+            r["fp64_polish"] = {m: {k2: p[m][k2] for k2 in ("lnL", "calls", "seconds", "omega2", "converged")}
+                                for m in ("alt", "null")}
+            r["fp64_polish"]["LRT"] = p["LRT"]
         if a.fd_sample > 0:
             # finite differences cost np lnL evaluations per gradient: time a sample
             lk = api.Likelihood(aln.tree, z, fp, pi, precision=prec)

@@ -30,6 +30,7 @@
 
 #include "handle.h"
 #include "adjoint_internal.h"
+#include "fast_device.cuh"
 
 namespace gb {
 
@@ -46,16 +47,28 @@ constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256 + 64) * sizeof(double);
 // the inverse eigenvalue differences of each w (for Phi)
 __global__ void __launch_bounds__(256) dmat_kernel(const DevParams *__restrict__ prm,
                                                    const GradParams *__restrict__ gp,
-                                                   double *__restrict__ Dm) {
+                                                   double *__restrict__ Dm, float2 *__restrict__ UVdf) {
     __shared__ double T[61 * 62];
     const int which = blockIdx.x;   // 0,1,2: kappa for w; 3: omega w0; 4: omega w2; 5,6,7: 1/(Root_m - Root_n) for w
     if (which >= 5) {
-        const double *R = prm->Root[which - 5];
+        const int w = which - 5;
+        const double *R = prm->Root[w];
         double *out = Dm + (size_t)which * 64 * 64;
         for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
             const int r = i / 64, c = i % 64;
             const double d = (r < 61 && c < 61) ? R[r] - R[c] : 0.0;
             out[i] = d != 0.0 ? 1.0 / d : 0.0;
+        }
+        if (UVdf) {   // V^T [k][n] and U [j][m] of this w as double-float, 64-column rows
+            float2 *vt = UVdf + (size_t)w * 2 * 61 * 64, *u = vt + 61 * 64;
+            for (int i = threadIdx.x; i < 61 * 64; i += blockDim.x) {
+                const int r = i / 64, c = i % 64;
+                const double a = c < 61 ? prm->V[w][c * 61 + r] : 0.0;
+                const double b = c < 61 ? prm->U[w][r * 61 + c] : 0.0;
+                const float ah = (float)a, bh = (float)b;
+                vt[i] = make_float2(ah, (float)(a - (double)ah));
+                u[i] = make_float2(bh, (float)(b - (double)bh));
+            }
         }
         return;
     }
@@ -349,8 +362,9 @@ __global__ void __launch_bounds__(256) gradH_df_kernel(const PairDesc *__restric
                                                        const int *__restrict__ label,
                                                        const double *__restrict__ tnode,
                                                        const DevParams *__restrict__ prm,
-                                                       const double *__restrict__ Gpart, int nchunk,
+                                                       const float2 *__restrict__ Gpart, int nchunk,
                                                        const double *__restrict__ Dm,
+                                                       const float2 *__restrict__ UVdf,
                                                        double *__restrict__ out) {
     extern __shared__ __align__(16) unsigned char smr[];
     float2 *GT = reinterpret_cast<float2 *>(smr);          // [61][64] G, then T
@@ -362,18 +376,17 @@ __global__ void __launch_bounds__(256) gradH_df_kernel(const PairDesc *__restric
     const PairDesc pd = pairs[p];
     const int w = pd.w;
     const double tp = tnode[pd.node] * prm->qf[label[pd.node]];
-    const double *U = prm->U[w];
-    const double *V = prm->V[w];
     const double *R = prm->Root[w];
     if (tid < 61) ex[tid] = exp(tp * R[tid]);
-    for (int i = tid; i < 61 * 64; i += blockDim.x) {
-        const int r = i / 64, c = i % 64;
-        double g = 0.0;
-        if (c < 61)
-            for (int q = 0; q < nchunk; q++) g += Gpart[((size_t)p * nchunk + q) * 64 * 64 + r * 64 + c];
-        GT[i] = df_of(g);
-        Vt[i] = c < 61 ? df_of(V[c * 61 + r]) : make_float2(0.f, 0.f);
-        Us[i] = c < 61 ? df_of(U[r * 61 + c]) : make_float2(0.f, 0.f);
+    {   // V^T and U of this w, already double-float (dP/dt kernel)
+        const float4 *src = reinterpret_cast<const float4 *>(UVdf + (size_t)w * 2 * 61 * 64);
+        float4 *dst = reinterpret_cast<float4 *>(Vt);
+        for (int i = tid; i < 61 * 64; i += blockDim.x) dst[i] = src[i];
+    }
+    for (int i = tid; i < 61 * 64; i += blockDim.x) {      // G = sum of the chunk partials
+        float2 g = make_float2(0.f, 0.f);
+        for (int q = 0; q < nchunk; q++) g = fastdev::df_add(g, Gpart[((size_t)p * nchunk + q) * 64 * 64 + i]);
+        GT[i] = (i % 64) < 61 ? g : make_float2(0.f, 0.f);
     }
     __syncthreads();
     const int r = tid >> 2, c0 = (tid & 3) * 16;
@@ -468,7 +481,7 @@ void adjoint_free(AdjointState *a) {
     if (!a) return;
     if (a->graph) cudaGraphExecDestroy(a->graph);
     void *dev[] = {a->d_bitems, a->d_contrib, a->d_coff, a->d_Ebar, a->d_Abar, a->d_Gpart,
-                   a->d_Dm, a->d_pout, a->d_fpart, a->d_gp};
+                   a->d_Dm, a->d_pout, a->d_fpart, a->d_gp, a->d_UVdf};
     for (void *p : dev)
         if (p) cudaFree(p);
     if (a->h_gp) cudaFreeHost(a->h_gp);
@@ -543,7 +556,8 @@ int adjoint_init(gb_handle *h) {
         (rc = dalloc(&a->d_Ebar, (size_t)h->nslot * MAXC * npad * 64)) ||
         (rc = dalloc(&a->d_Abar, (size_t)h->nslot * npad * 64)) ||
         (rc = dalloc(&a->d_Gpart, h->pairs.size() * a->nchunk * 64 * 64)) ||
-        (rc = dalloc(&a->d_Dm, DM_BLOCKS * 64 * 64)) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
+        (rc = dalloc(&a->d_Dm, DM_BLOCKS * 64 * 64)) ||
+        (h->precision != GB_PREC_FP64 && (rc = dalloc(&a->d_UVdf, 3 * 2 * 61 * 64))) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
         (rc = dalloc(&a->d_fpart, a->nfreq_blocks * 4)) || (rc = dalloc(&a->d_gp, 1)))
         return rc;
     if (cudaMallocHost((void **)&a->h_gp, sizeof(GradParams)) ||
@@ -563,7 +577,7 @@ int adjoint_init(gb_handle *h) {
 }
 
 void launch_dmat(gb_handle *h) {
-    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, h->adj->d_gp, h->adj->d_Dm);
+    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, h->adj->d_gp, h->adj->d_Dm, h->adj->d_UVdf);
 }
 
 void launch_gradH(gb_handle *h) {
@@ -576,7 +590,8 @@ void launch_gradH(gb_handle *h) {
 void launch_gradH_df(gb_handle *h) {
     AdjointState *a = h->adj;
     gradH_df_kernel<<<(unsigned)h->pairs.size(), 256, kGradHdfSmem, h->stream>>>(
-        h->d_pairs, h->d_label, h->d_tnode, h->d_prm, a->d_Gpart, a->nchunk, a->d_Dm, a->d_pout);
+        h->d_pairs, h->d_label, h->d_tnode, h->d_prm, reinterpret_cast<const float2 *>(a->d_Gpart), a->nchunk,
+        a->d_Dm, a->d_UVdf, a->d_pout);
 }
 
 void launch_freq(gb_handle *h, int nscale) {
@@ -590,7 +605,7 @@ namespace {
 int record_backward(gb_handle *h) {
     AdjointState *a = h->adj;
     int nk = 0;
-    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, a->d_gp, a->d_Dm);
+    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, a->d_gp, a->d_Dm, nullptr);
     prof_mark(h, GB_K_OTHER);
     nk++;
     for (size_t L = 0; L + 1 < a->blevel_off.size(); L++) {

@@ -47,6 +47,7 @@ struct AdjointState {
     int *d_coff = nullptr;
     double *d_Ebar = nullptr, *d_Abar = nullptr, *d_Gpart = nullptr, *d_Dm = nullptr;
     double *d_pout = nullptr, *d_fpart = nullptr;
+    float2 *d_UVdf = nullptr;        // split precision: [3][2][61][64] V^T and U as double-float
     GradParams *d_gp = nullptr, *h_gp = nullptr;
     double *h_pout = nullptr, *h_fpart = nullptr;
     cudaGraphExec_t graph = nullptr;

@@ -169,7 +169,8 @@ FastBwdArgs bwd_args(gb_handle *h) {
     b.contrib = ad->d_contrib;
     b.coff = ad->d_coff;
     b.z = h->d_z;
-    b.Gpart = ad->d_Gpart;
+    // the FP64 partials buffer holds 8 bytes per element: reused as double-float
+    b.Gpart = reinterpret_cast<float2 *>(ad->d_Gpart);
     b.err = f->err;
     b.nsP = f->ns;
     b.gchunk = ad->gchunk;

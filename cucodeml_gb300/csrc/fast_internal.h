@@ -75,7 +75,7 @@ struct FastBwdArgs {
     const Contrib *contrib;
     const int *coff;
     const unsigned char *z;
-    double *Gpart;               // [npair][nchunk][64][64]
+    float2 *Gpart;               // [npair][nchunk][64][64] dlnL/dP partials, double-float
     int *err;
     int nsP;                     // digit planes stored per pair in Bb
     int gchunk;                  // patterns per dlnL/dP partial

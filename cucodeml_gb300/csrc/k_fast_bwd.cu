@@ -266,14 +266,16 @@ __global__ void __launch_bounds__(256, 1) gradP_fast_kernel(FastBwdArgs a) {
         }
     }
     __syncthreads();
-    double *out = a.Gpart + ((size_t)p * a.nchunk + chunk) * 64 * 64;
+    float2 *out = a.Gpart + ((size_t)p * a.nchunk + chunk) * 64 * 64;
 #pragma unroll
     for (int nt = 0; nt < 4; nt++)
 #pragma unroll
         for (int q = 0; q < 4; q++) {
             const int j = mrow + g + 8 * (q >> 1);
             const int k = ncol + nt * 8 + 2 * t + (q & 1);
-            out[j * 64 + k] = acc[nt][q] + Gs[j * 65 + k];
+            const double v = acc[nt][q] + Gs[j * 65 + k];
+            const float hi = (float)v;
+            out[j * 64 + k] = make_float2(hi, (float)(v - (double)hi));
         }
 }
 

@@ -65,8 +65,8 @@ struct GSm {
     static constexpr int OFF_B = NB * A_PLANE;
     static constexpr int PLANES = NB * (A_PLANE + B_PLANE);
     static constexpr int OFF_MISC = PLANES > 4 * 4096 * 8 ? PLANES : 4 * 4096 * 8;   // also holds the tip partials
-    static constexpr int OFF_XS = OFF_MISC + 64;              // int [64] exponents
-    static constexpr int OFF_RED = OFF_XS + 256;              // int [16] reductions
+    static constexpr int OFF_XS = OFF_MISC + 64;              // int [128] exponents
+    static constexpr int OFF_RED = OFF_XS + 512;              // int [16] reductions
     static constexpr int OFF_ARGS = OFF_RED + 64;
     static constexpr int NEED = OFF_ARGS + ARGS_BYTES;
     static constexpr int BYTES = NEED > MIN_SMEM ? NEED : MIN_SMEM;
@@ -169,7 +169,8 @@ __device__ __forceinline__ void start_B(const __nv_bfloat16 *__restrict__ B, uns
 // Shared-memory descriptor start addresses are in 16-byte units in the low
 // 14 bits, so plane and K-step offsets are added to the base descriptors.
 template <int NS>
-__device__ __forceinline__ void issue_levels(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t leader) {
+__device__ __forceinline__ void issue_levels(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t leader,
+                                             uint32_t accumulate) {
     constexpr uint32_t idesc = umma::make_idesc(128, 64);
 #pragma unroll
     for (int L = 2; L <= NS + 1; L++) {
@@ -182,7 +183,8 @@ __device__ __forceinline__ void issue_levels(uint32_t tmem, uint64_t adesc, uint
             for (int ks = 0; ks < 4; ks++) {
                 const uint64_t ad = adesc + (uint64_t)(((i - 1) * A_PLANE + ks * 256) >> 4);
                 const uint64_t bd = bdesc + (uint64_t)(((j - 1) * B_PLANE + ks * 256) >> 4);
-                umma::mma_bf16_leader(tmem + (L - 2) * 64, ad, bd, idesc, (i == ilo && ks == 0) ? 0u : 1u, leader);
+                umma::mma_bf16_leader(tmem + (L - 2) * 64, ad, bd, idesc, (i == ilo && ks == 0) ? accumulate : 1u,
+                                      leader);
             }
         }
     }
@@ -190,50 +192,62 @@ __device__ __forceinline__ void issue_levels(uint32_t tmem, uint64_t adesc, uint
 
 // All threads: the A planes in shared memory are complete (generic-proxy
 // stores); the B planes are complete or, with wait_b, arriving by bulk copy.
-// Warp 0 issues the MMAs and commits; every thread waits (bounded) and reads
-// its row's 16 columns of every level, accumulating
-//   C = (init ? 0 : C 2^sc_in) + 2^sc_new sum_L S_L 2^(-7L)
-// in double-float (exact power-of-two scalings).  Returns a block-uniform
-// success flag.
+// Warp 0 issues the MMAs (into the level accumulators, or adding to them with
+// accumulate) and commits; every thread waits (bounded).  Returns a
+// block-uniform success flag; the accumulators are then complete.
 template <int NS>
-__device__ __forceinline__ bool contract(unsigned char *sm, Misc *m, uint32_t &phase, float2 (&C)[NCOL],
-                                         int off_b, bool wait_b, bool init = true, int sc_in = 0,
-                                         int sc_new = 0) {
+__device__ __forceinline__ bool mma_round(unsigned char *sm, Misc *m, uint32_t &phase, int off_b, bool wait_b,
+                                          bool accumulate) {
     umma::fence_proxy_async();
     umma::fence_before();
     __syncthreads();
-    const int warp = threadIdx.x >> 5;
-    if (warp == 0) {
+    if ((threadIdx.x >> 5) == 0) {
         umma::fence_after();
         const bool okb = !wait_b || umma::mbar_wait(&m->mbar_b, phase);
         const uint32_t leader = umma::elect_one();
         if (okb)
             issue_levels<NS>(m->tmem, umma::make_desc(umma::smem_u32(sm)), umma::make_desc(umma::smem_u32(sm + off_b)),
-                             leader);
+                             leader, accumulate ? 1u : 0u);
         if (leader) {
             umma::commit(&m->mbar);
             m->okb = okb;
         }
     }
-    const int col = NCOL * (warp >> 2);
     bool ok = umma::mbar_wait(&m->mbar, phase);
     umma::fence_after();
-    if (ok) {
-        const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
-#pragma unroll
-        for (int c = 0; c < NCOL; c++) C[c] = init ? make_float2(0.f, 0.f) : df_scale(C[c], sc_in);
-#pragma unroll 1
-        for (int L = NS + 1; L >= 2; L--) {
-            float v[NCOL];
-            umma::tmem_ld16(m->tmem + lane_base + (L - 2) * 64 + col, v);
-            const float w = scalbnf(1.0f, -7 * L + sc_new);
-#pragma unroll
-            for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(v[c] * w, 0.f));
-        }
-    }
     phase ^= 1u;
-    umma::fence_before();
     ok = __syncthreads_and(ok) && m->okb;
+    return ok;
+}
+
+// Every thread reads its row's 16 columns of every level and accumulates
+//   C = (init ? 0 : C 2^sc_in) + 2^sc_new sum_L S_L 2^(-7L)
+// in double-float (exact power-of-two scalings).
+template <int NS>
+__device__ __forceinline__ void readout(Misc *m, float2 (&C)[NCOL], bool init, int sc_in, int sc_new) {
+    const int warp = threadIdx.x >> 5;
+    const int col = NCOL * (warp >> 2);
+    const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+#pragma unroll
+    for (int c = 0; c < NCOL; c++) C[c] = init ? make_float2(0.f, 0.f) : df_scale(C[c], sc_in);
+#pragma unroll 1
+    for (int L = NS + 1; L >= 2; L--) {
+        float v[NCOL];
+        umma::tmem_ld16(m->tmem + lane_base + (L - 2) * 64 + col, v);
+        const float w = scalbnf(1.0f, -7 * L + sc_new);
+#pragma unroll
+        for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(v[c] * w, 0.f));
+    }
+    umma::fence_before();
+}
+
+// one contraction: MMA round and read-out
+template <int NS>
+__device__ __forceinline__ bool contract(unsigned char *sm, Misc *m, uint32_t &phase, float2 (&C)[NCOL],
+                                         int off_b, bool wait_b, bool init = true, int sc_in = 0,
+                                         int sc_new = 0) {
+    const bool ok = mma_round<NS>(sm, m, phase, off_b, wait_b, false);
+    if (ok) readout<NS>(m, C, init, sc_in, sc_new);
     return ok;
 }
 
@@ -312,25 +326,37 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
     bool ok = true;
     float2 prod[NCOL];
     int expo = 0;
-    for (int ci = 0; ci < it.nchild && ok; ci++) {
-        float2 E[NCOL];
-        const int cs = it.cslot[ci];
-        if (cs < 0) {
-            const int zc = a.z[(size_t)it.child[ci] * npad + h];
-            load_row32(a.Pdf + (size_t)it.pidx[ci] * 4096 + zc * 64 + c0, E);
-        } else {
-            __syncthreads();                               // the previous contraction's planes are free
-            start_B<NS>(a.Bf + (size_t)it.pidx[ci] * NS * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
-            slice_A_cm<NS>(a.conP + ((size_t)cs * npad + h0) * 64, sm);
-            ok = contract<NS>(sm, m, phase, E, USm<NS>::OFF_B, true);
-            if (!ok) break;
-            expo += __ldcg(a.expo + (size_t)cs * npad + h);
-        }
-        // edge messages of internal children are kept for the adjoint; a tip's
-        // message is a row of P, gathered again there
-        if (a.E && cs >= 0) store_row32(a.E + ((size_t)(it.eslot + ci) * npad + h) * 64 + c0, E);
+    bool have = false;
+    // tip children first: their codons, then their rows of P (a tip's edge
+    // message, not stored: the adjoint gathers it again)
+    int zc[MAXC];
 #pragma unroll
-        for (int c = 0; c < NCOL; c++) prod[c] = ci == 0 ? E[c] : df_mul(prod[c], E[c]);
+    for (int ci = 0; ci < MAXC; ci++)
+        zc[ci] = (ci < it.nchild && it.cslot[ci] < 0) ? a.z[(size_t)it.child[ci] * npad + h] : 0;
+#pragma unroll
+    for (int ci = 0; ci < MAXC; ci++) {
+        if (ci >= it.nchild || it.cslot[ci] >= 0) continue;
+        float2 E[NCOL];
+        load_row32(a.Pdf + (size_t)it.pidx[ci] * 4096 + zc[ci] * 64 + c0, E);
+#pragma unroll
+        for (int c = 0; c < NCOL; c++) prod[c] = have ? df_mul(prod[c], E[c]) : E[c];
+        have = true;
+    }
+    for (int ci = 0; ci < it.nchild && ok; ci++) {
+        const int cs = it.cslot[ci];
+        if (cs < 0) continue;
+        float2 E[NCOL];
+        __syncthreads();                                   // the previous contraction's planes are free
+        start_B<NS>(a.Bf + (size_t)it.pidx[ci] * NS * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
+        slice_A_cm<NS>(a.conP + ((size_t)cs * npad + h0) * 64, sm);
+        ok = contract<NS>(sm, m, phase, E, USm<NS>::OFF_B, true);
+        if (!ok) break;
+        expo += __ldcg(a.expo + (size_t)cs * npad + h);
+        // edge messages of internal children are kept for the adjoint
+        if (a.E) store_row32(a.E + ((size_t)(it.eslot + ci) * npad + h) * 64 + c0, E);
+#pragma unroll
+        for (int c = 0; c < NCOL; c++) prod[c] = have ? df_mul(prod[c], E[c]) : E[c];
+        have = true;
     }
     if (!ok) {
         on_failure(a.err, m, phase, true);
@@ -452,6 +478,15 @@ __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsign
     for (int i = 0; i < it.nchild && ok; i++) {
         for (int k = 0; k < it.ncls; k++) {
             const int c = it.cls[k];
+            // the first sibling's message is requested before the upper partial
+            const int s1 = i == 0 ? 1 : 0;
+            float2 Ev[NCOL];
+            if (it.tslot[s1][k] < 0) {
+                const int zs = a.z[(size_t)it.child[s1] * npad + h];
+                load_row32(a.Pdf + (size_t)it.pidx[s1][k] * 4096 + zs * 64 + c0, Ev);
+            } else {
+                load_row32(a.E + ((size_t)(it.pslot[k] * MAXC + s1) * npad + h) * 64 + c0, Ev);
+            }
             float2 X[NCOL];
             int eX;
             if (it.is_root) {
@@ -468,14 +503,15 @@ __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsign
                 const int ea = __ldcg(a.aexp + (size_t)it.pslot[k] * npad + h);
                 eX = ea == ZERO_EXP ? ZERO_EXP : ea + eAs[k];
             }
-            for (int i2 = 0; i2 < it.nchild; i2++) {
-                if (i2 == i) continue;
-                float2 Ev[NCOL];
-                if (it.tslot[i2][k] < 0) {
-                    const int zc = a.z[(size_t)it.child[i2] * npad + h];
-                    load_row32(a.Pdf + (size_t)it.pidx[i2][k] * 4096 + zc * 64 + c0, Ev);
+#pragma unroll
+            for (int q = 0; q < NCOL; q++) X[q] = df_mul(X[q], Ev[q]);
+            if (it.nchild == 3) {                            // the root's second sibling
+                const int s2 = 3 - i - s1;
+                if (it.tslot[s2][k] < 0) {
+                    const int zs = a.z[(size_t)it.child[s2] * npad + h];
+                    load_row32(a.Pdf + (size_t)it.pidx[s2][k] * 4096 + zs * 64 + c0, Ev);
                 } else {
-                    load_row32(a.E + ((size_t)(it.pslot[k] * MAXC + i2) * npad + h) * 64 + c0, Ev);
+                    load_row32(a.E + ((size_t)(it.pslot[k] * MAXC + s2) * npad + h) * 64 + c0, Ev);
                 }
 #pragma unroll
                 for (int q = 0; q < NCOL; q++) X[q] = df_mul(X[q], Ev[q]);
@@ -628,9 +664,9 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
     atomicMax(&red[0], xl);
     __syncthreads();
     const int xr = red[0];
-    double *out = a.Gpart + ((size_t)p * a.nchunk + chunk) * 64 * 64;
+    float2 *out = a.Gpart + ((size_t)p * a.nchunk + chunk) * 64 * 64;
     if (xr == ZERO_EXP) {
-        for (int i = tid; i < 4096; i += NT) out[i] = 0.0;
+        for (int i = tid; i < 4096; i += NT) out[i] = make_float2(0.f, 0.f);
         return true;
     }
     // A rows 64..127 of every plane are zero (the tip partials below overwrite them)
@@ -650,51 +686,61 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
             any_tip = true;
             continue;
         }
-        for (int hb = hbeg; hb < hend && ok; hb += 64) {
-            const int nh = min(64, hend - hb);
-            __syncthreads();                                   // previous sub-chunk's smem use is over
-            if (tid < 64) xs[tid] = tid < nh ? a.ebexp[(size_t)cb.ebar * npad + hb + tid] : ZERO_EXP;
+        // 128 patterns per read-out: two 64-pattern MMA rounds add into the same
+        // level accumulators (level sums <= 7 * 128 * 127^2 + ... < 2^24 stay
+        // exact), rows scaled against the pair of sub-chunks' largest exponent
+        for (int hb = hbeg; hb < hend && ok; hb += 128) {
+            __syncthreads();                                   // previous read-out and exponents are done
+            if (tid < 128) xs[tid] = hb + tid < hend ? a.ebexp[(size_t)cb.ebar * npad + hb + tid] : ZERO_EXP;
             if (tid == 0) red[1] = ZERO_EXP;
             __syncthreads();
-            if (tid < 64) atomicMax(&red[1], xs[tid]);
+            if (tid < 128) atomicMax(&red[1], xs[tid]);
             __syncthreads();
             const int xmax = red[1];
             if (xmax == ZERO_EXP) continue;
-            // transposed digit planes: warp writes core matrices (j group, h group);
-            // all loads in flight first
-            float2 xe[4][2], yl[4][2];
+            for (int half = 0; half < 2 && ok; half++) {
+                const int hs = hb + 64 * half, nh = min(64, hend - hs);
+                if (nh <= 0) break;
+                const int* xh = xs + 64 * half;
+                // transposed digit planes: warp writes core matrices (j group, h group);
+                // all loads in flight first
+                float2 xe[4][2], yl[4][2];
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int cmi = warp * 4 + q;                  // 64 core matrices: jg = cmi / 8, hg = cmi % 8
-                const int j = (cmi >> 3) * 8 + rr, hh = (cmi & 7) * 8 + 2 * kp;
-                const float2 *eb = a.Ebar + ((size_t)cb.ebar * npad + hb + hh) * 64 + j;
-                const float2 *lb = a.conP + ((size_t)cb.tslot * npad + hb + hh) * 64 + j;
-                const float2 z = make_float2(0.f, 0.f);
-                xe[q][0] = hh < nh ? eb[0] : z;
-                xe[q][1] = hh + 1 < nh ? eb[64] : z;
-                yl[q][0] = hh < nh ? lb[0] : z;
-                yl[q][1] = hh + 1 < nh ? lb[64] : z;
+                for (int q = 0; q < 4; q++) {
+                    const int cmi = warp * 4 + q;              // 64 core matrices: jg = cmi / 8, hg = cmi % 8
+                    const int j = (cmi >> 3) * 8 + rr, hh = (cmi & 7) * 8 + 2 * kp;
+                    const float2 *eb = a.Ebar + ((size_t)cb.ebar * npad + hs + hh) * 64 + j;
+                    const float2 *lb = a.conP + ((size_t)cb.tslot * npad + hs + hh) * 64 + j;
+                    const float2 z = make_float2(0.f, 0.f);
+                    xe[q][0] = hh < nh ? eb[0] : z;
+                    xe[q][1] = hh + 1 < nh ? eb[64] : z;
+                    yl[q][0] = hh < nh ? lb[0] : z;
+                    yl[q][1] = hh + 1 < nh ? lb[64] : z;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int cmi = warp * 4 + q;
+                    const int hh = (cmi & 7) * 8 + 2 * kp;
+                    const int off = cmi * 128 + rr * 16 + kp * 4;
+                    int d0[NB], d1[NB];
+                    const float2 x0 = hh < nh ? df_scale(xe[q][0], max(xh[hh] - xmax, -1000)) : xe[q][0];
+                    const float2 x1 = hh + 1 < nh ? df_scale(xe[q][1], max(xh[hh + 1] - xmax, -1000)) : xe[q][1];
+                    digits_of<NB>(x0.x, x0.y, d0);
+                    digits_of<NB>(x1.x, x1.y, d1);
+#pragma unroll
+                    for (int s = 0; s < NB; s++)
+                        *reinterpret_cast<unsigned *>(sm + s * A_PLANE + off) = bf16_pair(d0[s], d1[s]);
+                    unsigned char *Bp = sm + GSm<NB>::OFF_B + off;
+                    digits_of<NB>(yl[q][0].x, yl[q][0].y, d0);
+                    digits_of<NB>(yl[q][1].x, yl[q][1].y, d1);
+#pragma unroll
+                    for (int s = 0; s < NB; s++)
+                        *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16_pair(d0[s], d1[s]);
+                }
+                ok = mma_round<NB>(sm, m, phase, GSm<NB>::OFF_B, false, half == 1);
             }
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const int cmi = warp * 4 + q;
-                const int hh = (cmi & 7) * 8 + 2 * kp;
-                const int off = cmi * 128 + rr * 16 + kp * 4;
-                int d0[NB], d1[NB];
-                const float2 x0 = hh < nh ? df_scale(xe[q][0], max(xs[hh] - xmax, -1000)) : xe[q][0];
-                const float2 x1 = hh + 1 < nh ? df_scale(xe[q][1], max(xs[hh + 1] - xmax, -1000)) : xe[q][1];
-                digits_of<NB>(x0.x, x0.y, d0);
-                digits_of<NB>(x1.x, x1.y, d1);
-#pragma unroll
-                for (int s = 0; s < NB; s++) *reinterpret_cast<unsigned *>(sm + s * A_PLANE + off) = bf16_pair(d0[s], d1[s]);
-                unsigned char *Bp = sm + GSm<NB>::OFF_B + off;
-                digits_of<NB>(yl[q][0].x, yl[q][0].y, d0);
-                digits_of<NB>(yl[q][1].x, yl[q][1].y, d1);
-#pragma unroll
-                for (int s = 0; s < NB; s++) *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16_pair(d0[s], d1[s]);
-            }
-            ok = contract<NB>(sm, m, phase, acc, GSm<NB>::OFF_B, false, false, 0, max(xmax - xr, -1000));
             if (!ok) break;
+            readout<NB>(m, acc, false, 0, max(xmax - xr, -1000));
         }
     }
     if (ok && any_tip) {
@@ -733,7 +779,7 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
     }
     if (row < 64)
 #pragma unroll
-        for (int c = 0; c < NCOL; c++) out[row * 64 + c0 + c] = ldexp((double)acc[c].x + (double)acc[c].y, xr);
+        for (int c = 0; c < NCOL; c++) out[row * 64 + c0 + c] = df_scale(acc[c], xr);
     return true;
 }
 

@@ -112,6 +112,14 @@ def make_workload(ns: int, ncodon: int, seed: int = 2024):
     return aln.tree, z, fpatt, pi
 
 
+# DRAM bytes (read + write) per launch of the persistent split-precision
+# kernels from one ncu capture at 32 taxa x 2000 codons (1974 patterns, 62
+# contractions, 910811496 contraction FLOPs), profiles/fast_kernels_32x2000.md;
+# scaled to another workload by its contraction FLOPs
+NCU_TRAFFIC_SMALL = {"prune": 6.94e6 + 70.79e6, "bwd": 75.29e6 + 141.88e6, "gradP": 190.39e6 + 12.81e6}
+NCU_FLOPS_SMALL = 910811496.0
+
+
 def count_flops(lk_tree, z, fpatt):
     """Algorithmic FLOPs of one lnL and one lnL+gradient evaluation.
 
@@ -377,6 +385,10 @@ def main():
             roof["executed_tensor_frac"] = roof["executed_tensor_tflops"] / peak
         roof["limiter"] = ("SIMT digit slicing and double-float level recombination around the MMAs, "
                            "latency-bound at one 16-warp CTA per SM (see profiles/)")
+        if top in NCU_TRAFFIC_SMALL:
+            roof["traffic"] = NCU_TRAFFIC_SMALL[top] * fl["flops_prune"] / NCU_FLOPS_SMALL
+            roof["traffic_source"] = ("ncu dram__bytes_read+write of the same kernel at 32 taxa x 2000 codons, "
+                                      "scaled by contraction work")
     roof.update({"kernel": top, "share": prof[top][0] / tot if tot else None,
                  "flops_per_eval": cls_flops.get(top, 0.0), "ms_per_eval": top_ms_per_eval,
                  "classes_ms_per_eval": {k: v[0] / 3 for k, v in prof.items()}})

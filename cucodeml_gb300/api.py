@@ -169,14 +169,14 @@ class Likelihood:
         return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(_lib.KCLASS)}
 
     def task_trace(self, kernel: int) -> np.ndarray:
-        """[ntask, 8] uint64 trace of the last evaluation's persistent kernel
+        """[ntask, 12] uint64 trace of the last evaluation's persistent kernel
         (0 pruning, 1 adjoint propagation, 2 dlnL/dP): gene, item, tile, 0,
-        claim ns, dependencies-met ns, end ns, SM.  Needs GBCODEML_TRACE=1 in
+        claim ns, dependencies-met ns, four phase stamps (0 if absent), end ns, SM.  Needs GBCODEML_TRACE=1 in
         the environment before the first evaluation of this handle."""
         n = self._L.gb_task_trace(self._h, int(kernel), None, 0)
         if n < 0:
             _lib.check(n)
-        out = np.zeros((n, 8), dtype=np.uint64)
+        out = np.zeros((n, 12), dtype=np.uint64)
         r = self._L.gb_task_trace(self._h, int(kernel), out.ctypes.data_as(C.POINTER(C.c_ulonglong)), n)
         if r < 0:
             _lib.check(r)
@@ -288,7 +288,7 @@ class Batch:
         n = self._L.gb_batch_task_trace(self._h, int(kernel), None, 0)
         if n < 0:
             _lib.check(n)
-        out = np.zeros((n, 8), dtype=np.uint64)
+        out = np.zeros((n, 12), dtype=np.uint64)
         r = self._L.gb_batch_task_trace(self._h, int(kernel), out.ctypes.data_as(C.POINTER(C.c_ulonglong)), n)
         if r < 0:
             _lib.check(r)

@@ -31,13 +31,13 @@
 #include "handle.h"
 #include "adjoint_internal.h"
 #include "fast_device.cuh"
+#include "batch_internal.h"
 
 namespace gb {
 
 namespace {
 
 constexpr int NCd = 61;
-constexpr int DM_BLOCKS = 8;   // Dm: 5 derivative matrices + 3 inverse-difference tables
 constexpr int kGradPSmem = (2 * TILE64 * 65 + 64 * 65) * sizeof(double);
 constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256 + 64) * sizeof(double);
 
@@ -45,11 +45,9 @@ constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256 + 64) * sizeof(double);
 
 // D matrices V dQ U for (kappa: w=0,1,2) and (omega: w=0,2), 64-padded, and
 // the inverse eigenvalue differences of each w (for Phi)
-__global__ void __launch_bounds__(256) dmat_kernel(const DevParams *__restrict__ prm,
-                                                   const GradParams *__restrict__ gp,
-                                                   double *__restrict__ Dm, float2 *__restrict__ UVdf) {
-    __shared__ double T[61 * 62];
-    const int which = blockIdx.x;   // 0,1,2: kappa for w; 3: omega w0; 4: omega w2; 5,6,7: 1/(Root_m - Root_n) for w
+__device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, const GradParams *__restrict__ gp,
+                                          double *__restrict__ Dm, float2 *__restrict__ UVdf, int which) {
+    __shared__ double T[61 * 62];   // 0,1,2: kappa for w; 3: omega w0; 4: omega w2; 5,6,7: 1/(Root_m - Root_n) for w
     if (which >= 5) {
         const int w = which - 5;
         const double *R = prm->Root[w];
@@ -92,6 +90,19 @@ __global__ void __launch_bounds__(256) dmat_kernel(const DevParams *__restrict__
             for (int k = 0; k < 61; k++) s = fma(V[r * 61 + k], T[k * 62 + c], s);
         out[i] = s;
     }
+}
+
+__global__ void __launch_bounds__(256) dmat_kernel(const DevParams *__restrict__ prm,
+                                                   const GradParams *__restrict__ gp,
+                                                   double *__restrict__ Dm, float2 *__restrict__ UVdf) {
+    dmat_body(prm, gp, Dm, UVdf, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256) dmat_batched_kernel(const DmatArgs *__restrict__ args,
+                                                           const int2 *__restrict__ map) {
+    const int2 g = map[blockIdx.x];
+    const DmatArgs &a = args[g.x];
+    dmat_body(a.prm, a.gp, a.Dm, a.UVdf, g.y);
 }
 
 // one CTA per (32-pattern tile, backward item)
@@ -358,21 +369,18 @@ __device__ __forceinline__ float2 df_of(double v) {
 
 constexpr int kGradHdfSmem = 3 * 61 * 64 * 8 + (64 + 3 * 256) * 8;
 
-__global__ void __launch_bounds__(256) gradH_df_kernel(const PairDesc *__restrict__ pairs,
-                                                       const int *__restrict__ label,
-                                                       const double *__restrict__ tnode,
-                                                       const DevParams *__restrict__ prm,
-                                                       const float2 *__restrict__ Gpart, int nchunk,
-                                                       const double *__restrict__ Dm,
-                                                       const float2 *__restrict__ UVdf,
-                                                       double *__restrict__ out) {
+__device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs, const int *__restrict__ label,
+                                              const double *__restrict__ tnode, const DevParams *__restrict__ prm,
+                                              const float2 *__restrict__ Gpart, int nchunk,
+                                              const double *__restrict__ Dm, const float2 *__restrict__ UVdf,
+                                              double *__restrict__ out, int p) {
     extern __shared__ __align__(16) unsigned char smr[];
     float2 *GT = reinterpret_cast<float2 *>(smr);          // [61][64] G, then T
     float2 *Vt = GT + 61 * 64;                              // [61][64] Vt[k][n] = V[n][k]
     float2 *Us = Vt + 61 * 64;                              // [61][64] U[j][m]
     double *ex = reinterpret_cast<double *>(Us + 61 * 64);  // [64]
     double (*red)[256] = reinterpret_cast<double (*)[256]>(ex + 64);
-    const int p = blockIdx.x, tid = threadIdx.x;
+    const int tid = threadIdx.x;
     const PairDesc pd = pairs[p];
     const int w = pd.w;
     const double tp = tnode[pd.node] * prm->qf[label[pd.node]];
@@ -448,13 +456,30 @@ __global__ void __launch_bounds__(256) gradH_df_kernel(const PairDesc *__restric
     if (tid < 3) out[p * 3 + tid] = red[tid][0];
 }
 
+__global__ void __launch_bounds__(256) gradH_df_kernel(const PairDesc *__restrict__ pairs,
+                                                       const int *__restrict__ label,
+                                                       const double *__restrict__ tnode,
+                                                       const DevParams *__restrict__ prm,
+                                                       const float2 *__restrict__ Gpart, int nchunk,
+                                                       const double *__restrict__ Dm,
+                                                       const float2 *__restrict__ UVdf,
+                                                       double *__restrict__ out) {
+    gradH_df_body(pairs, label, tnode, prm, Gpart, nchunk, Dm, UVdf, out, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256) gradH_batched_kernel(const GradHArgs *__restrict__ args,
+                                                            const int2 *__restrict__ map) {
+    const int2 g = map[blockIdx.x];
+    const GradHArgs &a = args[g.x];
+    gradH_df_body(a.pairs, a.label, a.tnode, a.prm, a.Gpart, a.nchunk, a.Dm, a.UVdf, a.out, g.y);
+}
+
 // dlnL/dfreqK_c (up to the 1/freqK_c factor) : sum_h fpatt_h f_c / R_h
-__global__ void __launch_bounds__(256) freq_kernel(const double *__restrict__ fhK,
-                                                   const double *__restrict__ lnf,
-                                                   const double *__restrict__ fpatt, int npatt,
-                                                   int npad, int nscale, double *__restrict__ part) {
+__device__ __forceinline__ void freq_body(const double *__restrict__ fhK, const double *__restrict__ lnf,
+                                          const double *__restrict__ fpatt, int npatt, int npad, int nscale,
+                                          double *__restrict__ part, int bid) {
     __shared__ double red[4][256];
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = bid * blockDim.x + threadIdx.x;
     double q[4] = {0, 0, 0, 0};
     if (h < npatt && fpatt[h] > 0) {
         const double L = lnf[h];
@@ -470,7 +495,21 @@ __global__ void __launch_bounds__(256) freq_kernel(const double *__restrict__ fh
             for (int c = 0; c < 4; c++) red[c][threadIdx.x] += red[c][threadIdx.x + s];
         __syncthreads();
     }
-    if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = red[threadIdx.x][0];
+    if (threadIdx.x < 4) part[bid * 4 + threadIdx.x] = red[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(256) freq_kernel(const double *__restrict__ fhK,
+                                                   const double *__restrict__ lnf,
+                                                   const double *__restrict__ fpatt, int npatt,
+                                                   int npad, int nscale, double *__restrict__ part) {
+    freq_body(fhK, lnf, fpatt, npatt, npad, nscale, part, blockIdx.x);
+}
+
+__global__ void __launch_bounds__(256) freq_batched_kernel(const FreqArgs *__restrict__ args,
+                                                           const int2 *__restrict__ map) {
+    const int2 g = map[blockIdx.x];
+    const FreqArgs &a = args[g.x];
+    freq_body(a.fhK, a.lnf, a.fpatt, a.npatt, a.npad, a.nscale, a.part, g.y);
 }
 
 }  // namespace
@@ -573,6 +612,7 @@ int adjoint_init(gb_handle *h) {
     CK(cudaFuncSetAttribute(gradP_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradPSmem));
     CK(cudaFuncSetAttribute(gradH_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHSmem));
     CK(cudaFuncSetAttribute(gradH_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHdfSmem));
+    CK(cudaFuncSetAttribute(gradH_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHdfSmem));
     return 0;
 }
 
@@ -592,6 +632,18 @@ void launch_gradH_df(gb_handle *h) {
     gradH_df_kernel<<<(unsigned)h->pairs.size(), 256, kGradHdfSmem, h->stream>>>(
         h->d_pairs, h->d_label, h->d_tnode, h->d_prm, reinterpret_cast<const float2 *>(a->d_Gpart), a->nchunk,
         a->d_Dm, a->d_UVdf, a->d_pout);
+}
+
+void launch_dmat_batched(const DmatArgs *args, const int2 *map, int nblocks, cudaStream_t st) {
+    if (nblocks > 0) dmat_batched_kernel<<<nblocks, 256, 0, st>>>(args, map);
+}
+
+void launch_gradH_batched(const GradHArgs *args, const int2 *map, int nblocks, cudaStream_t st) {
+    if (nblocks > 0) gradH_batched_kernel<<<nblocks, 256, kGradHdfSmem, st>>>(args, map);
+}
+
+void launch_freq_batched(const FreqArgs *args, const int2 *map, int nblocks, cudaStream_t st) {
+    if (nblocks > 0) freq_batched_kernel<<<nblocks, 256, 0, st>>>(args, map);
 }
 
 void launch_freq(gb_handle *h, int nscale) {

@@ -15,6 +15,7 @@ struct gb_handle;
 namespace gb {
 
 constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP
+constexpr int DM_BLOCKS = 8;  // dP/dt kernel: 5 derivative matrices + 3 inverse-difference tables
 
 struct BItem {                // backward work: (node, class family) of one level
     int node, ncls, is_root, nchild;

@@ -3,10 +3,12 @@
 // persistent kernels: the pruning recursion, the adjoint propagation and
 // dlnL/dP of ALL genes are one persistent launch each over a task list that
 // mixes the genes (tasks ordered by tree level, dependencies tracked per
-// (slot, tile) on the device); the small per-gene steps (P matrices and their
-// digit planes, the mixture, dP/dt, per-pair sums, copies) are independent
-// graph branches between them.  Otherwise every gene's whole evaluation is an
-// independent branch.  The host side (eigen solutions, Qfactors, chain rule of
+// (slot, tile) on the device), and the small per-gene steps (P matrices and
+// their digit planes, the mixture, dP/dt, per-pair sums) are one launch each
+// over all genes (a block-to-gene map); the genes' per-evaluation inputs and
+// results live in batch-wide staging buffers, so each is one copy.  Otherwise
+// (FP64, or genes without a shared persistent plan) every gene's whole
+// evaluation is an independent graph branch.  The host side (eigen solutions, Qfactors, chain rule of
 // the gradient) runs on a pool of host threads, one slice of genes per thread.
 #include <cuda_runtime.h>
 
@@ -17,6 +19,7 @@
 #include <vector>
 
 #include "adjoint_internal.h"
+#include "batch_internal.h"
 #include "fast_internal.h"
 #include "handle.h"
 
@@ -31,6 +34,29 @@ struct gb_batch {
     int kernels[2] = {0, 0};
     gb::PersistPlan plan;
     gb::Tuning tune;
+    // batch-wide staging of per-evaluation inputs / results (persistent path);
+    // each gene's handle points into them (its own buffers are swapped out and
+    // swapped back before it is destroyed)
+    struct Staging {
+        bool base = false, adj = false;
+        gb::DevParams *d_prm = nullptr, *h_prm = nullptr;
+        double *d_tnode = nullptr, *h_tnode = nullptr;
+        double *d_out = nullptr, *h_out = nullptr;
+        int *d_err = nullptr, *h_err = nullptr;
+        gb::GradParams *d_gp = nullptr, *h_gp = nullptr;
+        double *d_pout = nullptr, *h_pout = nullptr, *d_fpart = nullptr, *h_fpart = nullptr;
+        size_t ntnode = 0, npout = 0, nfpart = 0;
+        std::vector<gb::DevParams *> sv_dprm, sv_hprm;
+        std::vector<double *> sv_dt, sv_ht, sv_dout, sv_hout, sv_dpout, sv_hpout, sv_dfp, sv_hfp;
+        std::vector<int *> sv_derr, sv_herr;
+        std::vector<gb::GradParams *> sv_dgp, sv_hgp;
+    } st;
+    // batched launches: per-gene argument blocks and block-to-gene maps
+    struct Launch {
+        void *args = nullptr;
+        int2 *map = nullptr;
+        int nblocks = 0;
+    } l_pmat, l_pslice, l_mix, l_dmat, l_gradH, l_freq;
 };
 
 namespace {
@@ -52,9 +78,19 @@ void parallel_for(int n, int nthreads, F fn) {
     for (auto &x : th) x.join();
 }
 
+void unstage(gb_batch *b);
+
+void free_launch(gb_batch::Launch &l) {
+    if (l.args) cudaFree(l.args);
+    if (l.map) cudaFree(l.map);
+    l = gb_batch::Launch();
+}
+
 void batch_free(gb_batch *b) {
     if (!b) return;
     cudaSetDevice(b->device);
+    unstage(b);
+    for (auto *l : {&b->l_pmat, &b->l_pslice, &b->l_mix, &b->l_dmat, &b->l_gradH, &b->l_freq}) free_launch(*l);
     for (auto &g : b->graph)
         if (g) cudaGraphExecDestroy(g);
     for (auto e : b->join)
@@ -68,6 +104,169 @@ void batch_free(gb_batch *b) {
         if (h) gb_destroy(h);
     for (auto d : b->D) delete d;
     delete b;
+}
+
+// ---------------------------------------------------------------- staging
+
+template <class T>
+int hstage(T **p, size_t n) {
+    if (cudaMallocHost((void **)p, sizeof(T) * std::max<size_t>(n, 1)) != cudaSuccess) {
+        *p = nullptr;
+        return fail(GB_ERR_OOM, "batch staging: cudaMallocHost");
+    }
+    std::memset(*p, 0, sizeof(T) * std::max<size_t>(n, 1));
+    return 0;
+}
+
+// point every gene's parameter, branch-length and result buffers into the
+// batch-wide ones (adj: also the gradient inputs and per-pair / class sums)
+int stage(gb_batch *b, bool adj) {
+    auto &s = b->st;
+    int rc;
+    const int n = b->n;
+    if (!s.base) {
+        s.ntnode = 0;
+        for (auto h : b->h) s.ntnode += h->nnode;
+        if ((rc = dalloc(&s.d_prm, n)) || (rc = hstage(&s.h_prm, n)) || (rc = dalloc(&s.d_tnode, s.ntnode)) ||
+            (rc = hstage(&s.h_tnode, s.ntnode)) || (rc = dalloc(&s.d_out, 4 * (size_t)n)) ||
+            (rc = hstage(&s.h_out, 4 * (size_t)n)) || (rc = dalloc(&s.d_err, n)) || (rc = hstage(&s.h_err, n)))
+            return rc;
+        CK(cudaMemset(s.d_err, 0, sizeof(int) * n));
+        size_t off = 0;
+        for (int i = 0; i < n; i++) {
+            gb_handle *h = b->h[i];
+            // keep what the host already staged for the next evaluation
+            std::memcpy(s.h_prm + i, h->h_prm, sizeof(DevParams));
+            std::memcpy(s.h_tnode + off, h->h_tnode, sizeof(double) * h->nnode);
+            s.sv_dprm.push_back(h->d_prm), s.sv_hprm.push_back(h->h_prm);
+            s.sv_dt.push_back(h->d_tnode), s.sv_ht.push_back(h->h_tnode);
+            s.sv_dout.push_back(h->d_out), s.sv_hout.push_back(h->h_out);
+            h->d_prm = s.d_prm + i;
+            h->h_prm = s.h_prm + i;
+            h->d_tnode = s.d_tnode + off;
+            h->h_tnode = s.h_tnode + off;
+            h->d_out = s.d_out + 4 * (size_t)i;
+            h->h_out = s.h_out + 4 * (size_t)i;
+            int *de = s.d_err + i, *he = s.h_err + i;
+            fast_swap_err(h, de, he);
+            s.sv_derr.push_back(de), s.sv_herr.push_back(he);
+            off += h->nnode;
+        }
+        s.base = true;
+    }
+    if (adj && !s.adj) {
+        s.npout = s.nfpart = 0;
+        for (auto h : b->h) {
+            if (!h->adj) return fail(GB_ERR_STATE, "batch staging: adjoint buffers missing");
+            s.npout += h->pairs.size() * 3;
+            s.nfpart += (size_t)h->adj->nfreq_blocks * 4;
+        }
+        if ((rc = dalloc(&s.d_gp, n)) || (rc = hstage(&s.h_gp, n)) || (rc = dalloc(&s.d_pout, s.npout)) ||
+            (rc = hstage(&s.h_pout, s.npout)) || (rc = dalloc(&s.d_fpart, s.nfpart)) ||
+            (rc = hstage(&s.h_fpart, s.nfpart)))
+            return rc;
+        size_t op = 0, of = 0;
+        for (int i = 0; i < n; i++) {
+            AdjointState *a = b->h[i]->adj;
+            std::memcpy(s.h_gp + i, a->h_gp, sizeof(GradParams));
+            s.sv_dgp.push_back(a->d_gp), s.sv_hgp.push_back(a->h_gp);
+            s.sv_dpout.push_back(a->d_pout), s.sv_hpout.push_back(a->h_pout);
+            s.sv_dfp.push_back(a->d_fpart), s.sv_hfp.push_back(a->h_fpart);
+            a->d_gp = s.d_gp + i;
+            a->h_gp = s.h_gp + i;
+            a->d_pout = s.d_pout + op;
+            a->h_pout = s.h_pout + op;
+            a->d_fpart = s.d_fpart + of;
+            a->h_fpart = s.h_fpart + of;
+            op += b->h[i]->pairs.size() * 3;
+            of += (size_t)a->nfreq_blocks * 4;
+        }
+        s.adj = true;
+    }
+    return 0;
+}
+
+void unstage(gb_batch *b) {
+    auto &s = b->st;
+    for (int i = 0; i < (int)s.sv_dprm.size(); i++) {
+        gb_handle *h = b->h[i];
+        h->d_prm = s.sv_dprm[i], h->h_prm = s.sv_hprm[i];
+        h->d_tnode = s.sv_dt[i], h->h_tnode = s.sv_ht[i];
+        h->d_out = s.sv_dout[i], h->h_out = s.sv_hout[i];
+        fast_swap_err(h, s.sv_derr[i], s.sv_herr[i]);
+    }
+    for (int i = 0; i < (int)s.sv_dgp.size(); i++) {
+        AdjointState *a = b->h[i]->adj;
+        a->d_gp = s.sv_dgp[i], a->h_gp = s.sv_hgp[i];
+        a->d_pout = s.sv_dpout[i], a->h_pout = s.sv_hpout[i];
+        a->d_fpart = s.sv_dfp[i], a->h_fpart = s.sv_hfp[i];
+    }
+    void *dv[] = {s.d_prm, s.d_tnode, s.d_out, s.d_err, s.d_gp, s.d_pout, s.d_fpart};
+    for (void *p : dv)
+        if (p) cudaFree(p);
+    void *hv[] = {s.h_prm, s.h_tnode, s.h_out, s.h_err, s.h_gp, s.h_pout, s.h_fpart};
+    for (void *p : hv)
+        if (p) cudaFreeHost(p);
+    s = gb_batch::Staging();
+}
+
+// ---------------------------------------------------------------- batched launches
+
+// built once: captured graphs keep pointing at these arrays
+template <class A, class F>
+int make_launch(gb_batch *b, gb_batch::Launch &l, F per_gene) {   // per_gene(h, &args) -> blocks
+    if (l.args) return 0;
+    std::vector<A> args(b->n);
+    std::vector<int2> map;
+    for (int g = 0; g < b->n; g++) {
+        const int nb = per_gene(b->h[g], &args[g]);
+        for (int j = 0; j < nb; j++) map.push_back(make_int2(g, j));
+    }
+    int rc;
+    A *da = nullptr;
+    if ((rc = dalloc(&da, args.size())) || (rc = dalloc(&l.map, map.size()))) return rc;
+    l.args = da;
+    CK(cudaMemcpy(da, args.data(), sizeof(A) * args.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(l.map, map.data(), sizeof(int2) * std::max<size_t>(map.size(), 1), cudaMemcpyHostToDevice));
+    l.nblocks = (int)map.size();
+    return 0;
+}
+
+int build_launches(gb_batch *b, bool grad) {
+    int rc;
+    if ((rc = make_launch<PmatArgs>(b, b->l_pmat, [](gb_handle *h, PmatArgs *a) {
+             *a = PmatArgs{h->d_pairs, h->d_label, h->d_tnode, h->d_prm, h->d_Pt};
+             return (int)h->pairs.size();
+         })) ||
+        (rc = make_launch<PsliceArgs>(b, b->l_pslice, [](gb_handle *h, PsliceArgs *a) {
+             *a = fast_pslice_args(h);
+             return (int)h->pairs.size();
+         })) ||
+        (rc = make_launch<MixArgs>(b, b->l_mix, [](gb_handle *h, MixArgs *a) {
+             const int nb = (h->npatt + 255) / 256;
+             *a = MixArgs{h->d_fhK, h->d_fpatt, h->d_prm, h->npatt, h->npad, 1, nb,
+                          h->d_lnf, h->d_post, h->d_partial, h->d_ticket, h->d_out};
+             return nb;
+         })))
+        return rc;
+    if (!grad) return 0;
+    if ((rc = make_launch<DmatArgs>(b, b->l_dmat, [](gb_handle *h, DmatArgs *a) {
+             *a = DmatArgs{h->d_prm, h->adj->d_gp, h->adj->d_Dm, h->adj->d_UVdf};
+             return DM_BLOCKS;
+         })) ||
+        (rc = make_launch<GradHArgs>(b, b->l_gradH, [](gb_handle *h, GradHArgs *a) {
+             AdjointState *ad = h->adj;
+             *a = GradHArgs{h->d_pairs, h->d_label, h->d_tnode, h->d_prm,
+                            reinterpret_cast<const float2 *>(ad->d_Gpart), ad->nchunk, ad->d_Dm, ad->d_UVdf,
+                            ad->d_pout};
+             return (int)h->pairs.size();
+         })) ||
+        (rc = make_launch<FreqArgs>(b, b->l_freq, [](gb_handle *h, FreqArgs *a) {
+             *a = FreqArgs{h->d_fhK, h->d_lnf, h->d_fpatt, h->npatt, h->npad, 1, h->adj->d_fpart};
+             return h->adj->nfreq_blocks;
+         })))
+        return rc;
+    return 0;
 }
 
 // every gene's branch: origin -> gene stream -> fn(h) -> origin
@@ -97,25 +296,29 @@ bool batch_persistent(const gb_batch *b) {
 
 int record_persistent(gb_batch *b, bool grad) {
     const int ns = fast_ns(b->h[0], false), nsb = fast_ns(b->h[0], true);
-    launch_bump(b->plan.ctl, b->origin);
-    int nk = 1, r;
-    if ((r = fork_join(b, [&](gb_handle *h) {
-             const int rc = fast_rec_copies_in(h, grad);
-             return rc ? rc : fast_rec_pmat(h);
-         })) < 0)
-        return r;
-    nk += r + persist_record_fwd(&b->plan, grad, ns, b->origin, nullptr);
-    if ((r = fork_join(b, [&](gb_handle *h) { return fast_rec_mix(h) + (grad ? fast_rec_dmat(h) : 0); })) < 0)
-        return r;
-    nk += r;
-    if (grad) nk += persist_record_bwd(&b->plan, nsb, b->origin, nullptr);
-    if ((r = fork_join(b, [&](gb_handle *h) {
-             const int n = grad ? fast_rec_tail(h) : 0;
-             const int rc = fast_rec_copies_out(h, grad);
-             return rc ? rc : n;
-         })) < 0)
-        return r;
-    return nk + r;
+    auto &s = b->st;
+    cudaStream_t o = b->origin;
+    launch_bump(b->plan.ctl, o);
+    CK(cudaMemcpyAsync(s.d_prm, s.h_prm, sizeof(DevParams) * b->n, cudaMemcpyHostToDevice, o));
+    CK(cudaMemcpyAsync(s.d_tnode, s.h_tnode, sizeof(double) * s.ntnode, cudaMemcpyHostToDevice, o));
+    if (grad) CK(cudaMemcpyAsync(s.d_gp, s.h_gp, sizeof(GradParams) * b->n, cudaMemcpyHostToDevice, o));
+    launch_pmat_batched((const PmatArgs *)b->l_pmat.args, b->l_pmat.map, b->l_pmat.nblocks, o);
+    launch_pslice_batched((const PsliceArgs *)b->l_pslice.args, b->l_pslice.map, b->l_pslice.nblocks, ns, o);
+    int nk = 3 + persist_record_fwd(&b->plan, grad, ns, o, nullptr);
+    launch_mix_batched((const MixArgs *)b->l_mix.args, b->l_mix.map, b->l_mix.nblocks, o);
+    nk++;
+    if (grad) {
+        launch_dmat_batched((const DmatArgs *)b->l_dmat.args, b->l_dmat.map, b->l_dmat.nblocks, o);
+        nk += 1 + persist_record_bwd(&b->plan, nsb, o, nullptr);
+        launch_gradH_batched((const GradHArgs *)b->l_gradH.args, b->l_gradH.map, b->l_gradH.nblocks, o);
+        launch_freq_batched((const FreqArgs *)b->l_freq.args, b->l_freq.map, b->l_freq.nblocks, o);
+        nk += 2;
+        CK(cudaMemcpyAsync(s.h_pout, s.d_pout, sizeof(double) * s.npout, cudaMemcpyDeviceToHost, o));
+        CK(cudaMemcpyAsync(s.h_fpart, s.d_fpart, sizeof(double) * s.nfpart, cudaMemcpyDeviceToHost, o));
+    }
+    CK(cudaMemcpyAsync(s.h_out, s.d_out, sizeof(double) * 4 * b->n, cudaMemcpyDeviceToHost, o));
+    CK(cudaMemcpyAsync(s.h_err, s.d_err, sizeof(int) * b->n, cudaMemcpyDeviceToHost, o));
+    return nk;
 }
 
 int build_graph(gb_batch *b, bool grad) {
@@ -127,8 +330,10 @@ int build_graph(gb_batch *b, bool grad) {
     }
     const bool persist = batch_persistent(b);
     if (persist) {
-        int rc = persist_build(&b->plan, b->h.data(), b->n, grad, b->tune);
-        if (rc) return rc;
+        int rc;
+        if ((rc = stage(b, grad)) || (rc = persist_build(&b->plan, b->h.data(), b->n, grad, b->tune)) ||
+            (rc = build_launches(b, grad)))
+            return rc;
     }
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));

@@ -14,6 +14,7 @@
 #include "adjoint_internal.h"
 #include "fast_internal.h"
 #include "handle.h"
+#include "batch_internal.h"
 
 namespace gb {
 
@@ -326,7 +327,7 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const 
         pp->nftask = (int)t.size();
         const char *tr = std::getenv("GBCODEML_TRACE");
         pp->tracing = tr && std::strcmp(tr, "1") == 0;
-        if (pp->tracing && (rc = dalloc(&pp->trace[0], 4 * t.size()))) return rc;
+        if (pp->tracing && (rc = dalloc(&pp->trace[0], TRACE_WORDS * t.size()))) return rc;
         if ((rc = dalloc(&pp->d_ftask, t.size()))) return rc;
         CK(cudaMemcpy(pp->d_ftask, t.data(), sizeof(Task) * t.size(), cudaMemcpyHostToDevice));
     }
@@ -357,7 +358,7 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const 
             for (int d = 0; d < maxB; d++)
                 for (int g = 0; g < n; g++) push_blevel(g, d);
         pp->nbtask = (int)t.size();
-        if (pp->tracing && (rc = dalloc(&pp->trace[1], 4 * t.size()))) return rc;
+        if (pp->tracing && (rc = dalloc(&pp->trace[1], TRACE_WORDS * t.size()))) return rc;
         if ((rc = dalloc(&pp->d_btask, t.size()))) return rc;
         CK(cudaMemcpy(pp->d_btask, t.data(), sizeof(Task) * t.size(), cudaMemcpyHostToDevice));
         // dlnL/dP: independent (gene, pair, chunk) tasks, heaviest first
@@ -375,7 +376,7 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const 
         t.clear();
         for (auto &x : gt) t.push_back(x.second);
         pp->ngtask = (int)t.size();
-        if (pp->tracing && (rc = dalloc(&pp->trace[2], 4 * t.size()))) return rc;
+        if (pp->tracing && (rc = dalloc(&pp->trace[2], TRACE_WORDS * t.size()))) return rc;
         if ((rc = dalloc(&pp->d_gtask, t.size()))) return rc;
         CK(cudaMemcpy(pp->d_gtask, t.data(), sizeof(Task) * t.size(), cudaMemcpyHostToDevice));
     }
@@ -455,8 +456,18 @@ int fast_prepare(gb_handle *h, bool grad) {
 
 bool fast_persistent(const gb_handle *h) { return h->fast && h->fast->persist; }
 
+PsliceArgs fast_pslice_args(gb_handle *h) {
+    FastState *f = h->fast;
+    return PsliceArgs{h->d_Pt, f->Pdf, f->Bf, f->Bb};
+}
+
+void fast_swap_err(gb_handle *h, int *&d_err, int *&h_err) {
+    std::swap(h->fast->err, d_err);
+    std::swap(h->fast->h_err, h_err);
+}
+
 // the last evaluation's task trace of one persistent kernel of a plan:
-// 8 words per task (gene, item, tile, 0, claim ns, dependencies met ns, end ns, SM)
+// TRACE_OUT words per task (gene, item, tile, 0, then the kernel's TRACE_WORDS)
 int persist_task_trace(PersistPlan *pp, int kernel, unsigned long long *out, int cap) {
     if (kernel < 0 || kernel > 2) return fail(GB_ERR_ARG, "task trace: kernel must be 0, 1 or 2");
     const Task *dt[3] = {pp->d_ftask, pp->d_btask, pp->d_gtask};
@@ -467,15 +478,17 @@ int persist_task_trace(PersistPlan *pp, int kernel, unsigned long long *out, int
     if (out && n > 0) {
         CK(cudaDeviceSynchronize());
         std::vector<Task> t(n);
-        std::vector<unsigned long long> tr(4 * (size_t)n);
+        std::vector<unsigned long long> tr((size_t)TRACE_WORDS * n);
         CK(cudaMemcpy(t.data(), dt[kernel], sizeof(Task) * n, cudaMemcpyDeviceToHost));
-        CK(cudaMemcpy(tr.data(), pp->trace[kernel], sizeof(unsigned long long) * 4 * n, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(tr.data(), pp->trace[kernel], sizeof(unsigned long long) * TRACE_WORDS * n,
+                      cudaMemcpyDeviceToHost));
         for (int i = 0; i < n; i++) {
-            out[8 * i + 0] = (unsigned long long)t[i].gene;
-            out[8 * i + 1] = (unsigned long long)t[i].item;
-            out[8 * i + 2] = (unsigned long long)t[i].tile;
-            out[8 * i + 3] = 0;
-            for (int q = 0; q < 4; q++) out[8 * i + 4 + q] = tr[4 * i + q];
+            unsigned long long *o = out + (size_t)TRACE_OUT * i;
+            o[0] = (unsigned long long)t[i].gene;
+            o[1] = (unsigned long long)t[i].item;
+            o[2] = (unsigned long long)t[i].tile;
+            o[3] = 0;
+            for (int q = 0; q < TRACE_WORDS; q++) o[4 + q] = tr[(size_t)TRACE_WORDS * i + q];
         }
     }
     return nt[kernel];

@@ -95,7 +95,10 @@ void launch_gradP_fast(const FastBwdArgs &a, int ns, int npair, cudaStream_t st)
 void launch_pslice(const FastFwdArgs &a, int ns, int npair, bool cm, cudaStream_t st);
 void launch_prune_fast(const FastFwdArgs &a, int ns, int nitems, int ntile, cudaStream_t st);
 void launch_bump(unsigned *ctl, cudaStream_t st);
-// trace: nullable, 4 words per task (claim ns, dependencies met ns, end ns, SM)
+// trace: nullable, TRACE_WORDS per task (claim ns, dependencies met ns, four
+// phase stamps, end ns, SM); gb_task_trace returns TRACE_OUT words per task
+constexpr int TRACE_WORDS = 8;
+constexpr int TRACE_OUT = 4 + TRACE_WORDS;
 void launch_prune_persist(const FastFwdArgs *genes, const Task *tasks, int ntask, unsigned *ctl, int ns,
                           int nblock, unsigned long long *trace, cudaStream_t st);
 void launch_bwd_persist(const FastBwdArgs *genes, const Task *tasks, int ntask, unsigned *ctl, int ns,

@@ -133,6 +133,9 @@ int fast_rec_dmat(gb_handle *h);      // dP/dt terms of the adjoint
 int fast_rec_tail(gb_handle *h);      // per-pair and class-weight gradient sums
 int fast_rec_copies_out(gb_handle *h, bool grad);
 bool fast_persistent(const gb_handle *h);
+struct PsliceArgs;
+PsliceArgs fast_pslice_args(gb_handle *h);                      // P digit-plane buffers (batched launches)
+void fast_swap_err(gb_handle *h, int *&d_err, int *&h_err);     // exchange the error word (batch staging)
 int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);
 int persist_task_trace(PersistPlan *pp, int kernel, unsigned long long *out, int cap);
 int fast_ns(const gb_handle *h, bool adjoint);

@@ -26,6 +26,7 @@
 
 #include "internal.h"
 #include "fast_internal.h"
+#include "batch_internal.h"
 #include "fast_device.cuh"
 
 namespace gb {
@@ -50,10 +51,9 @@ __device__ __forceinline__ int cm_index(int n, int k) {
 // row-major planes (cm = 0, mma.sync kernels) or core-matrix planes (cm = 1,
 // tcgen05 kernels, copied to shared memory as they are)
 template <int NS>
-__global__ void __launch_bounds__(256) pslice_kernel(const double *__restrict__ Pt, float2 *__restrict__ Pdf,
-                                                     __nv_bfloat16 *__restrict__ Bf,
-                                                     __nv_bfloat16 *__restrict__ Bb, int cm) {
-    const int p = blockIdx.x;
+__device__ __forceinline__ void pslice_body(const double *__restrict__ Pt, float2 *__restrict__ Pdf,
+                                            __nv_bfloat16 *__restrict__ Bf, __nv_bfloat16 *__restrict__ Bb,
+                                            int cm, int p) {
     const double *P = Pt + (size_t)p * 4096;
     float2 *D = Pdf + (size_t)p * 4096;
     __nv_bfloat16 *bf = Bf + (size_t)p * NS * 4096;
@@ -73,6 +73,22 @@ __global__ void __launch_bounds__(256) pslice_kernel(const double *__restrict__ 
             bb[(size_t)s * 4096 + (cm ? cm_index(k, j) : k * 64 + j)] = b;
         }
     }
+}
+
+template <int NS>
+__global__ void __launch_bounds__(256) pslice_kernel(const double *__restrict__ Pt, float2 *__restrict__ Pdf,
+                                                     __nv_bfloat16 *__restrict__ Bf,
+                                                     __nv_bfloat16 *__restrict__ Bb, int cm) {
+    pslice_body<NS>(Pt, Pdf, Bf, Bb, cm, blockIdx.x);
+}
+
+// many genes in one launch (core-matrix planes, for the tcgen05 kernels)
+template <int NS>
+__global__ void __launch_bounds__(256) pslice_batched_kernel(const PsliceArgs *__restrict__ args,
+                                                             const int2 *__restrict__ map) {
+    const int2 g = map[blockIdx.x];
+    const PsliceArgs &a = args[g.x];
+    pslice_body<NS>(a.Pt64, a.Pdf, a.Bf, a.Bb, 1, g.y);
 }
 
 // ---------------------------------------------------------------- forward level
@@ -229,6 +245,16 @@ void launch_pslice(const FastFwdArgs &a, int ns, int npair, bool cm, cudaStream_
         case 6: launch_fwd_ns<6>(a, 0, 0, true, npair, st, cm); break;
         case 7: launch_fwd_ns<7>(a, 0, 0, true, npair, st, cm); break;
         case 8: launch_fwd_ns<8>(a, 0, 0, true, npair, st, cm); break;
+    }
+}
+
+void launch_pslice_batched(const PsliceArgs *args, const int2 *map, int nblocks, int ns, cudaStream_t st) {
+    if (nblocks <= 0) return;
+    switch (ns) {
+        case 5: pslice_batched_kernel<5><<<nblocks, 256, 0, st>>>(args, map); break;
+        case 6: pslice_batched_kernel<6><<<nblocks, 256, 0, st>>>(args, map); break;
+        case 7: pslice_batched_kernel<7><<<nblocks, 256, 0, st>>>(args, map); break;
+        case 8: pslice_batched_kernel<8><<<nblocks, 256, 0, st>>>(args, map); break;
     }
 }
 

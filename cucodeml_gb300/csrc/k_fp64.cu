@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "internal.h"
+#include "batch_internal.h"
 
 namespace gb {
 
@@ -25,18 +26,16 @@ namespace {
 
 constexpr int NC = 61;
 
-__global__ void __launch_bounds__(256) pmat_fp64_kernel(const PairDesc *__restrict__ pairs,
-                                                        const int *__restrict__ label,
-                                                        const double *__restrict__ tnode,
-                                                        const DevParams *__restrict__ prm,
-                                                        double *__restrict__ Pt) {
+__device__ __forceinline__ void pmat_body(const PairDesc *__restrict__ pairs, const int *__restrict__ label,
+                                          const double *__restrict__ tnode, const DevParams *__restrict__ prm,
+                                          double *__restrict__ Pt, int pair) {
     extern __shared__ double sm[];
     double *UeT = sm;             // [61][64]: UeT[m][j] = U[j][m] e^{Root_m t}
     double *Vs = sm + NC * 64;    // [61][64]: Vs[m][k] = V[m][k]
-    const PairDesc pd = pairs[blockIdx.x];
+    const PairDesc pd = pairs[pair];
     const int w = pd.w;
     const double t = tnode[pd.node] * prm->qf[label[pd.node]];
-    double *out = Pt + (size_t)blockIdx.x * 64 * 64;
+    double *out = Pt + (size_t)pair * 64 * 64;
     const int tid = threadIdx.x;
     if (t < 1e-100) {
         for (int i = tid; i < 64 * 64; i += blockDim.x) out[i] = (i / 64 == i % 64 && i / 64 < NC) ? 1.0 : 0.0;
@@ -71,6 +70,22 @@ __global__ void __launch_bounds__(256) pmat_fp64_kernel(const PairDesc *__restri
         if (p < 0.0 || k >= NC) p = 0.0;
         out[k * 64 + j0 + i] = p;
     }
+}
+
+__global__ void __launch_bounds__(256) pmat_fp64_kernel(const PairDesc *__restrict__ pairs,
+                                                        const int *__restrict__ label,
+                                                        const double *__restrict__ tnode,
+                                                        const DevParams *__restrict__ prm,
+                                                        double *__restrict__ Pt) {
+    pmat_body(pairs, label, tnode, prm, Pt, blockIdx.x);
+}
+
+// many genes in one launch: block b works on pair map[b].y of gene map[b].x
+__global__ void __launch_bounds__(256) pmat_batched_kernel(const PmatArgs *__restrict__ args,
+                                                           const int2 *__restrict__ map) {
+    const int2 g = map[blockIdx.x];
+    const PmatArgs &a = args[g.x];
+    pmat_body(a.pairs, a.label, a.tnode, a.prm, a.Pt, g.y);
 }
 
 // 128 threads: row group rg = tid/16 owns tile rows 4rg..4rg+3, column group
@@ -198,17 +213,14 @@ __global__ void __launch_bounds__(128) prune_fp64_kernel(
 }
 
 // mixture over the 4 classes, log, fpatt-weighted sum; post[c][h] = class posterior
-__global__ void __launch_bounds__(256) mix_kernel(const double *__restrict__ fhK,
-                                                  const double *__restrict__ fpatt,
-                                                  const DevParams *__restrict__ prm, int npatt,
-                                                  int npad, int nscale, double *__restrict__ lnf,
-                                                  double *__restrict__ post,
-                                                  double *__restrict__ partial,
-                                                  unsigned *__restrict__ ticket,
-                                                  double *__restrict__ out) {
+__device__ __forceinline__ void mix_body(const double *__restrict__ fhK, const double *__restrict__ fpatt,
+                                         const DevParams *__restrict__ prm, int npatt, int npad, int nscale,
+                                         double *__restrict__ lnf, double *__restrict__ post,
+                                         double *__restrict__ partial, unsigned *__restrict__ ticket,
+                                         double *__restrict__ out, int bid, int nb) {
     __shared__ double red[256];
     __shared__ bool last;
-    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = bid * blockDim.x + threadIdx.x;
     double contrib = 0.0;
     if (h < npatt) {
         double v[4], fk[4];
@@ -259,17 +271,17 @@ __global__ void __launch_bounds__(256) mix_kernel(const double *__restrict__ fhK
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        partial[blockIdx.x] = red[0];
+        partial[bid] = red[0];
         __threadfence();
         unsigned prev = atomicAdd(ticket, 1u);
-        last = (prev == gridDim.x - 1);
+        last = (prev == (unsigned)nb - 1);
     }
     __syncthreads();
     if (last) {
         // the last block sums the block partials in a fixed order
         __threadfence();
         double s = 0.0;
-        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) s += ((volatile double *)partial)[i];
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) s += ((volatile double *)partial)[i];
         red[threadIdx.x] = s;
         __syncthreads();
         for (int k = 128; k > 0; k >>= 1) {
@@ -283,12 +295,41 @@ __global__ void __launch_bounds__(256) mix_kernel(const double *__restrict__ fhK
     }
 }
 
+__global__ void __launch_bounds__(256) mix_kernel(const double *__restrict__ fhK,
+                                                  const double *__restrict__ fpatt,
+                                                  const DevParams *__restrict__ prm, int npatt,
+                                                  int npad, int nscale, double *__restrict__ lnf,
+                                                  double *__restrict__ post,
+                                                  double *__restrict__ partial,
+                                                  unsigned *__restrict__ ticket,
+                                                  double *__restrict__ out) {
+    mix_body(fhK, fpatt, prm, npatt, npad, nscale, lnf, post, partial, ticket, out, blockIdx.x, gridDim.x);
+}
+
+__global__ void __launch_bounds__(256) mix_batched_kernel(const MixArgs *__restrict__ args,
+                                                          const int2 *__restrict__ map) {
+    const int2 g = map[blockIdx.x];
+    const MixArgs &a = args[g.x];
+    mix_body(a.fhK, a.fpatt, a.prm, a.npatt, a.npad, a.nscale, a.lnf, a.post, a.partial, a.ticket, a.out, g.y,
+             a.nblocks);
+}
+
 }  // namespace
 
 constexpr int kPmatSmem = 2 * NC * 64 * sizeof(double);
 
 cudaError_t init_fp64_kernels() {
-    return cudaFuncSetAttribute(pmat_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPmatSmem);
+    cudaError_t e = cudaFuncSetAttribute(pmat_fp64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPmatSmem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(pmat_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kPmatSmem);
+}
+
+void launch_pmat_batched(const PmatArgs *args, const int2 *map, int nblocks, cudaStream_t st) {
+    if (nblocks > 0) pmat_batched_kernel<<<nblocks, 256, kPmatSmem, st>>>(args, map);
+}
+
+void launch_mix_batched(const MixArgs *args, const int2 *map, int nblocks, cudaStream_t st) {
+    if (nblocks > 0) mix_batched_kernel<<<nblocks, 256, 0, st>>>(args, map);
 }
 
 void launch_pmat_fp64(const PairDesc *pairs, int npair, const int *label, const double *tnode,

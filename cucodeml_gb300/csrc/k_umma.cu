@@ -117,9 +117,11 @@ __device__ __forceinline__ unsigned smid() {
     return s;
 }
 
-// optional task trace: per task (claim time, dependencies met, end time, SM)
+// optional task trace, TRACE_WORDS per task: claim time, dependencies met,
+// four phase stamps inside the task (0 when absent), end time, SM
+enum { TR_CLAIM = 0, TR_READY = 1, TR_P0 = 2, TR_SLICED = 3, TR_MMA = 4, TR_READOUT = 5, TR_END = 6, TR_SM = 7 };
 __device__ __forceinline__ void trace_put(unsigned long long *trace, int idx, int slot, unsigned long long v) {
-    if (trace && threadIdx.x == 0) trace[(size_t)idx * 4 + slot] = v;
+    if (trace && threadIdx.x == 0) trace[(size_t)idx * TRACE_WORDS + slot] = v;
 }
 
 // claim the next task index (block-uniform)
@@ -315,7 +317,7 @@ __device__ __forceinline__ void on_failure(int *err, Misc *m, uint32_t phase, bo
 // has an internal child.  Returns the block-uniform success flag.
 template <int NS>
 __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsigned char *sm, Misc *m,
-                           uint32_t &phase) {
+                           uint32_t &phase, unsigned long long *tr = nullptr, int tidx = 0) {
     float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_RMAX);
     double *rsum = reinterpret_cast<double *>(sm + USm<NS>::OFF_RSUM);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -342,6 +344,8 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
         for (int c = 0; c < NCOL; c++) prod[c] = have ? df_mul(prod[c], E[c]) : E[c];
         have = true;
     }
+    trace_put(tr, tidx, TR_P0, umma::global_ns());
+    bool first = true;
     for (int ci = 0; ci < it.nchild && ok; ci++) {
         const int cs = it.cslot[ci];
         if (cs < 0) continue;
@@ -349,8 +353,16 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
         __syncthreads();                                   // the previous contraction's planes are free
         start_B<NS>(a.Bf + (size_t)it.pidx[ci] * NS * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
         slice_A_cm<NS>(a.conP + ((size_t)cs * npad + h0) * 64, sm);
-        ok = contract<NS>(sm, m, phase, E, USm<NS>::OFF_B, true);
+        if (first && tr) {                                 // tracing only: all planes are cut
+            __syncthreads();
+            trace_put(tr, tidx, TR_SLICED, umma::global_ns());
+        }
+        ok = mma_round<NS>(sm, m, phase, USm<NS>::OFF_B, true, false);
         if (!ok) break;
+        if (first) trace_put(tr, tidx, TR_MMA, umma::global_ns());
+        readout<NS>(m, E, true, 0, 0);
+        if (first) trace_put(tr, tidx, TR_READOUT, umma::global_ns());
+        first = false;
         expo += __ldcg(a.expo + (size_t)cs * npad + h);
         // edge messages of internal children are kept for the adjoint
         if (a.E) store_row32(a.E + ((size_t)(it.eslot + ci) * npad + h) * 64 + c0, E);
@@ -427,7 +439,7 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
     for (;;) {
         const int idx = claim(ctl + CTL_FWD, m);
         if (idx >= ntask) break;
-        trace_put(trace, idx, 0, umma::global_ns());
+        trace_put(trace, idx, TR_CLAIM, umma::global_ns());
         const Task t = tasks[idx];
         stage(a, genes + t.gene);
         __syncthreads();
@@ -442,11 +454,11 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
             if (threadIdx.x == 0) atomicExch(a->err, 1);
             break;
         }
-        trace_put(trace, idx, 1, umma::global_ns());
-        if (!prune_tile<NS>(*a, *it, t.tile, sm, m, phase)) break;
+        trace_put(trace, idx, TR_READY, umma::global_ns());
+        if (!prune_tile<NS>(*a, *it, t.tile, sm, m, phase, trace, idx)) break;
         __syncthreads();                                   // the tile's rows are written
-        trace_put(trace, idx, 2, umma::global_ns());
-        trace_put(trace, idx, 3, smid());
+        trace_put(trace, idx, TR_END, umma::global_ns());
+        trace_put(trace, idx, TR_SM, smid());
         if (threadIdx.x == 0 && !it->is_root) set_flag(a->ready + (size_t)it->slot * a->ntile + t.tile, epoch);
     }
     tmem_teardown(m);
@@ -599,7 +611,7 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
     for (;;) {
         const int idx = claim(ctl + CTL_BWD, m);
         if (idx >= ntask) break;
-        trace_put(trace, idx, 0, umma::global_ns());
+        trace_put(trace, idx, TR_CLAIM, umma::global_ns());
         const Task t = tasks[idx];
         stage(a, genes + t.gene);
         __syncthreads();
@@ -613,11 +625,11 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
             if (threadIdx.x == 0) atomicExch(a->err, 1);
             break;
         }
-        trace_put(trace, idx, 1, umma::global_ns());
+        trace_put(trace, idx, TR_READY, umma::global_ns());
         if (!bwd_tile<NS>(*a, *it, t.tile, sm, m, phase)) break;
         __syncthreads();
-        trace_put(trace, idx, 2, umma::global_ns());
-        trace_put(trace, idx, 3, smid());
+        trace_put(trace, idx, TR_END, umma::global_ns());
+        trace_put(trace, idx, TR_SM, smid());
         // publish the children's slots that received an upper partial; the
         // staged item and arguments are not rewritten before the next claim's
         // barrier, which thread 0 reaches only after this
@@ -808,15 +820,15 @@ __global__ void __launch_bounds__(NT, 1) gradP_persist_kernel(const FastBwdArgs 
     for (;;) {
         const int idx = claim(ctl + CTL_GRADP, m);
         if (idx >= ntask) break;
-        trace_put(trace, idx, 0, umma::global_ns());
+        trace_put(trace, idx, TR_CLAIM, umma::global_ns());
         const Task t = tasks[idx];
         stage(a, genes + t.gene);
         __syncthreads();
-        trace_put(trace, idx, 1, umma::global_ns());
+        trace_put(trace, idx, TR_READY, umma::global_ns());
         if (!gradP_task<NB>(*a, t.item, t.tile, sm, m, phase)) break;
         __syncthreads();
-        trace_put(trace, idx, 2, umma::global_ns());
-        trace_put(trace, idx, 3, smid());
+        trace_put(trace, idx, TR_END, umma::global_ns());
+        trace_put(trace, idx, TR_SM, smid());
     }
     tmem_teardown(m);
 }

@@ -57,3 +57,25 @@ def test_batch_fast_matches_fp64(genes):
         va = np.concatenate([a["blength"], [a[k] for k in ("kappa", "omega0", "omega2", "p0", "p1")]])
         vb = np.concatenate([b["blength"], [b[k] for k in ("kappa", "omega0", "omega2", "p0", "p1")]])
         assert np.max(np.abs(va - vb) / np.maximum(1.0, np.abs(va))) <= 1e-5
+
+
+def test_batch_fast_alternating_modes(genes):
+    """lnL-only, then lnL + gradient, then lnL-only again on one batch (the
+    batch-wide staging buffers and both captured graphs), each equal to the
+    genes evaluated one by one."""
+    b = api.Batch([(a.tree, z, fp, pi) for a, z, fp, pi in genes], precision="fast")
+    singles = [api.Likelihood(a.tree, z, fp, pi, precision="fast") for a, z, fp, pi in genes]
+    for rep, (scale, grad) in enumerate(((1.0, False), (1.1, True), (0.9, False), (1.2, True))):
+        prm = [params_of(a, scale) for a, _, _, _ in genes]
+        f, g, _ = b.evaluate(prm, grad=grad)
+        for i, lk in enumerate(singles):
+            p = prm[i]
+            r = lk.evaluate(p["blength"], p["kappa"], p["omega0"], p["omega2"], p["p0"], p["p1"], grad=grad)
+            assert abs(f[i] - r.neg_lnL) <= 1e-12 * abs(r.neg_lnL), (rep, i)
+            if grad:
+                assert np.allclose(g[i]["blength"], r.grad["blength"], rtol=1e-10, atol=1e-10), (rep, i)
+                for k in ("kappa", "omega0", "omega2", "p0", "p1"):
+                    assert abs(g[i][k] - r.grad[k]) <= 1e-10 * max(1.0, abs(r.grad[k])), (rep, i, k)
+    for lk in singles:
+        lk.close()
+    b.close()

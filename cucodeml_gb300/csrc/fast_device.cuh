@@ -33,7 +33,14 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
 }
 
-__device__ __forceinline__ float2 df_scale(float2 a, int e) {   // exact 2^e scaling
+// exact 2^e scaling: a multiplication by 2^e built from its exponent bits when
+// 2^e is a normal float (the product is then rounded exactly as scalbnf
+// rounds it), scalbnf otherwise
+__device__ __forceinline__ float2 df_scale(float2 a, int e) {
+    if (e >= -126 && e <= 127) {
+        const float s = __int_as_float((127 + e) << 23);
+        return make_float2(a.x * s, a.y * s);
+    }
     return make_float2(scalbnf(a.x, e), scalbnf(a.y, e));
 }
 

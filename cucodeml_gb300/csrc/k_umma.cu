@@ -12,11 +12,12 @@
 // pair (i, j) with i + j = L into that level's 64 TMEM columns (NS = 8:
 // 8 levels = all 512 columns), and commits to an mbarrier.  The level sums
 // are exact integers in FP32;
-// each thread reads one row (TMEM lane) x 16 columns per level with
+// each thread reads one row (TMEM lane) x NCOL columns per level with
 // tcgen05.ld and combines the levels in double-float.
-// 16 warps (512 threads) per CTA: warp w reads TMEM lanes 32 (w % 4) .. + 31 and
-// columns 16 (w / 4) .. + 15, so thread (w, lane) owns pattern row
-// 32 (w % 4) + lane and states 16 (w / 4) + 0..15.
+// NWARP warps per CTA: warp w reads TMEM lanes 32 (w % 4) .. + 31 (a warp may
+// only access its quarter of the lanes) and columns NCOL (w / 4) .. + NCOL-1,
+// so thread (w, lane) owns pattern row 32 (w % 4) + lane and states
+// NCOL (w / 4) + 0..NCOL-1.
 // Every mbarrier wait is bounded; on timeout the CTA sets *err, skips its
 // remaining work and still frees its TMEM.
 #include <cuda_runtime.h>
@@ -33,8 +34,13 @@ namespace {
 
 using namespace fastdev;
 constexpr int NC = 61;
-constexpr int NT = 512;            // threads per CTA
-constexpr int NCOL = 16;           // states per thread in the epilogues
+constexpr int NT = 512;            // threads per CTA (16 warps; 32 measured no faster)
+constexpr int NWARP = NT / 32;
+constexpr int NCG = NWARP / 4;     // column groups: warps sharing a TMEM lane quarter
+constexpr int NCOL = 64 / NCG;     // states per thread in the epilogues
+constexpr int ACM = 128 / NWARP;   // A-plane core matrices cut per warp (128 x 64 tile)
+constexpr int GCM = 64 / NWARP;    // core matrices per warp in the 64 x 64 dlnL/dP planes
+static_assert(NCOL % 2 == 0 && ACM >= 1 && GCM >= 1, "thread layout");
 constexpr int A_PLANE = 128 * 64 * 2;
 constexpr int B_PLANE = 64 * 64 * 2;
 
@@ -51,9 +57,9 @@ template <int NS>
 struct USm {
     static constexpr int OFF_B = NS * A_PLANE;
     static constexpr int OFF_MISC = OFF_B + NS * B_PLANE;
-    static constexpr int OFF_RMAX = OFF_MISC + 64;            // float [4][128]
-    static constexpr int OFF_RSUM = OFF_RMAX + 2048;          // double [4][128]
-    static constexpr int OFF_ARGS = OFF_RSUM + 4096;
+    static constexpr int OFF_RMAX = OFF_MISC + 64;            // float [2][NCG][128]
+    static constexpr int OFF_RSUM = OFF_RMAX + 2 * NCG * 128 * 4;   // double [NCG][128]
+    static constexpr int OFF_ARGS = OFF_RSUM + NCG * 128 * 8;
     static constexpr int OFF_ITEM = OFF_ARGS + ARGS_BYTES;
     static constexpr int NEED = OFF_ITEM + ITEM_BYTES;
     static constexpr int BYTES = NEED > MIN_SMEM ? NEED : MIN_SMEM;
@@ -135,16 +141,16 @@ template <int NS>
 __device__ __forceinline__ void slice_A_cm(const float2 *__restrict__ src, unsigned char *A) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rr = lane >> 2, kp = lane & 3;
-    float4 v[8];
+    float4 v[ACM];
 #pragma unroll
-    for (int q = 0; q < 8; q++) {                        // all loads in flight first
-        const int cmi = warp * 8 + q;                    // core matrix: row group cmi/8, k group cmi%8
+    for (int q = 0; q < ACM; q++) {                      // all loads in flight first
+        const int cmi = warp * ACM + q;                  // core matrix: row group cmi/8, k group cmi%8
         const int row = (cmi >> 3) * 8 + rr, k = (cmi & 7) * 8 + 2 * kp;
         v[q] = __ldcg(reinterpret_cast<const float4 *>(src + (size_t)row * 64 + k));
     }
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-        const int cmi = warp * 8 + q;
+    for (int q = 0; q < ACM; q++) {
+        const int cmi = warp * ACM + q;
         int d0[NS], d1[NS];
         digits_of<NS>(v[q].x, v[q].y, d0);
         digits_of<NS>(v[q].z, v[q].w, d1);
@@ -222,7 +228,7 @@ __device__ __forceinline__ bool mma_round(unsigned char *sm, Misc *m, uint32_t &
     return ok;
 }
 
-// Every thread reads its row's 16 columns of every level and accumulates
+// Every thread reads its row's NCOL columns of every level and accumulates
 //   C = (init ? 0 : C 2^sc_in) + 2^sc_new sum_L S_L 2^(-7L)
 // in double-float (exact power-of-two scalings).
 template <int NS>
@@ -232,13 +238,22 @@ __device__ __forceinline__ void readout(Misc *m, float2 (&C)[NCOL], bool init, i
     const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
 #pragma unroll
     for (int c = 0; c < NCOL; c++) C[c] = init ? make_float2(0.f, 0.f) : df_scale(C[c], sc_in);
+    // two levels per TMEM wait, smallest first
 #pragma unroll 1
-    for (int L = NS + 1; L >= 2; L--) {
-        float v[NCOL];
-        umma::tmem_ld16(m->tmem + lane_base + (L - 2) * 64 + col, v);
-        const float w = scalbnf(1.0f, -7 * L + sc_new);
+    for (int L = NS + 1; L >= 2; L -= 2) {
+        const int L2 = L - 1 >= 2 ? L - 1 : L;
+        uint32_t r0[NCOL], r1[NCOL];
+        umma::tmem_ld_nowait(m->tmem + lane_base + (L - 2) * 64 + col, r0);
+        umma::tmem_ld_nowait(m->tmem + lane_base + (L2 - 2) * 64 + col, r1);
+        umma::tmem_wait_ld();
+        const float w0 = scalbnf(1.0f, -7 * L + sc_new);
 #pragma unroll
-        for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(v[c] * w, 0.f));
+        for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(__uint_as_float(r0[c]) * w0, 0.f));
+        if (L2 != L) {
+            const float w1 = scalbnf(1.0f, -7 * L2 + sc_new);
+#pragma unroll
+            for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(__uint_as_float(r1[c]) * w1, 0.f));
+        }
     }
     umma::fence_before();
 }
@@ -268,16 +283,23 @@ __device__ __forceinline__ void store_row32(float2 *p, const float2 (&v)[NCOL]) 
         reinterpret_cast<float4 *>(p)[c] = make_float4(v[2 * c].x, v[2 * c].y, v[2 * c + 1].x, v[2 * c + 1].y);
 }
 
-// row maximum over the valid states of the four threads sharing a row
-__device__ __forceinline__ float row_max(const float2 (&v)[NCOL], int col0, float *rmax, int row, int ch) {
+// row maximum over the valid states of the NCG threads sharing a row (in
+// NCG warps): one barrier, two alternating buffers (a buffer is rewritten
+// only after the next call's barrier, which every reader of the previous
+// call has passed)
+__device__ __forceinline__ float row_max(const float2 (&v)[NCOL], int col0, float *rmax, int row, int ch,
+                                         int &par) {
     float m = 0.f;
 #pragma unroll
     for (int c = 0; c < NCOL; c++)
         if (col0 + c < NC) m = fmaxf(m, v[c].x);
-    rmax[ch * 128 + row] = m;
+    float *buf = rmax + par * (NCG * 128);
+    buf[ch * 128 + row] = m;
     __syncthreads();
-    m = fmaxf(fmaxf(rmax[row], rmax[128 + row]), fmaxf(rmax[256 + row], rmax[384 + row]));
-    __syncthreads();
+    m = buf[row];
+#pragma unroll
+    for (int g = 1; g < NCG; g++) m = fmaxf(m, buf[g * 128 + row]);
+    par ^= 1;
     return m;
 }
 
@@ -374,7 +396,8 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
         on_failure(a.err, m, phase, true);
         return false;
     }
-    const float mx = row_max(prod, c0, rmax, row, ch);
+    int par = 0;
+    const float mx = row_max(prod, c0, rmax, row, ch, par);
     const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
     expo += sh;
 #pragma unroll
@@ -390,7 +413,9 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
         rsum[ch * 128 + row] = f;
         __syncthreads();
         if (ch == 0) {
-            f = (rsum[row] + rsum[128 + row]) + (rsum[256 + row] + rsum[384 + row]);
+            f = rsum[row];
+#pragma unroll
+            for (int g = 1; g < NCG; g++) f += rsum[g * 128 + row];
             if (f <= 0.0) f = 1e-300;
             const double sl = (double)expo * 0.69314718055994530942;
             a.fbar[(size_t)it.cls * npad + h] = f;
@@ -468,7 +493,8 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
 
 template <int NS>
 __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsigned char *sm, Misc *m,
-                         uint32_t &phase) {
+                         uint32_t &phase, unsigned long long *tr = nullptr, int tidx = 0) {
+    bool first = true;
     float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_RMAX);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int ch = warp >> 2;
@@ -477,6 +503,7 @@ __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsign
     const size_t h0 = (size_t)tile * 128, h = h0 + row;
     bool ok = true;
 
+    int par = 0;           // row_max buffer parity
     int eAs[2] = {0, 0};   // exponent of A_a 2^{-sh_a} per class for this row
     for (int k = 0; k < it.ncls; k++) {
         const int c = it.cls[k];
@@ -528,7 +555,7 @@ __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsign
 #pragma unroll
                 for (int q = 0; q < NCOL; q++) X[q] = df_mul(X[q], Ev[q]);
             }
-            const float mx = row_max(X, c0, rmax, row, ch);
+            const float mx = row_max(X, c0, rmax, row, ch, par);
             const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
 #pragma unroll
             for (int q = 0; q < NCOL; q++) X[q] = df_scale(X[q], -sh);
@@ -546,22 +573,30 @@ __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsign
             for (int k = kbeg; k < kend; k++) {
                 const size_t eb = (size_t)(it.pslot[k] * MAXC + i);
                 __syncthreads();        // this tile's Ebar rows are written and visible
+                if (first) trace_put(tr, tidx, TR_P0, umma::global_ns());
                 start_B<NS>(a.Bb + (size_t)it.pidx[i][k] * a.nsP * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
                 slice_A_cm<NS>(a.Ebar + (eb * npad + h0) * 64, sm);
+                if (first && tr) {
+                    __syncthreads();
+                    trace_put(tr, tidx, TR_SLICED, umma::global_ns());
+                }
                 const int eC = a.ebexp[eb * npad + h];
+                ok = mma_round<NS>(sm, m, phase, USm<NS>::OFF_B, true, false);
+                if (!ok) break;
+                if (first) trace_put(tr, tidx, TR_MMA, umma::global_ns());
                 if (k == kbeg) {
-                    ok = contract<NS>(sm, m, phase, acc, USm<NS>::OFF_B, true);
+                    readout<NS>(m, acc, true, 0, 0);
                     eacc = eC;
                 } else {                                   // acc 2^eacc + C 2^eC on the larger exponent
                     const int e = max(eacc, eC);
-                    ok = contract<NS>(sm, m, phase, acc, USm<NS>::OFF_B, true, false, max(eacc - e, -1000),
-                                      max(eC - e, -1000));
+                    readout<NS>(m, acc, false, max(eacc - e, -1000), max(eC - e, -1000));
                     eacc = e;
                 }
-                if (!ok) break;
+                if (first) trace_put(tr, tidx, TR_READOUT, umma::global_ns());
+                first = false;
             }
             if (!ok) break;
-            const float mx = row_max(acc, c0, rmax, row, ch);
+            const float mx = row_max(acc, c0, rmax, row, ch, par);
             const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
 #pragma unroll
             for (int q = 0; q < NCOL; q++) acc[q] = df_scale(acc[q], -sh);
@@ -626,7 +661,7 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
             break;
         }
         trace_put(trace, idx, TR_READY, umma::global_ns());
-        if (!bwd_tile<NS>(*a, *it, t.tile, sm, m, phase)) break;
+        if (!bwd_tile<NS>(*a, *it, t.tile, sm, m, phase, trace, idx)) break;
         __syncthreads();
         trace_put(trace, idx, TR_END, umma::global_ns());
         trace_put(trace, idx, TR_SM, smid());
@@ -654,7 +689,7 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
 // xr (the chunk's largest), with no FP64 arithmetic until the final write.
 // Children that are tips (one-hot rows) are summed by a segmented scatter in
 // shared memory instead.  Threads of TMEM lanes 0..63 (warps w with
-// w % 4 < 2) own output rows j, 16 columns each.
+// w % 4 < 2) own output rows j, NCOL columns each.
 template <int NB>
 __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char *sm, Misc *m, uint32_t &phase) {
     int *xs = reinterpret_cast<int *>(sm + GSm<NB>::OFF_XS);
@@ -716,10 +751,10 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
                 const int* xh = xs + 64 * half;
                 // transposed digit planes: warp writes core matrices (j group, h group);
                 // all loads in flight first
-                float2 xe[4][2], yl[4][2];
+                float2 xe[GCM][2], yl[GCM][2];
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int cmi = warp * 4 + q;              // 64 core matrices: jg = cmi / 8, hg = cmi % 8
+                for (int q = 0; q < GCM; q++) {
+                    const int cmi = warp * GCM + q;            // 64 core matrices: jg = cmi / 8, hg = cmi % 8
                     const int j = (cmi >> 3) * 8 + rr, hh = (cmi & 7) * 8 + 2 * kp;
                     const float2 *eb = a.Ebar + ((size_t)cb.ebar * npad + hs + hh) * 64 + j;
                     const float2 *lb = a.conP + ((size_t)cb.tslot * npad + hs + hh) * 64 + j;
@@ -730,8 +765,8 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
                     yl[q][1] = hh + 1 < nh ? lb[64] : z;
                 }
 #pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    const int cmi = warp * 4 + q;
+                for (int q = 0; q < GCM; q++) {
+                    const int cmi = warp * GCM + q;
                     const int hh = (cmi & 7) * 8 + 2 * kp;
                     const int off = cmi * 128 + rr * 16 + kp * 4;
                     int d0[NB], d1[NB];

@@ -367,7 +367,13 @@ __device__ __forceinline__ float2 df_of(double v) {
     return make_float2(hi, (float)(v - (double)hi));
 }
 
-constexpr int kGradHdfSmem = 3 * 61 * 64 * 8 + (64 + 3 * 256) * 8;
+constexpr int kGradHdfSmem = (61 * 66 + 2 * 61 * 64) * 8 + (64 + 3 * 256) * 8;
+
+// Shared-memory layout: G (then T) rows padded to GS = 66 double-float so that
+// the 8 rows a warp reads at one k fall in different banks; thread
+// (r = tid / 4, q = tid % 4) owns row r and the interleaved columns q + 4 i,
+// so the 4 column groups of a warp read 4 consecutive entries (no conflict).
+constexpr int GS = 66;
 
 __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs, const int *__restrict__ label,
                                               const double *__restrict__ tnode, const DevParams *__restrict__ prm,
@@ -375,8 +381,8 @@ __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs
                                               const double *__restrict__ Dm, const float2 *__restrict__ UVdf,
                                               double *__restrict__ out, int p) {
     extern __shared__ __align__(16) unsigned char smr[];
-    float2 *GT = reinterpret_cast<float2 *>(smr);          // [61][64] G, then T
-    float2 *Vt = GT + 61 * 64;                              // [61][64] Vt[k][n] = V[n][k]
+    float2 *GT = reinterpret_cast<float2 *>(smr);          // [61][GS] G, then T
+    float2 *Vt = GT + 61 * GS;                              // [61][64] Vt[k][n] = V[n][k]
     float2 *Us = Vt + 61 * 64;                              // [61][64] U[j][m]
     double *ex = reinterpret_cast<double *>(Us + 61 * 64);  // [64]
     double (*red)[256] = reinterpret_cast<double (*)[256]>(ex + 64);
@@ -394,26 +400,26 @@ __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs
     for (int i = tid; i < 61 * 64; i += blockDim.x) {      // G = sum of the chunk partials
         float2 g = make_float2(0.f, 0.f);
         for (int q = 0; q < nchunk; q++) g = fastdev::df_add(g, Gpart[((size_t)p * nchunk + q) * 64 * 64 + i]);
-        GT[i] = (i % 64) < 61 ? g : make_float2(0.f, 0.f);
+        GT[(i >> 6) * GS + (i & 63)] = (i & 63) < 61 ? g : make_float2(0.f, 0.f);
     }
     __syncthreads();
-    const int r = tid >> 2, c0 = (tid & 3) * 16;
+    const int r = tid >> 2, q4 = tid & 3;
     float s[16], e[16];
-    // T[r][n] = sum_k G[r][k] Vt[k][n]
+    // T[r][n] = sum_k G[r][k] Vt[k][n], n = q4 + 4 i
 #pragma unroll
     for (int i = 0; i < 16; i++) s[i] = e[i] = 0.f;
     if (r < 61)
         for (int k = 0; k < 61; k++) {
-            const float2 g = GT[r * 64 + k];
+            const float2 g = GT[r * GS + k];
 #pragma unroll
-            for (int i = 0; i < 16; i++) dot2_step(s[i], e[i], g, Vt[k * 64 + c0 + i]);
+            for (int i = 0; i < 16; i++) dot2_step(s[i], e[i], g, Vt[k * 64 + q4 + 4 * i]);
         }
     __syncthreads();                                        // every read of G is done
     if (r < 61)
 #pragma unroll
         for (int i = 0; i < 16; i++) {
             const float hi = s[i] + e[i];
-            GT[r * 64 + c0 + i] = make_float2(hi, e[i] - (hi - s[i]));
+            GT[r * GS + q4 + 4 * i] = make_float2(hi, e[i] - (hi - s[i]));
         }
     __syncthreads();
     // H[r][n] = sum_j U[j][r] T[j][n]
@@ -423,7 +429,7 @@ __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs
         for (int j = 0; j < 61; j++) {
             const float2 u = Us[j * 64 + r];
 #pragma unroll
-            for (int i = 0; i < 16; i++) dot2_step(s[i], e[i], u, GT[j * 64 + c0 + i]);
+            for (int i = 0; i < 16; i++) dot2_step(s[i], e[i], u, GT[j * GS + q4 + 4 * i]);
         }
     double sdt = 0, sk = 0, sw = 0;
     const double *Dk = Dm + (size_t)w * 64 * 64;
@@ -434,7 +440,7 @@ __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs
         const double am = tp * R[r], em = ex[r];
 #pragma unroll
         for (int i = 0; i < 16; i++) {
-            const int n = c0 + i;
+            const int n = q4 + 4 * i;
             if (n >= 61) continue;
             const double hmn = (double)s[i] + (double)e[i];
             const double phi = phi_of(am, tp * R[n], em, ex[n], inv[r * 64 + n], rtp);

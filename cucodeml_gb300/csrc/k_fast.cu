@@ -50,6 +50,27 @@ __device__ __forceinline__ int cm_index(int n, int k) {
 //   Bb[s][k][j] = digit s of Pt[k][j]            (adjoint:  out[h][k] = sum_j E[h][j] P[j][k])
 // row-major planes (cm = 0, mma.sync kernels) or core-matrix planes (cm = 1,
 // tcgen05 kernels, copied to shared memory as they are)
+// q = floor(v 2^(7 NS)) of an FP64 value of P (P >= 0 after the clamp)
+template <int NS>
+__device__ __forceinline__ unsigned long long p_fixed(double v) {
+    return v > 0.0 ? (unsigned long long)floor(v * ldexp(1.0, 7 * NS)) : 0ull;
+}
+
+template <int NS>
+__device__ __forceinline__ int p_digit(unsigned long long q, int s) {
+    const int sh = 7 * (NS - 1 - s);
+    return s == 0 ? (int)(q >> sh) : (int)((q >> sh) & 127);
+}
+
+// 8 values' digit s as one 16-byte row of a core matrix (8 bf16)
+template <int NS>
+__device__ __forceinline__ uint4 p_row(const unsigned long long (&q)[8], int s) {
+    return make_uint4(bf16_pair(p_digit<NS>(q[0], s), p_digit<NS>(q[1], s)),
+                      bf16_pair(p_digit<NS>(q[2], s), p_digit<NS>(q[3], s)),
+                      bf16_pair(p_digit<NS>(q[4], s), p_digit<NS>(q[5], s)),
+                      bf16_pair(p_digit<NS>(q[6], s), p_digit<NS>(q[7], s)));
+}
+
 template <int NS>
 __device__ __forceinline__ void pslice_body(const double *__restrict__ Pt, float2 *__restrict__ Pdf,
                                             __nv_bfloat16 *__restrict__ Bf, __nv_bfloat16 *__restrict__ Bb,
@@ -58,19 +79,46 @@ __device__ __forceinline__ void pslice_body(const double *__restrict__ Pt, float
     float2 *D = Pdf + (size_t)p * 4096;
     __nv_bfloat16 *bf = Bf + (size_t)p * NS * 4096;
     __nv_bfloat16 *bb = Bb + (size_t)p * NS * 4096;
-    const double S = ldexp(1.0, 7 * NS);
+    if (!cm) {     // row-major planes (mma.sync kernels)
+        for (int i = threadIdx.x; i < 4096; i += blockDim.x) {
+            const int k = i >> 6, j = i & 63;
+            const double v = P[i];                       // Pt[k][j]
+            const float hi = (float)v;
+            D[i] = make_float2(hi, (float)(v - (double)hi));
+            const unsigned long long q = p_fixed<NS>(v);
+            for (int s = 0; s < NS; s++) {
+                const __nv_bfloat16 b = __float2bfloat16_rn((float)p_digit<NS>(q, s));
+                bf[(size_t)s * 4096 + j * 64 + k] = b;
+                bb[(size_t)s * 4096 + k * 64 + j] = b;
+            }
+        }
+        return;
+    }
+    // core-matrix planes: P staged in shared memory, then each thread writes
+    // whole 16-byte core-matrix rows (8 consecutive K elements) per plane
+    __shared__ double Ps[64 * 65];                       // Ps[k][j] = Pt[k][j], rows padded
     for (int i = threadIdx.x; i < 4096; i += blockDim.x) {
-        const int k = i >> 6, j = i & 63;
-        const double v = P[i];                       // Pt[k][j]
+        const double v = P[i];
         const float hi = (float)v;
         D[i] = make_float2(hi, (float)(v - (double)hi));
-        unsigned long long q = v > 0.0 ? (unsigned long long)floor(v * S) : 0ull;
-        for (int s = 0; s < NS; s++) {
-            const int sh = 7 * (NS - 1 - s);
-            const int dgt = s == 0 ? (int)(q >> sh) : (int)((q >> sh) & 127);
-            const __nv_bfloat16 b = __float2bfloat16_rn((float)dgt);
-            bf[(size_t)s * 4096 + (cm ? cm_index(j, k) : j * 64 + k)] = b;
-            bb[(size_t)s * 4096 + (cm ? cm_index(k, j) : k * 64 + j)] = b;
+        Ps[(i >> 6) * 65 + (i & 63)] = v;
+    }
+    __syncthreads();
+    for (int u = threadIdx.x; u < 1024; u += blockDim.x) {
+        const int n = (u >> 3) & 63, g = u & 7;
+        unsigned long long q[8];
+        if (u < 512) {         // forward: B[n = j][k], row = 8 consecutive k
+#pragma unroll
+            for (int t = 0; t < 8; t++) q[t] = p_fixed<NS>(Ps[(8 * g + t) * 65 + n]);
+#pragma unroll
+            for (int s = 0; s < NS; s++)
+                *reinterpret_cast<uint4 *>(bf + (size_t)s * 4096 + cm_index(n, 8 * g)) = p_row<NS>(q, s);
+        } else {               // adjoint: B[n = k][j], row = 8 consecutive j
+#pragma unroll
+            for (int t = 0; t < 8; t++) q[t] = p_fixed<NS>(Ps[n * 65 + 8 * g + t]);
+#pragma unroll
+            for (int s = 0; s < NS; s++)
+                *reinterpret_cast<uint4 *>(bb + (size_t)s * 4096 + cm_index(n, 8 * g)) = p_row<NS>(q, s);
         }
     }
 }

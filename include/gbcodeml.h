@@ -236,9 +236,13 @@ int gb_batch_tune(gb_batch *b, int knob, int value);
  * kernels are first set up, every task of the last evaluation records, from
  * the device's global timer, when it was claimed, when its dependencies were
  * met and when it ended, and the SM that ran it.  kernel: 0 pruning, 1 adjoint
- * propagation, 2 dlnL/dP.  Writes up to cap tasks, 8 words each (gene, item,
- * tile, 0, claim ns, ready ns, end ns, SM), and returns the kernel's task
- * count (GB_ERR_STATE when tracing is off or the kernel has not run).
+ * propagation, 2 dlnL/dP.  Writes up to cap tasks, 12 words each (gene, item,
+ * tile, 0, claim ns, ready ns, four phase stamps (pruning: tips gathered,
+ * first contraction's planes cut, its MMAs complete, its levels read; adjoint:
+ * the same for its first contraction, the first stamp after the first child's
+ * messages; 0 where a kernel records none), end ns, SM), and returns the
+ * kernel's task count
+ * (GB_ERR_STATE when tracing is off or the kernel has not run).
  */
 int gb_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);
 /* the same for a batch's persistent kernels (gene = index in the batch) */

@@ -70,6 +70,11 @@ def fit(lk, x0, fix_omega2: bool = False, gradient: str = "adjoint", gtol: float
 
     nb = lk.nnode - 1
     nev = {"f": 0, "g": 0}
+    # the objective is minimised as f - f(x0): same gradient, but L-BFGS-B's
+    # relative-reduction test then measures progress against the improvement
+    # itself instead of |lnL| (~1e6 for large alignments, where it would stop
+    # with lnL still moving in the 5th decimal)
+    base = {"f0": None}
 
     def full(x):
         return np.append(x, 1.0) if fix_omega2 else x
@@ -79,17 +84,21 @@ def fit(lk, x0, fix_omega2: bool = False, gradient: str = "adjoint", gtol: float
         if gradient == "adjoint":
             nev["g"] += 1
             f, dx = lk.dfun_x(full(x), lastround=False)
-            return f, (dx[:-1] if fix_omega2 else dx)
-        f = lk.evaluate_x(full(x), lastround=False).neg_lnL
-        nev["g"] += len(x)
-        g = fd_gradient(_Fixed(lk, fix_omega2), x, f)
-        return f, g
+            g = dx[:-1] if fix_omega2 else dx
+        else:
+            f = lk.evaluate_x(full(x), lastround=False).neg_lnL
+            nev["g"] += len(x)
+            g = fd_gradient(_Fixed(lk, fix_omega2), x, f)
+        if base["f0"] is None:
+            base["f0"] = f
+        return f - base["f0"], g
 
     t0 = time.perf_counter()
     res = minimize(fun, x0, jac=True, method="L-BFGS-B", bounds=bounds(nb, fix_omega2),
                    options={"maxiter": maxiter, "maxfun": 4 * maxiter, "gtol": gtol, "ftol": 1e-15,
                             "maxcor": 20})
     secs = time.perf_counter() - t0
+    res.fun = float(res.fun) + base["f0"]
     x = full(res.x)
     e = np.exp(x[nb + 1:nb + 3])
     p0, p1 = e / (1.0 + e.sum())

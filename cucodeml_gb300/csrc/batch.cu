@@ -413,21 +413,23 @@ int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *g
     parallel_for(b->n, b->nthreads, [&](int i) {
         gb_handle *h = b->h[i];
         ModelParams m{prm[i].kappa, prm[i].omega0, prm[i].omega2, prm[i].p0, prm[i].p1};
-        int rc = prm[i].blength ? derive(h->pi.data(), m, grad, b->D[i]) : GB_ERR_ARG;
+        int rc = prm[i].blength ? derive(h->pi.data(), m, grad, b->D[i], false) : GB_ERR_ARG;
         if (!rc) rc = stage_params(h, b->D[i], prm[i].blength);
         status[i] = rc;
     });
     for (int i = 0; i < b->n; i++)
         if (status[i]) return fail(status[i], "gb_batch_eval: gene " + std::to_string(i) + ": parameters out of range");
-    if (grad)
-        for (int i = 0; i < b->n; i++) {
+    if (grad) {
+        for (int i = 0; i < b->n; i++)
             if (!b->h[i]->adj) {
                 int rc = adjoint_init(b->h[i]);
                 if (rc) return rc;
             }
+        parallel_for(b->n, b->nthreads, [&](int i) {
             std::memcpy(b->h[i]->adj->h_gp->dQk, b->D[i]->dQk, sizeof(b->D[i]->dQk));
             std::memcpy(b->h[i]->adj->h_gp->dQw, b->D[i]->dQw, sizeof(b->D[i]->dQw));
-        }
+        });
+    }
     int rc = build_graph(b, grad);
     if (rc) return rc;
     CK(cudaEventRecord(b->ev0, b->origin));

@@ -269,7 +269,7 @@ int derive_scalars(const double *pi, const ModelParams &m, Derived *out) {
     return 0;
 }
 
-int derive(const double *pi, const ModelParams &m, bool want_grad, Derived *out) {
+int derive(const double *pi, const ModelParams &m, bool want_grad, Derived *out, bool threads) {
     int rc = derive_scalars(pi, m, out);
     if (rc) return rc;
     const double w[3] = {m.w0, 1.0, m.w2};
@@ -281,11 +281,17 @@ int derive(const double *pi, const ModelParams &m, bool want_grad, Derived *out)
         status[i] = eigen_qrev(Q, pi, out->U[i], out->V[i], out->Root[i]);
         if (want_grad && i == 1) std::memset(out->dQw[1], 0, sizeof(double) * NC * NC);
     };
-    // the three eigen problems are independent: run them side by side
-    std::thread t1(one, 1), t2(one, 2);
-    one(0);
-    t1.join();
-    t2.join();
+    // the three eigen problems are independent: side by side for a single
+    // alignment; one after the other when the caller is already parallel
+    // over alignments (a batch)
+    if (threads) {
+        std::thread t1(one, 1), t2(one, 2);
+        one(0);
+        t1.join();
+        t2.join();
+    } else {
+        for (int i = 0; i < 3; i++) one(i);
+    }
     for (int i = 0; i < 3; i++)
         if (status[i]) return GB_ERR_PARAM;
     return 0;

@@ -36,7 +36,7 @@ double build_q(const double *pi, double kappa, double omega, double *Q, double *
 int eigen_qrev(const double *Q, const double *pi, double *U, double *V, double *Root);
 
 // Fill everything a model-A evaluation needs; 0 or GB_ERR_PARAM.
-int derive(const double *pi, const ModelParams &m, bool want_grad, Derived *out);
+int derive(const double *pi, const ModelParams &m, bool want_grad, Derived *out, bool threads = true);
 
 // Only the parts that do not need an eigen solution (Qfactors, freqK and
 // their derivatives), for evaluations that receive U, V, Root from the host.

@@ -116,7 +116,7 @@ def make_workload(ns: int, ncodon: int, seed: int = 2024):
 # kernels from one ncu capture at 32 taxa x 2000 codons (1974 patterns, 62
 # contractions, 910811496 contraction FLOPs), profiles/fast_kernels_32x2000.md;
 # scaled to another workload by its contraction FLOPs
-NCU_TRAFFIC_SMALL = {"prune": 6.94e6 + 70.79e6, "bwd": 75.29e6 + 141.88e6, "gradP": 190.39e6 + 12.81e6}
+NCU_TRAFFIC_SMALL = {"prune": 7.16e6 + 70.72e6, "bwd": 76.15e6 + 142.30e6, "gradP": 190.43e6 + 13.35e6}
 NCU_FLOPS_SMALL = 910811496.0
 
 

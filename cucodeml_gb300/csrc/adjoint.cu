@@ -45,11 +45,19 @@ constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256 + 64) * sizeof(double);
 
 // D matrices V dQ U for (kappa: w=0,1,2) and (omega: w=0,2), 64-padded, and
 // the inverse eigenvalue differences of each w (for Phi)
+// Block bid: derivative matrix which = bid / DM_RB (0,1,2: kappa for w; 3: omega
+// w0; 4: omega w2), output rows 16 (bid % DM_RB) .. + 15 of D = V dQ U; the
+// last 3 blocks: 1/(Root_m - Root_n) for w (and U, V^T as double-float).
+// dQ has at most ~10 non-zeros per row (single-nucleotide neighbours and the
+// diagonal): T = dQ U runs over each row's non-zeros (dense past 16).
 __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, const GradParams *__restrict__ gp,
-                                          double *__restrict__ Dm, float2 *__restrict__ UVdf, int which) {
-    __shared__ double T[61 * 62];   // 0,1,2: kappa for w; 3: omega w0; 4: omega w2; 5,6,7: 1/(Root_m - Root_n) for w
-    if (which >= 5) {
-        const int w = which - 5;
+                                          double *__restrict__ Dm, float2 *__restrict__ UVdf, int bid) {
+    __shared__ double T[61 * 62];
+    __shared__ int nzk[61][16];
+    __shared__ double nzv[61][16];
+    __shared__ int nnz[61];
+    if (bid >= 5 * DM_RB) {
+        const int w = bid - 5 * DM_RB, which = 5 + w;
         const double *R = prm->Root[w];
         double *out = Dm + (size_t)which * 64 * 64;
         for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
@@ -70,25 +78,47 @@ __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, con
         }
         return;
     }
+    const int which = bid / DM_RB, rb = bid % DM_RB;
     const int w = which < 3 ? which : (which == 3 ? 0 : 2);
     const double *dQ = which < 3 ? gp->dQk[w] : gp->dQw[w];
     const double *U = prm->U[w];
     const double *V = prm->V[w];
+    if (threadIdx.x < 61) {               // non-zeros of row r of dQ
+        const int r = threadIdx.x;
+        int n = 0;
+        for (int c = 0; c < 61; c++) {
+            const double v = dQ[r * 61 + c];
+            if (v != 0.0) {
+                if (n < 16) {
+                    nzk[r][n] = c;
+                    nzv[r][n] = v;
+                }
+                n++;
+            }
+        }
+        nnz[r] = n;
+    }
+    __syncthreads();
     // T = dQ U
     for (int i = threadIdx.x; i < 61 * 61; i += blockDim.x) {
-        int r = i / 61, c = i % 61;
+        const int r = i / 61, c = i % 61;
         double s = 0;
-        for (int k = 0; k < 61; k++) s = fma(dQ[r * 61 + k], U[k * 61 + c], s);
+        if (nnz[r] <= 16) {
+            for (int q = 0; q < nnz[r]; q++) s = fma(nzv[r][q], U[nzk[r][q] * 61 + c], s);
+        } else {
+            for (int kk = 0; kk < 61; kk++) s = fma(dQ[r * 61 + kk], U[kk * 61 + c], s);
+        }
         T[r * 62 + c] = s;
     }
     __syncthreads();
     double *out = Dm + (size_t)which * 64 * 64;
-    for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
-        int r = i / 64, c = i % 64;
+    const int r0 = rb * (64 / DM_RB);
+    for (int i = threadIdx.x; i < (64 / DM_RB) * 64; i += blockDim.x) {
+        const int r = r0 + i / 64, c = i % 64;
         double s = 0;
         if (r < 61 && c < 61)
-            for (int k = 0; k < 61; k++) s = fma(V[r * 61 + k], T[k * 62 + c], s);
-        out[i] = s;
+            for (int kk = 0; kk < 61; kk++) s = fma(V[r * 61 + kk], T[kk * 62 + c], s);
+        out[r * 64 + c] = s;
     }
 }
 
@@ -601,7 +631,7 @@ int adjoint_init(gb_handle *h) {
         (rc = dalloc(&a->d_Ebar, (size_t)h->nslot * MAXC * npad * 64)) ||
         (rc = dalloc(&a->d_Abar, (size_t)h->nslot * npad * 64)) ||
         (rc = dalloc(&a->d_Gpart, h->pairs.size() * a->nchunk * 64 * 64)) ||
-        (rc = dalloc(&a->d_Dm, DM_BLOCKS * 64 * 64)) ||
+        (rc = dalloc(&a->d_Dm, DM_MATS * 64 * 64)) ||
         (h->precision != GB_PREC_FP64 && (rc = dalloc(&a->d_UVdf, 3 * 2 * 61 * 64))) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
         (rc = dalloc(&a->d_fpart, a->nfreq_blocks * 4)) || (rc = dalloc(&a->d_gp, 1)))
         return rc;

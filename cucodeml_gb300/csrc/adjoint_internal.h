@@ -15,7 +15,9 @@ struct gb_handle;
 namespace gb {
 
 constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP
-constexpr int DM_BLOCKS = 8;  // dP/dt kernel: 5 derivative matrices + 3 inverse-difference tables
+constexpr int DM_MATS = 8;    // dP/dt buffer: 5 derivative matrices + 3 inverse-difference tables
+constexpr int DM_RB = 4;      // dP/dt kernel: row blocks per derivative matrix
+constexpr int DM_BLOCKS = 5 * DM_RB + 3;
 
 struct BItem {                // backward work: (node, class family) of one level
     int node, ncls, is_root, nchild;

@@ -804,13 +804,24 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
             const unsigned char *zz = a.z + (size_t)cb.tip * npad;
             const int *xe = a.ebexp + (size_t)cb.ebar * npad;
             const float2 *eb = a.Ebar + (size_t)cb.ebar * npad * 64;
-#pragma unroll 4
-            for (int hh = hbeg + part; hh < hend; hh += 4) {
-                const int x = xe[hh];
-                if (x == ZERO_EXP) continue;
-                const float2 v = df_scale(eb[(size_t)hh * 64 + j], max(x - xr, -1000));
-                float2 *cell = Gt + (part * 64 + zz[hh]) * 64 + j;
-                *cell = df_add(*cell, v);
+            // eight patterns' loads in flight, then their eight updates (the
+            // shared-memory updates would otherwise hold back every next load)
+            for (int base = hbeg + part; base < hend; base += 32) {
+                int xv[8], zv[8];
+                float2 ev[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const int hh = base + 4 * u;
+                    xv[u] = hh < hend ? __ldcg(xe + hh) : ZERO_EXP;
+                    ev[u] = hh < hend ? __ldcg(eb + (size_t)hh * 64 + j) : make_float2(0.f, 0.f);
+                    zv[u] = hh < hend ? zz[hh] : 0;
+                }
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    if (xv[u] == ZERO_EXP) continue;
+                    float2 *cell = Gt + (part * 64 + zv[u]) * 64 + j;
+                    *cell = df_add(*cell, df_scale(ev[u], max(xv[u] - xr, -1000)));
+                }
             }
         }
         __syncthreads();

@@ -33,6 +33,22 @@ __device__ __forceinline__ float2 df_add(float2 a, float2 b) {
     return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
 }
 
+// (s, e) += S w for a power of two w: s <- fl(s + S w) and the exact rounding
+// error of that addition (TwoSum) added to e
+__device__ __forceinline__ void two_sum_acc(float2 &se, float S, float w) {
+    const float t = __fmaf_rn(S, w, se.x);
+    const float bb = __fsub_rn(t, se.x);
+    const float err = __fadd_rn(__fsub_rn(se.x, __fsub_rn(t, bb)), __fmaf_rn(S, w, -bb));
+    se.x = t;
+    se.y = __fadd_rn(se.y, err);
+}
+
+// (s + e) as a normalised double-float (|e| is small against |s| or s = 0)
+__device__ __forceinline__ float2 fast_two_sum(float s, float e) {
+    const float h = __fadd_rn(s, e);
+    return make_float2(h, __fsub_rn(e, __fsub_rn(h, s)));
+}
+
 // exact 2^e scaling: a multiplication by 2^e built from its exponent bits when
 // 2^e is a normal float (the product is then rounded exactly as scalbnf
 // rounds it), scalbnf otherwise
@@ -46,71 +62,48 @@ __device__ __forceinline__ float2 df_scale(float2 a, int e) {
 
 // ---------------------------------------------------------------- digits
 
-// Digits of v = hi + lo (a double-float in [0, 1]) in groups of three 7-bit
-// digits (21 bits) at a time.  floor(x + y) for a proper double-float equals
-// floor(x) unless x is an integer and y < 0; the remainder is renormalised
-// with an exact TwoSum before the next group.
-__device__ __forceinline__ void df_floor_step(float &x, float &y, float &c) {
-    const float fx = floorf(x);
-    const bool is_int = fx == x;
-    const bool neg = y < 0.f;
-    c = (is_int && neg) ? fx - 1.f : fx;
-    const float base = is_int ? (neg ? 1.f : 0.f) : __fsub_rn(x, fx);
-    const float s = __fadd_rn(base, y);
-    const float bb = __fsub_rn(s, base);
-    const float e = __fadd_rn(__fsub_rn(base, __fsub_rn(s, bb)), __fsub_rn(y, bb));
-    x = s;
-    y = e;
-}
-
-__device__ __forceinline__ int small_float_to_int(float c) {   // exact for 0 <= c < 2^23
-    return __float_as_int(__fadd_rn(c, 8388608.0f)) - 0x4B000000;
-}
-
-// floor(|x| * 2^B) from the bit fields of x (|x| = m 2^(e-150), m the 24-bit
-// significand), and whether the product had a fractional part
-template <int B>
-__device__ __forceinline__ unsigned long long fixed_of(float x, bool &inexact) {
-    const unsigned u = __float_as_uint(x) & 0x7fffffffu;
-    const int e = (int)(u >> 23);
-    inexact = false;
-    if (e == 0) {                                   // zero (a denormal is below 2^-126: no digit)
-        inexact = u != 0u;
-        return 0ull;
-    }
-    const unsigned m = (u & 0x7fffffu) | 0x800000u;
-    const int sh = e - 150 + B;
-    if (sh >= 0) return (unsigned long long)m << sh;
-    if (sh <= -24) {
-        inexact = true;
-        return 0ull;
-    }
-    inexact = (m & ((1u << -sh) - 1u)) != 0u;
-    return (unsigned long long)(m >> -sh);
-}
-
-// Digits of v = hi + lo (a double-float in [0, 1]): q = floor(v 2^(7 NS))
-// exactly (hi 2^(7NS) is an integer or truncates to one, lo is added as
-// floor(lo 2^(7NS)) with its sign), then d_s = bits 7(NS-1-s) .. +6 of q;
-// the first digit is 128 only for v = 1.
+// Signed digits of v = hi + lo (a double-float, 0 <= v <= 1, |lo| <= ulp(hi)/2):
+//   v = sum_s d_s 2^(-7(s+1)) + r,   |r| <= 2^(-7 NS - 1) + 2^-59  (2^(-7 NS) for NS <= 5),
+// d_0 in [0, 128], d_s in [-128, 128], every d_s an integer held exactly in a
+// bf16.  Each digit is the nearest integer (balanced digits), computed with the
+// exact FP32 step  d = rint(128 x) (by the 1.5 2^23 shifter), x <- 128 x - d,
+// so every remainder stays within half a unit.  hi gives digits 0..4; lo can
+// reach only digits 3 and up (|lo| 2^21 <= 2^-4) and gives its own digits 3
+// and 4; where both touch a digit it stays within 128 (hi's part there is at
+// most 64, lo's at most 64).  The two remainders (each within half a unit of
+// digit 4) are then added in FP32 (rounding error below 2^-59) and digits
+// 5..NS-1 come from the sum.
 template <int NS>
-__device__ __forceinline__ void digits_of(float hi, float lo, int (&d)[NS]) {
-    constexpr int B = 7 * NS;
-    bool ih, il;
-    const unsigned long long qh = fixed_of<B>(hi, ih);
-    const unsigned long long ql = fixed_of<B>(lo, il);
-    // a fractional hi 2^B is a multiple of 2^(-k) above |lo| 2^B <= 2^(-k-1)
-    // (|lo| <= ulp(hi) / 2), so lo cannot move the floor then
-    long long q = (long long)qh;
-    if (!ih) {
-        if (lo < 0.f) q -= (long long)ql + (il ? 1 : 0);
-        else q += (long long)ql;
-    }
-    if (q < 0) q = 0;
-    const unsigned long long uq = (unsigned long long)q;
-    d[0] = (int)(uq >> (B - 7));
+__device__ __forceinline__ void digits_of(float hi, float lo, float (&d)[NS]) {
+    static_assert(NS >= 4, "lo enters at digit 3");
+    constexpr int NH = NS < 5 ? NS : 5;
+    constexpr float SHIFT = 12582912.0f;      // 1.5 2^23: fl(y + SHIFT) - SHIFT = rint(y), |y| <= 2^22
+    float x = hi;
 #pragma unroll
-    for (int s = 1; s < NS; s++) d[s] = (int)((uq >> (B - 7 * (s + 1))) & 127ull);
+    for (int s = 0; s < NH; s++) {
+        d[s] = __fsub_rn(__fmaf_rn(x, 128.f, SHIFT), SHIFT);
+        x = __fmaf_rn(x, 128.f, -d[s]);
+    }
+    float w = __fmul_rn(lo, 2097152.0f);       // lo 2^21 (exact)
+#pragma unroll
+    for (int s = 3; s < NH; s++) {
+        const float e = __fsub_rn(__fmaf_rn(w, 128.f, SHIFT), SHIFT);
+        w = __fmaf_rn(w, 128.f, -e);
+        d[s] = __fadd_rn(d[s], e);
+    }
+    float r = __fadd_rn(x, w);
+#pragma unroll
+    for (int s = 5; s < NS; s++) {
+        d[s] = __fsub_rn(__fmaf_rn(r, 128.f, SHIFT), SHIFT);
+        if (s + 1 < NS) r = __fmaf_rn(r, 128.f, -d[s]);
+    }
+}
+
+// two integer-valued floats (|d| <= 256) as a bf16 pair, d0 in the low half
+__device__ __forceinline__ unsigned bf16x2(float d0, float d1) {
+    unsigned u;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(u) : "f"(d1), "f"(d0));
+    return u;
 }
 
 __device__ __forceinline__ float small_int_to_float(int d) {   // exact for 0 <= d < 2^23
@@ -156,13 +149,13 @@ __device__ __forceinline__ void slice_tile(const float2 *__restrict__ src, int l
 #pragma unroll 4
     for (int q = 0; q < 16; q++) {           // 2 columns per float4
         const float4 v = s4[q];
-        int d0[NS], d1[NS];
+        float d0[NS], d1[NS];
         digits_of<NS>(v.x, v.y, d0);
         digits_of<NS>(v.z, v.w, d1);
         const int k = k0 + 2 * q;
 #pragma unroll
         for (int s = 0; s < NS; s++)
-            a32[((size_t)s * MT * PITCH + r * PITCH + k) >> 1] = bf16_pair(d0[s], d1[s]);
+            a32[((size_t)s * MT * PITCH + r * PITCH + k) >> 1] = bf16x2(d0[s], d1[s]);
     }
 }
 

@@ -8,11 +8,13 @@
 //    conditional likelihoods normalised to max in [0.5, 1) with an integer
 //    power-of-two exponent per (slot, pattern) carried separately;
 //  * at contraction time each operand value v in [0, 1] is cut into NS
-//    unsigned 7-bit digits, v ~ sum_i d_i 2^{-7i} (d_i in 0..127, 128 only for
-//    v = 1), each held exactly in a bf16 (NS = 8 by default: 56 bits);
+//    balanced digits, v ~ sum_i d_i 2^{-7i} (d_i in -128..128, the first in
+//    0..128; fast_device.cuh digits_of), each held exactly in a bf16 (NS = 8 by
+//    default: 56 bits); P's planes are unsigned 7-bit digits (0..127, 128 only
+//    for P = 1);
 //  * digit products d_a d_b summed over K = 64 states and over the pairs of one
-//    significance level (i + j = L) stay below NS * 64 * 127 * 128 < 2^24, so the
-//    FP32 accumulation of mma.sync m16n8k16 bf16 is exact; levels
+//    significance level (i + j = L) stay within NS * 64 * 128 * 128 <= 2^23, so
+//    the FP32 accumulation of mma.sync m16n8k16 bf16 is exact; levels
 //    L = 2..NS+1 are kept (the triangular truncation) and combined in
 //    double-float with weights 2^{-7L};
 //  * children's messages are multiplied in double-float, each node's rows are

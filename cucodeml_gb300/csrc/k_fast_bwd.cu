@@ -8,8 +8,9 @@
 //   A_{s_i} += Ebar_i P_i                                 (digit planes, tensor cores)
 //   dlnL/dP_i += sum_h Ebar_i[h]^T L~_{s_i}[h]            (digit planes, tensor cores; tips: FP64 scatter)
 // with A_root = fpatt rho / f~ * pi.  Ebar and A rows are renormalised like L~
-// and carry their own exponents; all of them are non-negative, so the digit
-// planes stay unsigned and the tensor-core sums stay exact.
+// and carry their own exponents; all of them are non-negative and cut into
+// balanced digits (|d| <= 128), so the tensor-core sums over 64 patterns stay
+// within NS * 64 * 128^2 <= 2^23 and exact.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -241,19 +242,19 @@ __global__ void __launch_bounds__(256, 1) gradP_fast_kernel(FastBwdArgs a) {
                 unsigned *b32 = reinterpret_cast<unsigned *>(Bs);
 #pragma unroll 2
                 for (int u = 0; u < 8; u++) {
-                    int d0[NS], d1[NS];
+                    float d0[NS], d1[NS];
                     const float2 x0 = hA < nh ? df_scale(eA[u], dA) : make_float2(0.f, 0.f);
                     const float2 x1 = hB < nh ? df_scale(eB[u], dB) : make_float2(0.f, 0.f);
                     digits_of<NS>(x0.x, x0.y, d0);
                     digits_of<NS>(x1.x, x1.y, d1);
 #pragma unroll
-                    for (int s = 0; s < NS; s++) a32[((size_t)s * 64 * PITCH + (s0 + u) * PITCH + hA) >> 1] = bf16_pair(d0[s], d1[s]);
+                    for (int s = 0; s < NS; s++) a32[((size_t)s * 64 * PITCH + (s0 + u) * PITCH + hA) >> 1] = bf16x2(d0[s], d1[s]);
                     const float2 y0 = hA < nh ? lA[u] : make_float2(0.f, 0.f);
                     const float2 y1 = hB < nh ? lB[u] : make_float2(0.f, 0.f);
                     digits_of<NS>(y0.x, y0.y, d0);
                     digits_of<NS>(y1.x, y1.y, d1);
 #pragma unroll
-                    for (int s = 0; s < NS; s++) b32[((size_t)s * 64 * PITCH + (s0 + u) * PITCH + hA) >> 1] = bf16_pair(d0[s], d1[s]);
+                    for (int s = 0; s < NS; s++) b32[((size_t)s * 64 * PITCH + (s0 + u) * PITCH + hA) >> 1] = bf16x2(d0[s], d1[s]);
                 }
             }
             __syncthreads();

@@ -151,12 +151,12 @@ __device__ __forceinline__ void slice_A_cm(const float2 *__restrict__ src, unsig
 #pragma unroll
     for (int q = 0; q < ACM; q++) {
         const int cmi = warp * ACM + q;
-        int d0[NS], d1[NS];
+        float d0[NS], d1[NS];
         digits_of<NS>(v[q].x, v[q].y, d0);
         digits_of<NS>(v[q].z, v[q].w, d1);
         const int off = cmi * 128 + rr * 16 + kp * 4;
 #pragma unroll
-        for (int s = 0; s < NS; s++) *reinterpret_cast<unsigned *>(A + s * A_PLANE + off) = bf16_pair(d0[s], d1[s]);
+        for (int s = 0; s < NS; s++) *reinterpret_cast<unsigned *>(A + s * A_PLANE + off) = bf16x2(d0[s], d1[s]);
     }
 }
 
@@ -230,7 +230,11 @@ __device__ __forceinline__ bool mma_round(unsigned char *sm, Misc *m, uint32_t &
 
 // Every thread reads its row's NCOL columns of every level and accumulates
 //   C = (init ? 0 : C 2^sc_in) + 2^sc_new sum_L S_L 2^(-7L)
-// in double-float (exact power-of-two scalings).
+// The level sums S_L are exact integers and the weights powers of two: each
+// term is added smallest level first with an exact TwoSum into (s, e), the
+// rounding errors summed in e (a compensated sum, as accurate as double-float
+// additions at 7 instead of 12 FP32 operations), and (s, e) is renormalised
+// once at the end.
 template <int NS>
 __device__ __forceinline__ void readout(Misc *m, float2 (&C)[NCOL], bool init, int sc_in, int sc_new) {
     const int warp = threadIdx.x >> 5;
@@ -248,13 +252,15 @@ __device__ __forceinline__ void readout(Misc *m, float2 (&C)[NCOL], bool init, i
         umma::tmem_wait_ld();
         const float w0 = scalbnf(1.0f, -7 * L + sc_new);
 #pragma unroll
-        for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(__uint_as_float(r0[c]) * w0, 0.f));
+        for (int c = 0; c < NCOL; c++) two_sum_acc(C[c], __uint_as_float(r0[c]), w0);
         if (L2 != L) {
             const float w1 = scalbnf(1.0f, -7 * L2 + sc_new);
 #pragma unroll
-            for (int c = 0; c < NCOL; c++) C[c] = df_add(C[c], make_float2(__uint_as_float(r1[c]) * w1, 0.f));
+            for (int c = 0; c < NCOL; c++) two_sum_acc(C[c], __uint_as_float(r1[c]), w1);
         }
     }
+#pragma unroll
+    for (int c = 0; c < NCOL; c++) C[c] = fast_two_sum(C[c].x, C[c].y);
     umma::fence_before();
 }
 
@@ -734,7 +740,7 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
             continue;
         }
         // 128 patterns per read-out: two 64-pattern MMA rounds add into the same
-        // level accumulators (level sums <= 7 * 128 * 127^2 + ... < 2^24 stay
+        // level accumulators (level sums <= NB * 128 * 128^2 <= 2^24 stay
         // exact), rows scaled against the pair of sub-chunks' largest exponent
         for (int hb = hbeg; hb < hend && ok; hb += 128) {
             __syncthreads();                                   // previous read-out and exponents are done
@@ -769,20 +775,20 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
                     const int cmi = warp * GCM + q;
                     const int hh = (cmi & 7) * 8 + 2 * kp;
                     const int off = cmi * 128 + rr * 16 + kp * 4;
-                    int d0[NB], d1[NB];
+                    float d0[NB], d1[NB];
                     const float2 x0 = hh < nh ? df_scale(xe[q][0], max(xh[hh] - xmax, -1000)) : xe[q][0];
                     const float2 x1 = hh + 1 < nh ? df_scale(xe[q][1], max(xh[hh + 1] - xmax, -1000)) : xe[q][1];
                     digits_of<NB>(x0.x, x0.y, d0);
                     digits_of<NB>(x1.x, x1.y, d1);
 #pragma unroll
                     for (int s = 0; s < NB; s++)
-                        *reinterpret_cast<unsigned *>(sm + s * A_PLANE + off) = bf16_pair(d0[s], d1[s]);
+                        *reinterpret_cast<unsigned *>(sm + s * A_PLANE + off) = bf16x2(d0[s], d1[s]);
                     unsigned char *Bp = sm + GSm<NB>::OFF_B + off;
                     digits_of<NB>(yl[q][0].x, yl[q][0].y, d0);
                     digits_of<NB>(yl[q][1].x, yl[q][1].y, d1);
 #pragma unroll
                     for (int s = 0; s < NB; s++)
-                        *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16_pair(d0[s], d1[s]);
+                        *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16x2(d0[s], d1[s]);
                 }
                 ok = mma_round<NB>(sm, m, phase, GSm<NB>::OFF_B, false, half == 1);
             }

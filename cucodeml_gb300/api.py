@@ -170,7 +170,8 @@ class Likelihood:
 
     def task_trace(self, kernel: int) -> np.ndarray:
         """[ntask, 12] uint64 trace of the last evaluation's persistent kernel
-        (0 pruning, 1 adjoint propagation, 2 dlnL/dP): gene, item, tile, 0,
+        (0 pruning, 1 adjoint propagation, 2 dlnL/dP): gene, item, tile, edge
+        (adjoint: child edge of a split item, -1 as two's complement for a whole item),
         claim ns, dependencies-met ns, four phase stamps (0 if absent), end ns, SM.  Needs GBCODEML_TRACE=1 in
         the environment before the first evaluation of this handle."""
         n = self._L.gb_task_trace(self._h, int(kernel), None, 0)

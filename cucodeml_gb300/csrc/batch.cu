@@ -56,7 +56,7 @@ struct gb_batch {
         void *args = nullptr;
         int2 *map = nullptr;
         int nblocks = 0;
-    } l_pmat, l_pslice, l_mix, l_dmat, l_gradH, l_freq;
+    } l_pmat, l_pslice, l_mix, l_mixg, l_dmat, l_gradH, l_freq;   // l_mixg: with the adjoint's root seed
 };
 
 namespace {
@@ -90,7 +90,8 @@ void batch_free(gb_batch *b) {
     if (!b) return;
     cudaSetDevice(b->device);
     unstage(b);
-    for (auto *l : {&b->l_pmat, &b->l_pslice, &b->l_mix, &b->l_dmat, &b->l_gradH, &b->l_freq}) free_launch(*l);
+    for (auto *l : {&b->l_pmat, &b->l_pslice, &b->l_mix, &b->l_mixg, &b->l_dmat, &b->l_gradH, &b->l_freq})
+        free_launch(*l);
     for (auto &g : b->graph)
         if (g) cudaGraphExecDestroy(g);
     for (auto e : b->join)
@@ -242,10 +243,11 @@ int build_launches(gb_batch *b, bool grad) {
              *a = fast_pslice_args(h);
              return (int)h->pairs.size();
          })) ||
-        (rc = make_launch<MixArgs>(b, b->l_mix, [](gb_handle *h, MixArgs *a) {
+        (rc = make_launch<MixArgs>(b, grad ? b->l_mixg : b->l_mix, [grad](gb_handle *h, MixArgs *a) {
              const int nb = (h->npatt + 255) / 256;
              *a = MixArgs{h->d_fhK, h->d_fpatt, h->d_prm, h->npatt, h->npad, 1, nb,
-                          h->d_lnf, h->d_post, h->d_partial, h->d_ticket, h->d_out};
+                          h->d_lnf, h->d_post, h->d_partial, h->d_ticket, h->d_out, h->d_fbar,
+                          grad ? fast_groot(h) : nullptr};
              return nb;
          })))
         return rc;
@@ -305,7 +307,8 @@ int record_persistent(gb_batch *b, bool grad) {
     launch_pmat_batched((const PmatArgs *)b->l_pmat.args, b->l_pmat.map, b->l_pmat.nblocks, o);
     launch_pslice_batched((const PsliceArgs *)b->l_pslice.args, b->l_pslice.map, b->l_pslice.nblocks, ns, o);
     int nk = 3 + persist_record_fwd(&b->plan, grad, ns, o, nullptr);
-    launch_mix_batched((const MixArgs *)b->l_mix.args, b->l_mix.map, b->l_mix.nblocks, o);
+    const gb_batch::Launch &lm = grad ? b->l_mixg : b->l_mix;
+    launch_mix_batched((const MixArgs *)lm.args, lm.map, lm.nblocks, o);
     nk++;
     if (grad) {
         launch_dmat_batched((const DmatArgs *)b->l_dmat.args, b->l_dmat.map, b->l_dmat.nblocks, o);

@@ -34,6 +34,8 @@ struct MixArgs {
     double *lnf, *post, *partial;
     unsigned *ticket;
     double *out;
+    const double *fbar;          // split precision with a gradient: root sums f~ [4][npad] ...
+    float2 *groot;               // ... and the adjoint's root seed fpatt post / f~ as double-float (nullable)
 };
 
 struct DmatArgs {

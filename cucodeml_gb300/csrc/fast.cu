@@ -24,6 +24,8 @@ struct FastState {
     __nv_bfloat16 *Bf = nullptr, *Bb = nullptr;
     int *expo = nullptr, *expo_root = nullptr;
     int *ebexp = nullptr, *aexp = nullptr;     // adjoint exponents
+    float2 *groot = nullptr;                   // [4][npad] adjoint root seed (written by the mixture)
+    float2 *pidf = nullptr;                    // [64] codon frequencies as double-float (zero padded)
     int *err = nullptr, *h_err = nullptr;      // bounded-wait failure flag (device, pinned host)
     bool umma = true;                          // tcgen05 contractions (else mma.sync)
     bool persist = true;                       // persistent task-list kernels (tcgen05 only)
@@ -43,7 +45,7 @@ void fast_free(FastState *f) {
     if (f->h_err) cudaFreeHost(f->h_err);
     persist_free(&f->plan);
     void *p[] = {f->Pdf, f->conP, f->E, f->Bf, f->Bb, f->expo, f->expo_root, f->ebexp, f->aexp, f->err,
-                 f->ready_f, f->ready_b};
+                 f->ready_f, f->ready_b, f->groot, f->pidf};
     for (void *q : p)
         if (q) cudaFree(q);
     delete f;
@@ -167,6 +169,8 @@ FastBwdArgs bwd_args(gb_handle *h) {
     b.post = h->d_post;
     b.fbar = h->d_fbar;
     b.pi = h->d_pi;
+    b.groot = f->groot;
+    b.pidf = f->pidf;
     b.contrib = ad->d_contrib;
     b.coff = ad->d_coff;
     b.z = h->d_z;
@@ -226,9 +230,17 @@ int fast_alloc(gb_handle *h, bool grad) {
     if ((rc = adjoint_init(h))) return rc;
     if (!f->ebexp) {
         if ((rc = dalloc(&f->ebexp, (size_t)h->nslot * MAXC * h->npad)) ||
-            (rc = dalloc(&f->aexp, (size_t)h->nslot * h->npad)))
+            (rc = dalloc(&f->aexp, (size_t)h->nslot * h->npad)) || (rc = dalloc(&f->groot, 4 * h->npad)) ||
+            (rc = dalloc(&f->pidf, 64)))
             return rc;
         CK(cudaMemset(f->aexp, 0, sizeof(int) * h->nslot * h->npad));
+        CK(cudaMemset(f->groot, 0, sizeof(float2) * 4 * h->npad));   // padded patterns stay 0
+        std::vector<float2> pd(64, make_float2(0.f, 0.f));
+        for (int j = 0; j < 61; j++) {
+            const float hi = (float)h->pi[j];
+            pd[j] = make_float2(hi, (float)(h->pi[j] - (double)hi));
+        }
+        CK(cudaMemcpy(f->pidf, pd.data(), sizeof(float2) * 64, cudaMemcpyHostToDevice));
         CK(init_fast_bwd_kernels(f->ns));
     }
     return 0;
@@ -346,8 +358,20 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const 
             const AdjointState *ad = hs[g]->adj;
             if (d + 1 >= (int)ad->blevel_off.size()) return;
             const int nt = hs[g]->npad / FAST_MT;
-            for (int i = ad->blevel_off[d]; i < ad->blevel_off[d + 1]; i++)
-                for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, 0});
+            for (int i = ad->blevel_off[d]; i < ad->blevel_off[d + 1]; i++) {
+                // an item with two or more internal children (the root has three
+                // children) is split into one task per child edge: each edge's
+                // contractions are the bulk of the work, and near the root the
+                // items are few
+                const BItem &b = ad->bitems[i];
+                int ninternal = 0;
+                for (int c = 0; c < b.nchild; c++) ninternal += b.tslot[c][0] >= 0;
+                if (ninternal >= 2)
+                    for (int c = 0; c < b.nchild; c++)
+                        for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, c});
+                else
+                    for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, -1});
+            }
         };
         int maxB = 0;
         for (int g = 0; g < n; g++) maxB = std::max(maxB, (int)hs[g]->adj->blevel_off.size() - 1);
@@ -413,7 +437,7 @@ int fast_rec_pmat(gb_handle *h) {
 int fast_rec_mix(gb_handle *h) {
     // every node is renormalised, so fhK is always in log form
     launch_mix(h->d_fhK, h->d_fpatt, h->d_prm, h->npatt, h->npad, 1, h->d_lnf, h->d_post, h->d_partial,
-               h->d_ticket, h->d_out, h->stream);
+               h->d_ticket, h->d_out, h->stream, h->d_fbar, h->fast->groot);
     prof_mark(h, GB_K_MIX);
     return 1;
 }
@@ -456,6 +480,8 @@ int fast_prepare(gb_handle *h, bool grad) {
 
 bool fast_persistent(const gb_handle *h) { return h->fast && h->fast->persist; }
 
+float2 *fast_groot(gb_handle *h) { return h->fast ? h->fast->groot : nullptr; }
+
 PsliceArgs fast_pslice_args(gb_handle *h) {
     FastState *f = h->fast;
     return PsliceArgs{h->d_Pt, f->Pdf, f->Bf, f->Bb};
@@ -487,7 +513,7 @@ int persist_task_trace(PersistPlan *pp, int kernel, unsigned long long *out, int
             o[0] = (unsigned long long)t[i].gene;
             o[1] = (unsigned long long)t[i].item;
             o[2] = (unsigned long long)t[i].tile;
-            o[3] = 0;
+            o[3] = (unsigned long long)(long long)t[i].edge;
             for (int q = 0; q < TRACE_WORDS; q++) o[4 + q] = tr[(size_t)TRACE_WORDS * i + q];
         }
     }

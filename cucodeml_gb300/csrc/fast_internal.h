@@ -15,7 +15,8 @@ constexpr int FAST_MT = 128;   // patterns per CTA tile in the split-precision k
 // one unit of work of a persistent kernel: (gene, item, tile); for dlnL/dP
 // item = pair and tile = pattern chunk
 struct Task {
-    int gene, item, tile, pad;
+    int gene, item, tile;
+    int edge;        // adjoint: the one child edge of the item this task handles (-1: all of them)
 };
 
 // control words of a persistent executor (device memory): the evaluation
@@ -82,6 +83,8 @@ struct FastBwdArgs {
     unsigned *ready;             // [nslot][ntile] epoch of the last Abar write of (slot, tile)
     int ntile;
     const float2 *Pdf;           // P as double-float (a tip's edge message is a row of it)
+    const float2 *groot;         // [4][npad] root seed fpatt post / f~ (double-float)
+    const float2 *pidf;          // [64] codon frequencies (double-float, zero padded)
 };
 
 cudaError_t init_fast_kernels(int ns);

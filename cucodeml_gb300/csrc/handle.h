@@ -134,6 +134,7 @@ int fast_rec_tail(gb_handle *h);      // per-pair and class-weight gradient sums
 int fast_rec_copies_out(gb_handle *h, bool grad);
 bool fast_persistent(const gb_handle *h);
 struct PsliceArgs;
+float2 *fast_groot(gb_handle *h);                               // adjoint root seed (nullptr without one)
 PsliceArgs fast_pslice_args(gb_handle *h);                      // P digit-plane buffers (batched launches)
 void fast_swap_err(gb_handle *h, int *&d_err, int *&h_err);     // exchange the error word (batch staging)
 int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);

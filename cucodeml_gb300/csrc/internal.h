@@ -58,6 +58,6 @@ void launch_prune_fp64(const Item *items, int nitems, int ntile, int npad, const
                        double *ssum, double *fhK, cudaStream_t st);
 void launch_mix(const double *fhK, const double *fpatt, const DevParams *prm, int npatt, int npad,
                 int nscale, double *lnf, double *post, double *partial, unsigned *ticket,
-                double *out, cudaStream_t st);
+                double *out, cudaStream_t st, const double *fbar = nullptr, float2 *groot = nullptr);
 
 }  // namespace gb

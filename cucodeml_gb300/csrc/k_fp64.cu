@@ -217,7 +217,8 @@ __device__ __forceinline__ void mix_body(const double *__restrict__ fhK, const d
                                          const DevParams *__restrict__ prm, int npatt, int npad, int nscale,
                                          double *__restrict__ lnf, double *__restrict__ post,
                                          double *__restrict__ partial, unsigned *__restrict__ ticket,
-                                         double *__restrict__ out, int bid, int nb) {
+                                         double *__restrict__ out, int bid, int nb,
+                                         const double *__restrict__ fbar, float2 *__restrict__ groot) {
     __shared__ double red[256];
     __shared__ bool last;
     const int h = bid * blockDim.x + threadIdx.x;
@@ -263,6 +264,14 @@ __device__ __forceinline__ void mix_body(const double *__restrict__ fhK, const d
         if (post)
 #pragma unroll
             for (int c = 0; c < 4; c++) post[(size_t)c * npad + h] = q[c];
+        if (groot)      // dlnL/df~_c = fpatt post_c / f~_c, the adjoint's root seed
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                const double f = fbar[(size_t)c * npad + h];
+                const double g = (fp > 0.0 && f > 0.0) ? fp * q[c] / f : 0.0;
+                const float gh = (float)g;
+                groot[(size_t)c * npad + h] = make_float2(gh, (float)(g - (double)gh));
+            }
     }
     red[threadIdx.x] = contrib;
     __syncthreads();
@@ -302,8 +311,11 @@ __global__ void __launch_bounds__(256) mix_kernel(const double *__restrict__ fhK
                                                   double *__restrict__ post,
                                                   double *__restrict__ partial,
                                                   unsigned *__restrict__ ticket,
-                                                  double *__restrict__ out) {
-    mix_body(fhK, fpatt, prm, npatt, npad, nscale, lnf, post, partial, ticket, out, blockIdx.x, gridDim.x);
+                                                  double *__restrict__ out,
+                                                  const double *__restrict__ fbar,
+                                                  float2 *__restrict__ groot) {
+    mix_body(fhK, fpatt, prm, npatt, npad, nscale, lnf, post, partial, ticket, out, blockIdx.x, gridDim.x,
+             fbar, groot);
 }
 
 __global__ void __launch_bounds__(256) mix_batched_kernel(const MixArgs *__restrict__ args,
@@ -311,7 +323,7 @@ __global__ void __launch_bounds__(256) mix_batched_kernel(const MixArgs *__restr
     const int2 g = map[blockIdx.x];
     const MixArgs &a = args[g.x];
     mix_body(a.fhK, a.fpatt, a.prm, a.npatt, a.npad, a.nscale, a.lnf, a.post, a.partial, a.ticket, a.out, g.y,
-             a.nblocks);
+             a.nblocks, a.fbar, a.groot);
 }
 
 }  // namespace
@@ -348,9 +360,10 @@ void launch_prune_fp64(const Item *items, int nitems, int ntile, int npad, const
 
 void launch_mix(const double *fhK, const double *fpatt, const DevParams *prm, int npatt, int npad,
                 int nscale, double *lnf, double *post, double *partial, unsigned *ticket,
-                double *out, cudaStream_t st) {
+                double *out, cudaStream_t st, const double *fbar, float2 *groot) {
     int nb = (npatt + 255) / 256;
-    mix_kernel<<<nb, 256, 0, st>>>(fhK, fpatt, prm, npatt, npad, nscale, lnf, post, partial, ticket, out);
+    mix_kernel<<<nb, 256, 0, st>>>(fhK, fpatt, prm, npatt, npad, nscale, lnf, post, partial, ticket, out, fbar,
+                                   groot);
 }
 
 }  // namespace gb

@@ -497,9 +497,89 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
 
 // ---------------------------------------------------------------- adjoint propagation
 
+// Ebar rows of child edge i under class k for one 128-pattern tile:
+//   Ebar_i = A 2^{-sh_a} prod_{siblings s} E_s
+// (A: the node's upper partial, or at the root the seed fpatt post / f~ times
+// pi), renormalised per row, with the row exponent in ebexp.  Warp-row
+// layout: warp w holds rows 8w..8w+7, lane l states 2l and 2l+1 of each, so
+// every row is read and written as 512 contiguous bytes and the row maxima
+// come from warp shuffles, with no block barrier.  Lane j < 8 loads the
+// per-row scalars (exponents, a tip sibling's codon) of row j.
+__device__ __forceinline__ void ebar_rows(const FastBwdArgs &a, const BItem &it, int tile, int i, int k) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t npad = a.npad;
+    const size_t r0 = (size_t)tile * 128 + 8 * warp;     // this warp's first row
+    const size_t hl = r0 + (lane & 7);                   // the row of this lane's scalars
+    const int c = it.cls[k], ps = it.pslot[k];
+    // exponent of A 2^{-sh_a}: sh_a = expo_a - sum over children of their expo
+    int ea = -(it.is_root ? a.expo_root[(size_t)c * npad + hl] : a.expo[(size_t)ps * npad + hl]);
+    for (int q = 0; q < it.nchild; q++)
+        if (it.tslot[q][k] >= 0) ea += a.expo[(size_t)it.tslot[q][k] * npad + hl];
+    int eX = ea;
+    if (!it.is_root) {
+        const int ax = __ldcg(a.aexp + (size_t)ps * npad + hl);
+        eX = ax == ZERO_EXP ? ZERO_EXP : ax + ea;
+    }
+    float4 X[8];
+    if (it.is_root) {
+        const float2 g = a.groot[(size_t)c * npad + hl];
+        const float2 p0 = __ldg(a.pidf + 2 * lane), p1 = __ldg(a.pidf + 2 * lane + 1);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float2 gj = make_float2(__shfl_sync(0xffffffffu, g.x, j), __shfl_sync(0xffffffffu, g.y, j));
+            const float2 x0 = df_mul(gj, p0), x1 = df_mul(gj, p1);
+            X[j] = make_float4(x0.x, x0.y, x1.x, x1.y);
+        }
+    } else {
+        const float4 *src = reinterpret_cast<const float4 *>(a.Abar + ((size_t)ps * npad + r0) * 64) + lane;
+#pragma unroll
+        for (int j = 0; j < 8; j++) X[j] = __ldcg(src + 32 * j);
+    }
+    for (int s = 0; s < it.nchild; s++) {
+        if (s == i) continue;
+        float4 E[8];
+        if (it.tslot[s][k] < 0) {                      // a tip: its message is the row of P for its codon
+            const int zl = a.z[(size_t)it.child[s] * npad + hl];
+            const float4 *P = reinterpret_cast<const float4 *>(a.Pdf + (size_t)it.pidx[s][k] * 4096) + lane;
+#pragma unroll
+            for (int j = 0; j < 8; j++) E[j] = __ldcg(P + 32 * __shfl_sync(0xffffffffu, zl, j));
+        } else {
+            const float4 *src =
+                reinterpret_cast<const float4 *>(a.E + ((size_t)(ps * MAXC + s) * npad + r0) * 64) + lane;
+#pragma unroll
+            for (int j = 0; j < 8; j++) E[j] = __ldcg(src + 32 * j);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float2 x0 = df_mul(make_float2(X[j].x, X[j].y), make_float2(E[j].x, E[j].y));
+            const float2 x1 = df_mul(make_float2(X[j].z, X[j].w), make_float2(E[j].z, E[j].w));
+            X[j] = make_float4(x0.x, x0.y, x1.x, x1.y);
+        }
+    }
+    const size_t eb = (size_t)(ps * MAXC + i);
+    float4 *dst = reinterpret_cast<float4 *>(a.Ebar + (eb * npad + r0) * 64) + lane;
+    int shl = 0;
+    float mxl = 0.f;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        float m = fmaxf(2 * lane < NC ? X[j].x : 0.f, 2 * lane + 1 < NC ? X[j].z : 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        const int sh = m > 0.f ? ilogbf(m) + 1 : 0;
+        const float2 x0 = df_scale(make_float2(X[j].x, X[j].y), -sh);
+        const float2 x1 = df_scale(make_float2(X[j].z, X[j].w), -sh);
+        dst[32 * j] = make_float4(x0.x, x0.y, x1.x, x1.y);
+        if ((lane & 7) == j) {
+            shl = sh;
+            mxl = m;
+        }
+    }
+    if (lane < 8) a.ebexp[eb * npad + hl] = (!(mxl > 0.f) || eX == ZERO_EXP) ? ZERO_EXP : eX + shl;
+}
+
 template <int NS>
 __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsigned char *sm, Misc *m,
-                         uint32_t &phase, unsigned long long *tr = nullptr, int tidx = 0) {
+                         uint32_t &phase, unsigned long long *tr = nullptr, int tidx = 0, int only = -1) {
     bool first = true;
     float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_RMAX);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -510,65 +590,10 @@ __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsign
     bool ok = true;
 
     int par = 0;           // row_max buffer parity
-    int eAs[2] = {0, 0};   // exponent of A_a 2^{-sh_a} per class for this row
-    for (int k = 0; k < it.ncls; k++) {
-        const int c = it.cls[k];
-        const int ep = it.is_root ? a.expo_root[(size_t)c * npad + h] : a.expo[(size_t)it.pslot[k] * npad + h];
-        int ec = 0;
-        for (int i = 0; i < it.nchild; i++)
-            if (it.tslot[i][k] >= 0) ec += a.expo[(size_t)it.tslot[i][k] * npad + h];
-        eAs[k] = -(ep - ec);
-    }
 
     for (int i = 0; i < it.nchild && ok; i++) {
-        for (int k = 0; k < it.ncls; k++) {
-            const int c = it.cls[k];
-            // the first sibling's message is requested before the upper partial
-            const int s1 = i == 0 ? 1 : 0;
-            float2 Ev[NCOL];
-            if (it.tslot[s1][k] < 0) {
-                const int zs = a.z[(size_t)it.child[s1] * npad + h];
-                load_row32(a.Pdf + (size_t)it.pidx[s1][k] * 4096 + zs * 64 + c0, Ev);
-            } else {
-                load_row32(a.E + ((size_t)(it.pslot[k] * MAXC + s1) * npad + h) * 64 + c0, Ev);
-            }
-            float2 X[NCOL];
-            int eX;
-            if (it.is_root) {
-                const double g = a.fpatt[h] * a.post[(size_t)c * npad + h] / a.fbar[(size_t)c * npad + h];
-#pragma unroll
-                for (int q = 0; q < NCOL; q++) {
-                    const double v = (c0 + q < NC) ? g * a.pi[c0 + q] : 0.0;
-                    const float hi = (float)v;
-                    X[q] = make_float2(hi, (float)(v - (double)hi));
-                }
-                eX = eAs[k];
-            } else {
-                load_row32(a.Abar + ((size_t)it.pslot[k] * npad + h) * 64 + c0, X);
-                const int ea = __ldcg(a.aexp + (size_t)it.pslot[k] * npad + h);
-                eX = ea == ZERO_EXP ? ZERO_EXP : ea + eAs[k];
-            }
-#pragma unroll
-            for (int q = 0; q < NCOL; q++) X[q] = df_mul(X[q], Ev[q]);
-            if (it.nchild == 3) {                            // the root's second sibling
-                const int s2 = 3 - i - s1;
-                if (it.tslot[s2][k] < 0) {
-                    const int zs = a.z[(size_t)it.child[s2] * npad + h];
-                    load_row32(a.Pdf + (size_t)it.pidx[s2][k] * 4096 + zs * 64 + c0, Ev);
-                } else {
-                    load_row32(a.E + ((size_t)(it.pslot[k] * MAXC + s2) * npad + h) * 64 + c0, Ev);
-                }
-#pragma unroll
-                for (int q = 0; q < NCOL; q++) X[q] = df_mul(X[q], Ev[q]);
-            }
-            const float mx = row_max(X, c0, rmax, row, ch, par);
-            const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
-#pragma unroll
-            for (int q = 0; q < NCOL; q++) X[q] = df_scale(X[q], -sh);
-            const size_t eb = (size_t)(it.pslot[k] * MAXC + i);
-            store_row32(a.Ebar + (eb * npad + h) * 64 + c0, X);
-            if (ch == 0) a.ebexp[eb * npad + h] = (!(mx > 0.f) || eX == ZERO_EXP) ? ZERO_EXP : eX + sh;
-        }
+        if (only >= 0 && i != only) continue;
+        for (int k = 0; k < it.ncls; k++) ebar_rows(a, it, tile, i, k);
         if (it.tslot[i][0] < 0) continue;
         const bool shared = it.ncls == 1 || it.tslot[i][0] == it.tslot[i][1];
         const int ntarget = shared ? 1 : 2;
@@ -667,7 +692,7 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
             break;
         }
         trace_put(trace, idx, TR_READY, umma::global_ns());
-        if (!bwd_tile<NS>(*a, *it, t.tile, sm, m, phase, trace, idx)) break;
+        if (!bwd_tile<NS>(*a, *it, t.tile, sm, m, phase, trace, idx, t.edge)) break;
         __syncthreads();
         trace_put(trace, idx, TR_END, umma::global_ns());
         trace_put(trace, idx, TR_SM, smid());
@@ -676,7 +701,7 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
         // barrier, which thread 0 reaches only after this
         if (threadIdx.x == 0)
             for (int i = 0; i < it->nchild; i++) {
-                if (it->tslot[i][0] < 0) continue;
+                if (it->tslot[i][0] < 0 || (t.edge >= 0 && i != t.edge)) continue;
                 set_flag(a->ready + (size_t)it->tslot[i][0] * a->ntile + t.tile, epoch);
                 if (it->ncls == 2 && it->tslot[i][1] != it->tslot[i][0])
                     set_flag(a->ready + (size_t)it->tslot[i][1] * a->ntile + t.tile, epoch);

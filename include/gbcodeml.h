@@ -237,7 +237,8 @@ int gb_batch_tune(gb_batch *b, int knob, int value);
  * the device's global timer, when it was claimed, when its dependencies were
  * met and when it ended, and the SM that ran it.  kernel: 0 pruning, 1 adjoint
  * propagation, 2 dlnL/dP.  Writes up to cap tasks, 12 words each (gene, item,
- * tile, 0, claim ns, ready ns, four phase stamps (pruning: tips gathered,
+ * tile, edge (adjoint: the child edge a split item's task handles, -1 for the
+ * whole item; 0 otherwise, as two's complement), claim ns, ready ns, four phase stamps (pruning: tips gathered,
  * first contraction's planes cut, its MMAs complete, its levels read; adjoint:
  * the same for its first contraction, the first stamp after the first child's
  * messages; 0 where a kernel records none), end ns, SM), and returns the

@@ -70,7 +70,10 @@ template <int NB>
 struct GSm {
     static constexpr int OFF_B = NB * A_PLANE;
     static constexpr int PLANES = NB * (A_PLANE + B_PLANE);
-    static constexpr int OFF_MISC = PLANES > 4 * 4096 * 8 ? PLANES : 4 * 4096 * 8;   // also holds the tip partials
+    // the planes' space also holds the tip partials [4][64][64] and, while
+    // they are summed, the read-out accumulators [64][64] (double-float)
+    static constexpr int OFF_STASH = 4 * 4096 * 8;
+    static constexpr int OFF_MISC = PLANES > OFF_STASH + 4096 * 8 ? PLANES : OFF_STASH + 4096 * 8;
     static constexpr int OFF_XS = OFF_MISC + 64;              // int [128] exponents
     static constexpr int OFF_RED = OFF_XS + 512;              // int [16] reductions
     static constexpr int OFF_ARGS = OFF_RED + 64;
@@ -722,7 +725,20 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
 // shared memory instead.  Threads of TMEM lanes 0..63 (warps w with
 // w % 4 < 2) own output rows j, NCOL columns each.
 template <int NB>
-__device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char *sm, Misc *m, uint32_t &phase) {
+__device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char *sm, Misc *m, uint32_t &phase,
+                           unsigned long long *tr = nullptr, int tidx = 0) {
+    // tracing only: time spent per phase (exponents, operand planes, MMAs,
+    // read-outs), measured by thread 0 between block barriers
+    unsigned long long tlast = tr ? umma::global_ns() : 0, tdur[4] = {0, 0, 0, 0};
+    auto tick = [&](int slot) {
+        if (!tr) return;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const unsigned long long now = umma::global_ns();
+            tdur[slot] += now - tlast;
+            tlast = now;
+        }
+    };
     int *xs = reinterpret_cast<int *>(sm + GSm<NB>::OFF_XS);
     int *red = reinterpret_cast<int *>(sm + GSm<NB>::OFF_RED);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -742,6 +758,7 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
     atomicMax(&red[0], xl);
     __syncthreads();
     const int xr = red[0];
+    tick(0);
     float2 *out = a.Gpart + ((size_t)p * a.nchunk + chunk) * 64 * 64;
     if (xr == ZERO_EXP) {
         for (int i = tid; i < 4096; i += NT) out[i] = make_float2(0.f, 0.f);
@@ -769,12 +786,17 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         // exact), rows scaled against the pair of sub-chunks' largest exponent
         for (int hb = hbeg; hb < hend && ok; hb += 128) {
             __syncthreads();                                   // previous read-out and exponents are done
-            if (tid < 128) xs[tid] = hb + tid < hend ? a.ebexp[(size_t)cb.ebar * npad + hb + tid] : ZERO_EXP;
-            if (tid == 0) red[1] = ZERO_EXP;
+            if (tid < 128) {                                   // warps 0..3: exponents and their maximum
+                const int x = hb + tid < hend ? a.ebexp[(size_t)cb.ebar * npad + hb + tid] : ZERO_EXP;
+                xs[tid] = x;
+                int mx = x;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                if (lane == 0) red[4 + warp] = mx;
+            }
             __syncthreads();
-            if (tid < 128) atomicMax(&red[1], xs[tid]);
-            __syncthreads();
-            const int xmax = red[1];
+            const int xmax = max(max(red[4], red[5]), max(red[6], red[7]));
+            tick(0);
             if (xmax == ZERO_EXP) continue;
             for (int half = 0; half < 2 && ok; half++) {
                 const int hs = hb + 64 * half, nh = min(64, hend - hs);
@@ -815,10 +837,14 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
                     for (int s = 0; s < NB; s++)
                         *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16x2(d0[s], d1[s]);
                 }
+                tick(1);
                 ok = mma_round<NB>(sm, m, phase, GSm<NB>::OFF_B, false, half == 1);
+                tick(2);
             }
             if (!ok) break;
-            readout<NB>(m, acc, false, 0, max(xmax - xr, -1000));
+            // rows 64..127 (TMEM lanes of warps 2 and 3 of each group of four) are zero
+            if ((warp & 3) < 2) readout<NB>(m, acc, false, 0, max(xmax - xr, -1000));
+            tick(3);
         }
     }
     if (ok && any_tip) {
@@ -826,6 +852,10 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         // double-float partial sums in shared memory, 4 pattern partitions x 64 x 64
         __syncthreads();
         float2 *Gt = reinterpret_cast<float2 *>(sm);
+        float2 *stash = reinterpret_cast<float2 *>(sm + GSm<NB>::OFF_STASH);   // frees acc's registers
+        if (row < 64)
+#pragma unroll
+            for (int c = 0; c < NCOL; c++) stash[(c0 + c) * 64 + row] = acc[c];
         for (int i = tid; i < 4 * 4096; i += NT) Gt[i] = make_float2(0.f, 0.f);
         __syncthreads();
         const int j = tid & 63, part = tid >> 6;
@@ -835,20 +865,20 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
             const unsigned char *zz = a.z + (size_t)cb.tip * npad;
             const int *xe = a.ebexp + (size_t)cb.ebar * npad;
             const float2 *eb = a.Ebar + (size_t)cb.ebar * npad * 64;
-            // eight patterns' loads in flight, then their eight updates (the
+            // twelve patterns' loads in flight, then their twelve updates (the
             // shared-memory updates would otherwise hold back every next load)
-            for (int base = hbeg + part; base < hend; base += 32) {
-                int xv[8], zv[8];
-                float2 ev[8];
+            for (int base = hbeg + part; base < hend; base += 48) {
+                int xv[12], zv[12];
+                float2 ev[12];
 #pragma unroll
-                for (int u = 0; u < 8; u++) {
+                for (int u = 0; u < 12; u++) {
                     const int hh = base + 4 * u;
                     xv[u] = hh < hend ? __ldcg(xe + hh) : ZERO_EXP;
                     ev[u] = hh < hend ? __ldcg(eb + (size_t)hh * 64 + j) : make_float2(0.f, 0.f);
                     zv[u] = hh < hend ? zz[hh] : 0;
                 }
 #pragma unroll
-                for (int u = 0; u < 8; u++) {
+                for (int u = 0; u < 12; u++) {
                     if (xv[u] == ZERO_EXP) continue;
                     float2 *cell = Gt + (part * 64 + zv[u]) * 64 + j;
                     *cell = df_add(*cell, df_scale(ev[u], max(xv[u] - xr, -1000)));
@@ -857,9 +887,12 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         }
         __syncthreads();
         if (row < 64)
-#pragma unroll 4
-            for (int c = 0; c < NCOL; c++)
+#pragma unroll
+            for (int c = 0; c < NCOL; c++) {
+                acc[c] = stash[(c0 + c) * 64 + row];
+#pragma unroll
                 for (int pp = 0; pp < 4; pp++) acc[c] = df_add(acc[c], Gt[(pp * 64 + c0 + c) * 64 + row]);
+            }
         __syncthreads();                                       // partials read before the planes are reused
     }
     if (!ok) {
@@ -869,6 +902,7 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
     if (row < 64)
 #pragma unroll
         for (int c = 0; c < NCOL; c++) out[row * 64 + c0 + c] = df_scale(acc[c], xr);
+    for (int q = 0; q < 4; q++) trace_put(tr, tidx, TR_P0 + q, tdur[q]);
     return true;
 }
 
@@ -902,7 +936,7 @@ __global__ void __launch_bounds__(NT, 1) gradP_persist_kernel(const FastBwdArgs 
         stage(a, genes + t.gene);
         __syncthreads();
         trace_put(trace, idx, TR_READY, umma::global_ns());
-        if (!gradP_task<NB>(*a, t.item, t.tile, sm, m, phase)) break;
+        if (!gradP_task<NB>(*a, t.item, t.tile, sm, m, phase, trace, idx)) break;
         __syncthreads();
         trace_put(trace, idx, TR_END, umma::global_ns());
         trace_put(trace, idx, TR_SM, smid());

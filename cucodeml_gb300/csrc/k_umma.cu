@@ -70,10 +70,10 @@ template <int NB>
 struct GSm {
     static constexpr int OFF_B = NB * A_PLANE;
     static constexpr int PLANES = NB * (A_PLANE + B_PLANE);
-    // the planes' space also holds the tip partials [4][64][64] and, while
-    // they are summed, the read-out accumulators [64][64] (double-float)
-    static constexpr int OFF_STASH = 4 * 4096 * 8;
-    static constexpr int OFF_MISC = PLANES > OFF_STASH + 4096 * 8 ? PLANES : OFF_STASH + 4096 * 8;
+    // the planes' space also holds the tip partials [4][64][64] (double-float);
+    // the task's accumulators G[k][j] (double-float, [k][j]) follow
+    static constexpr int OFF_ACC = PLANES > 4 * 4096 * 8 ? PLANES : 4 * 4096 * 8;
+    static constexpr int OFF_MISC = OFF_ACC + 4096 * 8;
     static constexpr int OFF_XS = OFF_MISC + 64;              // int [128] exponents
     static constexpr int OFF_RED = OFF_XS + 512;              // int [16] reductions
     static constexpr int OFF_ARGS = OFF_RED + 64;
@@ -140,29 +140,6 @@ __device__ __forceinline__ int claim(unsigned *counter, Misc *m) {
     return m->task;
 }
 
-template <int NS>
-__device__ __forceinline__ void slice_A_cm(const float2 *__restrict__ src, unsigned char *A) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rr = lane >> 2, kp = lane & 3;
-    float4 v[ACM];
-#pragma unroll
-    for (int q = 0; q < ACM; q++) {                      // all loads in flight first
-        const int cmi = warp * ACM + q;                  // core matrix: row group cmi/8, k group cmi%8
-        const int row = (cmi >> 3) * 8 + rr, k = (cmi & 7) * 8 + 2 * kp;
-        v[q] = __ldcg(reinterpret_cast<const float4 *>(src + (size_t)row * 64 + k));
-    }
-#pragma unroll
-    for (int q = 0; q < ACM; q++) {
-        const int cmi = warp * ACM + q;
-        float d0[NS], d1[NS];
-        digits_of<NS>(v[q].x, v[q].y, d0);
-        digits_of<NS>(v[q].z, v[q].w, d1);
-        const int off = cmi * 128 + rr * 16 + kp * 4;
-#pragma unroll
-        for (int s = 0; s < NS; s++) *reinterpret_cast<unsigned *>(A + s * A_PLANE + off) = bf16x2(d0[s], d1[s]);
-    }
-}
-
 // thread 0: bulk copy of the first NS digit planes of P (global, core-matrix
 // layout, 8 KB per plane) into shared memory, completing on m->mbar_b
 template <int NS>
@@ -172,63 +149,6 @@ __device__ __forceinline__ void start_B(const __nv_bfloat16 *__restrict__ B, uns
 #pragma unroll
         for (int s = 0; s < NS; s++) umma::bulk_g2s(Bs + s * B_PLANE, B + (size_t)s * 4096, B_PLANE, mbar_b);
     }
-}
-
-// All MMAs of a contraction, issued by the calling warp (all lanes; the
-// instruction executes in the leader lane): level L = 2..NS+1 accumulates the
-// pairs (i, L - i) over K = 64 (4 steps of 16) into TMEM columns 64 (L - 2).
-// Shared-memory descriptor start addresses are in 16-byte units in the low
-// 14 bits, so plane and K-step offsets are added to the base descriptors.
-template <int NS>
-__device__ __forceinline__ void issue_levels(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t leader,
-                                             uint32_t accumulate) {
-    constexpr uint32_t idesc = umma::make_idesc(128, 64);
-#pragma unroll
-    for (int L = 2; L <= NS + 1; L++) {
-        const int ilo = L - NS > 1 ? L - NS : 1;
-#pragma unroll
-        for (int i = 1; i <= NS; i++) {
-            const int j = L - i;
-            if (i < ilo || j < 1) continue;
-#pragma unroll
-            for (int ks = 0; ks < 4; ks++) {
-                const uint64_t ad = adesc + (uint64_t)(((i - 1) * A_PLANE + ks * 256) >> 4);
-                const uint64_t bd = bdesc + (uint64_t)(((j - 1) * B_PLANE + ks * 256) >> 4);
-                umma::mma_bf16_leader(tmem + (L - 2) * 64, ad, bd, idesc, (i == ilo && ks == 0) ? accumulate : 1u,
-                                      leader);
-            }
-        }
-    }
-}
-
-// All threads: the A planes in shared memory are complete (generic-proxy
-// stores); the B planes are complete or, with wait_b, arriving by bulk copy.
-// Warp 0 issues the MMAs (into the level accumulators, or adding to them with
-// accumulate) and commits; every thread waits (bounded).  Returns a
-// block-uniform success flag; the accumulators are then complete.
-template <int NS>
-__device__ __forceinline__ bool mma_round(unsigned char *sm, Misc *m, uint32_t &phase, int off_b, bool wait_b,
-                                          bool accumulate) {
-    umma::fence_proxy_async();
-    umma::fence_before();
-    __syncthreads();
-    if ((threadIdx.x >> 5) == 0) {
-        umma::fence_after();
-        const bool okb = !wait_b || umma::mbar_wait(&m->mbar_b, phase);
-        const uint32_t leader = umma::elect_one();
-        if (okb)
-            issue_levels<NS>(m->tmem, umma::make_desc(umma::smem_u32(sm)), umma::make_desc(umma::smem_u32(sm + off_b)),
-                             leader, accumulate ? 1u : 0u);
-        if (leader) {
-            umma::commit(&m->mbar);
-            m->okb = okb;
-        }
-    }
-    bool ok = umma::mbar_wait(&m->mbar, phase);
-    umma::fence_after();
-    phase ^= 1u;
-    ok = __syncthreads_and(ok) && m->okb;
-    return ok;
 }
 
 // Every thread reads its row's NCOL columns of every level and accumulates
@@ -267,15 +187,134 @@ __device__ __forceinline__ void readout(Misc *m, float2 (&C)[NCOL], bool init, i
     umma::fence_before();
 }
 
-// one contraction: MMA round and read-out
-template <int NS>
-__device__ __forceinline__ bool contract(unsigned char *sm, Misc *m, uint32_t &phase, float2 (&C)[NCOL],
-                                         int off_b, bool wait_b, bool init = true, int sc_in = 0,
-                                         int sc_new = 0) {
-    const bool ok = mma_round<NS>(sm, m, phase, off_b, wait_b, false);
-    if (ok) readout<NS>(m, C, init, sc_in, sc_new);
-    return ok;
+// ---------------------------------------------------------------- pipelined contractions
+//
+// Warp-specialised contraction: warps 1..15 cut the operand planes K step by
+// K step (16 contraction indices = core-matrix columns 2 KS, 2 KS + 1), taking
+// the 32 core matrices of each step round-robin in step-major order
+// (n = 32 KS + t, warp 1 + n mod 15); a warp arrives on named barrier 1 + KS
+// (after its async-proxy fence) once it has cut its last core matrix of step
+// KS, without waiting.  Warp 0 cuts nothing: it waits on each step's barrier
+// and issues that step's MMAs, so the tensor pipe works on step KS while the
+// other warps cut the next steps, then commits; every thread waits for the
+// commit as in mma_round.  Each barrier id completes once per contraction; the
+// next contraction's arrivals come after this one's commit wait.
+constexpr int CUT_WARPS = NWARP - 1;
+constexpr int CUT_MAX = (128 + CUT_WARPS - 1) / CUT_WARPS;     // core matrices per cutting warp, at most
+
+// The MMAs of K step KS for every level: level L = 2..NS+1 sums the digit
+// pairs (i, L - i) into TMEM columns 64 (L - 2).  Consecutive B planes are
+// contiguous in the K-major core-matrix layout (a plane is 8 row groups of
+// 1024 B) and the levels are contiguous in TMEM, so A plane i against B planes
+// j0..j0+m-1 is one MMA of N = 64 m (m <= 4) into the columns of levels
+// i+j0..i+j0+m-1: 12 MMAs per step for NS = 8 instead of 36 of N = 64, each A
+// tile read from shared memory once per up to four B planes.  Plane 1 of A
+// meets every level once, so its MMAs of step 0 carry the accumulate flag
+// (overwrite the level sums unless accumulating) and all others add.
+// Shared-memory descriptor start addresses are in 16-byte units in the low
+// 14 bits, so plane and K-step offsets are added to the base descriptors.
+template <int NS, int KS>
+__device__ __forceinline__ void issue_kstep(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t leader,
+                                            uint32_t accumulate) {
+#pragma unroll
+    for (int i = 1; i <= NS; i++) {
+#pragma unroll
+        for (int j0 = 1; j0 <= NS + 1 - i; j0 += 4) {
+            const int mm = NS + 2 - i - j0 < 4 ? NS + 2 - i - j0 : 4;
+            const uint32_t idesc = umma::make_idesc(128, 64 * mm);
+            const uint64_t ad = adesc + (uint64_t)(((i - 1) * A_PLANE + KS * 256) >> 4);
+            const uint64_t bd = bdesc + (uint64_t)(((j0 - 1) * B_PLANE + KS * 256) >> 4);
+            umma::mma_bf16_leader(tmem + (i + j0 - 2) * 64, ad, bd, idesc, (i == 1 && KS == 0) ? accumulate : 1u,
+                                  leader);
+        }
+    }
 }
+
+template <int NS, int KS>
+__device__ __forceinline__ void issue_step(unsigned char *sm, Misc *m, uint32_t phase, int off_b, bool wait_b,
+                                           bool accumulate, bool &okb) {
+    umma::bar_sync(1 + KS, NT);
+    umma::fence_after();
+    if (KS == 0) okb = !wait_b || umma::mbar_wait(&m->mbar_b, phase);
+    const uint32_t leader = umma::elect_one();
+    if (okb)
+        issue_kstep<NS, KS>(m->tmem, umma::make_desc(umma::smem_u32(sm)), umma::make_desc(umma::smem_u32(sm + off_b)),
+                            leader, accumulate ? 1u : 0u);
+}
+
+// warp 0: issue the four steps as they are cut, then commit
+template <int NS>
+__device__ __forceinline__ void issue_steps(unsigned char *sm, Misc *m, uint32_t phase, int off_b, bool wait_b,
+                                            bool accumulate, unsigned long long *t_cut) {
+    bool okb = true;
+    issue_step<NS, 0>(sm, m, phase, off_b, wait_b, accumulate, okb);
+    issue_step<NS, 1>(sm, m, phase, off_b, wait_b, accumulate, okb);
+    issue_step<NS, 2>(sm, m, phase, off_b, wait_b, accumulate, okb);
+    issue_step<NS, 3>(sm, m, phase, off_b, wait_b, accumulate, okb);
+    if (t_cut && threadIdx.x == 0) *t_cut = umma::global_ns();
+    if (umma::elect_one()) {
+        umma::commit(&m->mbar);
+        m->okb = okb;
+    }
+}
+
+// cutting warp: core matrix n (step-major) is done; arrive when it was this
+// warp's last one of its step
+__device__ __forceinline__ void cut_done(int n) {
+    if (n + CUT_WARPS >= 32 * ((n >> 5) + 1)) {
+        umma::fence_proxy_async();
+        umma::fence_before();
+        umma::bar_arrive(1 + (n >> 5), NT);
+    }
+}
+
+// all threads, after the steps: wait (bounded) for the committed MMAs;
+// block-uniform success flag
+__device__ __forceinline__ bool kstep_finish(Misc *m, uint32_t &phase) {
+    bool ok = umma::mbar_wait(&m->mbar, phase);
+    umma::fence_after();
+    phase ^= 1u;
+    return __syncthreads_and(ok) && m->okb;
+}
+
+// slice_A_cm and mma_round, warp-specialised and pipelined: the 128 x 64
+// double-float tile at src (rows normalised to [0, 1]) is cut into NS planes
+// while the MMAs of the steps already cut run.  t_cut (nullable): when the
+// last step's MMAs were issued.
+template <int NS>
+__device__ __forceinline__ bool slice_contract(const float2 *__restrict__ src, unsigned char *sm, Misc *m,
+                                               uint32_t &phase, int off_b, bool wait_b,
+                                               unsigned long long *t_cut = nullptr) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        issue_steps<NS>(sm, m, phase, off_b, wait_b, false, t_cut);
+    } else {
+        const int rr = lane >> 2, kp = lane & 3;
+        float4 v[CUT_MAX];
+#pragma unroll
+        for (int u = 0; u < CUT_MAX; u++) {              // all loads in flight first
+            const int n = warp - 1 + CUT_WARPS * u, t = n & 31;
+            const int g = t >> 1, kg = 2 * (n >> 5) + (t & 1);      // row group, k group
+            if (n < 128)
+                v[u] = __ldcg(reinterpret_cast<const float4 *>(src + (size_t)(8 * g + rr) * 64 + 8 * kg + 2 * kp));
+        }
+#pragma unroll
+        for (int u = 0; u < CUT_MAX; u++) {
+            const int n = warp - 1 + CUT_WARPS * u, t = n & 31;
+            if (n >= 128) break;
+            const int g = t >> 1, kg = 2 * (n >> 5) + (t & 1);
+            float d0[NS], d1[NS];
+            digits_of<NS>(v[u].x, v[u].y, d0);
+            digits_of<NS>(v[u].z, v[u].w, d1);
+            const int off = (8 * g + kg) * 128 + rr * 16 + kp * 4;
+#pragma unroll
+            for (int s = 0; s < NS; s++) *reinterpret_cast<unsigned *>(sm + s * A_PLANE + off) = bf16x2(d0[s], d1[s]);
+            cut_done(n);
+        }
+    }
+    return kstep_finish(m, phase);
+}
+
 
 __device__ __forceinline__ void load_row32(const float2 *p, float2 (&v)[NCOL]) {
 #pragma unroll
@@ -383,12 +422,10 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
         float2 E[NCOL];
         __syncthreads();                                   // the previous contraction's planes are free
         start_B<NS>(a.Bf + (size_t)it.pidx[ci] * NS * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
-        slice_A_cm<NS>(a.conP + ((size_t)cs * npad + h0) * 64, sm);
-        if (first && tr) {                                 // tracing only: all planes are cut
-            __syncthreads();
-            trace_put(tr, tidx, TR_SLICED, umma::global_ns());
-        }
-        ok = mma_round<NS>(sm, m, phase, USm<NS>::OFF_B, true, false);
+        unsigned long long t_cut = 0;
+        ok = slice_contract<NS>(a.conP + ((size_t)cs * npad + h0) * 64, sm, m, phase, USm<NS>::OFF_B, true,
+                                tr ? &t_cut : nullptr);
+        if (first) trace_put(tr, tidx, TR_SLICED, t_cut);
         if (!ok) break;
         if (first) trace_put(tr, tidx, TR_MMA, umma::global_ns());
         readout<NS>(m, E, true, 0, 0);
@@ -609,13 +646,11 @@ __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsign
                 __syncthreads();        // this tile's Ebar rows are written and visible
                 if (first) trace_put(tr, tidx, TR_P0, umma::global_ns());
                 start_B<NS>(a.Bb + (size_t)it.pidx[i][k] * a.nsP * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
-                slice_A_cm<NS>(a.Ebar + (eb * npad + h0) * 64, sm);
-                if (first && tr) {
-                    __syncthreads();
-                    trace_put(tr, tidx, TR_SLICED, umma::global_ns());
-                }
                 const int eC = a.ebexp[eb * npad + h];
-                ok = mma_round<NS>(sm, m, phase, USm<NS>::OFF_B, true, false);
+                unsigned long long t_cut = 0;
+                ok = slice_contract<NS>(a.Ebar + (eb * npad + h0) * 64, sm, m, phase, USm<NS>::OFF_B, true,
+                                        tr ? &t_cut : nullptr);
+                if (first) trace_put(tr, tidx, TR_SLICED, t_cut);
                 if (!ok) break;
                 if (first) trace_put(tr, tidx, TR_MMA, umma::global_ns());
                 if (k == kbeg) {
@@ -727,8 +762,8 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
 template <int NB>
 __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char *sm, Misc *m, uint32_t &phase,
                            unsigned long long *tr = nullptr, int tidx = 0) {
-    // tracing only: time spent per phase (exponents, operand planes, MMAs,
-    // read-outs), measured by thread 0 between block barriers
+    // tracing only: time spent per phase (exponents, -, operand planes with
+    // their pipelined MMAs, read-outs), measured by thread 0 between block barriers
     unsigned long long tlast = tr ? umma::global_ns() : 0, tdur[4] = {0, 0, 0, 0};
     auto tick = [&](int slot) {
         if (!tr) return;
@@ -770,9 +805,12 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         reinterpret_cast<uint4 *>(sm + s * A_PLANE + A_PLANE / 2)[r] = make_uint4(0, 0, 0, 0);
     }
     bool ok = true;
-    float2 acc[NCOL];
+    // the accumulators wait in shared memory between read-outs (thread (row, c0..c0+15)
+    // owns G[c0 + c][row], row < 64), so the cutting warps have their registers
+    float2 *accs = reinterpret_cast<float2 *>(sm + GSm<NB>::OFF_ACC);
+    if (row < 64)
 #pragma unroll
-    for (int c = 0; c < NCOL; c++) acc[c] = make_float2(0.f, 0.f);
+        for (int c = 0; c < NCOL; c++) accs[(c0 + c) * 64 + row] = make_float2(0.f, 0.f);
     const int rr = lane >> 2, kp = lane & 3;
     bool any_tip = false;
     for (int ci = cbeg; ci < cend && ok; ci++) {
@@ -802,48 +840,59 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
                 const int hs = hb + 64 * half, nh = min(64, hend - hs);
                 if (nh <= 0) break;
                 const int* xh = xs + 64 * half;
-                // transposed digit planes: warp writes core matrices (j group, h group);
-                // all loads in flight first
-                float2 xe[GCM][2], yl[GCM][2];
+                // transposed digit planes of both operands, warp-specialised as in
+                // slice_contract: 128 core matrices per round, step-major
+                // (n = 32 KS + t; t < 16: Ebar's, else conP's; j group t / 2 mod 8,
+                // h group 2 KS + t mod 2), cut by warps 1..15, issued by warp 0
+                if (warp == 0) {
+                    issue_steps<NB>(sm, m, phase, GSm<NB>::OFF_B, false, half == 1, nullptr);
+                } else {
+                    float2 w0[CUT_MAX], w1[CUT_MAX];
 #pragma unroll
-                for (int q = 0; q < GCM; q++) {
-                    const int cmi = warp * GCM + q;            // 64 core matrices: jg = cmi / 8, hg = cmi % 8
-                    const int j = (cmi >> 3) * 8 + rr, hh = (cmi & 7) * 8 + 2 * kp;
-                    const float2 *eb = a.Ebar + ((size_t)cb.ebar * npad + hs + hh) * 64 + j;
-                    const float2 *lb = a.conP + ((size_t)cb.tslot * npad + hs + hh) * 64 + j;
-                    const float2 z = make_float2(0.f, 0.f);
-                    xe[q][0] = hh < nh ? eb[0] : z;
-                    xe[q][1] = hh + 1 < nh ? eb[64] : z;
-                    yl[q][0] = hh < nh ? lb[0] : z;
-                    yl[q][1] = hh + 1 < nh ? lb[64] : z;
+                    for (int u = 0; u < CUT_MAX; u++) {             // all loads in flight first
+                        const int n = warp - 1 + CUT_WARPS * u, t = n & 31;
+                        const int j = ((t & 15) >> 1) * 8 + rr, hh = (2 * (n >> 5) + (t & 1)) * 8 + 2 * kp;
+                        const float2 *src = t < 16 ? a.Ebar + ((size_t)cb.ebar * npad + hs + hh) * 64 + j
+                                                   : a.conP + ((size_t)cb.tslot * npad + hs + hh) * 64 + j;
+                        const float2 z = make_float2(0.f, 0.f);
+                        w0[u] = n < 128 && hh < nh ? src[0] : z;
+                        w1[u] = n < 128 && hh + 1 < nh ? src[64] : z;
+                    }
+#pragma unroll
+                    for (int u = 0; u < CUT_MAX; u++) {
+                        const int n = warp - 1 + CUT_WARPS * u, t = n & 31;
+                        if (n >= 128) break;
+                        const int jg = (t & 15) >> 1, hg = 2 * (n >> 5) + (t & 1), hh = hg * 8 + 2 * kp;
+                        float2 x0 = w0[u], x1 = w1[u];
+                        if (t < 16) {                                // Ebar rows against the block's largest exponent
+                            if (hh < nh) x0 = df_scale(x0, max(xh[hh] - xmax, -1000));
+                            if (hh + 1 < nh) x1 = df_scale(x1, max(xh[hh + 1] - xmax, -1000));
+                        }
+                        float d0[NB], d1[NB];
+                        digits_of<NB>(x0.x, x0.y, d0);
+                        digits_of<NB>(x1.x, x1.y, d1);
+                        const int off = (jg * 8 + hg) * 128 + rr * 16 + kp * 4;
+                        unsigned char *dst = t < 16 ? sm + off : sm + GSm<NB>::OFF_B + off;
+                        const int pitch = t < 16 ? A_PLANE : B_PLANE;
+#pragma unroll
+                        for (int s = 0; s < NB; s++)
+                            *reinterpret_cast<unsigned *>(dst + s * pitch) = bf16x2(d0[s], d1[s]);
+                        cut_done(n);
+                    }
                 }
-#pragma unroll
-                for (int q = 0; q < GCM; q++) {
-                    const int cmi = warp * GCM + q;
-                    const int hh = (cmi & 7) * 8 + 2 * kp;
-                    const int off = cmi * 128 + rr * 16 + kp * 4;
-                    float d0[NB], d1[NB];
-                    const float2 x0 = hh < nh ? df_scale(xe[q][0], max(xh[hh] - xmax, -1000)) : xe[q][0];
-                    const float2 x1 = hh + 1 < nh ? df_scale(xe[q][1], max(xh[hh + 1] - xmax, -1000)) : xe[q][1];
-                    digits_of<NB>(x0.x, x0.y, d0);
-                    digits_of<NB>(x1.x, x1.y, d1);
-#pragma unroll
-                    for (int s = 0; s < NB; s++)
-                        *reinterpret_cast<unsigned *>(sm + s * A_PLANE + off) = bf16x2(d0[s], d1[s]);
-                    unsigned char *Bp = sm + GSm<NB>::OFF_B + off;
-                    digits_of<NB>(yl[q][0].x, yl[q][0].y, d0);
-                    digits_of<NB>(yl[q][1].x, yl[q][1].y, d1);
-#pragma unroll
-                    for (int s = 0; s < NB; s++)
-                        *reinterpret_cast<unsigned *>(Bp + s * B_PLANE) = bf16x2(d0[s], d1[s]);
-                }
-                tick(1);
-                ok = mma_round<NB>(sm, m, phase, GSm<NB>::OFF_B, false, half == 1);
+                ok = kstep_finish(m, phase);
                 tick(2);
             }
             if (!ok) break;
             // rows 64..127 (TMEM lanes of warps 2 and 3 of each group of four) are zero
-            if ((warp & 3) < 2) readout<NB>(m, acc, false, 0, max(xmax - xr, -1000));
+            if ((warp & 3) < 2) {
+                float2 acc[NCOL];
+#pragma unroll
+                for (int c = 0; c < NCOL; c++) acc[c] = accs[(c0 + c) * 64 + row];
+                readout<NB>(m, acc, false, 0, max(xmax - xr, -1000));
+#pragma unroll
+                for (int c = 0; c < NCOL; c++) accs[(c0 + c) * 64 + row] = acc[c];
+            }
             tick(3);
         }
     }
@@ -852,10 +901,6 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         // double-float partial sums in shared memory, 4 pattern partitions x 64 x 64
         __syncthreads();
         float2 *Gt = reinterpret_cast<float2 *>(sm);
-        float2 *stash = reinterpret_cast<float2 *>(sm + GSm<NB>::OFF_STASH);   // frees acc's registers
-        if (row < 64)
-#pragma unroll
-            for (int c = 0; c < NCOL; c++) stash[(c0 + c) * 64 + row] = acc[c];
         for (int i = tid; i < 4 * 4096; i += NT) Gt[i] = make_float2(0.f, 0.f);
         __syncthreads();
         const int j = tid & 63, part = tid >> 6;
@@ -889,9 +934,10 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         if (row < 64)
 #pragma unroll
             for (int c = 0; c < NCOL; c++) {
-                acc[c] = stash[(c0 + c) * 64 + row];
+                float2 acc = accs[(c0 + c) * 64 + row];
 #pragma unroll
-                for (int pp = 0; pp < 4; pp++) acc[c] = df_add(acc[c], Gt[(pp * 64 + c0 + c) * 64 + row]);
+                for (int pp = 0; pp < 4; pp++) acc = df_add(acc, Gt[(pp * 64 + c0 + c) * 64 + row]);
+                accs[(c0 + c) * 64 + row] = acc;
             }
         __syncthreads();                                       // partials read before the planes are reused
     }
@@ -901,7 +947,7 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
     }
     if (row < 64)
 #pragma unroll
-        for (int c = 0; c < NCOL; c++) out[row * 64 + c0 + c] = df_scale(acc[c], xr);
+        for (int c = 0; c < NCOL; c++) out[row * 64 + c0 + c] = df_scale(accs[(c0 + c) * 64 + row], xr);
     for (int q = 0; q < 4; q++) trace_put(tr, tidx, TR_P0 + q, tdur[q]);
     return true;
 }

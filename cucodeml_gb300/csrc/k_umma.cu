@@ -517,10 +517,17 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
         stage(it, a->items + t.item);
         __syncthreads();
         int good = 1;
-        if (threadIdx.x == 0)
+        if (threadIdx.x == 0) {
+            // the internal children's tiles towards L2 while their flags are awaited
+            // (lines written after the prefetch are updated in L2 as usual)
+            for (int ci = 0; ci < it->nchild; ci++)
+                if (it->cslot[ci] >= 0)
+                    umma::prefetch_l2(a->conP + ((size_t)it->cslot[ci] * a->npad + (size_t)t.tile * 128) * 64,
+                                      128 * 64 * sizeof(float2));
             for (int ci = 0; ci < it->nchild && good; ci++)
                 if (it->cslot[ci] >= 0)
                     good = wait_flag(a->ready + (size_t)it->cslot[ci] * a->ntile + t.tile, epoch, a->err);
+        }
         if (!__syncthreads_and(good)) {
             if (threadIdx.x == 0) atomicExch(a->err, 1);
             break;
@@ -722,6 +729,18 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
         stage(it, a->bitems + t.item);
         __syncthreads();
         int good = 1;
+        if (threadIdx.x == 0) {
+            // this task's input tiles towards L2 while the flags are awaited: the
+            // upper partials and the internal siblings' edge messages
+            const size_t r0 = (size_t)t.tile * 128;
+            for (int k = 0; k < it->ncls; k++) {
+                const int ps = it->pslot[k];
+                if (!it->is_root) umma::prefetch_l2(a->Abar + ((size_t)ps * a->npad + r0) * 64, 128 * 64 * sizeof(float2));
+                for (int s = 0; s < it->nchild; s++)
+                    if (s != t.edge && it->tslot[s][k] >= 0)
+                        umma::prefetch_l2(a->E + ((size_t)(ps * MAXC + s) * a->npad + r0) * 64, 128 * 64 * sizeof(float2));
+            }
+        }
         if (threadIdx.x == 0 && !it->is_root)
             for (int k = 0; k < it->ncls && good; k++)
                 good = wait_flag(a->ready + (size_t)it->pslot[k] * a->ntile + t.tile, epoch, a->err);

@@ -65,14 +65,19 @@ struct USm {
     static constexpr int BYTES = NEED > MIN_SMEM ? NEED : MIN_SMEM;
 };
 
-// dlnL/dP kernel: A planes of 128 rows (rows 64..127 stay zero), B planes of 64 rows
+// dlnL/dP kernel: digit planes packed 8 KB apart (64 rows x 64 K each), so
+// that one M = 128 tile spans two consecutive planes.  Internal children: NB
+// planes of Ebar^T then NB of conP; tips: two buffers of NB planes of Ebar^T
+// and the one-hot plane.  The task's accumulators G[k][j] (double-float)
+// follow, then the usual misc block.
 template <int NB>
 struct GSm {
-    static constexpr int OFF_B = NB * A_PLANE;
-    static constexpr int PLANES = NB * (A_PLANE + B_PLANE);
-    // the planes' space also holds the tip partials [4][64][64] (double-float);
-    // the task's accumulators G[k][j] (double-float, [k][j]) follow
-    static constexpr int OFF_ACC = PLANES > 4 * 4096 * 8 ? PLANES : 4 * 4096 * 8;
+    static constexpr int PL = 8192;
+    static constexpr int OFF_B = NB * PL;
+    static constexpr int INT_BYTES = 2 * NB * PL;
+    static constexpr int TIP_BUF = (NB + 1) * PL;
+    static constexpr int PLANES = INT_BYTES > 2 * TIP_BUF ? INT_BYTES : 2 * TIP_BUF;
+    static constexpr int OFF_ACC = PLANES;
     static constexpr int OFF_MISC = OFF_ACC + 4096 * 8;
     static constexpr int OFF_XS = OFF_MISC + 64;              // int [128] exponents
     static constexpr int OFF_RED = OFF_XS + 512;              // int [16] reductions
@@ -83,7 +88,8 @@ struct GSm {
 
 struct Misc {
     uint64_t mbar;          // MMA completion
-    uint64_t mbar_b;        // bulk copy of the P planes
+    uint64_t mbar_b;        // bulk copy of the P planes (dlnL/dP tips: MMAs of buffer 1)
+    uint64_t mstep[4];      // dlnL/dP: MMAs of each K step of a round
     uint32_t tmem;
     int task;
     int okb;                // the P planes arrived (set by the issuing thread)
@@ -361,6 +367,7 @@ __device__ __forceinline__ void tmem_setup(Misc *m) {
     if (threadIdx.x == 0) {
         umma::mbar_init(&m->mbar, 1);
         umma::mbar_init(&m->mbar_b, 1);
+        for (int k = 0; k < 4; k++) umma::mbar_init(&m->mstep[k], 1);
     }
     umma::fence_before();
     __syncthreads();
@@ -778,8 +785,193 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
 // Children that are tips (one-hot rows) are summed by a segmented scatter in
 // shared memory instead.  Threads of TMEM lanes 0..63 (warps w with
 // w % 4 < 2) own output rows j, NCOL columns each.
+// per-CTA state of the dlnL/dP kernels across tasks: parities of the next
+// completions of m->mbar and m->mbar_b, and the rounds completed on m->mstep
+struct GState {
+    uint32_t phase = 0, phase_b = 0, nround = 0;
+};
+
+// read-out partials of the two TMEM lane halves (lanes 0..63: warps 0, 1 of
+// each group of four; lanes 64..127: warps 2, 3) for the same G[j][c0..c0+15]:
+// added into accs[k][j] one half after the other
+__device__ __forceinline__ void combine_halves(float2 *accs, const float2 (&part)[NCOL], int half, int c0, int j) {
+    for (int hp = 0; hp < 2; hp++) {
+        if (half == hp)
+#pragma unroll
+            for (int c = 0; c < NCOL; c++) {
+                float2 *cell = accs + (c0 + c) * 64 + j;
+                *cell = df_add(*cell, fast_two_sum(part[c].x, part[c].y));
+            }
+        __syncthreads();
+    }
+}
+
+// dlnL/dP of a pair whose child is a tip:
+//   G[j][k] += sum over the chunk's patterns h with the tip's codon z_h = k of Ebar[h][j] 2^{x_h - xr}
+// as tensor-core products A B: A = Ebar^T cut into NB digit planes (M = j,
+// K = h), packed so that one M = 128 tile holds planes 2m (rows 0..63) and
+// 2m + 1 (rows 64..127); B = the one-hot codon matrix of the round's 64
+// patterns (exact 0/1, one plane).  D block m (TMEM columns 64 m) accumulates
+// planes 2m and 2m + 1 over every 64-pattern round of the chunk and every
+// contribution (|sums| <= contributions x gchunk x 128 < 2^24, exact) and is
+// read out once.  Rounds alternate between two shared-memory buffers: warps
+// 1..15 load round r, wait until the MMAs of round r - 2 are done (committed
+// to m->mbar for buffer 0, m->mbar_b for buffer 1), cut, and arrive on named
+// barrier 1 + r mod 2; warp 0 issues.  The read-out adds G 2^-xr into accs.
 template <int NB>
-__device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char *sm, Misc *m, uint32_t &phase,
+__device__ bool gradP_tips(const FastBwdArgs &a, int cbeg, int cend, int hbeg, int hend, int xr, unsigned char *sm,
+                           Misc *m, GState &gs, float2 *accs) {
+    constexpr int NBP = (NB + 1) / 2;              // plane pairs = D blocks
+    constexpr int PL = GSm<NB>::PL, TBUF = GSm<NB>::TIP_BUF;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int rr = lane >> 2, kp = lane & 3;
+    const size_t npad = a.npad;
+    const uint32_t q0 = gs.phase & 1u, q1 = gs.phase_b & 1u;   // parities of the barriers' next completions
+    int r = 0;
+    bool ok = true;
+    for (int ci = cbeg; ci < cend; ci++) {
+        const Contrib cb = a.contrib[ci];
+        const unsigned char *zz = a.z + (size_t)cb.tip * npad;
+        const int *xe = a.ebexp + (size_t)cb.ebar * npad;
+        const float2 *eb = a.Ebar + (size_t)cb.ebar * npad * 64;
+        for (int hs = hbeg; hs < hend; hs += 64, r++) {
+            const int b = r & 1, nh = min(64, hend - hs);
+            unsigned char *buf = sm + b * TBUF;
+            uint64_t *bar = b ? &m->mbar_b : &m->mbar;
+            if (warp == 0) {
+                umma::bar_sync(1 + b, NT);
+                umma::fence_after();
+                const uint32_t leader = umma::elect_one();
+                constexpr uint32_t idesc = umma::make_idesc(128, 64);
+                const uint64_t ad = umma::make_desc(umma::smem_u32(buf));
+                const uint64_t bd = umma::make_desc(umma::smem_u32(buf + NB * PL));
+#pragma unroll
+                for (int ks = 0; ks < 4; ks++)
+#pragma unroll
+                    for (int mm = 0; mm < NBP; mm++)
+                        umma::mma_bf16_leader(m->tmem + 64 * mm, ad + (uint64_t)((2 * mm * PL + ks * 256) >> 4),
+                                              bd + (uint64_t)((ks * 256) >> 4), idesc, (r > 0 || ks > 0) ? 1u : 0u,
+                                              leader);
+                if (leader) umma::commit(bar);
+                continue;
+            }
+            // A: 64 core matrices (j group n / 8, h group n % 8), round-robin over warps 1..15;
+            // loads first, then the wait for the buffer
+            float2 v[5][2];
+            int x[5][2];
+#pragma unroll
+            for (int u = 0; u < 5; u++) {
+                const int n = warp - 1 + CUT_WARPS * u;
+                const int j = (n >> 3) * 8 + rr, hh = (n & 7) * 8 + 2 * kp;
+                const bool in0 = n < 64 && hh < nh, in1 = n < 64 && hh + 1 < nh;
+                v[u][0] = in0 ? __ldcg(eb + (size_t)(hs + hh) * 64 + j) : make_float2(0.f, 0.f);
+                v[u][1] = in1 ? __ldcg(eb + (size_t)(hs + hh + 1) * 64 + j) : make_float2(0.f, 0.f);
+                x[u][0] = in0 ? __ldcg(xe + hs + hh) : ZERO_EXP;
+                x[u][1] = in1 ? __ldcg(xe + hs + hh + 1) : ZERO_EXP;
+            }
+            const int tb = tid - 32;                        // B rows of this thread: tb and tb + 480 (< 512)
+            const uint2 zb0 = *reinterpret_cast<const uint2 *>(zz + hs + 8 * (tb >> 6));
+            const uint2 zb1 = tb + (NT - 32) < 512 ? *reinterpret_cast<const uint2 *>(zz + hs + 8 * ((tb + NT - 32) >> 6))
+                                                  : make_uint2(0xffffffffu, 0xffffffffu);
+            if (r >= 2) ok = umma::mbar_wait(bar, ((b ? q1 : q0) + ((r - 2) >> 1)) & 1u) && ok;
+#pragma unroll
+            for (int u = 0; u < 5; u++) {
+                const int n = warp - 1 + CUT_WARPS * u;
+                if (n >= 64) break;
+                const float2 y0 = df_scale(v[u][0], max(x[u][0] - xr, -1000));
+                const float2 y1 = df_scale(v[u][1], max(x[u][1] - xr, -1000));
+                float d0[NB], d1[NB];
+                digits_of<NB>(y0.x, y0.y, d0);
+                digits_of<NB>(y1.x, y1.y, d1);
+                const int off = n * 128 + rr * 16 + kp * 4;
+#pragma unroll
+                for (int s2 = 0; s2 < NB; s2++)
+                    *reinterpret_cast<unsigned *>(buf + s2 * PL + off) = bf16x2(d0[s2], d1[s2]);
+            }
+            // B: 512 16-byte rows (codon n = row mod 64, pattern group row / 64): 1.0 where z_h = n
+            for (int q2 = 0; q2 < 2; q2++) {
+                const int t = tb + q2 * (NT - 32);
+                if (t >= 512) break;
+                const int n = t & 63, kg = t >> 6;
+                const uint2 zb = q2 ? zb1 : zb0;
+                unsigned w[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const unsigned zw = q < 2 ? zb.x : zb.y, sh = 16 * (q & 1);
+                    const unsigned b0 = (zw >> sh) & 255u, b1 = (zw >> (sh + 8)) & 255u;
+                    w[q] = (b0 == (unsigned)n ? 0x3F80u : 0u) | (b1 == (unsigned)n ? 0x3F800000u : 0u);
+                }
+                *reinterpret_cast<uint4 *>(buf + NB * PL + ((n >> 3) * 8 + kg) * 128 + (n & 7) * 16) =
+                    make_uint4(w[0], w[1], w[2], w[3]);
+            }
+            umma::fence_proxy_async();
+            umma::fence_before();
+            umma::bar_arrive(1 + b, NT);
+        }
+    }
+    // the last two rounds' MMAs (a commit completes after every earlier MMA of its thread)
+    for (int rl = r - 2 > 0 ? r - 2 : 0; rl < r; rl++) {
+        const int bl = rl & 1;
+        ok = umma::mbar_wait(bl ? &m->mbar_b : &m->mbar, ((bl ? q1 : q0) + (rl >> 1)) & 1u) && ok;
+    }
+    umma::fence_after();
+    if (((r + 1) >> 1) & 1) gs.phase ^= 1u;        // rounds on buffer 0: (r + 1) / 2, on buffer 1: r / 2
+    if ((r >> 1) & 1) gs.phase_b ^= 1u;
+    if (!__syncthreads_and(ok)) return false;
+    const int qd = warp & 3, half = qd >> 1, j = 32 * (qd & 1) + lane, c0 = NCOL * (warp >> 2);
+    const uint32_t lane_base = (uint32_t)(32 * qd) << 16;
+    float2 part[NCOL];
+#pragma unroll
+    for (int c = 0; c < NCOL; c++) part[c] = make_float2(0.f, 0.f);
+#pragma unroll 1
+    for (int mm = NBP - 1; mm >= 0; mm--) {        // smallest first
+        const int sp = 2 * mm + half;
+        if (sp >= NB) continue;                    // rows 64..127 of an odd last pair
+        uint32_t rv[NCOL];
+        umma::tmem_ld_nowait(m->tmem + lane_base + 64 * mm + c0, rv);
+        umma::tmem_wait_ld();
+        const float w = scalbnf(1.0f, -7 * (sp + 1));
+#pragma unroll
+        for (int c = 0; c < NCOL; c++) two_sum_acc(part[c], __uint_as_float(rv[c]), w);
+    }
+    umma::fence_before();
+    combine_halves(accs, part, half, c0, j);
+    return true;
+}
+
+// One K step of an internal child's round: A = Ebar^T planes packed (tile m
+// = planes 2m, 2m + 1 in rows 0..63 / 64..127), B = conP planes (K-major,
+// consecutive planes contiguous).  Tile m against B planes j0..j0+c-1 is one
+// MMA of N = 64 c into TMEM blocks beta = 2m + j0 - 1 .. (block beta: level
+// beta + 2 in lanes 0..63, level beta + 3 in lanes 64..127).  Every pair
+// (i, j) with i + j <= NB + 1 is covered (for even i also j = NB + 2 - i:
+// level NB + 2, not read); tile 0 covers every block, so its step-0 MMAs of
+// a block's first round overwrite.  With NB odd the last tile's rows
+// 64..127 are the first conP plane (finite, feeding only level NB + 2).
+template <int NB, int KS>
+__device__ __forceinline__ void issue_int_step(unsigned char *sm, Misc *m, bool first) {
+    umma::bar_sync(1 + KS, NT);
+    umma::fence_after();
+    const uint32_t leader = umma::elect_one();
+    const uint64_t adesc = umma::make_desc(umma::smem_u32(sm));
+    const uint64_t bdesc = umma::make_desc(umma::smem_u32(sm + GSm<NB>::OFF_B));
+#pragma unroll
+    for (int mm = 0; mm <= (NB - 1) / 2; mm++) {
+#pragma unroll
+        for (int j0 = 1; j0 <= NB - 2 * mm; j0 += 4) {
+            const int cnt = NB - 2 * mm - j0 + 1 < 4 ? NB - 2 * mm - j0 + 1 : 4;
+            const uint32_t idesc = umma::make_idesc(128, 64 * cnt);
+            const uint64_t ad = adesc + (uint64_t)((2 * mm * GSm<NB>::PL + KS * 256) >> 4);
+            const uint64_t bd = bdesc + (uint64_t)(((j0 - 1) * GSm<NB>::PL + KS * 256) >> 4);
+            umma::mma_bf16_leader(m->tmem + (2 * mm + j0 - 1) * 64, ad, bd, idesc,
+                                  (mm == 0 && KS == 0 && first) ? 0u : 1u, leader);
+        }
+    }
+    if (leader) umma::commit(&m->mstep[KS]);
+}
+
+template <int NB>
+__device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char *sm, Misc *m, GState &gs,
                            unsigned long long *tr = nullptr, int tidx = 0) {
     // tracing only: time spent per phase (exponents, -, operand planes with
     // their pipelined MMAs, read-outs), measured by thread 0 between block barriers
@@ -818,57 +1010,65 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         for (int i = tid; i < 4096; i += NT) out[i] = make_float2(0.f, 0.f);
         return true;
     }
-    // A rows 64..127 of every plane are zero (the tip partials below overwrite them)
-    for (int i = tid; i < NB * (A_PLANE / 2) / 16; i += NT) {
-        const int s = i / (A_PLANE / 2 / 16), r = i % (A_PLANE / 2 / 16);
-        reinterpret_cast<uint4 *>(sm + s * A_PLANE + A_PLANE / 2)[r] = make_uint4(0, 0, 0, 0);
-    }
-    bool ok = true;
     // the accumulators wait in shared memory between read-outs (thread (row, c0..c0+15)
     // owns G[c0 + c][row], row < 64), so the cutting warps have their registers
     float2 *accs = reinterpret_cast<float2 *>(sm + GSm<NB>::OFF_ACC);
     if (row < 64)
 #pragma unroll
         for (int c = 0; c < NCOL; c++) accs[(c0 + c) * 64 + row] = make_float2(0.f, 0.f);
-    const int rr = lane >> 2, kp = lane & 3;
-    bool any_tip = false;
-    for (int ci = cbeg; ci < cend && ok; ci++) {
-        const Contrib cb = a.contrib[ci];
-        if (cb.tslot < 0) {          // one-hot children: segmented scatter below, no digit planes
-            any_tip = true;
-            continue;
-        }
-        // 128 patterns per read-out: two 64-pattern MMA rounds add into the same
-        // level accumulators (level sums <= NB * 128 * 128^2 <= 2^24 stay
-        // exact), rows scaled against the pair of sub-chunks' largest exponent
-        for (int hb = hbeg; hb < hend && ok; hb += 128) {
-            __syncthreads();                                   // previous read-out and exponents are done
-            if (tid < 128) {                                   // warps 0..3: exponents and their maximum
-                const int x = hb + tid < hend ? a.ebexp[(size_t)cb.ebar * npad + hb + tid] : ZERO_EXP;
-                xs[tid] = x;
-                int mx = x;
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-                if (lane == 0) red[4 + warp] = mx;
+    __syncthreads();
+    // the contributions of a pair share its child: all tips or all internal
+    if (a.contrib[cbeg].tslot < 0) {
+        if (!gradP_tips<NB>(a, cbeg, cend, hbeg, hend, xr, sm, m, gs, accs)) {
+            if (tid == 0) {
+                atomicExch(a.err, 1);
+                umma::mbar_wait(&m->mbar, gs.phase ^ 1u, 1000000000ull);
+                umma::mbar_wait(&m->mbar_b, gs.phase_b ^ 1u, 1000000000ull);
             }
-            __syncthreads();
-            const int xmax = max(max(red[4], red[5]), max(red[6], red[7]));
-            tick(0);
-            if (xmax == ZERO_EXP) continue;
-            for (int half = 0; half < 2 && ok; half++) {
-                const int hs = hb + 64 * half, nh = min(64, hend - hs);
-                if (nh <= 0) break;
-                const int* xh = xs + 64 * half;
-                // transposed digit planes of both operands, warp-specialised as in
-                // slice_contract: 128 core matrices per round, step-major
-                // (n = 32 KS + t; t < 16: Ebar's, else conP's; j group t / 2 mod 8,
-                // h group 2 KS + t mod 2), cut by warps 1..15, issued by warp 0
-                if (warp == 0) {
-                    issue_steps<NB>(sm, m, phase, GSm<NB>::OFF_B, false, half == 1, nullptr);
-                } else {
+            return false;
+        }
+        tick(2);
+    } else {
+        // Internal children: per block of 128 patterns (rows scaled against the
+        // block's largest exponent), two rounds of 64 add into the same level
+        // sums (<= 4 pairs x 128 x 128^2 per lane half: exact).  Warps 1..15 cut
+        // a round's 128 core matrices step-major (n = 32 KS + t; t < 16: Ebar's,
+        // else conP's; j group (t mod 16) / 2, h group 2 KS + t mod 2), each step
+        // after that step's MMAs of the previous round are done (m->mstep[KS]),
+        // and arrive on named barrier 1 + KS; warp 0 issues each step.
+        const int rr = lane >> 2, kp = lane & 3;
+        bool ok = true;
+        for (int ci = cbeg; ci < cend && ok; ci++) {
+            const Contrib cb = a.contrib[ci];
+            for (int hb = hbeg; hb < hend && ok; hb += 128) {
+                __syncthreads();                               // previous read-out and exponents are done
+                if (tid < 128) {                               // warps 0..3: exponents and their maximum
+                    const int x = hb + tid < hend ? a.ebexp[(size_t)cb.ebar * npad + hb + tid] : ZERO_EXP;
+                    xs[tid] = x;
+                    int mx = x;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+                    if (lane == 0) red[4 + warp] = mx;
+                }
+                __syncthreads();
+                const int xmax = max(max(red[4], red[5]), max(red[6], red[7]));
+                tick(0);
+                if (xmax == ZERO_EXP) continue;
+                for (int half = 0; half < 2; half++) {
+                    const int hs = hb + 64 * half, nh = min(64, hend - hs);
+                    if (nh <= 0) break;
+                    const uint32_t g = gs.nround++;            // this round's index on m->mstep
+                    if (warp == 0) {
+                        issue_int_step<NB, 0>(sm, m, half == 0);
+                        issue_int_step<NB, 1>(sm, m, half == 0);
+                        issue_int_step<NB, 2>(sm, m, half == 0);
+                        issue_int_step<NB, 3>(sm, m, half == 0);
+                        continue;
+                    }
+                    const int *xh = xs + 64 * half;
                     float2 w0[CUT_MAX], w1[CUT_MAX];
 #pragma unroll
-                    for (int u = 0; u < CUT_MAX; u++) {             // all loads in flight first
+                    for (int u = 0; u < CUT_MAX; u++) {         // all loads in flight first
                         const int n = warp - 1 + CUT_WARPS * u, t = n & 31;
                         const int j = ((t & 15) >> 1) * 8 + rr, hh = (2 * (n >> 5) + (t & 1)) * 8 + 2 * kp;
                         const float2 *src = t < 16 ? a.Ebar + ((size_t)cb.ebar * npad + hs + hh) * 64 + j
@@ -879,90 +1079,62 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
                     }
 #pragma unroll
                     for (int u = 0; u < CUT_MAX; u++) {
-                        const int n = warp - 1 + CUT_WARPS * u, t = n & 31;
+                        const int n = warp - 1 + CUT_WARPS * u, t = n & 31, ks = n >> 5;
                         if (n >= 128) break;
-                        const int jg = (t & 15) >> 1, hg = 2 * (n >> 5) + (t & 1), hh = hg * 8 + 2 * kp;
+                        // first core matrix of this warp in step ks: the previous round's step is done
+                        if (g > 0 && n - CUT_WARPS < 32 * ks) ok = umma::mbar_wait(&m->mstep[ks], (g - 1) & 1u) && ok;
+                        const int jg = (t & 15) >> 1, hg = 2 * ks + (t & 1), hh = hg * 8 + 2 * kp;
                         float2 x0 = w0[u], x1 = w1[u];
-                        if (t < 16) {                                // Ebar rows against the block's largest exponent
+                        if (t < 16) {                          // Ebar rows against the block's largest exponent
                             if (hh < nh) x0 = df_scale(x0, max(xh[hh] - xmax, -1000));
                             if (hh + 1 < nh) x1 = df_scale(x1, max(xh[hh + 1] - xmax, -1000));
                         }
                         float d0[NB], d1[NB];
                         digits_of<NB>(x0.x, x0.y, d0);
                         digits_of<NB>(x1.x, x1.y, d1);
-                        const int off = (jg * 8 + hg) * 128 + rr * 16 + kp * 4;
-                        unsigned char *dst = t < 16 ? sm + off : sm + GSm<NB>::OFF_B + off;
-                        const int pitch = t < 16 ? A_PLANE : B_PLANE;
+                        unsigned char *dst = sm + (t < 16 ? 0 : GSm<NB>::OFF_B) + (jg * 8 + hg) * 128 + rr * 16 + kp * 4;
 #pragma unroll
-                        for (int s = 0; s < NB; s++)
-                            *reinterpret_cast<unsigned *>(dst + s * pitch) = bf16x2(d0[s], d1[s]);
+                        for (int s2 = 0; s2 < NB; s2++)
+                            *reinterpret_cast<unsigned *>(dst + s2 * GSm<NB>::PL) = bf16x2(d0[s2], d1[s2]);
                         cut_done(n);
                     }
                 }
-                ok = kstep_finish(m, phase);
+                // the block's MMAs (the last commit completes after all earlier ones)
+                ok = umma::mbar_wait(&m->mstep[3], (gs.nround - 1) & 1u) && ok;
+                umma::fence_after();
+                ok = __syncthreads_and(ok);
                 tick(2);
-            }
-            if (!ok) break;
-            // rows 64..127 (TMEM lanes of warps 2 and 3 of each group of four) are zero
-            if ((warp & 3) < 2) {
-                float2 acc[NCOL];
+                if (!ok) break;
+                // read-out by all warps: lane half 0 holds level beta + 2, half 1 level beta + 3
+                const int qd = warp & 3, hl = qd >> 1, j = 32 * (qd & 1) + lane;
+                const uint32_t lane_base = (uint32_t)(32 * qd) << 16;
+                const int sc = max(xmax - xr, -1000);
+                float2 part[NCOL];
 #pragma unroll
-                for (int c = 0; c < NCOL; c++) acc[c] = accs[(c0 + c) * 64 + row];
-                readout<NB>(m, acc, false, 0, max(xmax - xr, -1000));
+                for (int c = 0; c < NCOL; c++) part[c] = make_float2(0.f, 0.f);
+#pragma unroll 1
+                for (int beta = NB - 1; beta >= 0; beta--) {   // smallest level first
+                    const int L = beta + 2 + hl;
+                    if (L > NB + 1) continue;
+                    uint32_t rv[NCOL];
+                    umma::tmem_ld_nowait(m->tmem + lane_base + 64 * beta + c0, rv);
+                    umma::tmem_wait_ld();
+                    const float w = scalbnf(1.0f, -7 * L + sc);
 #pragma unroll
-                for (int c = 0; c < NCOL; c++) accs[(c0 + c) * 64 + row] = acc[c];
-            }
-            tick(3);
-        }
-    }
-    if (ok && any_tip) {
-        // tips: G[j][k] += sum over patterns h with codon z_h = k of Ebar[h][j] 2^{x_h - xr},
-        // double-float partial sums in shared memory, 4 pattern partitions x 64 x 64
-        __syncthreads();
-        float2 *Gt = reinterpret_cast<float2 *>(sm);
-        for (int i = tid; i < 4 * 4096; i += NT) Gt[i] = make_float2(0.f, 0.f);
-        __syncthreads();
-        const int j = tid & 63, part = tid >> 6;
-        for (int ci = cbeg; ci < cend && tid < 256; ci++) {
-            const Contrib cb = a.contrib[ci];
-            if (cb.tslot >= 0) continue;
-            const unsigned char *zz = a.z + (size_t)cb.tip * npad;
-            const int *xe = a.ebexp + (size_t)cb.ebar * npad;
-            const float2 *eb = a.Ebar + (size_t)cb.ebar * npad * 64;
-            // twelve patterns' loads in flight, then their twelve updates (the
-            // shared-memory updates would otherwise hold back every next load)
-            for (int base = hbeg + part; base < hend; base += 48) {
-                int xv[12], zv[12];
-                float2 ev[12];
-#pragma unroll
-                for (int u = 0; u < 12; u++) {
-                    const int hh = base + 4 * u;
-                    xv[u] = hh < hend ? __ldcg(xe + hh) : ZERO_EXP;
-                    ev[u] = hh < hend ? __ldcg(eb + (size_t)hh * 64 + j) : make_float2(0.f, 0.f);
-                    zv[u] = hh < hend ? zz[hh] : 0;
+                    for (int c = 0; c < NCOL; c++) two_sum_acc(part[c], __uint_as_float(rv[c]), w);
                 }
-#pragma unroll
-                for (int u = 0; u < 12; u++) {
-                    if (xv[u] == ZERO_EXP) continue;
-                    float2 *cell = Gt + (part * 64 + zv[u]) * 64 + j;
-                    *cell = df_add(*cell, df_scale(ev[u], max(xv[u] - xr, -1000)));
-                }
+                umma::fence_before();
+                combine_halves(accs, part, hl, c0, j);
+                tick(3);
             }
         }
-        __syncthreads();
-        if (row < 64)
-#pragma unroll
-            for (int c = 0; c < NCOL; c++) {
-                float2 acc = accs[(c0 + c) * 64 + row];
-#pragma unroll
-                for (int pp = 0; pp < 4; pp++) acc = df_add(acc, Gt[(pp * 64 + c0 + c) * 64 + row]);
-                accs[(c0 + c) * 64 + row] = acc;
+        if (!ok) {
+            if (tid == 0) {
+                atomicExch(a.err, 1);
+                for (int k = 0; k < 4; k++) umma::mbar_wait(&m->mstep[k], (gs.nround - 1) & 1u, 1000000000ull);
             }
-        __syncthreads();                                       // partials read before the planes are reused
-    }
-    if (!ok) {
-        on_failure(a.err, m, phase, false);
-        return false;
+            return false;
+        }
     }
     if (row < 64)
 #pragma unroll
@@ -978,8 +1150,8 @@ __global__ void __launch_bounds__(NT, 1) gradP_umma_kernel(FastBwdArgs args) {
     FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + GSm<NB>::OFF_ARGS);
     stage(a, &args);
     tmem_setup(m);
-    uint32_t phase = 0;
-    gradP_task<NB>(*a, blockIdx.x, blockIdx.y, sm, m, phase);
+    GState gs;
+    gradP_task<NB>(*a, blockIdx.x, blockIdx.y, sm, m, gs);
     tmem_teardown(m);
 }
 
@@ -992,7 +1164,7 @@ __global__ void __launch_bounds__(NT, 1) gradP_persist_kernel(const FastBwdArgs 
     Misc *m = reinterpret_cast<Misc *>(sm + GSm<NB>::OFF_MISC);
     FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + GSm<NB>::OFF_ARGS);
     tmem_setup(m);
-    uint32_t phase = 0;
+    GState gs;
     for (;;) {
         const int idx = claim(ctl + CTL_GRADP, m);
         if (idx >= ntask) break;
@@ -1001,7 +1173,7 @@ __global__ void __launch_bounds__(NT, 1) gradP_persist_kernel(const FastBwdArgs 
         stage(a, genes + t.gene);
         __syncthreads();
         trace_put(trace, idx, TR_READY, umma::global_ns());
-        if (!gradP_task<NB>(*a, t.item, t.tile, sm, m, phase, trace, idx)) break;
+        if (!gradP_task<NB>(*a, t.item, t.tile, sm, m, gs, trace, idx)) break;
         __syncthreads();
         trace_put(trace, idx, TR_END, umma::global_ns());
         trace_put(trace, idx, TR_SM, smid());

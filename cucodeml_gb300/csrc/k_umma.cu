@@ -834,6 +834,11 @@ __device__ bool gradP_tips(const FastBwdArgs &a, int cbeg, int cend, int hbeg, i
         const unsigned char *zz = a.z + (size_t)cb.tip * npad;
         const int *xe = a.ebexp + (size_t)cb.ebar * npad;
         const float2 *eb = a.Ebar + (size_t)cb.ebar * npad * 64;
+        if (tid == 32) {                                   // the chunk's rows and exponents towards L2
+            umma::prefetch_l2(eb + (size_t)hbeg * 64, (uint32_t)(hend - hbeg) * 64 * sizeof(float2));
+            const uint32_t xb = (uint32_t)((hend - hbeg) * sizeof(int)) & ~15u;   // whole 16-byte units only
+            if (xb) umma::prefetch_l2(xe + hbeg, xb);
+        }
         for (int hs = hbeg; hs < hend; hs += 64, r++) {
             const int b = r & 1, nh = min(64, hend - hs);
             unsigned char *buf = sm + b * TBUF;
@@ -924,15 +929,23 @@ __device__ bool gradP_tips(const FastBwdArgs &a, int cbeg, int cend, int hbeg, i
 #pragma unroll
     for (int c = 0; c < NCOL; c++) part[c] = make_float2(0.f, 0.f);
 #pragma unroll 1
-    for (int mm = NBP - 1; mm >= 0; mm--) {        // smallest first
-        const int sp = 2 * mm + half;
-        if (sp >= NB) continue;                    // rows 64..127 of an odd last pair
-        uint32_t rv[NCOL];
+    for (int mm = NBP - 1; mm >= 0; mm -= 2) {     // smallest first, two blocks per TMEM wait
+        const int m2 = mm > 0 ? mm - 1 : mm;
+        const int sp = 2 * mm + half, sp2 = 2 * m2 + half;
+        uint32_t rv[NCOL], rv2[NCOL];
         umma::tmem_ld_nowait(m->tmem + lane_base + 64 * mm + c0, rv);
+        umma::tmem_ld_nowait(m->tmem + lane_base + 64 * m2 + c0, rv2);
         umma::tmem_wait_ld();
-        const float w = scalbnf(1.0f, -7 * (sp + 1));
+        if (sp < NB) {                             // (not the rows 64..127 of an odd last pair)
+            const float w = scalbnf(1.0f, -7 * (sp + 1));
 #pragma unroll
-        for (int c = 0; c < NCOL; c++) two_sum_acc(part[c], __uint_as_float(rv[c]), w);
+            for (int c = 0; c < NCOL; c++) two_sum_acc(part[c], __uint_as_float(rv[c]), w);
+        }
+        if (m2 != mm && sp2 < NB) {
+            const float w = scalbnf(1.0f, -7 * (sp2 + 1));
+#pragma unroll
+            for (int c = 0; c < NCOL; c++) two_sum_acc(part[c], __uint_as_float(rv2[c]), w);
+        }
     }
     umma::fence_before();
     combine_halves(accs, part, half, c0, j);
@@ -1040,6 +1053,11 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         bool ok = true;
         for (int ci = cbeg; ci < cend && ok; ci++) {
             const Contrib cb = a.contrib[ci];
+            if (tid == 32) {                               // the chunk's rows towards L2
+                const uint32_t bytes = (uint32_t)(hend - hbeg) * 64 * sizeof(float2);
+                umma::prefetch_l2(a.Ebar + ((size_t)cb.ebar * npad + hbeg) * 64, bytes);
+                umma::prefetch_l2(a.conP + ((size_t)cb.tslot * npad + hbeg) * 64, bytes);
+            }
             for (int hb = hbeg; hb < hend && ok; hb += 128) {
                 __syncthreads();                               // previous read-out and exponents are done
                 if (tid < 128) {                               // warps 0..3: exponents and their maximum
@@ -1113,15 +1131,23 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
 #pragma unroll
                 for (int c = 0; c < NCOL; c++) part[c] = make_float2(0.f, 0.f);
 #pragma unroll 1
-                for (int beta = NB - 1; beta >= 0; beta--) {   // smallest level first
-                    const int L = beta + 2 + hl;
-                    if (L > NB + 1) continue;
-                    uint32_t rv[NCOL];
+                for (int beta = NB - 1; beta >= 0; beta -= 2) {   // smallest level first, two blocks per wait
+                    const int b2 = beta > 0 ? beta - 1 : beta;
+                    const int L = beta + 2 + hl, L2 = b2 + 2 + hl;
+                    uint32_t rv[NCOL], rv2[NCOL];
                     umma::tmem_ld_nowait(m->tmem + lane_base + 64 * beta + c0, rv);
+                    umma::tmem_ld_nowait(m->tmem + lane_base + 64 * b2 + c0, rv2);
                     umma::tmem_wait_ld();
-                    const float w = scalbnf(1.0f, -7 * L + sc);
+                    if (L <= NB + 1) {
+                        const float w = scalbnf(1.0f, -7 * L + sc);
 #pragma unroll
-                    for (int c = 0; c < NCOL; c++) two_sum_acc(part[c], __uint_as_float(rv[c]), w);
+                        for (int c = 0; c < NCOL; c++) two_sum_acc(part[c], __uint_as_float(rv[c]), w);
+                    }
+                    if (b2 != beta && L2 <= NB + 1) {
+                        const float w = scalbnf(1.0f, -7 * L2 + sc);
+#pragma unroll
+                        for (int c = 0; c < NCOL; c++) two_sum_acc(part[c], __uint_as_float(rv2[c]), w);
+                    }
                 }
                 umma::fence_before();
                 combine_halves(accs, part, hl, c0, j);

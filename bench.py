@@ -116,7 +116,7 @@ def make_workload(ns: int, ncodon: int, seed: int = 2024):
 # kernels from one ncu capture at 32 taxa x 2000 codons (1974 patterns, 62
 # contractions, 910811496 contraction FLOPs), profiles/fast_kernels_32x2000.md;
 # scaled to another workload by its contraction FLOPs
-NCU_TRAFFIC_SMALL = {"prune": 7.16e6 + 70.72e6, "bwd": 76.15e6 + 142.30e6, "gradP": 190.43e6 + 13.35e6}
+NCU_TRAFFIC_SMALL = {"prune": 21.92e6 + 70.83e6, "bwd": 84.80e6 + 136.92e6, "gradP": 194.31e6 + 9.91e6}
 NCU_FLOPS_SMALL = 910811496.0
 
 
@@ -383,8 +383,8 @@ def main():
             ex = cls_flops[top] * pairs[top] * (64.0 * 64.0) / (61.0 * 61.0)
             roof["executed_tensor_tflops"] = ex / (top_ms_per_eval * 1e-3) / 1e12
             roof["executed_tensor_frac"] = roof["executed_tensor_tflops"] / peak
-        roof["limiter"] = ("SIMT digit slicing and double-float level recombination around the MMAs, "
-                           "latency-bound at one 16-warp CTA per SM (see profiles/)")
+        roof["limiter"] = ("SIMT work around the MMAs (cutting operands into digit planes, level "
+                           "read-outs, double-float products), one 16-warp CTA per SM (see profiles/)")
         if top in NCU_TRAFFIC_SMALL:
             roof["traffic"] = NCU_TRAFFIC_SMALL[top] * fl["flops_prune"] / NCU_FLOPS_SMALL
             roof["traffic_source"] = ("ncu dram__bytes_read+write of the same kernel at 32 taxa x 2000 codons, "

@@ -236,7 +236,7 @@ int make_launch(gb_batch *b, gb_batch::Launch &l, F per_gene) {   // per_gene(h,
 int build_launches(gb_batch *b, bool grad) {
     int rc;
     if ((rc = make_launch<PmatArgs>(b, b->l_pmat, [](gb_handle *h, PmatArgs *a) {
-             *a = PmatArgs{h->d_pairs, h->d_label, h->d_tnode, h->d_prm, h->d_Pt};
+             *a = PmatArgs{h->d_pairs, h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->d_pi};
              return (int)h->pairs.size();
          })) ||
         (rc = make_launch<PsliceArgs>(b, b->l_pslice, [](gb_handle *h, PsliceArgs *a) {

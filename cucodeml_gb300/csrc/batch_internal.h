@@ -19,6 +19,7 @@ struct PmatArgs {
     const double *tnode;
     const DevParams *prm;
     double *Pt;
+    const double *pi;            // codon frequencies (symmetric form of P, see launch_pmat_fp64)
 };
 
 struct PsliceArgs {

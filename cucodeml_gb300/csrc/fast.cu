@@ -426,7 +426,8 @@ int persist_record_bwd(PersistPlan *pp, int nsb, cudaStream_t st, gb_handle *pro
 // ---------------------------------------------------------------- per-gene pieces
 
 int fast_rec_pmat(gb_handle *h) {
-    launch_pmat_fp64(h->d_pairs, (int)h->pairs.size(), h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->stream);
+    launch_pmat_fp64(h->d_pairs, (int)h->pairs.size(), h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->stream,
+                     h->d_pi);
     prof_mark(h, GB_K_PMAT);
     FastFwdArgs a = fwd_args(h, false);
     launch_pslice(a, h->fast->ns, (int)h->pairs.size(), h->fast->umma, h->stream);
@@ -564,6 +565,7 @@ int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg
     }
     std::memcpy(h->h_prm->qf, D->qf, sizeof(double) * 2);
     std::memcpy(h->h_prm->freqK, D->freqK, sizeof(double) * 4);
+    h->h_prm->sym = D->sym;
     for (int n = 0; n < h->nnode; n++) {
         double t = n == h->root ? 0.0 : blength[n];
         if (!(t >= 0.0)) return fail(GB_ERR_PARAM, "negative or non-finite branch length");

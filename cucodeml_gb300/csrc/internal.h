@@ -46,12 +46,17 @@ struct DevParams {            // uploaded per evaluation
     double Root[3][61];
     double qf[2];
     double freqK[4];
+    int sym;                   // V[m][k] = U[k][m] pi_k (symmetrised eigenproblem): P from its symmetric part;
+                               // after the GB_MODEL_DOUBLES of the no-alloc model block, never read from one
 };
 
 // ---- kernel launchers (k_fp64.cu) ----
 cudaError_t init_fp64_kernels();   // function attributes; call before any capture
+// pi (nullable): the codon frequencies of a model whose U and V come from the
+// symmetrised eigenproblem (V[m][k] = U[k][m] pi_k): P is then formed from its
+// symmetric part S = U diag(e) U^T at about half the FP64 work
 void launch_pmat_fp64(const PairDesc *pairs, int npair, const int *label, const double *tnode,
-                      const DevParams *prm, double *Pt, cudaStream_t st);
+                      const DevParams *prm, double *Pt, cudaStream_t st, const double *pi = nullptr);
 void launch_prune_fp64(const Item *items, int nitems, int ntile, int npad, const unsigned char *z,
                        const double *Pt, double *conP, double *E, double *scaleF,
                        const int *scale_list, int nscale, const double *pi, double *fbar,

@@ -1,7 +1,11 @@
 // FP64 kernels of the drop-in path.
 //
 //   pmat_fp64   P(t) = U diag(exp(Root t)) V for every unique (branch, omega)
-//               pair, stored transposed and zero padded to 64x64
+//               pair, stored transposed and zero padded to 64x64.  With the
+//               codon frequencies given, U and V come from the symmetrised
+//               eigenproblem (V[m][k] = U[k][m] pi_k, eigen_qrev), so
+//               P[j][k] = pi_k S[j][k] with S = U diag(e) U^T symmetric: only
+//               its upper-triangular 8 x 8 blocks are formed (36 of 64).
 //               (PMatUVRoot tools.c:515-546: negatives clamped to 0, t < 1e-100
 //               gives the identity; cuda-codeml.cu:679-742 computes the same per
 //               node and class, here once per unique pair).
@@ -28,10 +32,10 @@ constexpr int NC = 61;
 
 __device__ __forceinline__ void pmat_body(const PairDesc *__restrict__ pairs, const int *__restrict__ label,
                                           const double *__restrict__ tnode, const DevParams *__restrict__ prm,
-                                          double *__restrict__ Pt, int pair) {
+                                          double *__restrict__ Pt, int pair, const double *__restrict__ pi) {
     extern __shared__ double sm[];
     double *UeT = sm;             // [61][64]: UeT[m][j] = U[j][m] e^{Root_m t}
-    double *Vs = sm + NC * 64;    // [61][64]: Vs[m][k] = V[m][k]
+    double *Vs = sm + NC * 64;    // [61][64]: Vs[m][k] = V[m][k] (symmetric form: U[k][m])
     const PairDesc pd = pairs[pair];
     const int w = pd.w;
     const double t = tnode[pd.node] * prm->qf[label[pd.node]];
@@ -43,15 +47,43 @@ __device__ __forceinline__ void pmat_body(const PairDesc *__restrict__ pairs, co
     }
     const double *U = prm->U[w];
     const double *V = prm->V[w];
+    if (pi && !prm->sym) pi = nullptr;                // general U, V: the full product (the flag is read only
+                                                      // with pi: callers without it pass a shorter model block)
     __shared__ double ex[64];
     if (tid < NC) ex[tid] = exp(t * prm->Root[w][tid]);
     __syncthreads();
     for (int i = tid; i < NC * 64; i += blockDim.x) {
         int m = i / 64, c = i % 64;
         UeT[i] = c < NC ? U[c * NC + m] * ex[m] : 0.0;
-        Vs[i] = c < NC ? V[m * NC + c] : 0.0;
+        Vs[i] = c < NC ? (pi ? U[c * NC + m] : V[m * NC + c]) : 0.0;
     }
     __syncthreads();
+    if (pi) {
+        // S[j][k] on the 36 upper-triangular 8 x 8 blocks (R <= C): thread tid
+        // takes entry (tid mod 64) of blocks 4q + tid / 64, q = 0..8; then
+        // Pt[k][j] = P[j][k] = pi_k S[j][k] and Pt[j][k] = pi_j S[j][k]
+        const int e = tid & 63, i8 = e >> 3, j8 = e & 7;
+#pragma unroll 1
+        for (int q = 0; q < 9; q++) {
+            int u = 4 * q + (tid >> 6), R = 0;
+            while (u >= 8 - R) {                      // block u of rows R, R+1, ... (8 - R blocks in row R)
+                u -= 8 - R;
+                R++;
+            }
+            const int C = R + u;
+            if (R == C && i8 > j8) continue;          // a diagonal block's lower half is the upper one mirrored
+            const int j = 8 * R + i8, k = 8 * C + j8;
+            double acc = 0.0;
+            for (int m = 0; m < NC; m++) acc = fma(UeT[m * 64 + j], Vs[m * 64 + k], acc);
+            const bool in = j < NC && k < NC;
+            double pjk = in ? acc * pi[k] : 0.0, pkj = in ? acc * pi[j] : 0.0;
+            if (pjk < 0.0) pjk = 0.0;
+            if (pkj < 0.0) pkj = 0.0;
+            out[k * 64 + j] = pjk;
+            out[j * 64 + k] = pkj;
+        }
+        return;
+    }
     // thread -> row k of Pt (child state), 16 consecutive parent states j
     const int k = tid >> 2;
     const int j0 = (tid & 3) * 16;
@@ -76,8 +108,9 @@ __global__ void __launch_bounds__(256) pmat_fp64_kernel(const PairDesc *__restri
                                                         const int *__restrict__ label,
                                                         const double *__restrict__ tnode,
                                                         const DevParams *__restrict__ prm,
-                                                        double *__restrict__ Pt) {
-    pmat_body(pairs, label, tnode, prm, Pt, blockIdx.x);
+                                                        double *__restrict__ Pt,
+                                                        const double *__restrict__ pi) {
+    pmat_body(pairs, label, tnode, prm, Pt, blockIdx.x, pi);
 }
 
 // many genes in one launch: block b works on pair map[b].y of gene map[b].x
@@ -85,7 +118,7 @@ __global__ void __launch_bounds__(256) pmat_batched_kernel(const PmatArgs *__res
                                                            const int2 *__restrict__ map) {
     const int2 g = map[blockIdx.x];
     const PmatArgs &a = args[g.x];
-    pmat_body(a.pairs, a.label, a.tnode, a.prm, a.Pt, g.y);
+    pmat_body(a.pairs, a.label, a.tnode, a.prm, a.Pt, g.y, a.pi);
 }
 
 // 128 threads: row group rg = tid/16 owns tile rows 4rg..4rg+3, column group
@@ -345,8 +378,8 @@ void launch_mix_batched(const MixArgs *args, const int2 *map, int nblocks, cudaS
 }
 
 void launch_pmat_fp64(const PairDesc *pairs, int npair, const int *label, const double *tnode,
-                      const DevParams *prm, double *Pt, cudaStream_t st) {
-    pmat_fp64_kernel<<<npair, 256, kPmatSmem, st>>>(pairs, label, tnode, prm, Pt);
+                      const DevParams *prm, double *Pt, cudaStream_t st, const double *pi) {
+    pmat_fp64_kernel<<<npair, 256, kPmatSmem, st>>>(pairs, label, tnode, prm, Pt, pi);
 }
 
 void launch_prune_fp64(const Item *items, int nitems, int ntile, int npad, const unsigned char *z,

@@ -20,6 +20,7 @@ struct Derived {
     double U[3][NC * NC], V[3][NC * NC], Root[3][NC];
     double qf[2];        // Qfactor_NS_branch: background, foreground
     double freqK[4];     // p0, p1, p2a, p2b
+    int sym = 1;         // V[m][k] = U[k][m] pi_k (true for eigen_qrev's solutions)
     // derivatives (filled when requested)
     double dqf[2][5];    // d qf[b] / d (kappa, w0, w2, p0, p1)
     double dfreqK[4][2]; // d freqK[c] / d (p0, p1)

@@ -200,7 +200,8 @@ void free_all(gb_handle *h) {
 // record the forward launches on h->stream; returns the number of kernels
 int record_forward(gb_handle *h, bool keepE) {
     int nk = 0;
-    launch_pmat_fp64(h->d_pairs, (int)h->pairs.size(), h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->stream);
+    launch_pmat_fp64(h->d_pairs, (int)h->pairs.size(), h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->stream,
+                     h->d_pi);
     prof_mark(h, GB_K_PMAT);
     nk++;
     int H = (int)h->level_off.size() - 1;
@@ -248,6 +249,7 @@ int upload_and_run(gb_handle *h, const Derived *D, const double *blength, bool k
     }
     std::memcpy(h->h_prm->qf, D->qf, sizeof(double) * 2);
     std::memcpy(h->h_prm->freqK, D->freqK, sizeof(double) * 4);
+    h->h_prm->sym = D->sym;
     for (int n = 0; n < h->nnode; n++) {
         double t = n == h->root ? 0.0 : blength[n];
         if (!(t >= 0.0) || !std::isfinite(t)) return fail(GB_ERR_PARAM, "negative or non-finite branch length");
@@ -293,6 +295,7 @@ int stage_params(gb_handle *h, const Derived *D, const double *blength) {
     }
     std::memcpy(h->h_prm->qf, D->qf, sizeof(double) * 2);
     std::memcpy(h->h_prm->freqK, D->freqK, sizeof(double) * 4);
+    h->h_prm->sym = D->sym;
     for (int n = 0; n < h->nnode; n++) {
         double t = n == h->root ? 0.0 : blength[n];
         if (!(t >= 0.0) || !std::isfinite(t)) return fail(GB_ERR_PARAM, "negative or non-finite branch length");
@@ -440,6 +443,8 @@ int gb_eval_uvr(gb_handle *h, const double *const U[3], const double *const V[3]
     }
     std::memcpy(D->qf, qfactor, sizeof(double) * 2);
     std::memcpy(D->freqK, freqK, sizeof(double) * 4);
+    // the caller's eigen solutions: P = U diag(e) V formed as codeml's PMatUVRoot does
+    D->sym = 0;
     double v = 0;
     int rc = upload_and_run(h, D, blength, false, &v, fhK, lnf, stats);
     delete D;

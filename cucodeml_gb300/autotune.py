@@ -24,6 +24,7 @@ BATCH_CANDIDATES = [
     {"mma": 1, "persist": 1, "gchunk": 256, "order": 0},
     {"mma": 1, "persist": 1, "gchunk": 1024, "order": 0},
     {"mma": 1, "persist": 1, "gchunk": 512, "order": 1},
+    {"mma": 1, "persist": 1, "gchunk": 512, "order": 2},
     {"mma": 1, "persist": 0, "gchunk": 512},
     {"mma": 0, "persist": 0, "gchunk": 512},
 ]

@@ -2,7 +2,7 @@
 // gene, and ONE CUDA graph per batch evaluation.  Split precision with the
 // persistent kernels: the pruning recursion, the adjoint propagation and
 // dlnL/dP of ALL genes are one persistent launch each over a task list that
-// mixes the genes (tasks ordered by tree level, dependencies tracked per
+// mixes the genes (tasks in critical-path order, dependencies tracked per
 // (slot, tile) on the device), and the small per-gene steps (P matrices and
 // their digit planes, the mixture, dP/dt, per-pair sums) are one launch each
 // over all genes (a block-to-gene map); the genes' per-evaluation inputs and
@@ -467,7 +467,7 @@ int gb_batch_tune(gb_batch *b, int knob, int value) {
     if (!b) return fail(GB_ERR_ARG, "gb_batch_tune: null batch");
     if (b->graph[0] || b->graph[1] || b->plan.ctl) return fail(GB_ERR_STATE, "gb_batch_tune: batch already evaluated");
     if (knob == GB_TUNE_ORDER) {
-        if (value != 0 && value != 1) return fail(GB_ERR_ARG, "gb_batch_tune: order must be 0 or 1");
+        if (value < 0 || value > 2) return fail(GB_ERR_ARG, "gb_batch_tune: order must be 0, 1 or 2");
         b->tune.order = value;
         return GB_OK;
     }

@@ -318,8 +318,11 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const 
         CK(cudaMemcpy(pp->d_fargs[k], fa.data(), sizeof(FastFwdArgs) * n, cudaMemcpyHostToDevice));
     }
     if (!pp->d_ftask) {
-        // children before parents: level by level (tree height), all genes per
-        // level (order 0) or gene by gene (order 1)
+        // children before parents.  Order 0 (critical path first): by depth
+        // below the root, deepest first, all genes together, so that the nodes
+        // with the longest chain of ancestors still to compute start first and
+        // every gene's root comes in the last group; 1: gene by gene, level by
+        // level (tree height); 2: level by level across genes
         std::vector<Task> t;
         auto push_level = [&](int g, int L) {
             const gb_handle *h = hs[g];
@@ -330,12 +333,29 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const 
         };
         int maxH = 0;
         for (int g = 0; g < n; g++) maxH = std::max(maxH, (int)hs[g]->level_off.size() - 1);
-        if (tune.order == 1)
+        if (tune.order == 1) {
             for (int g = 0; g < n; g++)
                 for (int L = 0; L < maxH; L++) push_level(g, L);
-        else
+        } else if (tune.order == 2) {
             for (int L = 0; L < maxH; L++)
                 for (int g = 0; g < n; g++) push_level(g, L);
+        } else {
+            struct Key { int depth, g, i; };
+            std::vector<Key> keys;
+            for (int g = 0; g < n; g++) {
+                const gb_handle *h = hs[g];
+                for (int i = 0; i < (int)h->items.size(); i++) {
+                    int d = 0;
+                    for (int a = h->items[i].node; a != h->root; a = h->father[a]) d++;
+                    keys.push_back(Key{d, g, i});
+                }
+            }
+            std::stable_sort(keys.begin(), keys.end(), [](const Key &x, const Key &y) { return x.depth > y.depth; });
+            for (const Key &k : keys) {
+                const int nt = hs[k.g]->npad / FAST_MT;
+                for (int tl = 0; tl < nt; tl++) t.push_back(Task{k.g, k.i, tl, 0});
+            }
+        }
         pp->nftask = (int)t.size();
         const char *tr = std::getenv("GBCODEML_TRACE");
         pp->tracing = tr && std::strcmp(tr, "1") == 0;
@@ -354,33 +374,48 @@ int persist_build(PersistPlan *pp, gb_handle *const *hs, int n, bool bwd, const 
     if (!pp->d_btask) {
         // parents before children: backward levels from each gene's root down
         std::vector<Task> t;
+        auto push_item = [&](int g, int i) {
+            // an item with two or more internal children (the root has three
+            // children) is split into one task per child edge: each edge's
+            // contractions are the bulk of the work, and near the root the
+            // items are few
+            const BItem &b = hs[g]->adj->bitems[i];
+            const int nt = hs[g]->npad / FAST_MT;
+            int ninternal = 0;
+            for (int c = 0; c < b.nchild; c++) ninternal += b.tslot[c][0] >= 0;
+            if (ninternal >= 2)
+                for (int c = 0; c < b.nchild; c++)
+                    for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, c});
+            else
+                for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, -1});
+        };
         auto push_blevel = [&](int g, int d) {
             const AdjointState *ad = hs[g]->adj;
             if (d + 1 >= (int)ad->blevel_off.size()) return;
-            const int nt = hs[g]->npad / FAST_MT;
-            for (int i = ad->blevel_off[d]; i < ad->blevel_off[d + 1]; i++) {
-                // an item with two or more internal children (the root has three
-                // children) is split into one task per child edge: each edge's
-                // contractions are the bulk of the work, and near the root the
-                // items are few
-                const BItem &b = ad->bitems[i];
-                int ninternal = 0;
-                for (int c = 0; c < b.nchild; c++) ninternal += b.tslot[c][0] >= 0;
-                if (ninternal >= 2)
-                    for (int c = 0; c < b.nchild; c++)
-                        for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, c});
-                else
-                    for (int tl = 0; tl < nt; tl++) t.push_back(Task{g, i, tl, -1});
-            }
+            for (int i = ad->blevel_off[d]; i < ad->blevel_off[d + 1]; i++) push_item(g, i);
         };
         int maxB = 0;
         for (int g = 0; g < n; g++) maxB = std::max(maxB, (int)hs[g]->adj->blevel_off.size() - 1);
-        if (tune.order == 1)
+        if (tune.order == 1) {
             for (int g = 0; g < n; g++)
                 for (int d = 0; d < maxB; d++) push_blevel(g, d);
-        else
+        } else if (tune.order == 2) {
             for (int d = 0; d < maxB; d++)
                 for (int g = 0; g < n; g++) push_blevel(g, d);
+        } else {
+            // parents before children, critical path first: by the height of
+            // the subtree below the node (the longest chain of descendants
+            // still to compute), tallest first, all genes together
+            struct Key { int height, g, i; };
+            std::vector<Key> keys;
+            for (int g = 0; g < n; g++) {
+                const AdjointState *ad = hs[g]->adj;
+                for (int i = 0; i < (int)ad->bitems.size(); i++)
+                    keys.push_back(Key{hs[g]->height[ad->bitems[i].node], g, i});
+            }
+            std::stable_sort(keys.begin(), keys.end(), [](const Key &x, const Key &y) { return x.height > y.height; });
+            for (const Key &k : keys) push_item(k.g, k.i);
+        }
         pp->nbtask = (int)t.size();
         if (pp->tracing && (rc = dalloc(&pp->trace[1], TRACE_WORDS * t.size()))) return rc;
         if ((rc = dalloc(&pp->d_btask, t.size()))) return rc;

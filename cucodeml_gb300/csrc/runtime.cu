@@ -577,7 +577,7 @@ int gb_tune(gb_handle *h, int knob, int value) {
             h->tune.gchunk = value;
             return GB_OK;
         case GB_TUNE_ORDER:
-            if (value != 0 && value != 1) return fail(GB_ERR_ARG, "gb_tune: order must be 0 or 1");
+            if (value < 0 || value > 2) return fail(GB_ERR_ARG, "gb_tune: order must be 0, 1 or 2");
             h->tune.order = value;
             return GB_OK;
         case GB_TUNE_GRID:

@@ -217,8 +217,11 @@ int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches
  *                    kernels (default; tcgen05 only)
  *   GB_TUNE_GCHUNK   patterns per partial sum of dlnL/dP (multiple of 64 in
  *                    [64, 8192]; default 512)
- *   GB_TUNE_ORDER    batches: 0 tasks ordered by tree level across genes
- *                    (default), 1 gene by gene
+ *   GB_TUNE_ORDER    task order of the persistent kernels: 0 critical path
+ *                    first (forward: deepest nodes below the root first;
+ *                    adjoint: tallest subtrees first; all genes together;
+ *                    default), 1 gene by gene by tree level, 2 by tree level
+ *                    across genes
  *   GB_TUNE_GRID     CTAs per persistent launch (0: one per SM, the default)
  * Environment defaults: GBCODEML_MMA=sync, GBCODEML_PERSIST=0.
  */

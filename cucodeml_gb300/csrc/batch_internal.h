@@ -44,6 +44,8 @@ struct DmatArgs {
     const GradParams *gp;
     double *Dm;
     float2 *UVdf;
+    __nv_bfloat16 *UVpl;
+    int *UVe;
 };
 
 struct GradHArgs {
@@ -56,6 +58,8 @@ struct GradHArgs {
     const double *Dm;
     const float2 *UVdf;
     double *out;
+    const __nv_bfloat16 *UVpl;
+    const int *UVe;
 };
 
 struct FreqArgs {

@@ -50,21 +50,12 @@ constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256 + 64) * sizeof(double);
 // last 3 blocks: 1/(Root_m - Root_n) for w (and U, V^T as double-float).
 // dQ has at most ~10 non-zeros per row (single-nucleotide neighbours and the
 // diagonal): T = dQ U runs over each row's non-zeros (dense past 16).
-__device__ __forceinline__ void uv_planes(const DevParams *__restrict__ prm, __nv_bfloat16 *__restrict__ UVpl,
-                                          int *__restrict__ UVe, int w, int which);
-
 __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, const GradParams *__restrict__ gp,
-                                          double *__restrict__ Dm, float2 *__restrict__ UVdf,
-                                          __nv_bfloat16 *__restrict__ UVpl, int *__restrict__ UVe, int bid) {
+                                          double *__restrict__ Dm, float2 *__restrict__ UVdf, int bid) {
     __shared__ double T[61 * 62];
     __shared__ int nzk[61][16];
     __shared__ double nzv[61][16];
     __shared__ int nnz[61];
-    if (bid >= 5 * DM_RB + 3) {                    // digit planes of V (which 0) and U^T (which 1) of omega w
-        const int q = bid - 5 * DM_RB - 3;
-        if (UVpl) uv_planes(prm, UVpl, UVe, q >> 1, q & 1);
-        return;
-    }
     if (bid >= 5 * DM_RB) {
         const int w = bid - 5 * DM_RB, which = 5 + w;
         const double *R = prm->Root[w];
@@ -133,16 +124,15 @@ __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, con
 
 __global__ void __launch_bounds__(256) dmat_kernel(const DevParams *__restrict__ prm,
                                                    const GradParams *__restrict__ gp,
-                                                   double *__restrict__ Dm, float2 *__restrict__ UVdf,
-                                                   __nv_bfloat16 *__restrict__ UVpl, int *__restrict__ UVe) {
-    dmat_body(prm, gp, Dm, UVdf, UVpl, UVe, blockIdx.x);
+                                                   double *__restrict__ Dm, float2 *__restrict__ UVdf) {
+    dmat_body(prm, gp, Dm, UVdf, blockIdx.x);
 }
 
 __global__ void __launch_bounds__(256) dmat_batched_kernel(const DmatArgs *__restrict__ args,
                                                            const int2 *__restrict__ map) {
     const int2 g = map[blockIdx.x];
     const DmatArgs &a = args[g.x];
-    dmat_body(a.prm, a.gp, a.Dm, a.UVdf, a.UVpl, a.UVe, g.y);
+    dmat_body(a.prm, a.gp, a.Dm, a.UVdf, g.y);
 }
 
 // one CTA per (32-pattern tile, backward item)
@@ -502,181 +492,6 @@ __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs
     if (tid < 3) out[p * 3 + tid] = red[tid][0];
 }
 
-// The same per-pair sums with the two 61^3 products on the tensor cores: each
-// product A B^T is cut into GH_NS balanced digit planes per operand (rows
-// scaled by exact powers of two to max in [0.5, 1), digits |d| <= 128 as in the
-// contractions, fastdev::digits_of) and summed level by level with mma.sync
-// (bf16 -> FP32 exact, levels combined in double-float: fastdev::ozaki_mma_block).
-//   T[r][n] = sum_k G[r][k] V[n][k]         A = G (rows r), B = V (rows n)
-//   H[r][n] = sum_j U[j][r] T[j][n]         A = U^T (rows r), B = T^T (rows n)
-// Warp w computes rows 16 (w mod 4).., columns 16 (w / 4)..; the Phi-weighted
-// sums of H follow in FP64 as in gradH_df_body.  512 threads per pair.
-static_assert(GH_PITCH == fastdev::PITCH, "plane layout of the mma.sync fragments");
-constexpr int GH_MP = 66;        // row pitch (double-float) of the shared matrix
-constexpr int kGradHmmaSmem = 64 * GH_MP * 8 + 2 * GH_PL * 2 + 2 * 64 * 4 + 64 * 8 + 3 * 512 * 8;
-
-// row maxima (exponents) of a 64 x 64 double-float source: 8 threads per row
-template <class F>
-__device__ __forceinline__ void gh_row_exp(F src, int *e) {
-    const int c8 = threadIdx.x & 7;
-    for (int row = threadIdx.x >> 3; row < 64; row += blockDim.x >> 3) {
-        float m = 0.f;
-#pragma unroll
-        for (int k = c8; k < 64; k += 8) m = fmaxf(m, fabsf(src(row, k).x));
-#pragma unroll
-        for (int o = 4; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (c8 == 0) e[row] = m > 0.f ? ilogbf(m) + 1 : 0;
-    }
-}
-
-// planes P[s][row][k] (row pitch GH_PITCH) of src(row, k) 2^-e[row]
-template <class F>
-__device__ __forceinline__ void gh_slice(F src, const int *e, __nv_bfloat16 *P) {
-    unsigned *p32 = reinterpret_cast<unsigned *>(P);
-    for (int i = threadIdx.x; i < 64 * 32; i += blockDim.x) {
-        const int row = i >> 5, k = 2 * (i & 31);
-        const float2 v0 = fastdev::df_scale(src(row, k), -e[row]);
-        const float2 v1 = fastdev::df_scale(src(row, k + 1), -e[row]);
-        float d0[GH_NS], d1[GH_NS];
-        fastdev::digits_of<GH_NS>(v0.x, v0.y, d0);
-        fastdev::digits_of<GH_NS>(v1.x, v1.y, d1);
-#pragma unroll
-        for (int q = 0; q < GH_NS; q++)
-            p32[((size_t)q * 64 * GH_PITCH + row * GH_PITCH + k) >> 1] = fastdev::bf16x2(d0[q], d1[q]);
-    }
-}
-
-// once per evaluation and omega (dP/dt launch): the planes of V (which 0: rows
-// n, K = k) and of U^T (which 1: rows r, K = j) with their row exponents
-__device__ __forceinline__ void uv_planes(const DevParams *__restrict__ prm, __nv_bfloat16 *__restrict__ UVpl,
-                                          int *__restrict__ UVe, int w, int which) {
-    __shared__ int e[64];
-    const double *M = which ? prm->U[w] : prm->V[w];
-    auto src = [&](int row, int k) {
-        if (row >= 61 || k >= 61) return make_float2(0.f, 0.f);
-        const double v = which ? M[k * 61 + row] : M[row * 61 + k];
-        const float hi = (float)v;
-        return make_float2(hi, (float)(v - (double)hi));
-    };
-    gh_row_exp(src, e);
-    __syncthreads();
-    gh_slice(src, e, UVpl + (size_t)(2 * w + which) * GH_PL);
-    if (threadIdx.x < 64) UVe[(2 * w + which) * 64 + threadIdx.x] = e[threadIdx.x];
-}
-
-// GH_PL bf16 of prebuilt planes into shared memory
-__device__ __forceinline__ void gh_copy(const __nv_bfloat16 *__restrict__ src, __nv_bfloat16 *dst) {
-    const uint4 *s4 = reinterpret_cast<const uint4 *>(src);
-    uint4 *d4 = reinterpret_cast<uint4 *>(dst);
-    for (int i = threadIdx.x; i < GH_PL / 8; i += blockDim.x) d4[i] = __ldg(s4 + i);
-}
-
-__device__ __forceinline__ void gradH_mma_body(const PairDesc *__restrict__ pairs, const int *__restrict__ label,
-                                               const double *__restrict__ tnode, const DevParams *__restrict__ prm,
-                                               const float2 *__restrict__ Gpart, int nchunk,
-                                               const double *__restrict__ Dm, const __nv_bfloat16 *__restrict__ UVpl,
-                                               const int *__restrict__ UVe, double *__restrict__ out, int p) {
-    extern __shared__ __align__(16) unsigned char smr[];
-    float2 *M = reinterpret_cast<float2 *>(smr);                                   // [64][GH_MP]: G, then T^T
-    __nv_bfloat16 *Ap = reinterpret_cast<__nv_bfloat16 *>(M + 64 * GH_MP);        // [GH_NS][64][PITCH]
-    __nv_bfloat16 *Bp = Ap + GH_PL;
-    int *eA = reinterpret_cast<int *>(Bp + GH_PL);                                // [64]
-    int *eB = eA + 64;                                                            // [64]
-    double *ex = reinterpret_cast<double *>(eB + 64);                             // [64]
-    double (*red)[512] = reinterpret_cast<double (*)[512]>(ex + 64);
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const PairDesc pd = pairs[p];
-    const int w = pd.w;
-    const double tp = tnode[pd.node] * prm->qf[label[pd.node]];
-    const double *R = prm->Root[w];
-    if (tid < 61) ex[tid] = exp(tp * R[tid]);
-    const float2 zero = make_float2(0.f, 0.f);
-    gh_copy(UVpl + (size_t)(2 * w) * GH_PL, Bp);           // V: rows n, K = k
-    if (tid < 64) eB[tid] = UVe[2 * w * 64 + tid];
-    for (int i = tid; i < 64 * 64; i += blockDim.x) {      // G = sum of the chunk partials
-        const int r = i >> 6, k = i & 63;
-        float2 g = zero;
-        if (r < 61 && k < 61)
-            for (int q = 0; q < nchunk; q++) g = fastdev::df_add(g, Gpart[((size_t)p * nchunk + q) * 64 * 64 + i]);
-        M[r * GH_MP + k] = g;
-    }
-    __syncthreads();
-    auto srcG = [&](int r, int k) { return M[r * GH_MP + k]; };
-    gh_row_exp(srcG, eA);
-    __syncthreads();
-    gh_slice(srcG, eA, Ap);
-    __syncthreads();
-    const int rb = warp & 3, cb = warp >> 2, g = lane >> 2, t = lane & 3;
-    float2 acc[2][4];
-    fastdev::ozaki_mma_block<GH_NS, 2>(Ap, 64, 16 * rb, Bp, 16 * cb, acc);
-    // T^T into M: M[n][r] = T[r][n] = T~ 2^{eA[r] + eB[n]} (G is no longer read)
-#pragma unroll
-    for (int nt = 0; nt < 2; nt++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int r = 16 * rb + g + 8 * (q >> 1), n = 16 * cb + 8 * nt + 2 * t + (q & 1);
-            M[n * GH_MP + r] = fastdev::df_scale(acc[nt][q], eA[r] + eB[n]);
-        }
-    __syncthreads();
-    auto srcT = [&](int n, int j) { return M[n * GH_MP + j]; };
-    gh_copy(UVpl + (size_t)(2 * w + 1) * GH_PL, Ap);       // U^T: rows r, K = j
-    if (tid < 64) eA[tid] = UVe[(2 * w + 1) * 64 + tid];
-    gh_row_exp(srcT, eB);
-    __syncthreads();
-    gh_slice(srcT, eB, Bp);
-    __syncthreads();
-    fastdev::ozaki_mma_block<GH_NS, 2>(Ap, 64, 16 * rb, Bp, 16 * cb, acc);
-    double sdt = 0, sk = 0, sw = 0;
-    const double *Dk = Dm + (size_t)w * 64 * 64;
-    const double *Dw = w == 0 ? Dm + 3 * 64 * 64 : (w == 2 ? Dm + 4 * 64 * 64 : nullptr);
-    const double *inv = Dm + (size_t)(5 + w) * 64 * 64;
-    const double rtp = tp > 0.0 ? 1.0 / tp : 0.0;
-#pragma unroll
-    for (int nt = 0; nt < 2; nt++)
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-            const int r = 16 * rb + g + 8 * (q >> 1), n = 16 * cb + 8 * nt + 2 * t + (q & 1);
-            if (r >= 61 || n >= 61) continue;
-            const float2 hd = fastdev::df_scale(acc[nt][q], eA[r] + eB[n]);
-            const double hmn = (double)hd.x + (double)hd.y;
-            const double am = tp * R[r], em = ex[r];
-            const double phi = phi_of(am, tp * R[n], em, ex[n], inv[r * 64 + n], rtp);
-            if (r == n) sdt += R[r] * em * hmn;
-            const double hp = hmn * phi * tp;
-            sk = fma(hp, Dk[r * 64 + n], sk);
-            if (Dw) sw = fma(hp, Dw[r * 64 + n], sw);
-        }
-    red[0][tid] = sdt;
-    red[1][tid] = sk;
-    red[2][tid] = sw;
-    __syncthreads();
-    for (int st = 256; st > 0; st >>= 1) {
-        if (tid < st)
-            for (int q = 0; q < 3; q++) red[q][tid] += red[q][tid + st];
-        __syncthreads();
-    }
-    if (tid < 3) out[p * 3 + tid] = red[tid][0];
-}
-
-__global__ void __launch_bounds__(512, 1) gradH_mma_kernel(const PairDesc *__restrict__ pairs,
-                                                           const int *__restrict__ label,
-                                                           const double *__restrict__ tnode,
-                                                           const DevParams *__restrict__ prm,
-                                                           const float2 *__restrict__ Gpart, int nchunk,
-                                                           const double *__restrict__ Dm,
-                                                           const __nv_bfloat16 *__restrict__ UVpl,
-                                                           const int *__restrict__ UVe,
-                                                           double *__restrict__ out) {
-    gradH_mma_body(pairs, label, tnode, prm, Gpart, nchunk, Dm, UVpl, UVe, out, blockIdx.x);
-}
-
-__global__ void __launch_bounds__(512, 1) gradH_mma_batched_kernel(const GradHArgs *__restrict__ args,
-                                                                   const int2 *__restrict__ map) {
-    const int2 g = map[blockIdx.x];
-    const GradHArgs &a = args[g.x];
-    gradH_mma_body(a.pairs, a.label, a.tnode, a.prm, a.Gpart, a.nchunk, a.Dm, a.UVpl, a.UVe, a.out, g.y);
-}
-
 __global__ void __launch_bounds__(256) gradH_df_kernel(const PairDesc *__restrict__ pairs,
                                                        const int *__restrict__ label,
                                                        const double *__restrict__ tnode,
@@ -741,7 +556,7 @@ void adjoint_free(AdjointState *a) {
     if (!a) return;
     if (a->graph) cudaGraphExecDestroy(a->graph);
     void *dev[] = {a->d_bitems, a->d_contrib, a->d_coff, a->d_Ebar, a->d_Abar, a->d_Gpart,
-                   a->d_Dm, a->d_pout, a->d_fpart, a->d_gp, a->d_UVdf, a->d_UVpl, a->d_UVe};
+                   a->d_Dm, a->d_pout, a->d_fpart, a->d_gp, a->d_UVdf};
     for (void *p : dev)
         if (p) cudaFree(p);
     if (a->h_gp) cudaFreeHost(a->h_gp);
@@ -817,9 +632,7 @@ int adjoint_init(gb_handle *h) {
         (rc = dalloc(&a->d_Abar, (size_t)h->nslot * npad * 64)) ||
         (rc = dalloc(&a->d_Gpart, h->pairs.size() * a->nchunk * 64 * 64)) ||
         (rc = dalloc(&a->d_Dm, DM_MATS * 64 * 64)) ||
-        (h->precision != GB_PREC_FP64 && (rc = dalloc(&a->d_UVdf, 3 * 2 * 61 * 64))) ||
-        (h->precision != GB_PREC_FP64 && (rc = dalloc(&a->d_UVpl, 3 * 2 * GH_PL))) ||
-        (h->precision != GB_PREC_FP64 && (rc = dalloc(&a->d_UVe, 3 * 2 * 64))) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
+        (h->precision != GB_PREC_FP64 && (rc = dalloc(&a->d_UVdf, 3 * 2 * 61 * 64))) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
         (rc = dalloc(&a->d_fpart, a->nfreq_blocks * 4)) || (rc = dalloc(&a->d_gp, 1)))
         return rc;
     if (cudaMallocHost((void **)&a->h_gp, sizeof(GradParams)) ||
@@ -836,14 +649,11 @@ int adjoint_init(gb_handle *h) {
     CK(cudaFuncSetAttribute(gradH_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHSmem));
     CK(cudaFuncSetAttribute(gradH_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHdfSmem));
     CK(cudaFuncSetAttribute(gradH_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHdfSmem));
-    CK(cudaFuncSetAttribute(gradH_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHmmaSmem));
-    CK(cudaFuncSetAttribute(gradH_mma_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHmmaSmem));
     return 0;
 }
 
 void launch_dmat(gb_handle *h) {
-    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, h->adj->d_gp, h->adj->d_Dm, h->adj->d_UVdf,
-                                                  h->adj->d_UVpl, h->adj->d_UVe);
+    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, h->adj->d_gp, h->adj->d_Dm, h->adj->d_UVdf);
 }
 
 void launch_gradH(gb_handle *h) {
@@ -855,9 +665,9 @@ void launch_gradH(gb_handle *h) {
 
 void launch_gradH_df(gb_handle *h) {
     AdjointState *a = h->adj;
-    gradH_mma_kernel<<<(unsigned)h->pairs.size(), 512, kGradHmmaSmem, h->stream>>>(
+    gradH_df_kernel<<<(unsigned)h->pairs.size(), 256, kGradHdfSmem, h->stream>>>(
         h->d_pairs, h->d_label, h->d_tnode, h->d_prm, reinterpret_cast<const float2 *>(a->d_Gpart), a->nchunk,
-        a->d_Dm, a->d_UVpl, a->d_UVe, a->d_pout);
+        a->d_Dm, a->d_UVdf, a->d_pout);
 }
 
 void launch_dmat_batched(const DmatArgs *args, const int2 *map, int nblocks, cudaStream_t st) {
@@ -865,7 +675,7 @@ void launch_dmat_batched(const DmatArgs *args, const int2 *map, int nblocks, cud
 }
 
 void launch_gradH_batched(const GradHArgs *args, const int2 *map, int nblocks, cudaStream_t st) {
-    if (nblocks > 0) gradH_mma_batched_kernel<<<nblocks, 512, kGradHmmaSmem, st>>>(args, map);
+    if (nblocks > 0) gradH_batched_kernel<<<nblocks, 256, kGradHdfSmem, st>>>(args, map);
 }
 
 void launch_freq_batched(const FreqArgs *args, const int2 *map, int nblocks, cudaStream_t st) {
@@ -883,7 +693,7 @@ namespace {
 int record_backward(gb_handle *h) {
     AdjointState *a = h->adj;
     int nk = 0;
-    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, a->d_gp, a->d_Dm, nullptr, nullptr, nullptr);
+    dmat_kernel<<<DM_BLOCKS, 256, 0, h->stream>>>(h->d_prm, a->d_gp, a->d_Dm, nullptr);
     prof_mark(h, GB_K_OTHER);
     nk++;
     for (size_t L = 0; L + 1 < a->blevel_off.size(); L++) {

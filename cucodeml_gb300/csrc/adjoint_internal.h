@@ -3,7 +3,6 @@
 #pragma once
 
 #include <cuda_runtime.h>
-#include <cuda_bf16.h>
 
 #include <vector>
 
@@ -18,11 +17,7 @@ namespace gb {
 constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP
 constexpr int DM_MATS = 8;    // dP/dt buffer: 5 derivative matrices + 3 inverse-difference tables
 constexpr int DM_RB = 4;      // dP/dt kernel: row blocks per derivative matrix
-constexpr int DM_BLOCKS = 5 * DM_RB + 3 + 6;   // + digit planes of V and U^T per omega
-// digit planes of the gradient transform's tensor-core products (split precision)
-constexpr int GH_NS = 7;                      // planes per operand
-constexpr int GH_PITCH = 72;                  // bf16 per plane row (64 + 8: conflict-free fragments)
-constexpr int GH_PL = GH_NS * 64 * GH_PITCH;  // bf16 per operand
+constexpr int DM_BLOCKS = 5 * DM_RB + 3;
 
 struct BItem {                // backward work: (node, class family) of one level
     int node, ncls, is_root, nchild;
@@ -56,8 +51,6 @@ struct AdjointState {
     double *d_Ebar = nullptr, *d_Abar = nullptr, *d_Gpart = nullptr, *d_Dm = nullptr;
     double *d_pout = nullptr, *d_fpart = nullptr;
     float2 *d_UVdf = nullptr;        // split precision: [3][2][61][64] V^T and U as double-float
-    __nv_bfloat16 *d_UVpl = nullptr; // split precision: [3][2][GH_PL] digit planes of V and U^T
-    int *d_UVe = nullptr;            // [3][2][64] their row exponents
     GradParams *d_gp = nullptr, *h_gp = nullptr;
     double *h_pout = nullptr, *h_fpart = nullptr;
     cudaGraphExec_t graph = nullptr;

@@ -253,14 +253,14 @@ int build_launches(gb_batch *b, bool grad) {
         return rc;
     if (!grad) return 0;
     if ((rc = make_launch<DmatArgs>(b, b->l_dmat, [](gb_handle *h, DmatArgs *a) {
-             *a = DmatArgs{h->d_prm, h->adj->d_gp, h->adj->d_Dm, h->adj->d_UVdf, h->adj->d_UVpl, h->adj->d_UVe};
+             *a = DmatArgs{h->d_prm, h->adj->d_gp, h->adj->d_Dm, h->adj->d_UVdf};
              return DM_BLOCKS;
          })) ||
         (rc = make_launch<GradHArgs>(b, b->l_gradH, [](gb_handle *h, GradHArgs *a) {
              AdjointState *ad = h->adj;
              *a = GradHArgs{h->d_pairs, h->d_label, h->d_tnode, h->d_prm,
                             reinterpret_cast<const float2 *>(ad->d_Gpart), ad->nchunk, ad->d_Dm, ad->d_UVdf,
-                            ad->d_pout, ad->d_UVpl, ad->d_UVe};
+                            ad->d_pout};
              return (int)h->pairs.size();
          })) ||
         (rc = make_launch<FreqArgs>(b, b->l_freq, [](gb_handle *h, FreqArgs *a) {

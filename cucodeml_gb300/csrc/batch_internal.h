@@ -44,8 +44,6 @@ struct DmatArgs {
     const GradParams *gp;
     double *Dm;
     float2 *UVdf;
-    __nv_bfloat16 *UVpl;
-    int *UVe;
 };
 
 struct GradHArgs {
@@ -58,8 +56,6 @@ struct GradHArgs {
     const double *Dm;
     const float2 *UVdf;
     double *out;
-    const __nv_bfloat16 *UVpl;
-    const int *UVe;
 };
 
 struct FreqArgs {

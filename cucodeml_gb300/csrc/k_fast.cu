@@ -58,6 +58,19 @@ __device__ __forceinline__ unsigned long long p_fixed(double v) {
     return v > 0.0 ? (unsigned long long)floor(v * ldexp(1.0, 7 * NS)) : 0ull;
 }
 
+// the same from the bit fields of v (integer operations only: v = m 2^(e - 1075)
+// with the 53-bit significand m, v in [0, 1]), so that the FP64 pipe is not used
+template <int NS>
+__device__ __forceinline__ unsigned long long p_fixed_bits(double v) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)((u >> 52) & 0x7ff);
+    if ((u >> 63) || e == 0) return 0ull;                  // negative, zero or subnormal (< 2^-1022)
+    const unsigned long long m = (u & 0xfffffffffffffull) | (1ull << 52);
+    const int sh = e - 1075 + 7 * NS;
+    if (sh >= 0) return m << sh;                           // v <= 1: sh <= 7 NS - 52 (< 11 bits)
+    return sh <= -64 ? 0ull : m >> -sh;
+}
+
 template <int NS>
 __device__ __forceinline__ int p_digit(unsigned long long q, int s) {
     const int sh = 7 * (NS - 1 - s);
@@ -98,12 +111,12 @@ __device__ __forceinline__ void pslice_body(const double *__restrict__ Pt, float
     }
     // core-matrix planes: P staged in shared memory, then each thread writes
     // whole 16-byte core-matrix rows (8 consecutive K elements) per plane
-    __shared__ double Ps[64 * 65];                       // Ps[k][j] = Pt[k][j], rows padded
+    __shared__ unsigned long long Ps[64 * 65];           // floor(Pt[k][j] 2^(7 NS)), rows padded
     for (int i = threadIdx.x; i < 4096; i += blockDim.x) {
         const double v = P[i];
         const float hi = (float)v;
         D[i] = make_float2(hi, (float)(v - (double)hi));
-        Ps[(i >> 6) * 65 + (i & 63)] = v;
+        Ps[(i >> 6) * 65 + (i & 63)] = p_fixed_bits<NS>(v);
     }
     __syncthreads();
     for (int u = threadIdx.x; u < 1024; u += blockDim.x) {
@@ -111,13 +124,13 @@ __device__ __forceinline__ void pslice_body(const double *__restrict__ Pt, float
         unsigned long long q[8];
         if (u < 512) {         // forward: B[n = j][k], row = 8 consecutive k
 #pragma unroll
-            for (int t = 0; t < 8; t++) q[t] = p_fixed<NS>(Ps[(8 * g + t) * 65 + n]);
+            for (int t = 0; t < 8; t++) q[t] = Ps[(8 * g + t) * 65 + n];
 #pragma unroll
             for (int s = 0; s < NS; s++)
                 *reinterpret_cast<uint4 *>(bf + (size_t)s * 4096 + cm_index(n, 8 * g)) = p_row<NS>(q, s);
         } else {               // adjoint: B[n = k][j], row = 8 consecutive j
 #pragma unroll
-            for (int t = 0; t < 8; t++) q[t] = p_fixed<NS>(Ps[n * 65 + 8 * g + t]);
+            for (int t = 0; t < 8; t++) q[t] = Ps[n * 65 + 8 * g + t];
 #pragma unroll
             for (int s = 0; s < NS; s++)
                 *reinterpret_cast<uint4 *>(bb + (size_t)s * 4096 + cm_index(n, 8 * g)) = p_row<NS>(q, s);

@@ -106,3 +106,29 @@ def test_level_sums_stay_exact_in_fp32():
     # NB = 7 one over K = 128 (dlnL/dP): every partial sum is an integer <= 2^24
     assert 8 * 64 * 128 * 128 <= 2 ** 23
     assert 7 * 128 * 128 * 128 <= 2 ** 24
+
+
+def p_fixed_bits(v: float, ns: int) -> int:
+    """The digit-plane kernel's floor(v 2^(7 ns)) from the bit fields of a double
+    in [0, 1] (k_fast.cu p_fixed_bits), restated."""
+    import struct
+    u = struct.unpack("<Q", struct.pack("<d", v))[0]
+    e = (u >> 52) & 0x7FF
+    if (u >> 63) or e == 0:
+        return 0
+    m = (u & ((1 << 52) - 1)) | (1 << 52)
+    sh = e - 1075 + 7 * ns
+    if sh >= 0:
+        return m << sh
+    return 0 if sh <= -64 else m >> -sh
+
+
+@pytest.mark.parametrize("ns", [5, 6, 7, 8])
+def test_p_fixed_bits_equals_floor(ns):
+    import math
+    rng = np.random.default_rng(ns)
+    vals = [0.0, 1.0, 0.5, 2.0 ** -56, 2.0 ** -57, 2.0 ** -1000, 5e-324, 1.0 - 2.0 ** -53, -0.0, -1e-300]
+    vals += list(rng.random(2000)) + list(rng.random(500) * 2.0 ** -30) + list(2.0 ** -rng.integers(1, 70, 500))
+    for v in vals:
+        want = math.floor(v * 2.0 ** (7 * ns)) if v > 0 else 0
+        assert p_fixed_bits(float(v), ns) == want, v

@@ -50,6 +50,11 @@ constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256 + 64) * sizeof(double);
 // last 3 blocks: 1/(Root_m - Root_n) for w (and U, V^T as double-float).
 // dQ has at most ~10 non-zeros per row (single-nucleotide neighbours and the
 // diagonal): T = dQ U runs over each row's non-zeros (dense past 16).
+__device__ __forceinline__ float2 df_of(double v) {
+    const float hi = (float)v;
+    return make_float2(hi, (float)(v - (double)hi));
+}
+
 __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, const GradParams *__restrict__ gp,
                                           double *__restrict__ Dm, float2 *__restrict__ UVdf, int bid) {
     __shared__ double T[61 * 62];
@@ -64,6 +69,7 @@ __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, con
             const int r = i / 64, c = i % 64;
             const double d = (r < 61 && c < 61) ? R[r] - R[c] : 0.0;
             out[i] = d != 0.0 ? 1.0 / d : 0.0;
+            if (UVdf) UVdf[UVDF_DM + (size_t)which * 64 * 64 + i] = df_of(out[i]);
         }
         if (UVdf) {   // V^T [k][n] and U [j][m] of this w as double-float, 64-column rows
             float2 *vt = UVdf + (size_t)w * 2 * 61 * 64, *u = vt + 61 * 64;
@@ -119,6 +125,7 @@ __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, con
         if (r < 61 && c < 61)
             for (int kk = 0; kk < 61; kk++) s = fma(V[r * 61 + kk], T[kk * 62 + c], s);
         out[r * 64 + c] = s;
+        if (UVdf) UVdf[UVDF_DM + (size_t)which * 64 * 64 + r * 64 + c] = df_of(s);
     }
 }
 
@@ -392,12 +399,8 @@ __device__ __forceinline__ void dot2_step(float &s, float &c, float2 a, float2 b
     s = t;
 }
 
-__device__ __forceinline__ float2 df_of(double v) {
-    const float hi = (float)v;
-    return make_float2(hi, (float)(v - (double)hi));
-}
 
-constexpr int kGradHdfSmem = (61 * 66 + 2 * 61 * 64) * 8 + (64 + 3 * 256) * 8;
+constexpr int kGradHdfSmem = (61 * 66 + 2 * 61 * 64) * 8 + (64 + 3 * 256) * 8 + 2 * 64 * 8;
 
 // Shared-memory layout: G (then T) rows padded to GS = 66 double-float so that
 // the 8 rows a warp reads at one k fall in different banks; thread
@@ -416,12 +419,18 @@ __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs
     float2 *Us = Vt + 61 * 64;                              // [61][64] U[j][m]
     double *ex = reinterpret_cast<double *>(Us + 61 * 64);  // [64]
     double (*red)[256] = reinterpret_cast<double (*)[256]>(ex + 64);
+    float2 *exd = reinterpret_cast<float2 *>(red[3]);       // [64] ex as double-float
+    float2 *Rd = exd + 64;                                  // [64] Root as double-float
     const int tid = threadIdx.x;
     const PairDesc pd = pairs[p];
     const int w = pd.w;
     const double tp = tnode[pd.node] * prm->qf[label[pd.node]];
     const double *R = prm->Root[w];
-    if (tid < 61) ex[tid] = exp(tp * R[tid]);
+    if (tid < 61) {
+        ex[tid] = exp(tp * R[tid]);
+        exd[tid] = df_of(ex[tid]);
+        Rd[tid] = df_of(R[tid]);
+    }
     {   // V^T and U of this w, already double-float (dP/dt kernel)
         const float4 *src = reinterpret_cast<const float4 *>(UVdf + (size_t)w * 2 * 61 * 64);
         float4 *dst = reinterpret_cast<float4 *>(Vt);
@@ -461,28 +470,42 @@ __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs
 #pragma unroll
             for (int i = 0; i < 16; i++) dot2_step(s[i], e[i], u, GT[j * GS + q4 + 4 * i]);
         }
-    double sdt = 0, sk = 0, sw = 0;
-    const double *Dk = Dm + (size_t)w * 64 * 64;
-    const double *Dw = w == 0 ? Dm + 3 * 64 * 64 : (w == 2 ? Dm + 4 * 64 * 64 : nullptr);
-    const double *inv = Dm + (size_t)(5 + w) * 64 * 64;
+    // Phi-weighted sums in double-float on the FP32 pipe (the dP/dt and
+    // inverse-difference tables in their double-float copies): with
+    // d = t' (R_r - R_n), Phi = (e_r - e_n) inv_rn / t' except for |d| < 1e-3,
+    // where the series of the FP64 path is used
+    float2 sdt = make_float2(0.f, 0.f), sk = sdt, sw = sdt;
+    const float2 *Tdf = UVdf + UVDF_DM;
+    const float2 *Dk = Tdf + (size_t)w * 64 * 64;
+    const float2 *Dw = w == 0 ? Tdf + 3 * 64 * 64 : (w == 2 ? Tdf + 4 * 64 * 64 : nullptr);
+    const float2 *inv = Tdf + (size_t)(5 + w) * 64 * 64;
     const double rtp = tp > 0.0 ? 1.0 / tp : 0.0;
+    const float2 rtpd = df_of(rtp), tpd = df_of(tp);
+    const float tpf = (float)tp;
     if (r < 61) {
-        const double am = tp * R[r], em = ex[r];
+        const float Rr = (float)R[r];
 #pragma unroll
         for (int i = 0; i < 16; i++) {
             const int n = q4 + 4 * i;
             if (n >= 61) continue;
-            const double hmn = (double)s[i] + (double)e[i];
-            const double phi = phi_of(am, tp * R[n], em, ex[n], inv[r * 64 + n], rtp);
-            if (r == n) sdt += R[r] * em * hmn;
-            const double hp = hmn * phi * tp;
-            sk = fma(hp, Dk[r * 64 + n], sk);
-            if (Dw) sw = fma(hp, Dw[r * 64 + n], sw);
+            const float2 hmn = fastdev::fast_two_sum(s[i], e[i]);
+            float2 phi;
+            if (fabsf(tpf * (Rr - (float)R[n])) < 1e-3f) {
+                const double dd = tp * R[r] - tp * R[n], d2 = dd * dd;
+                phi = df_of(sqrt(ex[r] * ex[n]) * (1.0 + d2 * (1.0 / 24.0 + d2 * (1.0 / 1920.0))));
+            } else {
+                const float2 de = fastdev::df_add(exd[r], make_float2(-exd[n].x, -exd[n].y));
+                phi = fastdev::df_mul(fastdev::df_mul(de, inv[r * 64 + n]), rtpd);
+            }
+            if (r == n) sdt = fastdev::df_add(sdt, fastdev::df_mul(fastdev::df_mul(Rd[r], exd[r]), hmn));
+            const float2 hp = fastdev::df_mul(fastdev::df_mul(hmn, phi), tpd);
+            sk = fastdev::df_add(sk, fastdev::df_mul(hp, Dk[r * 64 + n]));
+            if (Dw) sw = fastdev::df_add(sw, fastdev::df_mul(hp, Dw[r * 64 + n]));
         }
     }
-    red[0][tid] = sdt;
-    red[1][tid] = sk;
-    red[2][tid] = sw;
+    red[0][tid] = (double)sdt.x + (double)sdt.y;
+    red[1][tid] = (double)sk.x + (double)sk.y;
+    red[2][tid] = (double)sw.x + (double)sw.y;
     __syncthreads();
     for (int st = 128; st > 0; st >>= 1) {
         if (tid < st)
@@ -632,7 +655,7 @@ int adjoint_init(gb_handle *h) {
         (rc = dalloc(&a->d_Abar, (size_t)h->nslot * npad * 64)) ||
         (rc = dalloc(&a->d_Gpart, h->pairs.size() * a->nchunk * 64 * 64)) ||
         (rc = dalloc(&a->d_Dm, DM_MATS * 64 * 64)) ||
-        (h->precision != GB_PREC_FP64 && (rc = dalloc(&a->d_UVdf, 3 * 2 * 61 * 64))) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
+        (h->precision != GB_PREC_FP64 && (rc = dalloc(&a->d_UVdf, UVDF_DM + DM_MATS * 64 * 64))) || (rc = dalloc(&a->d_pout, h->pairs.size() * 3)) ||
         (rc = dalloc(&a->d_fpart, a->nfreq_blocks * 4)) || (rc = dalloc(&a->d_gp, 1)))
         return rc;
     if (cudaMallocHost((void **)&a->h_gp, sizeof(GradParams)) ||

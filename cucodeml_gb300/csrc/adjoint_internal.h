@@ -18,6 +18,7 @@ constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP
 constexpr int DM_MATS = 8;    // dP/dt buffer: 5 derivative matrices + 3 inverse-difference tables
 constexpr int DM_RB = 4;      // dP/dt kernel: row blocks per derivative matrix
 constexpr int DM_BLOCKS = 5 * DM_RB + 3;
+constexpr int UVDF_DM = 3 * 2 * 61 * 64;   // offset of the double-float tables in d_UVdf
 
 struct BItem {                // backward work: (node, class family) of one level
     int node, ncls, is_root, nchild;
@@ -50,7 +51,8 @@ struct AdjointState {
     int *d_coff = nullptr;
     double *d_Ebar = nullptr, *d_Abar = nullptr, *d_Gpart = nullptr, *d_Dm = nullptr;
     double *d_pout = nullptr, *d_fpart = nullptr;
-    float2 *d_UVdf = nullptr;        // split precision: [3][2][61][64] V^T and U as double-float
+    float2 *d_UVdf = nullptr;        // split precision, double-float: [3][2][61][64] V^T and U, then (at
+                                     // UVDF_DM) [DM_MATS][64][64] the dP/dt and inverse-difference tables
     GradParams *d_gp = nullptr, *h_gp = nullptr;
     double *h_pout = nullptr, *h_fpart = nullptr;
     cudaGraphExec_t graph = nullptr;

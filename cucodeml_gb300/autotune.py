@@ -20,22 +20,22 @@ from . import api
 
 #: candidates for batches; the first is the library default and the reference
 BATCH_CANDIDATES = [
-    {"mma": 1, "persist": 1, "gchunk": 512, "order": 0},
-    {"mma": 1, "persist": 1, "gchunk": 256, "order": 0},
+    {"mma": 1, "persist": 1, "gchunk": 2048, "order": 0},
     {"mma": 1, "persist": 1, "gchunk": 1024, "order": 0},
-    {"mma": 1, "persist": 1, "gchunk": 512, "order": 1},
-    {"mma": 1, "persist": 1, "gchunk": 512, "order": 2},
-    {"mma": 1, "persist": 0, "gchunk": 512},
-    {"mma": 0, "persist": 0, "gchunk": 512},
+    {"mma": 1, "persist": 1, "gchunk": 4096, "order": 0},
+    {"mma": 1, "persist": 1, "gchunk": 2048, "order": 2},
+    {"mma": 1, "persist": 1, "gchunk": 2048, "order": 1},
+    {"mma": 1, "persist": 0, "gchunk": 2048},
+    {"mma": 0, "persist": 0, "gchunk": 2048},
 ]
 
 #: candidates for a single alignment
 SINGLE_CANDIDATES = [
-    {"mma": 1, "persist": 1, "gchunk": 512},
-    {"mma": 1, "persist": 1, "gchunk": 256},
+    {"mma": 1, "persist": 1, "gchunk": 2048},
     {"mma": 1, "persist": 1, "gchunk": 1024},
-    {"mma": 1, "persist": 0, "gchunk": 512},
-    {"mma": 0, "persist": 0, "gchunk": 512},
+    {"mma": 1, "persist": 1, "gchunk": 4096},
+    {"mma": 1, "persist": 0, "gchunk": 2048},
+    {"mma": 0, "persist": 0, "gchunk": 2048},
 ]
 
 

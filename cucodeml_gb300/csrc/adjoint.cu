@@ -643,8 +643,21 @@ int adjoint_init(gb_handle *h) {
         a->coff[p + 1] = a->coff[p] + (int)per[p].size();
         for (auto &c : per[p]) a->contrib.push_back(c);
     }
-    // the FP64 kernel works in chunks of GCHUNK; the split-precision ones as tuned
-    a->gchunk = (h->precision != GB_PREC_FP64 && h->tune.gchunk > 0) ? h->tune.gchunk : GCHUNK;
+    // the FP64 kernel works in chunks of GCHUNK; the split-precision ones as
+    // tuned, else GCHUNK_FAST halved (down to GCHUNK) until the (pair, chunk)
+    // tasks are at least four per SM
+    if (h->precision == GB_PREC_FP64) {
+        a->gchunk = GCHUNK;
+    } else if (h->tune.gchunk > 0) {
+        a->gchunk = h->tune.gchunk;
+    } else {
+        int dev = 0, nsm = 152;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev))
+            nsm = 152;
+        a->gchunk = GCHUNK_FAST;
+        while (a->gchunk > GCHUNK && (long)h->pairs.size() * ((h->npatt + a->gchunk - 1) / a->gchunk) < 4L * nsm)
+            a->gchunk /= 2;
+    }
     a->nchunk = (h->npatt + a->gchunk - 1) / a->gchunk;
     a->nfreq_blocks = (h->npatt + 255) / 256;
     const size_t npad = h->npad;

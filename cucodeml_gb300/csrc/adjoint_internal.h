@@ -14,7 +14,10 @@ struct gb_handle;
 
 namespace gb {
 
-constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP
+constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP (FP64 kernel)
+constexpr int GCHUNK_FAST = 2048;   // default of the split-precision kernels (measured fastest on a
+                                    // single 64 x 5000 alignment and on a 512-gene batch; a single
+                                    // small alignment halves it while its tasks are too few)
 constexpr int DM_MATS = 8;    // dP/dt buffer: 5 derivative matrices + 3 inverse-difference tables
 constexpr int DM_RB = 4;      // dP/dt kernel: row blocks per derivative matrix
 constexpr int DM_BLOCKS = 5 * DM_RB + 3;

@@ -379,6 +379,9 @@ int gb_batch_create(int ngene, const gb_problem *probs, gb_batch **out) {
         if (probs[i].device != b->device) { batch_free(b); return fail(GB_ERR_ARG, "gb_batch_create: one device per batch"); }
         int rc = gb_create(&probs[i], &b->h[i]);
         if (rc) { batch_free(b); return rc; }
+        // a batch's dlnL/dP tasks come from all genes: the long chunks need no
+        // per-gene adjustment (gb_batch_tune may still set another)
+        b->h[i]->tune.gchunk = GCHUNK_FAST;
         b->D[i] = new Derived;
     }
     if (cudaSetDevice(b->device) != cudaSuccess ||

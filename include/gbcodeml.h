@@ -216,7 +216,8 @@ int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches
  *   GB_TUNE_PERSIST  0: one launch per tree level, 1: persistent task-list
  *                    kernels (default; tcgen05 only)
  *   GB_TUNE_GCHUNK   patterns per partial sum of dlnL/dP (multiple of 64 in
- *                    [64, 8192]; default 512)
+ *                    [64, 8192]; default 2048, for a single alignment halved
+ *                    down to 512 until there are four (pair, chunk) tasks per SM)
  *   GB_TUNE_ORDER    task order of the persistent kernels: 0 critical path
  *                    first (forward: deepest nodes below the root first;
  *                    adjoint: tallest subtrees first; all genes together;

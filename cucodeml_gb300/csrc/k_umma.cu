@@ -79,8 +79,8 @@ struct GSm {
     static constexpr int PLANES = INT_BYTES > 2 * TIP_BUF ? INT_BYTES : 2 * TIP_BUF;
     static constexpr int OFF_ACC = PLANES;
     static constexpr int OFF_MISC = OFF_ACC + 4096 * 8;
-    static constexpr int OFF_XS = OFF_MISC + 64;              // int [128] exponents
-    static constexpr int OFF_RED = OFF_XS + 512;              // int [16] reductions
+    static constexpr int OFF_XS = OFF_MISC + 64;              // int [256] exponents
+    static constexpr int OFF_RED = OFF_XS + 1024;             // int [16] reductions
     static constexpr int OFF_ARGS = OFF_RED + 64;
     static constexpr int NEED = OFF_ARGS + ARGS_BYTES;
     static constexpr int BYTES = NEED > MIN_SMEM ? NEED : MIN_SMEM;
@@ -1042,9 +1042,10 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
         }
         tick(2);
     } else {
-        // Internal children: per block of 128 patterns (rows scaled against the
-        // block's largest exponent), two rounds of 64 add into the same level
-        // sums (<= 4 pairs x 128 x 128^2 per lane half: exact).  Warps 1..15 cut
+        // Internal children: per block of 256 patterns (rows scaled against the
+        // block's largest exponent), four rounds of 64 add into the same level
+        // sums (each TMEM lane half holds at most 4 digit pairs of a level:
+        // <= 4 x 256 x 128^2 = 2^24, exact in FP32).  Warps 1..15 cut
         // a round's 128 core matrices step-major (n = 32 KS + t; t < 16: Ebar's,
         // else conP's; j group (t mod 16) / 2, h group 2 KS + t mod 2), each step
         // after that step's MMAs of the previous round are done (m->mstep[KS]),
@@ -1058,9 +1059,9 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
                 umma::prefetch_l2(a.Ebar + ((size_t)cb.ebar * npad + hbeg) * 64, bytes);
                 umma::prefetch_l2(a.conP + ((size_t)cb.tslot * npad + hbeg) * 64, bytes);
             }
-            for (int hb = hbeg; hb < hend && ok; hb += 128) {
+            for (int hb = hbeg; hb < hend && ok; hb += 256) {
                 __syncthreads();                               // previous read-out and exponents are done
-                if (tid < 128) {                               // warps 0..3: exponents and their maximum
+                if (tid < 256) {                               // warps 0..7: exponents and their maximum
                     const int x = hb + tid < hend ? a.ebexp[(size_t)cb.ebar * npad + hb + tid] : ZERO_EXP;
                     xs[tid] = x;
                     int mx = x;
@@ -1069,10 +1070,12 @@ __device__ bool gradP_task(const FastBwdArgs &a, int p, int chunk, unsigned char
                     if (lane == 0) red[4 + warp] = mx;
                 }
                 __syncthreads();
-                const int xmax = max(max(red[4], red[5]), max(red[6], red[7]));
+                int xmax = red[4];
+#pragma unroll
+                for (int q = 5; q < 12; q++) xmax = max(xmax, red[q]);
                 tick(0);
                 if (xmax == ZERO_EXP) continue;
-                for (int half = 0; half < 2; half++) {
+                for (int half = 0; half < 4; half++) {
                     const int hs = hb + 64 * half, nh = min(64, hend - hs);
                     if (nh <= 0) break;
                     const uint32_t g = gs.nround++;            // this round's index on m->mstep

@@ -377,8 +377,10 @@ def main():
     if precision != "fp64":
         # executed tensor work of the digit-plane contractions (not algorithmic):
         # NS = 8 forward planes -> 36 digit pairs, NB = 7 adjoint planes -> 28,
-        # over 64 x 64 padded states; dlnL/dP runs M = 128 with 64 zero rows
-        pairs = {"prune": 36, "bwd": 28, "gradP": 2 * 28}
+        # over 64 x 64 padded states; dlnL/dP packs two planes per M = 128 tile:
+        # 16 tiles per K step = 32 plane pairs for an internal child (28 kept
+        # levels + 4 beyond them; a tip's one-hot product executes 8)
+        pairs = {"prune": 36, "bwd": 28, "gradP": 32}
         if top in pairs:
             ex = cls_flops[top] * pairs[top] * (64.0 * 64.0) / (61.0 * 61.0)
             roof["executed_tensor_tflops"] = ex / (top_ms_per_eval * 1e-3) / 1e12

@@ -1,25 +1,28 @@
-// tcgen05 versions of the split-precision forward and adjoint-propagation
-// kernels (same numerics as k_fast.cu / k_fast_bwd.cu, see there).
+// tcgen05 versions of the split-precision kernels (forward, adjoint
+// propagation, dlnL/dP; same numerics as k_fast.cu / k_fast_bwd.cu, see there).
 //
 // Per (128-pattern tile, node, class) task and per internal child: one thread
 // starts a bulk copy (cp.async.bulk, completion on an mbarrier) of the NS
 // digit planes of P, stored in global memory already in the K-major
-// core-matrix layout; meanwhile the SIMT threads cut the child's 128 x 64
-// double-float tile into NS digit planes in shared memory.  Warp 0 then
-// issues (one elected lane; descriptors computed warp-uniformly from
-// compile-time offsets), for every significance level L = 2..NS+1, the
-// tcgen05.mma (M = 128, N = 64, K = 16, bf16 x bf16 -> FP32) of every digit
-// pair (i, j) with i + j = L into that level's 64 TMEM columns (NS = 8:
-// 8 levels = all 512 columns), and commits to an mbarrier.  The level sums
-// are exact integers in FP32;
-// each thread reads one row (TMEM lane) x NCOL columns per level with
-// tcgen05.ld and combines the levels in double-float.
+// core-matrix layout.  The contraction is warp-specialised and pipelined over
+// its four K steps (slice_contract): warps 1..15 cut the child's 128 x 64
+// double-float tile into NS digit planes in shared memory step by step and
+// arrive on a named barrier per step; warp 0 (one elected lane, descriptors
+// from compile-time offsets) issues each step's tcgen05.mma (M = 128, bf16 x
+// bf16 -> FP32) as soon as the step is cut and commits to an mbarrier.  Level
+// L = 2..NS+1 sums the digit pairs (i, L - i) in TMEM columns 64 (L - 2) (NS =
+// 8: all 512 columns); consecutive B planes being contiguous, A plane i against
+// B planes j0..j0+3 is one MMA of N = 256 (issue_kstep).  The level sums are
+// exact integers in FP32; each thread reads one row (TMEM lane) x NCOL columns
+// per level with tcgen05.ld and combines the levels by a compensated sum.
 // NWARP warps per CTA: warp w reads TMEM lanes 32 (w % 4) .. + 31 (a warp may
 // only access its quarter of the lanes) and columns NCOL (w / 4) .. + NCOL-1,
 // so thread (w, lane) owns pattern row 32 (w % 4) + lane and states
-// NCOL (w / 4) + 0..NCOL-1.
-// Every mbarrier wait is bounded; on timeout the CTA sets *err, skips its
-// remaining work and still frees its TMEM.
+// NCOL (w / 4) + 0..NCOL-1.  The adjoint's edge messages use a warp-row layout
+// instead (ebar_rows).  dlnL/dP (gradP_task) packs two digit planes per M = 128
+// tile and handles tip children as one-hot products.
+// Every mbarrier and flag wait is bounded; on timeout the CTA sets *err, lets
+// its in-flight MMAs and copies drain (bounded), and still frees its TMEM.
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -38,9 +41,7 @@ constexpr int NT = 512;            // threads per CTA (16 warps; 32 measured no 
 constexpr int NWARP = NT / 32;
 constexpr int NCG = NWARP / 4;     // column groups: warps sharing a TMEM lane quarter
 constexpr int NCOL = 64 / NCG;     // states per thread in the epilogues
-constexpr int ACM = 128 / NWARP;   // A-plane core matrices cut per warp (128 x 64 tile)
-constexpr int GCM = 64 / NWARP;    // core matrices per warp in the 64 x 64 dlnL/dP planes
-static_assert(NCOL % 2 == 0 && ACM >= 1 && GCM >= 1, "thread layout");
+static_assert(NCOL % 2 == 0 && NWARP == 16, "thread layout: 16 warps, four column groups of 16 states");
 constexpr int A_PLANE = 128 * 64 * 2;
 constexpr int B_PLANE = 64 * 64 * 2;
 

@@ -391,6 +391,53 @@ __device__ __forceinline__ void on_failure(int *err, Misc *m, uint32_t phase, bo
     }
 }
 
+// An item whose children are all tips (not the root): the product of the
+// tips' rows of P for their codons, renormalised per row, in the warp-row
+// layout of ebar_rows (warp w rows 8w..8w+7, lane l states 2l and 2l+1): every
+// P row is one coalesced 512-byte gather, every conP row one 512-byte store,
+// and the row maxima are warp shuffles (no block barrier).
+__device__ __forceinline__ void tip_rows(const FastFwdArgs &a, const Item &it, int tile) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const size_t npad = a.npad;
+    const size_t r0 = (size_t)tile * 128 + 8 * warp;
+    const size_t hl = r0 + (lane & 7);                 // the row of this lane's codons
+    float4 X[8];
+    {
+        const int zl = a.z[(size_t)it.child[0] * npad + hl];
+        const float4 *P = reinterpret_cast<const float4 *>(a.Pdf + (size_t)it.pidx[0] * 4096) + lane;
+#pragma unroll
+        for (int j = 0; j < 8; j++) X[j] = __ldg(P + 32 * __shfl_sync(0xffffffffu, zl, j));
+    }
+#pragma unroll 1
+    for (int ci = 1; ci < it.nchild; ci++) {
+        const int zl = a.z[(size_t)it.child[ci] * npad + hl];
+        const float4 *P = reinterpret_cast<const float4 *>(a.Pdf + (size_t)it.pidx[ci] * 4096) + lane;
+        float4 E[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) E[j] = __ldg(P + 32 * __shfl_sync(0xffffffffu, zl, j));
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float2 x0 = df_mul(make_float2(X[j].x, X[j].y), make_float2(E[j].x, E[j].y));
+            const float2 x1 = df_mul(make_float2(X[j].z, X[j].w), make_float2(E[j].z, E[j].w));
+            X[j] = make_float4(x0.x, x0.y, x1.x, x1.y);
+        }
+    }
+    float4 *dst = reinterpret_cast<float4 *>(a.conP + ((size_t)it.slot * npad + r0) * 64) + lane;
+    int shl = 0;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        float m = fmaxf(2 * lane < NC ? X[j].x : 0.f, 2 * lane + 1 < NC ? X[j].z : 0.f);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        const int sh = m > 0.f ? ilogbf(m) + 1 : 0;
+        const float2 x0 = df_scale(make_float2(X[j].x, X[j].y), -sh);
+        const float2 x1 = df_scale(make_float2(X[j].z, X[j].w), -sh);
+        dst[32 * j] = make_float4(x0.x, x0.y, x1.x, x1.y);
+        if ((lane & 7) == j) shl = sh;
+    }
+    if (lane < 8) a.expo[(size_t)it.slot * npad + hl] = shl;
+}
+
 // One (node, class) item on one 128-pattern tile.  Needs TMEM when the item
 // has an internal child.  Returns the block-uniform success flag.
 template <int NS>
@@ -404,6 +451,14 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
     const size_t npad = a.npad;
     const size_t h0 = (size_t)tile * 128, h = h0 + row;
     bool ok = true;
+    if (!it.is_root) {
+        bool all_tips = true;
+        for (int ci = 0; ci < it.nchild; ci++) all_tips = all_tips && it.cslot[ci] < 0;
+        if (all_tips) {
+            tip_rows(a, it, tile);
+            return true;
+        }
+    }
     float2 prod[NCOL];
     int expo = 0;
     bool have = false;

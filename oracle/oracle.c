@@ -24,6 +24,11 @@
  *   node_scale        NodeScale treesub.c:6940-6975, SetNodeScale 6917-6937
  *   fx_r / lfundG     fx_r treesub.c:7485-7551, lfundG treesub.c:7342-7394
  *   gradientB         gradientB tools.c:6326-6350 (Small_Diff = 1e-6)
+ *   oracle_beb        Bayes empirical Bayes site-class posteriors of model A:
+ *                     lfunNSsites_ACD codeml.c:6617-6826,
+ *                     get_grid_para_like_ACD 6419-6530, get_pclassM_iw_ACD
+ *                     6532-6615, GetIndexTernary tools.c:4441-4461, and the
+ *                     BEB branch of GetPMatBranch treesub.c:7289-7301
  *
  * The pattern loop is split over OpenMP threads (each thread walks the whole
  * tree for its own pattern range), which is the multi-core CPU baseline.
@@ -470,6 +475,215 @@ double oracle_lnL(const oracle_problem *pb, const double *x, int lastround,
     if (fhK_out) memcpy(fhK_out, fhK, sizeof(double) * 4 * np);
     free(P); free(scale); free(Pall); free(conP); free(scaleF); free(fhK); free(tnode);
     return lnL;
+}
+
+/* --------------------------------------------------------------- BEB */
+
+#define BEB_D 10                                  /* grid points per dimension */
+#define BEB_NW (BEB_D + 1 + BEB_D * BEB_D + BEB_D)  /* 121 omega sets */
+#define BEB_NG (BEB_D * BEB_D * BEB_D * BEB_D)     /* (p0,p1) x w0 x w2 grid */
+
+/* Root log f + scale logs for every pattern, one full pruning with the
+   per-node transition matrices Pall (the root-sum step of fx_r,
+   get_grid_para_like_ACD codeml.c:6504-6514: log taken whatever NnodeScale). */
+static void root_logf(const oracle_problem *pb, const double *Pall, const char *scale, double *conP,
+                      double *scaleF, double *out) {
+    int n = NC, np = pb->npatt, nn = pb->nnode, nth = pb->nthreads;
+#ifdef _OPENMP
+    if (nth <= 0) nth = omp_get_max_threads();
+#else
+    nth = 1;
+#endif
+    walk_t w = {pb, Pall, conP, scale, scaleF};
+    int chunks = nth * 4;
+    if (chunks > np) chunks = np;
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nth)
+    for (int c = 0; c < chunks; c++) {
+        int pos0 = (int)((long)np * c / chunks), pos1 = (int)((long)np * (c + 1) / chunks);
+        if (pos1 <= pos0) continue;
+        cond_node(&w, pb->root, pos0, pos1);
+        const double *cr = conP + (size_t)pb->root * np * n;
+        for (int h = pos0; h < pos1; h++) {
+            double fh = 0;
+            for (int i = 0; i < n; i++) fh += pb->pi[i] * cr[h * n + i];
+            if (fh <= 0) fh = 1e-300;
+            fh = log(fh);
+            for (int k = 0; k < nn; k++)
+                if (scale[k]) fh += scaleF[(size_t)k * np + h];
+            out[h] = fh;
+        }
+    }
+}
+
+/* omega index (0..9 grid w0, 10 = w1 = 1, 11..20 grid w2) of the background
+   and foreground branches for omega set iw: 10 sets (w0, w0), 1 set (1, 1),
+   100 sets (w0_i, w2_j) with iw = 11 + 10 i + j, 10 sets (1, w2_j). */
+static void beb_omega_set(int iw, int *eb, int *ef) {
+    if (iw < BEB_D) { *eb = *ef = iw; }
+    else if (iw == BEB_D) { *eb = *ef = BEB_D; }
+    else if (iw < BEB_D + 1 + BEB_D * BEB_D) {
+        *eb = (iw - BEB_D - 1) / BEB_D;
+        *ef = BEB_D + 1 + (iw - BEB_D - 1) % BEB_D;
+    } else { *eb = BEB_D; *ef = BEB_D + 1 + (iw - BEB_D - 1 - BEB_D * BEB_D); }
+}
+
+/*
+ * Bayes empirical Bayes under branch-site model A at x (normally the MLE).
+ * The synonymous branch lengths stay at the MLE: Qfactor_NS_branch and kappa
+ * come from x, while omega runs over the grid (w0 in (0,1), w2 in (1,11),
+ * 10 points each) and (p0, p1) over 100 triangles of the ternary plot.
+ * Outputs (each may be NULL):
+ *   lnfw[121*npatt]  log f(x_h | omega set) before rescaling
+ *   post[4*npatt]    posterior of the site classes 0, 1, 2a, 2b per pattern
+ *   grid[4*10]       posterior of the grid values of p0, p1 (-1: not
+ *                    computed), w0, w2 (codeml's "Posterior on the grid")
+ *   p0p1[100]        posterior over the ternary (p0, p1) triangles
+ *   lnfX[3]          log f(X) as codeml prints it, and its scale terms S1, S2
+ * Returns 0, or -1 on a parameter error.
+ */
+int oracle_beb(const oracle_problem *pb, const double *x, int lastround, double *lnfw_out,
+               double *post, double *grid, double *p0p1, double *lnfX) {
+    int n = NC, np = pb->npatt, nn = pb->nnode;
+    params_t *P = (params_t *)malloc(sizeof(params_t));
+    if (set_params(pb, x, lastround, P)) { free(P); return -1; }
+    /* the 21 omega values and their eigen solutions (unscaled Q: eigenQcodon
+       with meanrate 1, the Qfactor of the MLE applied to t) */
+    double wv[2 * BEB_D + 1];
+    for (int i = 0; i < BEB_D; i++) {
+        wv[i] = (i + 0.5) / BEB_D;
+        wv[BEB_D + 1 + i] = 1 + (i + 0.5) * (11 - 1) / BEB_D;
+    }
+    wv[BEB_D] = 1;
+    int ne = 2 * BEB_D + 1;
+    double *U = (double *)malloc(sizeof(double) * ne * n * n);
+    double *V = (double *)malloc(sizeof(double) * ne * n * n);
+    double *R = (double *)malloc(sizeof(double) * ne * n);
+    double *Q = (double *)malloc(sizeof(double) * n * n);
+    for (int e = 0; e < ne; e++) {
+        build_q(pb->pi, P->kappa, wv[e], Q);
+        eigen_uvr(Q, pb->pi, U + (size_t)e * n * n, V + (size_t)e * n * n, R + (size_t)e * n);
+    }
+    char *scale = (char *)calloc(nn, 1);
+    int nscale = 0;
+    set_node_scale(pb, pb->root, scale, &nscale);
+    double *tnode = (double *)calloc(nn, sizeof(double));
+    for (int ib = 0; ib < nn - 1; ib++) tnode[pb->bnode[ib]] = x[ib];
+    double *Pall = (double *)malloc(sizeof(double) * nn * n * n);
+    double *conP = (double *)malloc(sizeof(double) * (size_t)nn * np * n);
+    double *scaleF = (double *)calloc((size_t)nn * np, sizeof(double));
+    double *F = (double *)malloc(sizeof(double) * (size_t)BEB_NW * np);
+    for (int iw = 0; iw < BEB_NW; iw++) {
+        int eb, ef;
+        beb_omega_set(iw, &eb, &ef);
+        for (int i = 0; i < nn; i++) {
+            if (i == pb->root) continue;
+            int lab = pb->label[i], e = lab ? ef : eb;
+            pmat(Pall + (size_t)i * n * n, tnode[i] * P->qf[lab], U + (size_t)e * n * n,
+                 V + (size_t)e * n * n, R + (size_t)e * n);
+        }
+        root_logf(pb, Pall, scale, conP, scaleF, F + (size_t)iw * np);
+    }
+    if (lnfw_out) memcpy(lnfw_out, F, sizeof(double) * BEB_NW * np);
+    /* per-pattern rescaling by the largest of the 121 values (S1) */
+    double S1 = 0;
+    for (int h = 0; h < np; h++) {
+        double m = F[h];
+        for (int k = 1; k < BEB_NW; k++)
+            if (F[(size_t)k * np + h] > m) m = F[(size_t)k * np + h];
+        for (int k = 0; k < BEB_NW; k++) F[(size_t)k * np + h] = exp(F[(size_t)k * np + h] - m);
+        S1 += m * pb->fpatt[h];
+    }
+    /* grid: class proportions (ternary centroids, 2a/2b split p2 by p0:p1) and
+       the omega set each class reads */
+    double *pcl = (double *)malloc(sizeof(double) * BEB_NG * 4);
+    int *iwg = (int *)malloc(sizeof(int) * BEB_NG * 4);
+    for (int g = 0; g < BEB_NG; g++) {
+        int ip[4];
+        for (int j = 3, it = g; j >= 0; j--) { ip[j] = it % BEB_D; it /= BEB_D; }
+        int t = ip[0] * BEB_D + ip[1];
+        int ix = (int)sqrt((double)t), iy = t - ix * ix;
+        double p[3];
+        p[0] = (1 + (iy / 2) * 3 + (iy % 2)) / (3. * BEB_D);
+        p[1] = (1 + (BEB_D - 1 - ix) * 3 + (iy % 2)) / (3. * BEB_D);
+        p[2] = 1 - p[0] - p[1];
+        pcl[g * 4 + 0] = p[0];
+        pcl[g * 4 + 1] = p[1];
+        pcl[g * 4 + 2] = p[2] * p[0] / (1 - p[2]);
+        pcl[g * 4 + 3] = p[2] * p[1] / (1 - p[2]);
+        iwg[g * 4 + 0] = ip[2];
+        iwg[g * 4 + 1] = BEB_D;
+        iwg[g * 4 + 2] = BEB_D + 1 + ip[2] * BEB_D + ip[3];
+        iwg[g * 4 + 3] = BEB_D + 1 + BEB_D * BEB_D + ip[3];
+    }
+    /* marginal likelihood f(X) over the grid, with codeml's running scale S2 */
+    double *lnfXs = (double *)malloc(sizeof(double) * BEB_NG);
+    double pp[4][BEB_D], pq[BEB_D * BEB_D];
+    memset(pp, 0, sizeof pp);
+    memset(pq, 0, sizeof pq);
+    double fX = 1, S2 = -1e300;
+    for (int g = 0; g < BEB_NG; g++) {
+        int ip[4];
+        for (int j = 3, it = g; j >= 0; j--) { ip[j] = it % BEB_D; it /= BEB_D; }
+        double s = 0;
+        for (int h = 0; h < np; h++) {
+            double fh = 0;
+            for (int k = 0; k < 4; k++) fh += pcl[g * 4 + k] * F[(size_t)iwg[g * 4 + k] * np + h];
+            if (fh < 1e-300) continue;
+            s += log(fh) * pb->fpatt[h];
+        }
+        lnfXs[g] = s;
+        double t = s - S2;
+        if (t > 10) {
+            t = t < 200 ? exp(-t) : 0;
+            fX = fX * t + 1;
+            for (int j = 0; j < 4; j++)
+                for (int k = 0; k < BEB_D; k++) pp[j][k] *= t;
+            for (int k = 0; k < BEB_D * BEB_D; k++) pq[k] *= t;
+            for (int j = 0; j < 4; j++) pp[j][ip[j]] += 1;
+            pq[ip[0] * BEB_D + ip[1]] += 1;
+            S2 = s;
+        } else if (t > -200) {
+            t = exp(t);
+            fX += t;
+            for (int j = 0; j < 4; j++) pp[j][ip[j]] += t;
+            pq[ip[0] * BEB_D + ip[1]] += t;
+        }
+    }
+    for (int j = 0; j < 4; j++)
+        for (int k = 0; k < BEB_D; k++) pp[j][k] /= fX;
+    for (int k = 0; k < BEB_D * BEB_D; k++) pq[k] /= fX;
+    double lfX = log(fX) + S2;
+    if (lnfX) {
+        lnfX[0] = lfX + S1 - 4 * log((double)BEB_D);
+        lnfX[1] = S1;
+        lnfX[2] = S2;
+    }
+    if (grid) {
+        for (int k = 0; k < BEB_D; k++) grid[k] = grid[BEB_D + k] = -1;
+        for (int j = 2; j < 4; j++)
+            for (int k = 0; k < BEB_D; k++) grid[j * BEB_D + k] = pp[j][k];
+    }
+    if (p0p1) memcpy(p0p1, pq, sizeof pq);
+    /* posterior of the four site classes per pattern */
+    if (post) {
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int h = 0; h < np; h++) {
+            double acc[4] = {0, 0, 0, 0};
+            for (int g = 0; g < BEB_NG; g++) {
+                double fk[4], fh = 0;
+                for (int k = 0; k < 4; k++)
+                    fh += fk[k] = pcl[g * 4 + k] * F[(size_t)iwg[g * 4 + k] * np + h];
+                for (int k = 0; k < 4; k++) {
+                    double t = log(fk[k] / fh) + lnfXs[g] - lfX;
+                    if (t > -300) acc[k] += exp(t);
+                }
+            }
+            for (int k = 0; k < 4; k++) post[k * np + h] = acc[k];
+        }
+    }
+    free(P); free(U); free(V); free(R); free(Q); free(scale); free(tnode); free(Pall);
+    free(conP); free(scaleF); free(F); free(pcl); free(iwg); free(lnfXs);
+    return 0;
 }
 
 /* Model quantities codeml derives from x, for parity tests of the CUDA

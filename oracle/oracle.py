@@ -57,6 +57,8 @@ def lib():
         L.oracle_pmat.restype = None
         L.oracle_pmat.argtypes = [dp, C.c_double, dp, dp, dp]
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_beb.restype = C.c_int
+        L.oracle_beb.argtypes = [C.POINTER(_Problem), dp, C.c_int, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -137,6 +139,26 @@ class Problem:
         g = np.zeros(len(x))
         lib().oracle_gradientB(C.byref(self._s), _dp(x), len(x), int(lastround), int(central), _dp(g))
         return g
+
+
+    def beb(self, x, lastround: bool = True, want_lnfw: bool = True):
+        """Bayes empirical Bayes of model A at x (oracle.c oracle_beb): a dict
+        with lnfw [121, npatt], post [4, npatt], grid [4, 10], p0p1 [100] and
+        lnfX, S1, S2."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        lnfw = np.zeros(121 * self.npatt) if want_lnfw else None
+        post = np.zeros(4 * self.npatt)
+        grid = np.zeros(40)
+        p0p1 = np.zeros(100)
+        fx = np.zeros(3)
+        rc = lib().oracle_beb(C.byref(self._s), _dp(x), int(lastround),
+                              _dp(lnfw) if lnfw is not None else None, _dp(post), _dp(grid),
+                              _dp(p0p1), _dp(fx))
+        if rc:
+            raise ValueError("parameter error")
+        return {"lnfw": lnfw.reshape(121, self.npatt) if lnfw is not None else None,
+                "post": post.reshape(4, self.npatt), "grid": grid.reshape(4, 10), "p0p1": p0p1,
+                "lnfX": fx[0], "S1": fx[1], "S2": fx[2]}
 
 
 def build_q(pi, kappa, omega):

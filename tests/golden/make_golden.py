@@ -15,6 +15,13 @@ fixture keeps: the codon alignment, tree, x, codeml's lnL (out file, 6 dp),
 per-pattern log f (10 dp), pattern codons and counts (pattern order), and the
 F3x4 codon frequencies (out file, 8 dp).
 
+With fix_omega = 0 codeml then runs its Bayes empirical Bayes analysis
+(lfunNSsites_rate codeml.c:5215 -> lfunNSsites_ACD 6617-6826) at the same x;
+the fixture also keeps its per-site posteriors of the four site classes (rst,
+5 dp), the posterior on the w0 / w2 grid and on the p0-p1 triangles (out
+file, 3 dp) and the printed log f(X) with its scale terms S1, S2 (stdout, 6
+dp).
+
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -94,10 +101,11 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, zero_br
             f.write("-1 " + " ".join(repr(float(v)) for v in x) + "\n")
         with open(os.path.join(d, "codeml.ctl"), "w") as f:
             f.write(CTL)
-        subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True,
-                       stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        r = subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
         out = open(os.path.join(d, "out.txt")).read()
         lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
+        rst = open(os.path.join(d, "rst")).read()
+    beb = parse_beb(out, rst, r.stdout)
     m = re.search(r"lnL\(ntime:\s*(\d+)\s+np:\s*(\d+)\):\s*(-?\d+\.\d+)", out)
     lnL = float(m.group(3))
     i0 = out.index("Codon frequencies under model")
@@ -120,7 +128,34 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, zero_br
         "x": [float(v) for v in x], "lastround": 1,
         "codeml_lnL": lnL, "codeml_np": int(m.group(2)),
         "lnf": lnf, "fpatt": fp, "patterns": [" ".join(p) for p in pats], "pi_8dp": pi8,
+        "beb": beb,
     }
+
+
+def parse_beb(out: str, rst: str, stdout: str) -> dict:
+    """codeml's BEB results: per-site class posteriors (rst), grid posteriors
+    (out) and log f(X), S1, S2 (stdout)."""
+    i0 = rst.index("Bayes Empirical Bayes (BEB) probabilities")
+    site = []
+    for ln in rst[i0:].splitlines()[3:]:
+        parts = ln.split()
+        if len(parts) < 7 or not parts[0].isdigit():
+            break
+        site.append([float(v) for v in parts[2:6]])
+    j0 = out.index("Posterior on the grid")
+    rows = {}
+    for ln in out[j0:].splitlines()[1:6]:
+        parts = ln.split()
+        if parts and parts[0] in ("w0:", "w2:"):
+            rows[parts[0][:2]] = [float(v) for v in parts[1:]]
+    k0 = out.index("Posterior for p0-p1")
+    k1 = out.index("sum of density on p0-p1")
+    p0p1 = [float(v) for v in out[k0:k1].split("\n", 1)[1].split()]
+    m = re.search(r"log\(fX\) =\s*(-?\d+\.\d+)\s+S =\s*(-?\d+\.\d+)\s+(-?\d+\.\d+)",
+                  stdout.replace("\r", "\n"))
+    return {"site_post_5dp": site, "w0_post_3dp": rows["w0"], "w2_post_3dp": rows["w2"],
+            "p0p1_post_3dp": p0p1, "lnfX_6dp": float(m.group(1)), "S1_6dp": float(m.group(2)),
+            "S2_6dp": float(m.group(3))}
 
 
 def main():

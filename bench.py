@@ -220,6 +220,45 @@ def batched_leg(args, dev):
     return out
 
 
+def beb_leg(args, dev, tree, z, fpatt, pi, bl0):
+    """Bayes empirical Bayes site analysis of model A (gb_beb, FP64) on the
+    bench alignment at the bench parameters: device and end-to-end time of one
+    analysis; with the CPU leg, the oracle's BEB on a pattern subset, scaled by
+    patterns (every part of the analysis is linear in the pattern count)."""
+    from cucodeml_gb300 import api
+    lk = api.Likelihood(tree, z, fpatt, pi, precision="fp64", device=dev)
+    args_beb = (bl0, PARAMS["kappa"], PARAMS["omega0"], PARAMS["omega2"], PARAMS["p0"], PARAMS["p1"])
+    r = lk.beb(*args_beb)
+    runs = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        r = lk.beb(*args_beb)
+        runs.append((time.perf_counter() - t0, r["ms_device"]))
+    lk.close()
+    e2e = min(t for t, _ in runs)
+    out = {"workload": f"BEB of model A, {args.ns} taxa x {args.ncodon} codons: f(x_h|w) for 121 omega sets "
+                       f"(FP64 prunings) and the 10^4-point grid integral",
+           "ms_device": min(d for _, d in runs), "ms_e2e": 1000.0 * e2e, "kernels": r["kernels"],
+           "max_abs_post_sum_minus_1": float(np.max(np.abs(r["post"].sum(axis=0) - 1.0))),
+           "lnfX": r["lnfX"]}
+    if not args.no_cpu:
+        from oracle import oracle as O
+        S = min(256, len(fpatt))
+        pb = O.Problem(tree, np.ascontiguousarray(z[:, :S]), np.ascontiguousarray(fpatt[:S]), pi,
+                       nthreads=O.max_threads())
+        x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
+                                                      PARAMS["omega0"], PARAMS["omega2"]]])
+        t0 = time.perf_counter()
+        pb.beb(x, want_lnfw=False)
+        dt = time.perf_counter() - t0
+        est = dt * len(fpatt) / S
+        out["cpu_baseline"] = {"value_ms": 1000.0 * est, "cores": O.max_threads(), "kind": "port",
+                               "sample": f"oracle BEB on the first {S} of {len(fpatt)} patterns, "
+                                         f"{dt:.2f} s, scaled by patterns"}
+        out["e2e_speedup_vs_cpu"] = est / e2e
+    return out
+
+
 def cpu_baseline(tree, z, fpatt, pi, threads: int, seconds: float = 12.0, min_evals: int = 2):
     """Time the oracle's lnL on the host cores; lnL+gradient = (np+1) lnL evals."""
     from oracle import oracle as O
@@ -287,6 +326,7 @@ def main():
     ap.add_argument("--ns", type=int, default=64)
     ap.add_argument("--ncodon", type=int, default=5000)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-beb", action="store_true", help="skip the Bayes empirical Bayes leg")
     ap.add_argument("--batch", type=int, default=512, help="genes in the batched leg (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--no-tune", action="store_true", help="batched leg: skip the autotuner (library defaults)")
@@ -429,6 +469,8 @@ def main():
         lk64.close()
     if args.batch > 0:
         line["batched"] = batched_leg(args, dev)
+    if not args.no_beb:
+        line["beb"] = beb_leg(args, dev, tree, z, fpatt, pi, bl0)
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         line["cpu_baseline"] = cpu_baseline(tree, z, fpatt, pi, O.max_threads())

@@ -197,6 +197,40 @@ class Likelihood:
             p0, p1 = e / (1 + e.sum())
         return self.evaluate(bl, kappa, w0, w2, p0, p1, grad=grad)
 
+    def beb(self, blength, kappa, omega0, omega2, p0, p1, want_lnfw: bool = False) -> dict:
+        """Bayes empirical Bayes site analysis of model A at these (MLE)
+        parameters (gb_beb; codeml's lfunNSsites_ACD, codeml.c:6617-6826).
+        Needs an FP64 handle.  Returns post [4, npatt] (classes 0, 1, 2a, 2b),
+        grid [4, 10] (rows p0, p1 = -1, w0, w2), p0p1 [100], lnfX, S1, S2,
+        lnfw [121, npatt] when asked for, and the call's device / host ms."""
+        bl = np.ascontiguousarray(blength, dtype=np.float64)
+        prm = _lib.Params(_ptr(bl), kappa, omega0, omega2, p0, p1)
+        lnfw = np.zeros((121, self.npatt)) if want_lnfw else None
+        post = np.zeros((4, self.npatt))
+        grid = np.zeros((4, 10))
+        p0p1 = np.zeros(100)
+        fx = np.zeros(3)
+        st = _lib.Stats()
+        _lib.check(self._L.gb_beb(self._h, C.byref(prm), _ptr(lnfw) if want_lnfw else None, _ptr(post),
+                                  _ptr(grid), _ptr(p0p1), _ptr(fx), C.byref(st)))
+        return {"post": post, "grid": grid, "p0p1": p0p1, "lnfX": float(fx[0]), "S1": float(fx[1]),
+                "S2": float(fx[2]), "lnfw": lnfw, "ms_device": st.ms_device, "ms_host": st.ms_host,
+                "kernels": st.kernels}
+
+    def beb_x(self, x, lastround: bool = True, want_lnfw: bool = False) -> dict:
+        """beb() from codeml's x vector."""
+        x = np.asarray(x, dtype=np.float64)
+        nb = self.nnode - 1
+        bl = np.zeros(self.nnode)
+        bl[self.bnode] = x[:nb]
+        kappa, w0, w2 = x[nb], x[nb + 3], x[nb + 4]
+        if lastround:
+            p0, p1 = x[nb + 1], x[nb + 2]
+        else:
+            e = np.exp(x[nb + 1:nb + 3])
+            p0, p1 = e / (1 + e.sum())
+        return self.beb(bl, kappa, w0, w2, p0, p1, want_lnfw=want_lnfw)
+
     def dfun_x(self, x, lastround: bool = True):
         """(f, dx) as ming2's dfun hook: f = -lnL, dx = d(-lnL)/dx in codeml's x space."""
         x = np.ascontiguousarray(x, dtype=np.float64)

@@ -1,0 +1,393 @@
+// Bayes empirical Bayes (BEB) site analysis of branch-site model A on the
+// device: the work of codeml's lfunNSsites_ACD (codeml.c:6617-6826).
+//
+// 1. f(x_h | w) for 121 omega sets (get_grid_para_like_ACD codeml.c:6419-6530).
+//    A set gives the background and the foreground branches their own omega;
+//    kappa, the branch lengths and the two branch Qfactors stay at the MLE
+//    (GetPMatBranch's BEB branch, treesub.c:7289-7301, applies
+//    Qfactor_NS_branch to t with the unscaled Q of the set's omega).  The
+//    handle's FP64 forward already computes four such sets per launch: its
+//    site classes 0 and 1 are full trees with one omega everywhere, and
+//    classes 2a and 2b re-prune only the foreground branch's path to the root
+//    from class 0 / class 1 subtrees.  So with the three eigen slots set to
+//    (w0_i, 1, w2_j) one launch yields sets i, 10, 11 + 10 i + j and 111 + j,
+//    and for j > 0 only the path items (classes 2a, 2b) need running again:
+//    10 full forwards and 90 path-only forwards, each a replayed CUDA graph;
+//    the eigen solutions of the 21 omega values are uploaded once and copied
+//    into the parameter block on the device between launches.
+// 2. Per pattern, the 121 log values are rescaled by their maximum (the S1
+//    term), the 10^4-point grid integral log f(X) (get_pclassM_iw_ACD
+//    6532-6615, then 6700-6756) and the site-class posteriors (6758-6775).
+//    The marginal over the grid with codeml's running scale S2 is a short
+//    sequential loop over 10^4 numbers on the host; the two 10^4 x npatt
+//    reductions are device kernels.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstddef>
+#include <cstring>
+#include <vector>
+
+#include "gbcodeml.h"
+#include "handle.h"
+#include "internal.h"
+#include "model.h"
+
+namespace gb {
+namespace {
+
+constexpr int BD = GB_BEB_GRID;                 // grid points per dimension
+constexpr int BNW = GB_BEB_OMEGA_SETS;          // omega sets
+constexpr int BNE = 2 * BD + 1;                 // distinct omega values: w0 grid, 1, w2 grid
+constexpr int BNT = BD * BD;                    // (p0, p1) triangles
+constexpr int BNG = BNT * BD * BD;              // grid points (triangle, w0, w2)
+constexpr int EIG = 2 * NC * NC + NC;           // U, V, Root of one omega
+static_assert(BNW == BD + 1 + BD * BD + BD, "omega set count");
+
+// log table (in place, when the forward wrote linear f), per-pattern maximum
+// and the rescaled table exp(log f - max)
+__global__ void __launch_bounds__(256) beb_rescale_kernel(double *__restrict__ lnfw, double *__restrict__ F,
+                                                          double *__restrict__ mrow, int npatt, int npad,
+                                                          int linear) {
+    const int h = blockIdx.x * blockDim.x + threadIdx.x;
+    if (h >= npatt) return;
+    double m = 0.0;
+    for (int k = 0; k < BNW; k++) {
+        double v = lnfw[(size_t)k * npad + h];
+        if (linear) {
+            v = log(v);
+            lnfw[(size_t)k * npad + h] = v;
+        }
+        if (k == 0 || v > m) m = v;
+    }
+    for (int k = 0; k < BNW; k++) F[(size_t)k * npad + h] = exp(lnfw[(size_t)k * npad + h] - m);
+    mrow[h] = m;
+}
+
+// the omega sets the four classes read at grid point g = ((t * 10) + i) * 10 + j
+// (t: (p0, p1) triangle, i: w0 index, j: w2 index)
+__device__ __forceinline__ void beb_sets(int g, int &t, int &s0, int &s2a, int &s2b) {
+    t = g / (BD * BD);
+    const int q = g - t * BD * BD;
+    const int i = q / BD;
+    s0 = i;
+    s2a = BD + 1 + q;
+    s2b = BD + 1 + BD * BD + (q - i * BD);
+}
+
+// lnfXs[g] = sum_h fpatt_h log sum_k p_k(g) F[set_k(g)][h]; one block per grid point
+__global__ void __launch_bounds__(256) beb_grid_kernel(const double *__restrict__ F,
+                                                       const double *__restrict__ fpatt,
+                                                       const double *__restrict__ pcl, int npatt, int npad,
+                                                       double *__restrict__ lnfXs) {
+    __shared__ double red[8];
+    const int g = blockIdx.x;
+    int t, s0, s2a, s2b;
+    beb_sets(g, t, s0, s2a, s2b);
+    const double p0 = pcl[t * 4 + 0], p1 = pcl[t * 4 + 1], p2 = pcl[t * 4 + 2], p3 = pcl[t * 4 + 3];
+    const double *r0 = F + (size_t)s0 * npad, *r1 = F + (size_t)BD * npad;
+    const double *r2 = F + (size_t)s2a * npad, *r3 = F + (size_t)s2b * npad;
+    double s = 0.0;
+    for (int h = threadIdx.x; h < npatt; h += blockDim.x) {
+        double fh = p0 * r0[h];
+        fh += p1 * r1[h];
+        fh += p2 * r2[h];
+        fh += p3 * r3[h];
+        if (fh < 1e-300) continue;   // codeml skips such a pattern ("strange: f[h] very small")
+        s += log(fh) * fpatt[h];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) v += red[w];
+        lnfXs[g] = v;
+    }
+}
+
+// post[k][h] = sum_g [ratio > thr_g] ratio * w_g, ratio = p_k F_k / sum_k p_k F_k and
+// w_g = exp(lnfXs[g] - log f(X)): codeml's sum of exp(log(ratio) + lnfXs[g] - log f(X))
+// over the terms above exp(-300).  One warp per pattern, lanes over the grid.
+__global__ void __launch_bounds__(256) beb_post_kernel(const double *__restrict__ F,
+                                                       const double *__restrict__ pcl,
+                                                       const double2 *__restrict__ wt, int npatt, int npad,
+                                                       double *__restrict__ post) {
+    __shared__ double fs[8][BNW + 7];
+    __shared__ double ps[BNT * 4];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < BNT * 4; i += blockDim.x) ps[i] = pcl[i];
+    const int h = blockIdx.x * 8 + warp;
+    if (h < npatt)
+        for (int k = lane; k < BNW; k += 32) fs[warp][k] = F[(size_t)k * npad + h];
+    __syncthreads();
+    if (h >= npatt) return;
+    const double *f = fs[warp];
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    for (int g = lane; g < BNG; g += 32) {
+        int t, s0, s2a, s2b;
+        beb_sets(g, t, s0, s2a, s2b);
+        const double2 w = wt[g];
+        const double f0 = ps[t * 4 + 0] * f[s0], f1 = ps[t * 4 + 1] * f[BD];
+        const double f2 = ps[t * 4 + 2] * f[s2a], f3 = ps[t * 4 + 3] * f[s2b];
+        const double inv = 1.0 / (((f0 + f1) + f2) + f3);
+        double r = f0 * inv;
+        if (r > w.y) a0 += r * w.x;
+        r = f1 * inv;
+        if (r > w.y) a1 += r * w.x;
+        r = f2 * inv;
+        if (r > w.y) a2 += r * w.x;
+        r = f3 * inv;
+        if (r > w.y) a3 += r * w.x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a0 += __shfl_down_sync(0xffffffffu, a0, o);
+        a1 += __shfl_down_sync(0xffffffffu, a1, o);
+        a2 += __shfl_down_sync(0xffffffffu, a2, o);
+        a3 += __shfl_down_sync(0xffffffffu, a3, o);
+    }
+    if (lane == 0) {
+        post[h] = a0;
+        post[(size_t)npad + h] = a1;
+        post[(size_t)2 * npad + h] = a2;
+        post[(size_t)3 * npad + h] = a3;
+    }
+}
+
+// device scratch of one gb_beb call, freed on every exit
+struct BebBuffers {
+    double *eig = nullptr, *lnfw = nullptr, *F = nullptr, *mrow = nullptr, *pcl = nullptr;
+    double *lnfXs = nullptr, *post = nullptr;
+    double2 *wt = nullptr;
+    ~BebBuffers() {
+        void *p[] = {eig, lnfw, F, mrow, pcl, lnfXs, post, wt};
+        for (void *q : p)
+            if (q) cudaFree(q);
+    }
+};
+
+// CUDA graph of the forward restricted to the class-2a/2b items: P(t) of every
+// (branch, omega) pair, then the path items level by level
+int ensure_fg_graph(gb_handle *h) {
+    if (h->graph_fg) return 0;
+    std::vector<Item> fg;
+    h->fg_off.assign(h->level_off.size(), 0);
+    for (size_t L = 0; L + 1 < h->level_off.size(); L++) {
+        h->fg_off[L] = (int)fg.size();
+        for (int i = h->level_off[L]; i < h->level_off[L + 1]; i++)
+            if (h->items[i].cls >= 2) fg.push_back(h->items[i]);
+    }
+    h->fg_off.back() = (int)fg.size();
+    int rc = dalloc(&h->d_items_fg, fg.size());
+    if (rc) return rc;
+    CK(cudaMemcpy(h->d_items_fg, fg.data(), sizeof(Item) * fg.size(), cudaMemcpyHostToDevice));
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int nk = 1;
+    launch_pmat_fp64(h->d_pairs, (int)h->pairs.size(), h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->stream,
+                     h->d_pi);
+    for (size_t L = 0; L + 1 < h->fg_off.size(); L++) {
+        const int n = h->fg_off[L + 1] - h->fg_off[L];
+        if (n == 0) continue;
+        launch_prune_fp64(h->d_items_fg + h->fg_off[L], n, h->ntile, h->npad, h->d_z, h->d_Pt, h->d_conP,
+                          nullptr, h->d_scaleF, h->d_scale_list, h->nscale, h->d_pi, h->d_fbar, h->d_ssum,
+                          h->d_fhK, h->stream);
+        nk++;
+    }
+    CK(cudaStreamEndCapture(h->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&h->graph_fg, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(GB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+    h->graph_fg_kernels = nk;
+    return 0;
+}
+
+// class proportions at the centroid of (p0, p1) triangle t of the ternary plot
+// (GetIndexTernary tools.c:4441-4461); 2a and 2b split p2 in the ratio p0 : p1
+void triangle_classes(int t, double p[4]) {
+    const int ix = (int)std::sqrt((double)t), iy = t - ix * ix;
+    const double a = (1 + (iy / 2) * 3 + (iy % 2)) / (3. * BD);
+    const double b = (1 + (BD - 1 - ix) * 3 + (iy % 2)) / (3. * BD);
+    const double c = 1 - a - b;
+    p[0] = a;
+    p[1] = b;
+    p[2] = c * a / (1 - c);
+    p[3] = c * b / (1 - c);
+}
+
+}  // namespace
+}  // namespace gb
+
+using namespace gb;
+
+int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw_out, double *post_out, double *grid_out,
+           double *p0p1_out, double *lnfX_out, gb_stats *stats) {
+    if (!h) return fail(GB_ERR_STATE, "null handle");
+    if (!prm || !prm->blength) return fail(GB_ERR_ARG, "null argument");
+    if (h->precision != GB_PREC_FP64) return fail(GB_ERR_STATE, "gb_beb needs a GB_PREC_FP64 handle");
+    const double t0 = now_ms();
+    // Qfactors and kappa at prm; eigen solutions of the 21 omega values
+    std::vector<Derived> Dv(1);
+    Derived &D = Dv[0];
+    ModelParams m{prm->kappa, prm->omega0, prm->omega2, prm->p0, prm->p1};
+    int rc = derive_scalars(h->pi.data(), m, &D);
+    if (rc) return fail(rc, "model parameters out of range");
+    double wv[BNE];
+    for (int i = 0; i < BD; i++) {
+        wv[i] = (i + 0.5) / BD;                          // w0 in (0, 1)
+        wv[BD + 1 + i] = 1 + (i + 0.5) * (11 - 1) / BD;  // w2 in (1, 11)
+    }
+    wv[BD] = 1;
+    std::vector<double> eig((size_t)BNE * EIG);
+    for (int e = 0; e < BNE; e++) {
+        std::vector<double> Q(NC * NC);
+        build_q(h->pi.data(), prm->kappa, wv[e], Q.data(), nullptr, nullptr);
+        double *E = &eig[(size_t)e * EIG];
+        if (eigen_qrev(Q.data(), h->pi.data(), E, E + NC * NC, E + 2 * NC * NC))
+            return fail(GB_ERR_PARAM, "eigen solution failed");
+    }
+    // the parameter block starts as (w0_0, 1, w2_0) with the Qfactors of prm
+    for (int s = 0; s < 3; s++) {
+        const int e = s == 0 ? 0 : (s == 1 ? BD : BD + 1);
+        std::memcpy(D.U[s], &eig[(size_t)e * EIG], sizeof(double) * NC * NC);
+        std::memcpy(D.V[s], &eig[(size_t)e * EIG + NC * NC], sizeof(double) * NC * NC);
+        std::memcpy(D.Root[s], &eig[(size_t)e * EIG + 2 * NC * NC], sizeof(double) * NC);
+    }
+    D.sym = 1;
+    if ((rc = stage_params(h, &D, prm->blength))) return rc;
+    if ((rc = fp64_prepare(h, false))) return rc;
+    if ((rc = ensure_fg_graph(h))) return rc;
+    const size_t npad = h->npad;
+    const int npatt = h->npatt;
+    BebBuffers B;
+    if ((rc = dalloc(&B.eig, eig.size())) || (rc = dalloc(&B.lnfw, (size_t)BNW * npad)) ||
+        (rc = dalloc(&B.F, (size_t)BNW * npad)) || (rc = dalloc(&B.mrow, npad)) ||
+        (rc = dalloc(&B.pcl, BNT * 4)) || (rc = dalloc(&B.lnfXs, BNG)) || (rc = dalloc(&B.post, 4 * npad)) ||
+        (rc = dalloc(&B.wt, BNG)))
+        return rc;
+    std::vector<double> pcl(BNT * 4);
+    for (int t = 0; t < BNT; t++) triangle_classes(t, &pcl[t * 4]);
+    cudaStream_t st = h->stream;
+    CK(cudaEventRecord(h->ev0, st));
+    CK(cudaMemcpyAsync(B.eig, eig.data(), sizeof(double) * eig.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(B.pcl, pcl.data(), sizeof(double) * pcl.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->d_prm, h->h_prm, sizeof(DevParams), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(h->d_tnode, h->h_tnode, sizeof(double) * h->nnode, cudaMemcpyHostToDevice, st));
+    // eigen slot s of the device parameter block <- omega value e
+    char *prm_base = reinterpret_cast<char *>(h->d_prm);
+    auto set_slot = [&](int s, int e) -> int {
+        const double *E = B.eig + (size_t)e * EIG;
+        const size_t mat = sizeof(double) * NC * NC, vec = sizeof(double) * NC;
+        CK(cudaMemcpyAsync(prm_base + offsetof(DevParams, U) + s * mat, E, mat, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(prm_base + offsetof(DevParams, V) + s * mat, E + NC * NC, mat,
+                           cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(prm_base + offsetof(DevParams, Root) + s * vec, E + 2 * NC * NC, vec,
+                           cudaMemcpyDeviceToDevice, st));
+        return 0;
+    };
+    auto keep = [&](int cls, int set) -> int {
+        CK(cudaMemcpyAsync(B.lnfw + (size_t)set * npad, h->d_fhK + (size_t)cls * npad, sizeof(double) * npad,
+                           cudaMemcpyDeviceToDevice, st));
+        return 0;
+    };
+    int kernels = 0;
+    for (int i = 0; i < BD; i++) {
+        if ((rc = set_slot(0, i))) return rc;
+        for (int j = 0; j < BD; j++) {
+            if ((rc = set_slot(2, BD + 1 + j))) return rc;
+            if (j == 0) {
+                CK(cudaGraphLaunch(h->graph[0], st));
+                kernels += h->graph_kernels;
+                if ((rc = keep(0, i))) return rc;
+                if (i == 0 && (rc = keep(1, BD))) return rc;
+            } else {
+                CK(cudaGraphLaunch(h->graph_fg, st));
+                kernels += h->graph_fg_kernels;
+            }
+            if ((rc = keep(2, BD + 1 + i * BD + j))) return rc;
+            if (i == 0 && (rc = keep(3, BD + 1 + BD * BD + j))) return rc;
+        }
+    }
+    beb_rescale_kernel<<<(npatt + 255) / 256, 256, 0, st>>>(B.lnfw, B.F, B.mrow, npatt, (int)npad,
+                                                            h->nscale == 0);
+    beb_grid_kernel<<<BNG, 256, 0, st>>>(B.F, h->d_fpatt, B.pcl, npatt, (int)npad, B.lnfXs);
+    kernels += 2;
+    CK(cudaGetLastError());
+    std::vector<double> mrow(npatt), lnfXs(BNG);
+    CK(cudaMemcpyAsync(mrow.data(), B.mrow, sizeof(double) * npatt, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(lnfXs.data(), B.lnfXs, sizeof(double) * BNG, cudaMemcpyDeviceToHost, st));
+    if (lnfw_out)
+        CK(cudaMemcpy2DAsync(lnfw_out, sizeof(double) * npatt, B.lnfw, sizeof(double) * npad,
+                             sizeof(double) * npatt, BNW, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // S1, then the marginal over the grid with codeml's running scale S2
+    // (lfunNSsites_ACD codeml.c:6700-6747): a new largest term rescales the sum
+    double S1 = 0;
+    for (int hh = 0; hh < npatt; hh++) S1 += mrow[hh] * h->fpatt[hh];
+    double pp[4][BD], pq[BNT];
+    std::memset(pp, 0, sizeof pp);
+    std::memset(pq, 0, sizeof pq);
+    double fX = 1, S2 = -1e300;
+    for (int g = 0; g < BNG; g++) {
+        int ip[4];
+        for (int j = 3, it = g; j >= 0; j--) { ip[j] = it % BD; it /= BD; }
+        double t = lnfXs[g] - S2;
+        if (t > 10) {
+            t = t < 200 ? std::exp(-t) : 0;
+            fX = fX * t + 1;
+            for (int j = 0; j < 4; j++)
+                for (int k = 0; k < BD; k++) pp[j][k] *= t;
+            for (int k = 0; k < BNT; k++) pq[k] *= t;
+            for (int j = 0; j < 4; j++) pp[j][ip[j]] += 1;
+            pq[ip[0] * BD + ip[1]] += 1;
+            S2 = lnfXs[g];
+        } else if (t > -200) {
+            t = std::exp(t);
+            fX += t;
+            for (int j = 0; j < 4; j++) pp[j][ip[j]] += t;
+            pq[ip[0] * BD + ip[1]] += t;
+        }
+    }
+    const double lfX = std::log(fX) + S2;
+    if (lnfX_out) {
+        lnfX_out[0] = lfX + S1 - 4 * std::log((double)BD);
+        lnfX_out[1] = S1;
+        lnfX_out[2] = S2;
+    }
+    if (grid_out)
+        for (int j = 0; j < 4; j++)
+            for (int k = 0; k < BD; k++) grid_out[j * BD + k] = j < 2 ? -1.0 : pp[j][k] / fX;
+    if (p0p1_out)
+        for (int k = 0; k < BNT; k++) p0p1_out[k] = pq[k] / fX;
+    if (post_out) {
+        std::vector<double2> wt(BNG);
+        for (int g = 0; g < BNG; g++) {
+            const double lw = lnfXs[g] - lfX;
+            wt[g] = make_double2(std::exp(lw), std::exp(-300 - lw));
+        }
+        CK(cudaMemcpyAsync(B.wt, wt.data(), sizeof(double2) * BNG, cudaMemcpyHostToDevice, st));
+        beb_post_kernel<<<(npatt + 7) / 8, 256, 0, st>>>(B.F, B.pcl, B.wt, npatt, (int)npad, B.post);
+        kernels++;
+        CK(cudaGetLastError());
+        CK(cudaMemcpy2DAsync(post_out, sizeof(double) * npatt, B.post, sizeof(double) * npad,
+                             sizeof(double) * npatt, 4, cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaEventRecord(h->ev1, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    if (stats) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+        stats->ms_device = ms;
+        stats->ms_host = now_ms() - t0;
+        stats->kernels = kernels;
+        stats->nscale = h->nscale;
+        stats->h2d_bytes = sizeof(double) * (eig.size() + pcl.size() + h->nnode) + sizeof(DevParams) +
+                           (post_out ? sizeof(double2) * BNG : 0);
+        stats->d2h_bytes = sizeof(double) * (npatt + BNG + (lnfw_out ? (size_t)BNW * npatt : 0) +
+                                             (post_out ? 4 * npatt : 0));
+    }
+    return GB_OK;
+}

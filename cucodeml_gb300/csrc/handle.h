@@ -107,6 +107,12 @@ struct gb_handle {
     // CUDA graphs of the forward evaluation (without / with E messages kept)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_kernels = 0;
+    // BEB: the forward restricted to the class-2a/2b items (the foreground
+    // branch's path to the root), by level
+    gb::Item *d_items_fg = nullptr;
+    std::vector<int> fg_off;
+    cudaGraphExec_t graph_fg = nullptr;
+    int graph_fg_kernels = 0;
 
     gb::AdjointState *adj = nullptr;
     gb::FastState *fast = nullptr;

@@ -36,6 +36,10 @@
  *   gb_patterns              PatternWeight + EncodeSeqs (treesub.c:1075-1143,
  *                            1302-1439) and F3x4 codon frequencies
  *                            (codeml.c:3475-3570, 3732-3742) for clean codon data.
+ *   gb_beb                   the Bayes empirical Bayes site analysis of model A,
+ *                            lfunNSsites_ACD (codeml.c:6617-6826): 121 full
+ *                            prunings over an omega grid and the integration
+ *                            over a 10^4-point parameter grid, on the device.
  *
  * The five symbols codeml.c itself calls (CUDA_Init, CUDA_lfundG, CUDA_fx_r,
  * CUDA_ScheduleConditionalPNode, CUDA_FreeAll; codeml.h:67-85) are provided
@@ -158,6 +162,37 @@ int gb_eval_uvr(gb_handle *h, const double *const U[3], const double *const V[3]
  */
 int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad,
             double *fhK, double *lnf, gb_stats *stats);
+
+/*
+ * Bayes empirical Bayes (BEB) analysis of branch-site model A at prm
+ * (normally the MLE), as codeml's lfunNSsites_ACD (codeml.c:6617-6826, with
+ * get_grid_para_like_ACD 6419-6530, get_pclassM_iw_ACD 6532-6615 and the BEB
+ * branch of GetPMatBranch treesub.c:7289-7301) computes it after the
+ * optimisation.  kappa, the branch lengths and the branch Qfactors stay at
+ * prm; omega runs over a grid of GB_BEB_GRID values of w0 in (0, 1) and of w2
+ * in (1, 11), and (p0, p1) over GB_BEB_GRID^2 triangles of the ternary plot.
+ * f(x_h | w) is computed for the GB_BEB_OMEGA_SETS omega sets
+ *   [0, 10)        background = foreground = w0_i        (class 0)
+ *   10             background = foreground = 1           (class 1)
+ *   11 + 10 i + j  background w0_i, foreground w2_j      (class 2a)
+ *   111 + j        background 1, foreground w2_j         (class 2b)
+ * by full FP64 prunings on the device (sets sharing a background omega
+ * recompute only the foreground branch's path to the root); the grid
+ * integration runs on the device too.
+ * Outputs (each may be NULL):
+ *   lnfw[121*npatt]  log f(x_h | omega set) (log f + scale logs)
+ *   post[4*npatt]    posterior of site classes 0, 1, 2a, 2b per pattern
+ *                    (codeml's rst "BEB probabilities"; P(w>1) = 2a + 2b)
+ *   grid[4*10]       posterior of the grid values of p0, p1 (rows of -1, as
+ *                    codeml prints them), w0 and w2 ("Posterior on the grid")
+ *   p0p1[100]        posterior over the (p0, p1) triangles
+ *   lnfX[3]          log f(X) as codeml prints it, and its scale terms S1, S2
+ * Needs a GB_PREC_FP64 handle (GB_ERR_STATE otherwise).
+ */
+#define GB_BEB_GRID        10
+#define GB_BEB_OMEGA_SETS  121
+int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw, double *post, double *grid,
+           double *p0p1, double *lnfX, gb_stats *stats);
 
 /*
  * ming2-compatible gradient hook over codeml's parameter vector

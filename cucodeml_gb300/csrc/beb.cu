@@ -11,10 +11,12 @@
 //    classes 2a and 2b re-prune only the foreground branch's path to the root
 //    from class 0 / class 1 subtrees.  So with the three eigen slots set to
 //    (w0_i, 1, w2_j) one launch yields sets i, 10, 11 + 10 i + j and 111 + j,
-//    and for j > 0 only the path items (classes 2a, 2b) need running again:
-//    10 full forwards and 90 path-only forwards, each a replayed CUDA graph;
-//    the eigen solutions of the 21 omega values are uploaded once and copied
-//    into the parameter block on the device between launches.
+//    and each later (i, j) runs only the items of the classes whose set is
+//    new: one forward of all four classes, 9 full class-0 trees (with their
+//    class-2a paths), 9 paths of classes 2a + 2b and 81 class-2a paths, each
+//    a replayed CUDA graph; the eigen solutions of the 21 omega values are
+//    uploaded once and copied into the parameter block on the device between
+//    launches.
 // 2. Per pattern, the 121 log values are rescaled by their maximum (the S1
 //    term), the 10^4-point grid integral log f(X) (get_pclassM_iw_ACD
 //    6532-6615, then 6700-6756) and the site-class posteriors (6758-6775).
@@ -168,39 +170,43 @@ struct BebBuffers {
     }
 };
 
-// CUDA graph of the forward restricted to the class-2a/2b items: P(t) of every
-// (branch, omega) pair, then the path items level by level
-int ensure_fg_graph(gb_handle *h) {
-    if (h->graph_fg) return 0;
-    std::vector<Item> fg;
-    h->fg_off.assign(h->level_off.size(), 0);
+// CUDA graph of the forward restricted to the items of the classes in mask
+// (bit c: class c): P(t) of every (branch, omega) pair, then those items level
+// by level.  Items read their children's slots of the class they depend on
+// (classes 2a / 2b read clean subtrees from classes 0 / 1), so a mask runs
+// correctly when the classes it leaves out are already in place.
+int ensure_cls_graph(gb_handle *h, int mask) {
+    if (h->graph_cls[mask]) return 0;
+    std::vector<Item> sel;
+    std::vector<int> &off = h->cls_off[mask];
+    off.assign(h->level_off.size(), 0);
     for (size_t L = 0; L + 1 < h->level_off.size(); L++) {
-        h->fg_off[L] = (int)fg.size();
+        off[L] = (int)sel.size();
         for (int i = h->level_off[L]; i < h->level_off[L + 1]; i++)
-            if (h->items[i].cls >= 2) fg.push_back(h->items[i]);
+            if ((mask >> h->items[i].cls) & 1) sel.push_back(h->items[i]);
     }
-    h->fg_off.back() = (int)fg.size();
-    int rc = dalloc(&h->d_items_fg, fg.size());
+    off.back() = (int)sel.size();
+    int rc = dalloc(&h->d_items_cls[mask], sel.size());
     if (rc) return rc;
-    CK(cudaMemcpy(h->d_items_fg, fg.data(), sizeof(Item) * fg.size(), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(h->d_items_cls[mask], sel.data(), sizeof(Item) * sel.size(), cudaMemcpyHostToDevice));
     cudaGraph_t g;
     CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     int nk = 1;
     launch_pmat_fp64(h->d_pairs, (int)h->pairs.size(), h->d_label, h->d_tnode, h->d_prm, h->d_Pt, h->stream,
                      h->d_pi);
-    for (size_t L = 0; L + 1 < h->fg_off.size(); L++) {
-        const int n = h->fg_off[L + 1] - h->fg_off[L];
+    for (size_t L = 0; L + 1 < off.size(); L++) {
+        const int n = off[L + 1] - off[L];
         if (n == 0) continue;
-        launch_prune_fp64(h->d_items_fg + h->fg_off[L], n, h->ntile, h->npad, h->d_z, h->d_Pt, h->d_conP,
+        launch_prune_fp64(h->d_items_cls[mask] + off[L], n, h->ntile, h->npad, h->d_z, h->d_Pt, h->d_conP,
                           nullptr, h->d_scaleF, h->d_scale_list, h->nscale, h->d_pi, h->d_fbar, h->d_ssum,
                           h->d_fhK, h->stream);
         nk++;
     }
     CK(cudaStreamEndCapture(h->stream, &g));
-    cudaError_t e = cudaGraphInstantiate(&h->graph_fg, g, 0);
+    cudaError_t e = cudaGraphInstantiate(&h->graph_cls[mask], g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(GB_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
-    h->graph_fg_kernels = nk;
+    h->graph_cls_kernels[mask] = nk;
     return 0;
 }
 
@@ -258,7 +264,11 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw_out, double *post_ou
     D.sym = 1;
     if ((rc = stage_params(h, &D, prm->blength))) return rc;
     if ((rc = fp64_prepare(h, false))) return rc;
-    if ((rc = ensure_fg_graph(h))) return rc;
+    // class masks: 2a + 2b on the path; 0 + 2a for a new w0 (class 1 and
+    // class 2b do not depend on w0); 2a alone for a new w2 under the same w0
+    constexpr int M_PATH = 0xC, M_W0 = 0x5, M_2A = 0x4;
+    for (int mask : {M_PATH, M_W0, M_2A})
+        if ((rc = ensure_cls_graph(h, mask))) return rc;
     const size_t npad = h->npad;
     const int npatt = h->npatt;
     BebBuffers B;
@@ -292,20 +302,24 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw_out, double *post_ou
                            cudaMemcpyDeviceToDevice, st));
         return 0;
     };
+    // (w0_0, 1, w2_0): every class; then per (i, j) only the classes whose
+    // omega set is new: sets i (class 0), 10 (class 1, once), 11 + 10 i + j
+    // (class 2a) and 111 + j (class 2b, under w0_0 only)
     int kernels = 0;
     for (int i = 0; i < BD; i++) {
         if ((rc = set_slot(0, i))) return rc;
         for (int j = 0; j < BD; j++) {
             if ((rc = set_slot(2, BD + 1 + j))) return rc;
-            if (j == 0) {
+            const int mask = j == 0 ? (i == 0 ? 0xF : M_W0) : (i == 0 ? M_PATH : M_2A);
+            if (mask == 0xF) {
                 CK(cudaGraphLaunch(h->graph[0], st));
                 kernels += h->graph_kernels;
-                if ((rc = keep(0, i))) return rc;
-                if (i == 0 && (rc = keep(1, BD))) return rc;
             } else {
-                CK(cudaGraphLaunch(h->graph_fg, st));
-                kernels += h->graph_fg_kernels;
+                CK(cudaGraphLaunch(h->graph_cls[mask], st));
+                kernels += h->graph_cls_kernels[mask];
             }
+            if (j == 0 && (rc = keep(0, i))) return rc;
+            if (i == 0 && j == 0 && (rc = keep(1, BD))) return rc;
             if ((rc = keep(2, BD + 1 + i * BD + j))) return rc;
             if (i == 0 && (rc = keep(3, BD + 1 + BD * BD + j))) return rc;
         }

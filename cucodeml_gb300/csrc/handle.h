@@ -107,12 +107,12 @@ struct gb_handle {
     // CUDA graphs of the forward evaluation (without / with E messages kept)
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int graph_kernels = 0;
-    // BEB: the forward restricted to the class-2a/2b items (the foreground
-    // branch's path to the root), by level
-    gb::Item *d_items_fg = nullptr;
-    std::vector<int> fg_off;
-    cudaGraphExec_t graph_fg = nullptr;
-    int graph_fg_kernels = 0;
+    // BEB: forwards restricted to the items of some site classes (bit c of
+    // the mask selects class c), each P(t) then those items level by level
+    gb::Item *d_items_cls[16] = {};
+    std::vector<int> cls_off[16];
+    cudaGraphExec_t graph_cls[16] = {};
+    int graph_cls_kernels[16] = {};
 
     gb::AdjointState *adj = nullptr;
     gb::FastState *fast = nullptr;

@@ -181,8 +181,11 @@ void free_all(gb_handle *h) {
     if (h->device >= 0) cudaSetDevice(h->device);
     for (auto &g : h->graph)
         if (g) cudaGraphExecDestroy(g);
-    if (h->graph_fg) cudaGraphExecDestroy(h->graph_fg);
-    void *dev[] = {h->d_items_fg, h->d_items, h->d_pairs, h->d_label, h->d_scale_list, h->d_z, h->d_fpatt, h->d_pi,
+    for (int m = 0; m < 16; m++) {
+        if (h->graph_cls[m]) cudaGraphExecDestroy(h->graph_cls[m]);
+        if (h->d_items_cls[m]) cudaFree(h->d_items_cls[m]);
+    }
+    void *dev[] = {h->d_items, h->d_pairs, h->d_label, h->d_scale_list, h->d_z, h->d_fpatt, h->d_pi,
                    h->d_tnode, h->d_prm, h->d_Pt, h->d_conP, h->d_E, h->d_scaleF, h->d_fbar,
                    h->d_ssum, h->d_fhK, h->d_lnf, h->d_post, h->d_partial, h->d_out, h->d_ticket};
     for (void *p : dev)

@@ -30,28 +30,25 @@ static void gb_die(const char *what, int rc) {
     exit(-1);
 }
 
-void CUDA_Init(double *x) {
+/* a library handle (FP64) for codeml's current tree and data */
+static gb_handle *make_handle(const char *who) {
     int i, j, rc;
     unsigned char *z;
     int *father, *label;
     char *scale = NULL;
     gb_problem p;
-    (void)x;
-    if (com.ngene != 1) gb_die("CUDA_Init (one gene only)", GB_ERR_ARG);
-    if (!com.cleandata) gb_die("CUDA_Init (cleandata = 1 only)", GB_ERR_ARG);
-    if (com.ncode != GB_NCODE) gb_die("CUDA_Init (universal code only)", GB_ERR_ARG);
+    gb_handle *h = NULL;
+    if (com.ngene != 1) gb_die(who, GB_ERR_ARG);
+    if (!com.cleandata) gb_die(who, GB_ERR_ARG);
+    if (com.ncode != GB_NCODE) gb_die(who, GB_ERR_ARG);
     z = (unsigned char *)malloc((size_t)com.ns * com.npatt);
     father = (int *)malloc(sizeof(int) * tree.nnode);
     label = (int *)malloc(sizeof(int) * tree.nnode);
-    g_blen = (double *)malloc(sizeof(double) * tree.nnode);
-    g_bnode = (int *)malloc(sizeof(int) * tree.nnode);
-    g_fhK = (double *)malloc(sizeof(double) * 4 * com.npatt);
-    if (!z || !father || !label || !g_blen || !g_bnode || !g_fhK) gb_die("CUDA_Init (host memory)", GB_ERR_OOM);
+    if (!z || !father || !label) gb_die(who, GB_ERR_OOM);
     for (j = 0; j < com.ns; j++) memcpy(z + (size_t)j * com.npatt, com.z[j], com.npatt);
     for (i = 0; i < tree.nnode; i++) {
         father[i] = nodes[i].father;
         label[i] = (i == tree.root) ? 0 : (int)nodes[i].label;
-        if (i != tree.root) g_bnode[nodes[i].ibranch] = i;
     }
     if (com.NnodeScale) scale = com.nodeScale;
     p.ns = com.ns;
@@ -70,12 +67,25 @@ void CUDA_Init(double *x) {
         scale = (char *)calloc(tree.nnode, 1);
         p.node_scale = scale;
     }
-    rc = gb_create(&p, &g_h);
+    rc = gb_create(&p, &h);
     if (scale && scale != com.nodeScale) free(scale);
     free(z);
     free(father);
     free(label);
     if (rc) gb_die("gb_create", rc);
+    return h;
+}
+
+void CUDA_Init(double *x) {
+    int i;
+    (void)x;
+    g_blen = (double *)malloc(sizeof(double) * tree.nnode);
+    g_bnode = (int *)malloc(sizeof(int) * tree.nnode);
+    g_fhK = (double *)malloc(sizeof(double) * 4 * com.npatt);
+    if (!g_blen || !g_bnode || !g_fhK) gb_die("CUDA_Init (host memory)", GB_ERR_OOM);
+    for (i = 0; i < tree.nnode; i++)
+        if (i != tree.root) g_bnode[nodes[i].ibranch] = i;
+    g_h = make_handle("CUDA_Init (one gene, cleandata = 1, universal code only)");
 }
 
 void CUDA_ScheduleConditionalPNode(int ir, int ig, double *x) {
@@ -105,5 +115,29 @@ void CUDA_FreeAll(void) {
 int GB_dfun(double x[], double *f, double dx[], int n) {
     int rc = gb_dfun_x(g_h, g_bnode, LASTROUND, x, n, f, dx);
     if (rc) gb_die("gb_dfun_x", rc);
+    return 0;
+}
+
+int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], double lnfX[]) {
+    int i, rc;
+    gb_params p;
+    gb_handle *h;
+    double *bl;
+    if (np != com.ntime + 5) gb_die("GB_BEB (model A parameter vector)", GB_ERR_ARG);
+    bl = (double *)calloc(tree.nnode, sizeof(double));
+    if (!bl) gb_die("GB_BEB (host memory)", GB_ERR_OOM);
+    for (i = 0; i < tree.nnode; i++)
+        if (i != tree.root) bl[i] = x[nodes[i].ibranch];
+    p.blength = bl;
+    p.kappa = x[com.ntime];
+    p.p0 = x[com.ntime + 1];
+    p.p1 = x[com.ntime + 2];
+    p.omega0 = x[com.ntime + 3];
+    p.omega2 = x[com.ntime + 4];
+    h = make_handle("GB_BEB (one gene, cleandata = 1, universal code only)");
+    rc = gb_beb(h, &p, NULL, postSite, grid, p0p1, lnfX, NULL);
+    gb_destroy(h);
+    free(bl);
+    if (rc) gb_die("gb_beb", rc);
     return 0;
 }

@@ -18,6 +18,16 @@
  *                                  (tools.c:6361-6363, `dfun`), the analytic
  *                                  gradient of -lnL in codeml's x space; pass it
  *                                  instead of NULL at codeml.c:688.
+ *   GB_BEB                         new: the Bayes empirical Bayes analysis of
+ *                                  model A on the GPU at codeml's final x
+ *                                  (natural p0, p1 after Forestry's
+ *                                  back-transform, codeml.c:713-729): fills
+ *                                  lfunNSsites_ACD's postSite[4*npatt], the w0
+ *                                  and w2 rows of its postpara (grid[20..39]),
+ *                                  postp0p1[100] and log f(X), S1, S2
+ *                                  (lnfX[3]); replaces codeml.c:6697-6775 for
+ *                                  model A.  Makes its own handle, since
+ *                                  CUDA_FreeAll has run by then.
  *
  * CUDA_lfundG and CUDA_fx_r stay codeml's own (treesub.c:7397, 7554).  On any
  * library error these functions print the library's message and exit(-1), as
@@ -35,6 +45,7 @@ void CUDA_Init(double *x);
 void CUDA_ScheduleConditionalPNode(int ir, int ig, double *x);
 void CUDA_FreeAll(void);
 int GB_dfun(double x[], double *f, double dx[], int n);
+int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], double lnfX[]);
 
 #ifdef __cplusplus
 }

@@ -259,6 +259,32 @@ def beb_leg(args, dev, tree, z, fpatt, pi, bl0):
     return out
 
 
+def se_leg(args, dev, tree, z, fpatt, pi, cpu_lnL_s=None):
+    """codeml's standard errors (getSE = 1: 2 np likelihood evaluations and
+    the outer-product Hessian, gb_se_opg, FP64) at the bench parameters; the
+    CPU figure is 2 np oracle lnL evaluations at the CPU leg's measured time."""
+    from cucodeml_gb300 import api
+    lk = api.Likelihood(tree, z, fpatt, pi, precision="fp64", device=dev)
+    x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
+                                                  PARAMS["omega0"], PARAMS["omega2"]]])
+    r = lk.se_opg(x)
+    t0 = time.perf_counter()
+    r = lk.se_opg(x)
+    e2e = time.perf_counter() - t0
+    lk.close()
+    n = len(x)
+    out = {"workload": f"standard errors (codeml getSE = 1), {args.ns} taxa x {args.ncodon} codons: "
+                       f"{2 * n} FP64 lnL evaluations and the {n} x {n} outer-product Hessian",
+           "ms_device": r["ms_device"], "ms_e2e": 1000.0 * e2e, "kernels": r["kernels"],
+           "se_all_positive": bool(np.all(r["se"] > 0))}
+    if cpu_lnL_s:
+        out["cpu_baseline"] = {"value_ms": 1000.0 * 2 * n * cpu_lnL_s, "kind": "port",
+                               "sample": f"2 np = {2 * n} oracle lnL evaluations at the CPU leg's "
+                                         f"{cpu_lnL_s:.3f} s each"}
+        out["e2e_speedup_vs_cpu"] = 2 * n * cpu_lnL_s / e2e
+    return out
+
+
 def cpu_baseline(tree, z, fpatt, pi, threads: int, seconds: float = 12.0, min_evals: int = 2):
     """Time the oracle's lnL on the host cores; lnL+gradient = (np+1) lnL evals."""
     from oracle import oracle as O
@@ -474,6 +500,9 @@ def main():
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         line["cpu_baseline"] = cpu_baseline(tree, z, fpatt, pi, O.max_threads())
+    if not args.no_beb:
+        line["se"] = se_leg(args, dev, tree, z, fpatt, pi,
+                            line.get("cpu_baseline", {}).get("lnL_eval_s"))
     lk.close()
     if rank == 0:
         print(json.dumps(line))

@@ -231,6 +231,32 @@ class Likelihood:
             p0, p1 = e / (1 + e.sum())
         return self.beb(bl, kappa, w0, w2, p0, p1, want_lnfw=want_lnfw)
 
+    def se_opg(self, x, small_diff: float = 1e-6) -> dict:
+        """codeml's standard errors (getSE = 1, HessianSKT2004) at codeml's x
+        with untransformed p0, p1 (gb_se_opg; FP64 handle): g = dlnL/dx,
+        H (codeml's, before negation) and se."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = len(x)
+        g = np.zeros(n)
+        H = np.zeros((n, n))
+        se = np.zeros(n)
+        st = _lib.Stats()
+        _lib.check(self._L.gb_se_opg(self._h, self.bnode.ctypes.data_as(C.POINTER(C.c_int)), _ptr(x), n,
+                                     float(small_diff), _ptr(g), _ptr(H), _ptr(se), C.byref(st)))
+        return {"g": g, "H": H, "se": se, "ms_device": st.ms_device, "ms_host": st.ms_host,
+                "kernels": st.kernels}
+
+    def hessian_x(self, x, lastround: bool = True, rel_step: float = 0.0):
+        """(H, se): the Hessian of -lnL over codeml's x by central differences
+        of the analytic gradient (gb_hessian_x) and the SEs from its inverse."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = len(x)
+        H = np.zeros((n, n))
+        se = np.zeros(n)
+        _lib.check(self._L.gb_hessian_x(self._h, self.bnode.ctypes.data_as(C.POINTER(C.c_int)),
+                                        int(lastround), _ptr(x), n, float(rel_step), _ptr(H), _ptr(se)))
+        return H, se
+
     def dfun_x(self, x, lastround: bool = True):
         """(f, dx) as ming2's dfun hook: f = -lnL, dx = d(-lnL)/dx in codeml's x space."""
         x = np.ascontiguousarray(x, dtype=np.float64)

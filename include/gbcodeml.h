@@ -36,6 +36,10 @@
  *   gb_patterns              PatternWeight + EncodeSeqs (treesub.c:1075-1143,
  *                            1302-1439) and F3x4 codon frequencies
  *                            (codeml.c:3475-3570, 3732-3742) for clean codon data.
+ *   gb_se_opg / gb_hessian_x standard errors: codeml's getSE = 1 Hessian
+ *                            approximation HessianSKT2004 (treesub.c:6979-7048)
+ *                            with its 2 np evaluations on the device; and the
+ *                            Hessian from differences of the analytic gradient.
  *   gb_beb                   the Bayes empirical Bayes site analysis of model A,
  *                            lfunNSsites_ACD (codeml.c:6617-6826): 121 full
  *                            prunings over an omega grid and the integration
@@ -193,6 +197,35 @@ int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad,
 #define GB_BEB_OMEGA_SETS  121
 int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw, double *post, double *grid,
            double *p0p1, double *lnfX, gb_stats *stats);
+
+/*
+ * Standard errors as codeml computes them with getSE = 1 (codeml.c:754-783):
+ * the Hessian approximation of HessianSKT2004 (treesub.c:6979-7048),
+ *   H = -sum_h fpatt_h s_h s_h^T,  s_h,i = (log f_h(x + e_i eh_i)
+ *       - log f_h(x - e_i eh_i)) / (2 eh_i),  eh_i = 2 small_diff (|x_i| + 1),
+ * and SE_i = sqrt([(-H)^-1]_ii), -1 where that is not positive.
+ *   x[n]: codeml's parameter vector as Forestry leaves it after the fit
+ *         (codeml.c:713-729): branch lengths by branch index (bnode[ib] is the
+ *         node of branch ib), kappa, p0, p1, w0, w2 (p0, p1 untransformed);
+ *         n = nnode - 1 + 5.  small_diff: codeml's Small_Diff.
+ * Outputs (each may be NULL): g[n] = dlnL/dx from the same 2n evaluations,
+ * H[n*n] (before codeml negates it), se[n].  The 2n FP64 evaluations run on
+ * the device back to back.  Needs a GB_PREC_FP64 handle.  Returns
+ * GB_ERR_PARAM (se all -1) when -H is singular.
+ */
+int gb_se_opg(gb_handle *h, const int *bnode, const double *x, int n, double small_diff, double *g,
+              double *H, double *se, gb_stats *stats);
+
+/*
+ * The Hessian of -lnL over codeml's x (the layout and p0/p1 convention of
+ * gb_dfun_x) by central differences of the analytic gradient, step
+ * rel_step (|x_i| + 1) (rel_step <= 0: 1e-5), symmetrised: 2n gradient
+ * evaluations in place of the 2n^2 likelihood evaluations of codeml's
+ * Hessian (tools.c:5774-5810).  se (may be NULL): sqrt of the diagonal of
+ * H^-1 (-1 where not positive).  Any precision.
+ */
+int gb_hessian_x(gb_handle *h, const int *bnode, int lastround, const double *x, int n, double rel_step,
+                 double *H, double *se);
 
 /*
  * ming2-compatible gradient hook over codeml's parameter vector

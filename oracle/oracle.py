@@ -161,6 +161,35 @@ class Problem:
                 "lnfX": fx[0], "S1": fx[1], "S2": fx[2]}
 
 
+    def opg_se(self, x, small_diff: float = 1e-6):
+        """codeml's standard errors (getSE = 1): HessianSKT2004
+        (treesub.c:6979-7048) -- per-pattern scores by central differences of
+        log f_h with step 2 small_diff (|x_i| + 1) at untransformed p0, p1,
+        H = -sum_h fpatt_h d_h d_h^T, g from the same lnL differences -- then
+        SE_i = sqrt([(-H)^-1]_ii), -1 where that is not positive
+        (codeml.c:754-783).  Returns (g, H, se)."""
+        x = np.asarray(x, dtype=np.float64)
+        n = len(x)
+        eh = 2 * small_diff * (np.abs(x) + 1)
+        lnL = np.zeros((2, n))
+        lnf = np.zeros((2, n, self.npatt))
+        for bf in range(2):
+            for i in range(n):
+                x1 = x.copy()
+                x1[i] = x[i] - eh[i] if bf == 0 else x[i] + eh[i]
+                v, _, f, _ = self.neg_lnL(x1, lastround=True, want_fhK=True)
+                lnL[bf, i] = -v
+                lnf[bf, i] = f
+        g = (lnL[1] - lnL[0]) / (eh * 2)
+        d = (lnf[1] - lnf[0]) / (eh * 2)[:, None]
+        H = -(d * self.fpatt[None, :]) @ d.T
+        H = 0.5 * (H + H.T)           # the matrix product is symmetric only up to its summation order
+        V = np.linalg.inv(-H)
+        dg = np.diag(V)
+        se = np.where(dg > 0, np.sqrt(np.abs(dg)), -1.0)
+        return g, H, se
+
+
 def build_q(pi, kappa, omega):
     Q = np.zeros((61, 61))
     pi = np.ascontiguousarray(pi, dtype=np.float64)

@@ -22,6 +22,13 @@ the fixture also keeps its per-site posteriors of the four site classes (rst,
 file, 3 dp) and the printed log f(X) with its scale terms S1, S2 (stdout, 6
 dp).
 
+A second run of the same case with getSE = 1 gives codeml's standard errors
+("SEs for parameters", out file, 6 dp): HessianSKT2004 (treesub.c:6979-7048)
+approximates the Hessian by the outer products of per-pattern score vectors
+from central differences of log f_h (step 2 Small_Diff (|x_i| + 1)), and the
+SEs are the square roots of the diagonal of its negated inverse
+(codeml.c:754-783).
+
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -105,7 +112,13 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, zero_br
         out = open(os.path.join(d, "out.txt")).read()
         lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
         rst = open(os.path.join(d, "rst")).read()
+        with open(os.path.join(d, "codeml.ctl"), "w") as f:
+            f.write(CTL.replace("getSE = 0", "getSE = 1"))
+        subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
+        out_se = open(os.path.join(d, "out.txt")).read()
     beb = parse_beb(out, rst, r.stdout)
+    k = out_se.index("SEs for parameters:")
+    se = [float(v) for v in out_se[k:].splitlines()[1].split()]
     m = re.search(r"lnL\(ntime:\s*(\d+)\s+np:\s*(\d+)\):\s*(-?\d+\.\d+)", out)
     lnL = float(m.group(3))
     i0 = out.index("Codon frequencies under model")
@@ -128,7 +141,7 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, zero_br
         "x": [float(v) for v in x], "lastround": 1,
         "codeml_lnL": lnL, "codeml_np": int(m.group(2)),
         "lnf": lnf, "fpatt": fp, "patterns": [" ".join(p) for p in pats], "pi_8dp": pi8,
-        "beb": beb,
+        "beb": beb, "se_6dp": se, "small_diff": 1e-6,
     }
 
 

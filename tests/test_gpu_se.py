@@ -7,8 +7,11 @@ oracle's restatement, H within 1e-7 of its largest entry, g within
 a Hessian condition number of 3.5e12 (measured on the CPU with the library's
 eigen solutions); against codeml's printed SEs, print rounding plus 1e-4 of
 the value.  gb_hessian_x (differences of the analytic gradient) against the
-oracle's second differences of lnL (step 1e-4 (|x| + 1)), within 1e-4 of the
-largest entry.
+oracle's second differences of lnL, Richardson-extrapolated from steps
+1e-4 (|x| + 1) and twice that, within 1e-4 of the largest entry.  (Plain
+second differences at 1e-4 are off by 8e-4 of the largest entry, the
+diagonal of a 0.003-long branch; the extrapolation and plain differences at
+1e-5 agree to 1.2e-5.)
 """
 import numpy as np
 import pytest
@@ -37,7 +40,7 @@ def test_se_opg_matches_oracle_and_codeml(name):
     lk.close()
 
 
-def oracle_hessian(pb, x, rel=1e-4):
+def second_differences(pb, x, rel):
     n = len(x)
     h = rel * (np.abs(x) + 1)
     f = lambda v: pb.neg_lnL(v, True)
@@ -55,6 +58,10 @@ def oracle_hessian(pb, x, rel=1e-4):
             else:
                 H[i, j] = H[j, i] = (at(1, 1) + at(-1, -1) - at(1, -1) - at(-1, 1)) / (4 * h[i] * h[j])
     return H
+
+
+def oracle_hessian(pb, x, rel=1e-4):
+    return (4 * second_differences(pb, x, rel) - second_differences(pb, x, 2 * rel)) / 3
 
 
 def test_hessian_from_adjoint_matches_second_differences():

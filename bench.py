@@ -220,6 +220,15 @@ def batched_leg(args, dev):
     return out
 
 
+def secondary_leg(fn, *a):
+    """A leg beside the headline (BEB, standard errors): its failure is
+    reported in its own object and does not take the headline line down."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001 -- reported, not swallowed
+        return {"error": f"{type(e).__name__}: {e}"}
+
+
 def beb_leg(args, dev, tree, z, fpatt, pi, bl0):
     """Bayes empirical Bayes site analysis of model A (gb_beb, FP64) on the
     bench alignment at the bench parameters: device and end-to-end time of one
@@ -496,13 +505,13 @@ def main():
     if args.batch > 0:
         line["batched"] = batched_leg(args, dev)
     if not args.no_beb:
-        line["beb"] = beb_leg(args, dev, tree, z, fpatt, pi, bl0)
+        line["beb"] = secondary_leg(beb_leg, args, dev, tree, z, fpatt, pi, bl0)
     if rank == 0 and not args.no_cpu:
         from oracle import oracle as O
         line["cpu_baseline"] = cpu_baseline(tree, z, fpatt, pi, O.max_threads())
     if not args.no_beb:
-        line["se"] = se_leg(args, dev, tree, z, fpatt, pi,
-                            line.get("cpu_baseline", {}).get("lnL_eval_s"))
+        line["se"] = secondary_leg(se_leg, args, dev, tree, z, fpatt, pi,
+                                   line.get("cpu_baseline", {}).get("lnL_eval_s"))
     lk.close()
     if rank == 0:
         print(json.dumps(line))

@@ -19,6 +19,7 @@
 extern double *_UU[NBTYPE + 2], *_VV[NBTYPE + 2], *_Root[NBTYPE + 2];
 extern double Qfactor_NS_branch[NBTYPE];
 extern int LASTROUND;
+extern double Small_Diff;
 
 static gb_handle *g_h = NULL;
 static double *g_fhK = NULL;      /* [4*npatt] all classes of the current evaluation */
@@ -139,5 +140,24 @@ int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], 
     gb_destroy(h);
     free(bl);
     if (rc) gb_die("gb_beb", rc);
+    return 0;
+}
+
+int GB_HessianSKT2004(double xmle[], double lnLm, double g[], double H[]) {
+    int ib, rc;
+    int *bnode;
+    gb_handle *h;
+    const int n = com.np;
+    (void)lnLm;
+    if (n != com.ntime + 5) gb_die("GB_HessianSKT2004 (model A parameter vector)", GB_ERR_ARG);
+    bnode = (int *)malloc(sizeof(int) * tree.nnode);
+    if (!bnode) gb_die("GB_HessianSKT2004 (host memory)", GB_ERR_OOM);
+    for (ib = 0; ib < tree.nnode; ib++)
+        if (ib != tree.root) bnode[nodes[ib].ibranch] = ib;
+    h = make_handle("GB_HessianSKT2004 (one gene, cleandata = 1, universal code only)");
+    rc = gb_se_opg(h, bnode, xmle, n, Small_Diff, g, H, NULL, NULL);
+    gb_destroy(h);
+    free(bnode);
+    if (rc) gb_die("gb_se_opg", rc);
     return 0;
 }

@@ -28,6 +28,12 @@
  *                                  (lnfX[3]); replaces codeml.c:6697-6775 for
  *                                  model A.  Makes its own handle, since
  *                                  CUDA_FreeAll has run by then.
+ *   GB_HessianSKT2004              new: HessianSKT2004 (treesub.c:6979-7048)
+ *                                  with the same arguments and results (g and
+ *                                  H at codeml's x, H before codeml negates
+ *                                  it), its 2 np likelihood evaluations on the
+ *                                  GPU; call it in place of HessianSKT2004 at
+ *                                  codeml.c:764 for getSE = 1.
  *
  * CUDA_lfundG and CUDA_fx_r stay codeml's own (treesub.c:7397, 7554).  On any
  * library error these functions print the library's message and exit(-1), as
@@ -46,6 +52,7 @@ void CUDA_ScheduleConditionalPNode(int ir, int ig, double *x);
 void CUDA_FreeAll(void);
 int GB_dfun(double x[], double *f, double dx[], int n);
 int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], double lnfX[]);
+int GB_HessianSKT2004(double xmle[], double lnLm, double g[], double H[]);
 
 #ifdef __cplusplus
 }

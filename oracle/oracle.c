@@ -258,6 +258,7 @@ typedef struct {
     const double *fpatt;      /* [npatt] */
     const double *pi;         /* [61] */
     int nthreads;             /* <=0: all available */
+    int model_b;              /* branch-site model B (NSsites = 3): w1 free, x = [..., w0, w1, w2] */
 } oracle_problem;
 
 typedef struct {
@@ -266,8 +267,12 @@ typedef struct {
     double kappa, w[3];
 } params_t;
 
-/* x = [t_0..t_{nb-1}, kappa, p0', p1', w0, w2]; p' are f_and_x-transformed
-   unless lastround (then p0, p1 directly). */
+/* x = [t_0..t_{nb-1}, kappa, p0', p1', w0, w2] (model B: w0, w1, w2); p'
+   are f_and_x-transformed unless lastround (then p0, p1 directly).  Model B
+   (SetParametersNSsites codeml.c:2427-2436 with NSdiscrete) differs from A
+   only in a free w1 where A fixes it at 1: in the site classes, the
+   background / foreground mean rates behind the Qfactors and the second
+   eigen solution. */
 static int set_params(const oracle_problem *pb, const double *x, int lastround, params_t *P) {
     int nb = pb->nnode - 1, k = nb;
     double Q[NC * NC];
@@ -284,13 +289,13 @@ static int set_params(const oracle_problem *pb, const double *x, int lastround, 
         for (int i = 0; i < 2; i++) f[2] -= (f[i] = x[k++]);
     }
     P->freqK[0] = f[0]; P->freqK[1] = f[1]; P->freqK[2] = f[2];
-    double w0 = x[k++], w2 = x[k++];
-    P->w[0] = w0; P->w[1] = 1; P->w[2] = w2;
+    double w0 = x[k++], w1 = pb->model_b ? x[k++] : 1, w2 = x[k++];
+    P->w[0] = w0; P->w[1] = w1; P->w[2] = w2;
     double t = P->freqK[0] + P->freqK[1];
     if (t < 1e-100) return -1;
     P->freqK[2] = (1 - t) * P->freqK[0] / t;
     P->freqK[3] = (1 - t) * P->freqK[1] / t;
-    double wb[2][3] = {{w0, 1, -1}, {w0, 1, w2}};
+    double wb[2][3] = {{w0, w1, -1}, {w0, w1, w2}};
     for (int i = 0; i < 2; i++) {
         double mr = 0;
         for (int j = 0; j < (i == 0 ? 2 : 3); j++) {

@@ -23,7 +23,7 @@ class _Problem(C.Structure):
         ("nson", C.POINTER(C.c_int)), ("sons", C.POINTER(C.c_int)),
         ("label", C.POINTER(C.c_int)), ("bnode", C.POINTER(C.c_int)),
         ("z", C.POINTER(C.c_ubyte)), ("fpatt", C.POINTER(C.c_double)),
-        ("pi", C.POINTER(C.c_double)), ("nthreads", C.c_int),
+        ("pi", C.POINTER(C.c_double)), ("nthreads", C.c_int), ("model_b", C.c_int),
     ]
 
 
@@ -86,7 +86,8 @@ def patterns(codons: np.ndarray):
 class Problem:
     """A tree + compressed patterns + codon frequencies, held for the C oracle."""
 
-    def __init__(self, tree, z: np.ndarray, fpatt: np.ndarray, pi: np.ndarray, nthreads: int = 0):
+    def __init__(self, tree, z: np.ndarray, fpatt: np.ndarray, pi: np.ndarray, nthreads: int = 0,
+                 model_b: bool = False):
         self.tree = tree
         nn = tree.nnode
         self.nson = np.array([len(tree.sons[i]) for i in range(nn)], dtype=np.int32)
@@ -101,13 +102,13 @@ class Problem:
         self.fpatt = np.ascontiguousarray(fpatt, dtype=np.float64)
         self.pi = np.ascontiguousarray(pi, dtype=np.float64)
         self.npatt = int(self.fpatt.shape[0])
-        self.np = tree.nbranch + 5
+        self.np = tree.nbranch + 5 + int(model_b)
         ip = C.POINTER(C.c_int)
         self._s = _Problem(tree.ns, nn, tree.root, self.npatt,
                            self.nson.ctypes.data_as(ip), self.sons.ctypes.data_as(ip),
                            self.label.ctypes.data_as(ip), self.bnode.ctypes.data_as(ip),
                            self.z.ctypes.data_as(C.POINTER(C.c_ubyte)), _dp(self.fpatt),
-                           _dp(self.pi), int(nthreads))
+                           _dp(self.pi), int(nthreads), int(model_b))
 
     def set_threads(self, n: int) -> None:
         self._s.nthreads = int(n)

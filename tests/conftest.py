@@ -17,8 +17,14 @@ def pytest_configure(config):
 
 
 def golden_names():
-    """Fixed-parameter fixtures (codeml lnL and per-pattern log f at given x)."""
-    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.endswith(".json") and not f.startswith("mle_"))
+    """Fixed-parameter model-A fixtures (codeml lnL and per-pattern log f at given x)."""
+    return sorted(f[:-5] for f in os.listdir(GOLDEN)
+                  if f.endswith(".json") and not f.startswith(("mle_", "mb")))
+
+
+def model_b_names():
+    """Fixed-parameter fixtures under branch-site model B (w1 free)."""
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("mb") and f.endswith(".json"))
 
 
 def mle_names():

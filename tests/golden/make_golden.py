@@ -29,6 +29,9 @@ from central differences of log f_h (step 2 Small_Diff (|x_i| + 1)), and the
 SEs are the square roots of the diagonal of its negated inverse
 (codeml.c:754-783).
 
+The mb_* fixtures are the same evaluation under branch-site model B
+(NSsites = 3, ncatG = 3: w1 free; x ends w0, w1, w2), lnL and log f only.
+
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -91,8 +94,16 @@ CASES = [
     ("c12x150_s6_long", 12, 150, 6, ModelA(), (2.0, 0.5, 0.3, 0.3, 3.0), 6.0),
 ]
 
+# branch-site model B (NSsites = 3, ncatG = 3: w1 free): evaluation params
+# (kappa, p0, p1, w0, w1, w2); lnL, lnf and patterns only
+CASES_B = [
+    ("mb8x300_s7", 8, 300, 7, ModelA(), (2.0, 0.5, 0.3, 0.2, 0.8, 3.0), 1.0),
+    ("mb24x400_s8", 24, 400, 8, ModelA(kappa=2.5, omega0=0.1, omega2=4.0),
+     (2.4, 0.45, 0.35, 0.1, 1.6, 4.0), 1.0),
+]
 
-def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, zero_branch=False):
+
+def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b=False):
     aln = simulate(ns, ncodon, seed=seed, model=model)
     tree = aln.tree
     xb = tree.x_branch_lengths() * bscale
@@ -106,19 +117,23 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, zero_br
             f.write(f"{ns} 1\n{tree.to_newick()}\n")
         with open(os.path.join(d, "in.codeml"), "w") as f:
             f.write("-1 " + " ".join(repr(float(v)) for v in x) + "\n")
+        ctl = CTL.replace("NSsites = 2", "NSsites = 3").replace("ncatG = 4", "ncatG = 3") if model_b else CTL
         with open(os.path.join(d, "codeml.ctl"), "w") as f:
-            f.write(CTL)
+            f.write(ctl)
         r = subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
         out = open(os.path.join(d, "out.txt")).read()
         lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
         rst = open(os.path.join(d, "rst")).read()
-        with open(os.path.join(d, "codeml.ctl"), "w") as f:
-            f.write(CTL.replace("getSE = 0", "getSE = 1"))
-        subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
-        out_se = open(os.path.join(d, "out.txt")).read()
-    beb = parse_beb(out, rst, r.stdout)
-    k = out_se.index("SEs for parameters:")
-    se = [float(v) for v in out_se[k:].splitlines()[1].split()]
+        if not model_b:
+            with open(os.path.join(d, "codeml.ctl"), "w") as f:
+                f.write(CTL.replace("getSE = 0", "getSE = 1"))
+            subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
+            out_se = open(os.path.join(d, "out.txt")).read()
+    extra = {"model": "B"}
+    if not model_b:
+        k = out_se.index("SEs for parameters:")
+        extra = {"beb": parse_beb(out, rst, r.stdout),
+                 "se_6dp": [float(v) for v in out_se[k:].splitlines()[1].split()], "small_diff": 1e-6}
     m = re.search(r"lnL\(ntime:\s*(\d+)\s+np:\s*(\d+)\):\s*(-?\d+\.\d+)", out)
     lnL = float(m.group(3))
     i0 = out.index("Codon frequencies under model")
@@ -141,7 +156,7 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, zero_br
         "x": [float(v) for v in x], "lastround": 1,
         "codeml_lnL": lnL, "codeml_np": int(m.group(2)),
         "lnf": lnf, "fpatt": fp, "patterns": [" ".join(p) for p in pats], "pi_8dp": pi8,
-        "beb": beb, "se_6dp": se, "small_diff": 1e-6,
+        **extra,
     }
 
 
@@ -175,7 +190,7 @@ def main():
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
     codeml = os.path.join(ROOT, "oracle", "_ref", "codeml")
     outdir = os.path.dirname(os.path.abspath(__file__))
-    for case in CASES:
+    for case in CASES + [c + (True,) for c in CASES_B]:
         fx = run_case(codeml, *case)
         with open(os.path.join(outdir, fx["name"] + ".json"), "w") as f:
             json.dump(fx, f, separators=(",", ":"))

@@ -45,6 +45,22 @@ def patterns(codons: np.ndarray):
     return z[: ns * n].reshape(ns, n).copy(), fp[:n].copy(), pi
 
 
+def ng86(z: np.ndarray, fpatt: np.ndarray):
+    """Pairwise Nei-Gojobori (1986) distances (gb_ng86): dict of dS, dN, dN/dS
+    (-1 where not applicable, as codeml prints them) and codeml's distance,
+    each [ns, ns]."""
+    L = _lib.load()
+    z = np.ascontiguousarray(z, dtype=np.uint8)
+    fp = np.ascontiguousarray(fpatt, dtype=np.float64)
+    ns, npatt = z.shape
+    dS = np.zeros((ns, ns)); dN = np.zeros((ns, ns)); dist = np.zeros((ns, ns))
+    _lib.check(L.gb_ng86(ns, npatt, z.ctypes.data_as(C.POINTER(C.c_ubyte)), _ptr(fp), _ptr(dS), _ptr(dN),
+                         _ptr(dist)))
+    w = np.where((dS > 0) & (dN > 0), dN / np.where(dS > 0, dS, 1.0), -1.0)
+    np.fill_diagonal(w, 0.0)
+    return {"dS": dS, "dN": dN, "dN_dS": w, "dist": dist}
+
+
 def model_setup(pi, kappa, omega0, omega2, p0, p1):
     """(U [3,61,61], V [3,61,61], Root [3,61], qf [2], freqK [4]) computed by the library's host code."""
     L = _lib.load()

@@ -36,6 +36,8 @@
  *   gb_patterns              PatternWeight + EncodeSeqs (treesub.c:1075-1143,
  *                            1302-1439) and F3x4 codon frequencies
  *                            (codeml.c:3475-3570, 3732-3742) for clean codon data.
+ *   gb_ng86                  DistanceMatNG86 (treesub.c:2270-2366): pairwise
+ *                            Nei-Gojobori dS, dN from per-codon-pair tables.
  *   gb_se_opg / gb_hessian_x standard errors: codeml's getSE = 1 Hessian
  *                            approximation HessianSKT2004 (treesub.c:6979-7048)
  *                            with its 2 np evaluations on the device; and the
@@ -246,6 +248,19 @@ int gb_dfun_x(gb_handle *h, const int *bnode, int lastround, const double *x, in
  */
 int gb_patterns(int ns, int ncodon, const int *codons, int *npatt, unsigned char *z,
                 double *fpatt, double *pi);
+
+/*
+ * Pairwise Nei-Gojobori (1986) distances of a clean codon alignment, as
+ * codeml prints them before the fit (DistanceMatNG86 treesub.c:2270-2366,
+ * difcodonNG tools.c:305-420).  Host only (no device).
+ *   z[ns*npatt], fpatt[npatt]: patterns as from gb_patterns.
+ * Outputs [ns*ns], symmetric, zero diagonal: dS and dN (-1 where NG86 does not
+ * apply, as codeml prints them); dist (may be NULL): codeml's SeqDistance,
+ * (S dS + N dN) 3 / (S + N) with inapplicable distances set to 3.
+ * codeml prints dN/dS as dN / dS where both are positive, else -1.
+ */
+int gb_ng86(int ns, int npatt, const unsigned char *z, const double *fpatt, double *dS, double *dN,
+            double *dist);
 
 /*
  * Batched evaluation of many independent alignments ("genes"), each with its

@@ -20,7 +20,9 @@ With fix_omega = 0 codeml then runs its Bayes empirical Bayes analysis
 the fixture also keeps its per-site posteriors of the four site classes (rst,
 5 dp), the posterior on the w0 / w2 grid and on the p0-p1 triangles (out
 file, 3 dp) and the printed log f(X) with its scale terms S1, S2 (stdout, 6
-dp).
+dp).  Every fixture also keeps the Nei-Gojobori (1986) pairwise dN/dS, dN,
+dS table codeml prints before the fit (DistanceMatNG86 treesub.c:2270-2366;
+out file, 4 dp).
 
 A second run of the same case with getSE = 1 gives codeml's standard errors
 ("SEs for parameters", out file, 6 dp): HessianSKT2004 (treesub.c:6979-7048)
@@ -129,10 +131,10 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
                 f.write(CTL.replace("getSE = 0", "getSE = 1"))
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
-    extra = {"model": "B"}
+    extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns)}
     if not model_b:
         k = out_se.index("SEs for parameters:")
-        extra = {"beb": parse_beb(out, rst, r.stdout),
+        extra = {"beb": parse_beb(out, rst, r.stdout), "ng86_4dp": parse_ng86(out, ns),
                  "se_6dp": [float(v) for v in out_se[k:].splitlines()[1].split()], "small_diff": 1e-6}
     m = re.search(r"lnL\(ntime:\s*(\d+)\s+np:\s*(\d+)\):\s*(-?\d+\.\d+)", out)
     lnL = float(m.group(3))
@@ -158,6 +160,23 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         "lnf": lnf, "fpatt": fp, "patterns": [" ".join(p) for p in pats], "pi_8dp": pi8,
         **extra,
     }
+
+
+def parse_ng86(out: str, ns: int) -> dict:
+    """codeml's Nei-Gojobori (1986) table (DistanceMatNG86 treesub.c:2270-2366,
+    printed before the fit): for each pair j < i, dN/dS, dN and dS (4 dp; -1
+    where NG86 does not apply)."""
+    i0 = out.index("Nei & Gojobori 1986. dN/dS (dN, dS)")
+    i1 = out.index("TREE #", i0)
+    rows = [ln for ln in out[i0:i1].splitlines()[4:] if ln.strip()]
+    assert len(rows) == ns
+    w, dn, ds = [], [], []
+    for i, ln in enumerate(rows):
+        vals = re.findall(r"(-?\d+\.\d+) ?\((-?\d+\.\d+) (-?\d+\.\d+)\)", ln)
+        assert len(vals) == i
+        for a, b, c in vals:
+            w.append(float(a)); dn.append(float(b)); ds.append(float(c))
+    return {"dN_dS": w, "dN": dn, "dS": ds}
 
 
 def parse_beb(out: str, rst: str, stdout: str) -> dict:

@@ -233,6 +233,26 @@ class Likelihood:
                 "S2": float(fx[2]), "lnfw": lnfw, "ms_device": st.ms_device, "ms_host": st.ms_host,
                 "kernels": st.kernels}
 
+    def neb_x(self, x, lastround: bool = True):
+        """(post [4, npatt], -lnL): the NEB posteriors of the four site classes
+        at codeml's x (gb_neb; FP64 handle)."""
+        x = np.asarray(x, dtype=np.float64)
+        nb = self.nnode - 1
+        bl = np.zeros(self.nnode)
+        bl[self.bnode] = x[:nb]
+        kappa, w0, w2 = x[nb], x[nb + 3], x[nb + 4]
+        if lastround:
+            p0, p1 = x[nb + 1], x[nb + 2]
+        else:
+            e = np.exp(x[nb + 1:nb + 3])
+            p0, p1 = e / (1 + e.sum())
+        bl = np.ascontiguousarray(bl)
+        prm = _lib.Params(_ptr(bl), kappa, w0, w2, p0, p1)
+        post = np.zeros((4, self.npatt))
+        f = C.c_double(0)
+        _lib.check(self._L.gb_neb(self._h, C.byref(prm), _ptr(post), C.byref(f)))
+        return post, f.value
+
     def beb_x(self, x, lastround: bool = True, want_lnfw: bool = False) -> dict:
         """beb() from codeml's x vector."""
         x = np.asarray(x, dtype=np.float64)

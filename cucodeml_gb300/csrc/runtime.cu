@@ -479,6 +479,25 @@ int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad, 
     return GB_OK;
 }
 
+int gb_neb(gb_handle *h, const gb_params *prm, double *post, double *neg_lnL) {
+    if (!h) return fail(GB_ERR_STATE, "null handle");
+    if (!prm || !prm->blength || !post) return fail(GB_ERR_ARG, "null argument");
+    if (h->precision != GB_PREC_FP64) return fail(GB_ERR_STATE, "gb_neb needs a GB_PREC_FP64 handle");
+    Derived *D = new Derived;
+    ModelParams m{prm->kappa, prm->omega0, prm->omega2, prm->p0, prm->p1};
+    int rc = derive(h->pi.data(), m, false, D);
+    if (rc) { delete D; return fail(rc, "model parameters out of range"); }
+    double v = 0;
+    rc = upload_and_run(h, D, prm->blength, false, &v, nullptr, nullptr, nullptr);
+    delete D;
+    if (rc) return rc;
+    // the mixture kernel's class posteriors of the evaluation just run
+    CK(cudaMemcpy2D(post, sizeof(double) * h->npatt, h->d_post, sizeof(double) * h->npad,
+                    sizeof(double) * h->npatt, 4, cudaMemcpyDeviceToHost));
+    if (neg_lnL) *neg_lnL = v;
+    return GB_OK;
+}
+
 int gb_dfun_x(gb_handle *h, const int *bnode, int lastround, const double *x, int n, double *f,
               double *dx) {
     if (!h) return fail(GB_ERR_STATE, "null handle");

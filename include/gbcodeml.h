@@ -36,6 +36,8 @@
  *   gb_patterns              PatternWeight + EncodeSeqs (treesub.c:1075-1143,
  *                            1302-1439) and F3x4 codon frequencies
  *                            (codeml.c:3475-3570, 3732-3742) for clean codon data.
+ *   gb_neb                   the NEB site-class posteriors codeml prints
+ *                            (lfunNSsites_rate codeml.c:5079-5129).
  *   gb_ng86                  DistanceMatNG86 (treesub.c:2270-2366): pairwise
  *                            Nei-Gojobori dS, dN from per-codon-pair tables.
  *   gb_se_opg / gb_hessian_x standard errors: codeml's getSE = 1 Hessian
@@ -199,6 +201,15 @@ int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad,
 #define GB_BEB_OMEGA_SETS  121
 int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw, double *post, double *grid,
            double *p0p1, double *lnfX, gb_stats *stats);
+
+/*
+ * Naive empirical Bayes (NEB) posteriors of the four site classes at prm, as
+ * codeml's lfunNSsites_rate prints them ("Naive Empirical Bayes (NEB)
+ * probabilities", codeml.c:5079-5129): post[c*npatt + h] = freqK_c f_c(h) /
+ * sum_k freqK_k f_k(h), from the mixture of one FP64 evaluation; *neg_lnL
+ * (may be NULL) its -lnL.  Needs a GB_PREC_FP64 handle.
+ */
+int gb_neb(gb_handle *h, const gb_params *prm, double *post, double *neg_lnL);
 
 /*
  * Standard errors as codeml computes them with getSE = 1 (codeml.c:754-783):

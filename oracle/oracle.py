@@ -162,6 +162,19 @@ class Problem:
                 "lnfX": fx[0], "S1": fx[1], "S2": fx[2]}
 
 
+    def neb(self, x, lastround: bool = True):
+        """NEB posteriors of the four site classes at x (lfunNSsites_rate
+        codeml.c:5079-5129): freqK_c f_c(h) normalised over c, from fhK (log
+        values shifted by their maximum when nodes are scaled)."""
+        v, fhK, lnf, nscale = self.neg_lnL(x, lastround=lastround, want_fhK=True)
+        fk = self.set_params(x, lastround)[4]
+        if nscale:
+            f = np.exp(fhK - fhK.max(axis=0))
+        else:
+            f = fhK
+        q = fk[:, None] * f
+        return q / q.sum(axis=0)
+
     def opg_se(self, x, small_diff: float = 1e-6):
         """codeml's standard errors (getSE = 1): HessianSKT2004
         (treesub.c:6979-7048) -- per-pattern scores by central differences of

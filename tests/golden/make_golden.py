@@ -20,6 +20,8 @@ With fix_omega = 0 codeml then runs its Bayes empirical Bayes analysis
 the fixture also keeps its per-site posteriors of the four site classes (rst,
 5 dp), the posterior on the w0 / w2 grid and on the p0-p1 triangles (out
 file, 3 dp) and the printed log f(X) with its scale terms S1, S2 (stdout, 6
+dp).  The fixtures also keep the naive empirical Bayes (NEB) per-site
+posteriors codeml prints first (lfunNSsites_rate codeml.c:5079-5129; rst, 5
 dp).  Every fixture also keeps the Nei-Gojobori (1986) pairwise dN/dS, dN,
 dS table codeml prints before the fit (DistanceMatNG86 treesub.c:2270-2366;
 out file, 4 dp).
@@ -131,10 +133,11 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
                 f.write(CTL.replace("getSE = 0", "getSE = 1"))
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
-    extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns)}
+    extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns), "neb_site_post_5dp": parse_site_post(rst, "Naive")}
     if not model_b:
         k = out_se.index("SEs for parameters:")
         extra = {"beb": parse_beb(out, rst, r.stdout), "ng86_4dp": parse_ng86(out, ns),
+                 "neb_site_post_5dp": parse_site_post(rst, "Naive"),
                  "se_6dp": [float(v) for v in out_se[k:].splitlines()[1].split()], "small_diff": 1e-6}
     m = re.search(r"lnL\(ntime:\s*(\d+)\s+np:\s*(\d+)\):\s*(-?\d+\.\d+)", out)
     lnL = float(m.group(3))
@@ -179,16 +182,26 @@ def parse_ng86(out: str, ns: int) -> dict:
     return {"dN_dS": w, "dN": dn, "dS": ds}
 
 
-def parse_beb(out: str, rst: str, stdout: str) -> dict:
-    """codeml's BEB results: per-site class posteriors (rst), grid posteriors
-    (out) and log f(X), S1, S2 (stdout)."""
-    i0 = rst.index("Bayes Empirical Bayes (BEB) probabilities")
+def parse_site_post(rst: str, which: str) -> list:
+    """Per-site posteriors of the four site classes from codeml's rst
+    (PrintProbNSsites codeml.c:4975-5030): the "Naive Empirical Bayes (NEB)"
+    or the "Bayes Empirical Bayes (BEB)" block, 5 dp."""
+    head = {"Naive": "Naive Empirical Bayes (NEB) probabilities",
+            "Bayes": "Bayes Empirical Bayes (BEB) probabilities"}[which]
+    i0 = rst.index(head)
     site = []
     for ln in rst[i0:].splitlines()[3:]:
         parts = ln.split()
         if len(parts) < 7 or not parts[0].isdigit():
             break
         site.append([float(v) for v in parts[2:6]])
+    return site
+
+
+def parse_beb(out: str, rst: str, stdout: str) -> dict:
+    """codeml's BEB results: per-site class posteriors (rst), grid posteriors
+    (out) and log f(X), S1, S2 (stdout)."""
+    site = parse_site_post(rst, "Bayes")
     j0 = out.index("Posterior on the grid")
     rows = {}
     for ln in out[j0:].splitlines()[1:6]:

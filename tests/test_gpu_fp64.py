@@ -108,3 +108,23 @@ def test_64x5000_matches_oracle():
     r = lk.evaluate(node_blength(tree, x), 2.0, 0.3, 3.0, 0.5, 0.3)
     assert lk.nscale > 0
     assert abs(r.neg_lnL - v) <= 1e-9 * abs(v)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_neb_matches_oracle_and_codeml(cases, name):
+    """gb_neb: the mixture's class posteriors of one FP64 evaluation against
+    the oracle (1e-9: per-class log f may differ by 2e-11 |log f| between the
+    two eigensolvers, as the per-pattern bar above allows) and
+    codeml's printed NEB posteriors (5 decimals)."""
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, z, fpatt, pi = cases[name]
+    x = np.array(fx["x"])
+    ref = O.Problem(tree, z, fpatt, pi).neb(x)
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    post, f = lk.neb_x(x)
+    assert np.max(np.abs(post - ref)) <= 1e-9
+    _, _, codons = load_golden(name)
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6
+    assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+    lk.close()

@@ -19,7 +19,31 @@ def pytest_configure(config):
 def golden_names():
     """Fixed-parameter model-A fixtures (codeml lnL and per-pattern log f at given x)."""
     return sorted(f[:-5] for f in os.listdir(GOLDEN)
-                  if f.endswith(".json") and not f.startswith(("mle_", "mb")))
+                  if f.endswith(".json") and not f.startswith(("mle_", "mb", "ms")))
+
+
+def site_model_names():
+    """Fixed-parameter fixtures under the site models M2a / M1a (no branch labels)."""
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("ms") and f.endswith(".json"))
+
+
+def as_model_a(fx, tree):
+    """A site-model fixture as the branch-site model A evaluation that equals
+    it: every branch labelled foreground, so site classes 2a and 2b both carry
+    w2 on every branch and together weigh 1 - p0 - p1 (M2a); M1a is that with
+    p1 = 1 - p0 (no w2 class; w2 then carries no weight and is set to 1).
+    Returns (tree with labels, model-A x)."""
+    import copy
+
+    t = copy.deepcopy(tree)
+    t.label[:] = 1
+    t.label[t.root] = 0
+    x = np.array(fx["x"], dtype=np.float64)
+    nb = tree.nbranch
+    if fx["model"] == "M1a":
+        kappa, p0, w0 = x[nb:nb + 3]
+        x = np.concatenate([x[:nb], [kappa, p0, 1.0 - p0, w0, 1.0]])
+    return t, x
 
 
 def model_b_names():

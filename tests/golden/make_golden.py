@@ -33,6 +33,8 @@ from central differences of log f_h (step 2 Small_Diff (|x_i| + 1)), and the
 SEs are the square roots of the diagonal of its negated inverse
 (codeml.c:754-783).
 
+The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
+x ends p0, p1, w0, w2 for M2a and p0, w0 for M1a), lnL, log f and NG86 only.
 The mb_* fixtures are the same evaluation under branch-site model B
 (NSsites = 3, ncatG = 3: w1 free; x ends w0, w1, w2), lnL and log f only.
 
@@ -107,9 +109,20 @@ CASES_B = [
 ]
 
 
-def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b=False):
+# site models without branch labels (model = 0): M2a (NSsites = 2, x ends p0,
+# p1, w0, w2) and M1a (NSsites = 1, x ends p0, w0); lnL, lnf, patterns, NG86
+CASES_SITE = [
+    ("msM2a8x300_s9", 8, 300, 9, ModelA(), (2.0, 0.6, 0.3, 0.2, 2.5), 1.0, "M2a"),
+    ("msM2a24x400_s10", 24, 400, 10, ModelA(omega2=4.0), (2.2, 0.5, 0.35, 0.15, 3.5), 1.0, "M2a"),
+    ("msM1a12x300_s11", 12, 300, 11, ModelA(), (2.0, 0.7, 0.25), 1.0, "M1a"),
+]
+
+
+def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b=False, site_model=None):
     aln = simulate(ns, ncodon, seed=seed, model=model)
     tree = aln.tree
+    if site_model:
+        tree.label[:] = 0          # site models: no foreground branch in the tree file
     xb = tree.x_branch_lengths() * bscale
     if name.startswith("c5x120"):
         xb[2] = 0.0          # internal branch with t = 0: P = I (PMatUVRoot, t < 1e-100)
@@ -122,19 +135,25 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         with open(os.path.join(d, "in.codeml"), "w") as f:
             f.write("-1 " + " ".join(repr(float(v)) for v in x) + "\n")
         ctl = CTL.replace("NSsites = 2", "NSsites = 3").replace("ncatG = 4", "ncatG = 3") if model_b else CTL
+        if site_model:
+            ctl = CTL.replace("model = 2", "model = 0").replace(
+                "NSsites = 2", "NSsites = " + {"M1a": "1", "M2a": "2"}[site_model])
         with open(os.path.join(d, "codeml.ctl"), "w") as f:
             f.write(ctl)
         r = subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
         out = open(os.path.join(d, "out.txt")).read()
         lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
         rst = open(os.path.join(d, "rst")).read()
-        if not model_b:
+        if not model_b and not site_model:
             with open(os.path.join(d, "codeml.ctl"), "w") as f:
                 f.write(CTL.replace("getSE = 0", "getSE = 1"))
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
-    extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns), "neb_site_post_5dp": parse_site_post(rst, "Naive")}
-    if not model_b:
+    if site_model:
+        extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
+    elif model_b:
+        extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns), "neb_site_post_5dp": parse_site_post(rst, "Naive")}
+    else:
         k = out_se.index("SEs for parameters:")
         extra = {"beb": parse_beb(out, rst, r.stdout), "ng86_4dp": parse_ng86(out, ns),
                  "neb_site_post_5dp": parse_site_post(rst, "Naive"),
@@ -222,7 +241,7 @@ def main():
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
     codeml = os.path.join(ROOT, "oracle", "_ref", "codeml")
     outdir = os.path.dirname(os.path.abspath(__file__))
-    for case in CASES + [c + (True,) for c in CASES_B]:
+    for case in CASES + [c + (True,) for c in CASES_B] + [c[:7] + (False, c[7]) for c in CASES_SITE]:
         fx = run_case(codeml, *case)
         with open(os.path.join(outdir, fx["name"] + ".json"), "w") as f:
             json.dump(fx, f, separators=(",", ":"))

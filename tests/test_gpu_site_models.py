@@ -1,0 +1,41 @@
+"""Site models M2a / M1a on the GPU as branch-site model A with every branch
+in the foreground (the equivalence is pinned on the CPU in
+tests/test_site_models_oracle.py): the FP64 drop-in's lnL and per-pattern
+log f against the reference codeml's own runs of M2a / M1a (1e-9 relative,
+print rounding + 2e-11 |log f|) and the oracle, and for M2a the adjoint
+gradient against 5-point differences of the oracle (1e-5, as for model A).
+Every node of such a tree is on a foreground path, so all four classes are
+pruned at every node: the schedule's other extreme from one foreground
+branch.
+"""
+import numpy as np
+import pytest
+
+from cucodeml_gb300 import api
+from oracle import oracle as O
+from tests.conftest import as_model_a, load_golden, site_model_names
+from tests.test_gpu_gradient import fd_grad
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", site_model_names())
+def test_site_model_fp64(name):
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, x = as_model_a(fx, tree)
+    pb = O.Problem(t, z, fpatt, pi, nthreads=4)
+    lk = api.Likelihood(t, z, fpatt, pi)
+    nb = t.nbranch
+    bl = np.zeros(t.nnode)
+    bl[t.branch_nodes()] = x[:nb]
+    r = lk.evaluate(bl, x[nb], x[nb + 3], x[nb + 4], x[nb + 1], x[nb + 2], want_site=True)
+    assert abs(-r.neg_lnL - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+    ref = np.array(fx["lnf"])
+    assert np.all(np.abs(r.lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))
+    assert abs(r.neg_lnL - pb.neg_lnL(x)) <= 1e-9 * abs(r.neg_lnL)
+    if fx["model"] == "M2a":
+        f, g = lk.dfun_x(x, True)
+        gfd = fd_grad(pb, x, True)
+        assert np.max(np.abs(g - gfd) / np.maximum(1.0, np.abs(gfd))) <= 1e-5
+    lk.close()

@@ -253,6 +253,24 @@ class Likelihood:
         _lib.check(self._L.gb_neb(self._h, C.byref(prm), _ptr(post), C.byref(f)))
         return post, f.value
 
+    def beb_qf(self, blength, kappa, qfactor, want_lnfw: bool = False) -> dict:
+        """beb() with the branch Qfactors given (gb_beb_qf): model B, or a
+        caller holding codeml's Qfactor_NS_branch."""
+        bl = np.ascontiguousarray(blength, dtype=np.float64)
+        qf = np.ascontiguousarray(qfactor, dtype=np.float64)
+        lnfw = np.zeros((121, self.npatt)) if want_lnfw else None
+        post = np.zeros((4, self.npatt))
+        grid = np.zeros((4, 10))
+        p0p1 = np.zeros(100)
+        fx = np.zeros(3)
+        st = _lib.Stats()
+        _lib.check(self._L.gb_beb_qf(self._h, _ptr(bl), float(kappa), _ptr(qf),
+                                     _ptr(lnfw) if want_lnfw else None, _ptr(post), _ptr(grid), _ptr(p0p1),
+                                     _ptr(fx), C.byref(st)))
+        return {"post": post, "grid": grid, "p0p1": p0p1, "lnfX": float(fx[0]), "S1": float(fx[1]),
+                "S2": float(fx[2]), "lnfw": lnfw, "ms_device": st.ms_device, "ms_host": st.ms_host,
+                "kernels": st.kernels}
+
     def beb_x(self, x, lastround: bool = True, want_lnfw: bool = False) -> dict:
         """beb() from codeml's x vector."""
         x = np.asarray(x, dtype=np.float64)

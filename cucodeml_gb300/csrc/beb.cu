@@ -232,14 +232,29 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw_out, double *post_ou
            double *p0p1_out, double *lnfX_out, gb_stats *stats) {
     if (!h) return fail(GB_ERR_STATE, "null handle");
     if (!prm || !prm->blength) return fail(GB_ERR_ARG, "null argument");
+    // the branch Qfactors of model A at prm (SetParametersNSsites codeml.c:2490-2512)
+    std::vector<Derived> Dv(1);
+    ModelParams m{prm->kappa, prm->omega0, prm->omega2, prm->p0, prm->p1};
+    int rc = derive_scalars(h->pi.data(), m, &Dv[0]);
+    if (rc) return fail(rc, "model parameters out of range");
+    return gb_beb_qf(h, prm->blength, prm->kappa, Dv[0].qf, lnfw_out, post_out, grid_out, p0p1_out, lnfX_out,
+                     stats);
+}
+
+int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qfactor[2], double *lnfw_out,
+              double *post_out, double *grid_out, double *p0p1_out, double *lnfX_out, gb_stats *stats) {
+    if (!h) return fail(GB_ERR_STATE, "null handle");
+    if (!blength || !qfactor) return fail(GB_ERR_ARG, "null argument");
     if (h->precision != GB_PREC_FP64) return fail(GB_ERR_STATE, "gb_beb needs a GB_PREC_FP64 handle");
+    if (!(kappa > 0) || !(qfactor[0] > 0) || !(qfactor[1] > 0)) return fail(GB_ERR_PARAM, "kappa or Qfactor");
     const double t0 = now_ms();
-    // Qfactors and kappa at prm; eigen solutions of the 21 omega values
+    int rc = 0;
+    // eigen solutions of the 21 omega values (unscaled Q; the Qfactors scale t)
     std::vector<Derived> Dv(1);
     Derived &D = Dv[0];
-    ModelParams m{prm->kappa, prm->omega0, prm->omega2, prm->p0, prm->p1};
-    int rc = derive_scalars(h->pi.data(), m, &D);
-    if (rc) return fail(rc, "model parameters out of range");
+    D.qf[0] = qfactor[0];
+    D.qf[1] = qfactor[1];
+    D.freqK[0] = D.freqK[1] = D.freqK[2] = D.freqK[3] = 0.25;   // the forward's mixture is not used
     double wv[BNE];
     for (int i = 0; i < BD; i++) {
         wv[i] = (i + 0.5) / BD;                          // w0 in (0, 1)
@@ -249,7 +264,7 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw_out, double *post_ou
     std::vector<double> eig((size_t)BNE * EIG);
     for (int e = 0; e < BNE; e++) {
         std::vector<double> Q(NC * NC);
-        build_q(h->pi.data(), prm->kappa, wv[e], Q.data(), nullptr, nullptr);
+        build_q(h->pi.data(), kappa, wv[e], Q.data(), nullptr, nullptr);
         double *E = &eig[(size_t)e * EIG];
         if (eigen_qrev(Q.data(), h->pi.data(), E, E + NC * NC, E + 2 * NC * NC))
             return fail(GB_ERR_PARAM, "eigen solution failed");
@@ -262,7 +277,7 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw_out, double *post_ou
         std::memcpy(D.Root[s], &eig[(size_t)e * EIG + 2 * NC * NC], sizeof(double) * NC);
     }
     D.sym = 1;
-    if ((rc = stage_params(h, &D, prm->blength))) return rc;
+    if ((rc = stage_params(h, &D, blength))) return rc;
     if ((rc = fp64_prepare(h, false))) return rc;
     // class masks: 2a + 2b on the path; 0 + 2a for a new w0 (class 1 and
     // class 2b do not depend on w0); 2a alone for a new w2 under the same w0

@@ -121,22 +121,17 @@ int GB_dfun(double x[], double *f, double dx[], int n) {
 
 int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], double lnfX[]) {
     int i, rc;
-    gb_params p;
     gb_handle *h;
     double *bl;
-    if (np != com.ntime + 5) gb_die("GB_BEB (model A parameter vector)", GB_ERR_ARG);
+    if (np < com.ntime + 1) gb_die("GB_BEB (parameter vector)", GB_ERR_ARG);
     bl = (double *)calloc(tree.nnode, sizeof(double));
     if (!bl) gb_die("GB_BEB (host memory)", GB_ERR_OOM);
     for (i = 0; i < tree.nnode; i++)
         if (i != tree.root) bl[i] = x[nodes[i].ibranch];
-    p.blength = bl;
-    p.kappa = x[com.ntime];
-    p.p0 = x[com.ntime + 1];
-    p.p1 = x[com.ntime + 2];
-    p.omega0 = x[com.ntime + 3];
-    p.omega2 = x[com.ntime + 4];
     h = make_handle("GB_BEB (one gene, cleandata = 1, universal code only)");
-    rc = gb_beb(h, &p, NULL, postSite, grid, p0p1, lnfX, NULL);
+    /* kappa from x, the Qfactors of the last SetParameters (at the MLE), as
+       codeml's BEB reads them (GetPMatBranch treesub.c:7289-7301): models A and B */
+    rc = gb_beb_qf(h, bl, x[com.ntime], Qfactor_NS_branch, NULL, postSite, grid, p0p1, lnfX, NULL);
     gb_destroy(h);
     free(bl);
     if (rc) gb_die("gb_beb", rc);

@@ -203,6 +203,16 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw, double *post, doubl
            double *p0p1, double *lnfX, gb_stats *stats);
 
 /*
+ * gb_beb with the two branch Qfactors given (codeml's Qfactor_NS_branch,
+ * which its BEB reads at the MLE, GetPMatBranch treesub.c:7289-7301) instead
+ * of derived from model A's parameters: the same analysis for branch-site
+ * model B, whose Qfactors involve its free w1 (codeml runs model A's BEB grid
+ * for it).  blength[nnode]: branch lengths by node.
+ */
+int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qfactor[2], double *lnfw,
+              double *post, double *grid, double *p0p1, double *lnfX, gb_stats *stats);
+
+/*
  * Naive empirical Bayes (NEB) posteriors of the four site classes at prm, as
  * codeml's lfunNSsites_rate prints them ("Naive Empirical Bayes (NEB)
  * probabilities", codeml.c:5079-5129): post[c*npatt + h] = freqK_c f_c(h) /

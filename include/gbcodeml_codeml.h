@@ -19,9 +19,10 @@
  *                                  gradient of -lnL in codeml's x space; pass it
  *                                  instead of NULL at codeml.c:688.
  *   GB_BEB                         new: the Bayes empirical Bayes analysis of
- *                                  model A on the GPU at codeml's final x
- *                                  (natural p0, p1 after Forestry's
- *                                  back-transform, codeml.c:713-729): fills
+ *                                  models A and B on the GPU at codeml's final
+ *                                  x (kappa and branch lengths; the Qfactors
+ *                                  are codeml's Qfactor_NS_branch, as its BEB
+ *                                  reads them): fills
  *                                  lfunNSsites_ACD's postSite[4*npatt], the w0
  *                                  and w2 rows of its postpara (grid[20..39]),
  *                                  postp0p1[100] and log f(X), S1, S2

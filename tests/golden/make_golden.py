@@ -33,6 +33,9 @@ from central differences of log f_h (step 2 Small_Diff (|x_i| + 1)), and the
 SEs are the square roots of the diagonal of its negated inverse
 (codeml.c:754-783).
 
+codeml runs the same BEB for model B (lfunNSsites_ACD treats model = 2 as
+model A's grid, w1 = 1 in class 1, with model B's Qfactors), kept for the
+mb* fixtures too.
 The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
 x ends p0, p1, w0, w2 for M2a and p0, w0 for M1a), lnL, log f and NG86 only.
 The mb_* fixtures are the same evaluation under branch-site model B
@@ -152,7 +155,8 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
     if site_model:
         extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
     elif model_b:
-        extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns), "neb_site_post_5dp": parse_site_post(rst, "Naive")}
+        extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns), "neb_site_post_5dp": parse_site_post(rst, "Naive"),
+                 "beb": parse_beb(out, rst, r.stdout)}
     else:
         k = out_se.index("SEs for parameters:")
         extra = {"beb": parse_beb(out, rst, r.stdout), "ng86_4dp": parse_ng86(out, ns),

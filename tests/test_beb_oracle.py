@@ -79,3 +79,20 @@ def test_beb_thread_invariant(nth):
     a = O.Problem(tree, z, fpatt, pi, nthreads=nth).beb(x)
     b = O.Problem(tree, z, fpatt, pi, nthreads=2).beb(x)
     assert np.array_equal(a["post"], b["post"]) and a["lnfX"] == b["lnfX"]
+
+
+@pytest.mark.parametrize("name", ["mb8x300_s7", "mb24x400_s8"])
+def test_beb_model_b_matches_codeml(name):
+    """codeml runs model A's BEB grid for model B too (w1 = 1 in class 1),
+    with model B's Qfactors (its free w1 in the mean rates)."""
+    from tests.conftest import load_golden
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    r = O.Problem(tree, z, fpatt, pi, nthreads=4, model_b=True).beb(np.array(fx["x"]))
+    g = fx["beb"]
+    site = r["post"][:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(g["site_post_5dp"]))) <= 5.01e-6
+    assert np.max(np.abs(r["grid"][2] - g["w0_post_3dp"])) <= 5.01e-4
+    assert np.max(np.abs(r["grid"][3] - g["w2_post_3dp"])) <= 5.01e-4
+    assert np.max(np.abs(r["p0p1"] - g["p0p1_post_3dp"])) <= 5.01e-4
+    assert abs(r["lnfX"] - g["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])

@@ -86,3 +86,25 @@ def test_beb_path_only_sets_match_full_evaluations():
             a, b = r["lnfw"][s], e.fhK[row]
             assert np.all(np.abs(a - b) <= 1e-10 + 2e-9 * np.abs(b)), (i, j, row)
     lk.close()
+
+
+@pytest.mark.parametrize("name", ["mb8x300_s7", "mb24x400_s8"])
+def test_beb_model_b_with_given_qfactors(name):
+    """gb_beb_qf with model B's Qfactors (the oracle's set-up of model B)
+    against the oracle's model-B BEB and codeml's output, same bars."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=4, model_b=True)
+    ref = pb.beb(x)
+    qf = pb.set_params(x)[3]
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[: tree.nbranch]
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    r = lk.beb_qf(bl, x[tree.nbranch], qf, want_lnfw=True)
+    assert np.all(np.abs(r["lnfw"] - ref["lnfw"]) <= 1e-10 + 2e-9 * np.abs(ref["lnfw"]))
+    assert np.max(np.abs(r["post"] - ref["post"])) <= 1e-8
+    assert abs(r["lnfX"] - ref["lnfX"]) <= 1e-9 * abs(ref["lnfX"])
+    site = r["post"][:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(fx["beb"]["site_post_5dp"]))) <= 5.01e-6
+    lk.close()

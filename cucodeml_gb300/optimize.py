@@ -160,6 +160,43 @@ def alt_null(tree, z, fpatt, pi, precision: str = "fast", gradient: str = "adjoi
         lk.close()
 
 
+def natural_x(x):
+    """codeml's x with transformed p0, p1 (f_and_x) -> the same with p0, p1 themselves."""
+    x = np.array(x, dtype=np.float64)
+    e = np.exp(x[-4:-2])
+    x[-4:-2] = e / (1.0 + e.sum())
+    return x
+
+
+def site_analysis(tree, codons, z, fpatt, pi, x_alt, cutoff: float = 0.5) -> dict:
+    """What codeml reports after the alternative fit, at its maximum x_alt
+    (codeml's x, transformed p0, p1): standard errors (getSE = 1,
+    gb_se_opg), NEB and BEB posteriors of the site classes (gb_neb, gb_beb),
+    and the sites whose BEB probability of w > 1 (classes 2a + 2b) exceeds
+    cutoff, with codeml's * (> 0.95) and ** (> 0.99) marks.  FP64 handle."""
+    xn = natural_x(x_alt)
+    lk = api.Likelihood(tree, z, fpatt, pi, precision="fp64")
+    try:
+        t0 = time.perf_counter()
+        se = lk.se_opg(xn)
+        neb, _ = lk.neb_x(xn)
+        beb = lk.beb_x(xn)
+        secs = time.perf_counter() - t0
+    finally:
+        lk.close()
+    key = {tuple(z[:, h]): h for h in range(z.shape[1])}
+    pose = np.array([key[tuple(codons[:, i])] for i in range(codons.shape[1])])
+    pos = []
+    for i, h in enumerate(pose):
+        pr = float(beb["post"][2, h] + beb["post"][3, h])
+        if pr > cutoff:
+            pos.append({"site": i + 1, "prob": pr, "mark": "**" if pr > 0.99 else ("*" if pr > 0.95 else "")})
+    return {"x": xn.tolist(), "se": se["se"].tolist(), "lnfX": beb["lnfX"],
+            "beb_grid_w0": beb["grid"][2].tolist(), "beb_grid_w2": beb["grid"][3].tolist(),
+            "positive_sites_beb": pos,
+            "neb_positive_sites": int(np.sum((neb[2] + neb[3])[pose] > cutoff)), "seconds": secs}
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--taxa", type=int, default=256)
@@ -171,6 +208,9 @@ def main(argv=None):
     ap.add_argument("--polish", action="store_true",
                     help="after each non-FP64 fit, continue with the FP64 path from its maxima")
     ap.add_argument("--out", default=None, help="write the JSON result here as well")
+    ap.add_argument("--sites", action="store_true",
+                    help="after the fits: standard errors, NEB and BEB at the alternative's maximum "
+                         "(first precision listed)")
     ap.add_argument("--fd-sample", type=int, default=24,
                     help="lnL evaluations timed per precision to cost codeml's finite-difference "
                          "gradient (np evaluations) and a finite-difference-driven fit")
@@ -210,6 +250,8 @@ def main(argv=None):
                                 "note": "estimate: sampled lnL evaluation time x (np + 1) per call, "
                                         "calls as in the adjoint-driven fits"}
         out["fits"].append(r)
+    if a.sites:
+        out["sites"] = site_analysis(aln.tree, aln.codons, z, fp, pi, out["fits"][0]["alt"]["x"])
     if len(out["fits"]) > 1:
         # each optimum re-evaluated with the FP64 path
         lk = api.Likelihood(aln.tree, z, fp, pi, precision="fp64")

@@ -37,7 +37,8 @@ codeml runs the same BEB for model B (lfunNSsites_ACD treats model = 2 as
 model A's grid, w1 = 1 in class 1, with model B's Qfactors), kept for the
 mb* fixtures too.
 The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
-x ends p0, p1, w0, w2 for M2a and p0, w0 for M1a), lnL, log f and NG86 only.
+x ends p0, p1, w0, w2 for M2a and p0, w0 for M1a): lnL, log f, NG86, and
+for M2a codeml's BEB (three classes).
 The mb_* fixtures are the same evaluation under branch-site model B
 (NSsites = 3, ncatG = 3: w1 free; x ends w0, w1, w2), lnL and log f only.
 
@@ -154,6 +155,8 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
             out_se = open(os.path.join(d, "out.txt")).read()
     if site_model:
         extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
+        if site_model == "M2a":       # BEB of M2a (lfunNSsites_M2M8 codeml.c:6190-6415): 3 classes
+            extra["beb"] = parse_beb(out, rst, r.stdout, ncls=3)
     elif model_b:
         extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns), "neb_site_post_5dp": parse_site_post(rst, "Naive"),
                  "beb": parse_beb(out, rst, r.stdout)}
@@ -205,7 +208,7 @@ def parse_ng86(out: str, ns: int) -> dict:
     return {"dN_dS": w, "dN": dn, "dS": ds}
 
 
-def parse_site_post(rst: str, which: str) -> list:
+def parse_site_post(rst: str, which: str, ncls: int = 4) -> list:
     """Per-site posteriors of the four site classes from codeml's rst
     (PrintProbNSsites codeml.c:4975-5030): the "Naive Empirical Bayes (NEB)"
     or the "Bayes Empirical Bayes (BEB)" block, 5 dp."""
@@ -215,16 +218,16 @@ def parse_site_post(rst: str, which: str) -> list:
     site = []
     for ln in rst[i0:].splitlines()[3:]:
         parts = ln.split()
-        if len(parts) < 7 or not parts[0].isdigit():
+        if len(parts) < ncls + 3 or not parts[0].isdigit():
             break
-        site.append([float(v) for v in parts[2:6]])
+        site.append([float(v) for v in parts[2:2 + ncls]])
     return site
 
 
-def parse_beb(out: str, rst: str, stdout: str) -> dict:
+def parse_beb(out: str, rst: str, stdout: str, ncls: int = 4) -> dict:
     """codeml's BEB results: per-site class posteriors (rst), grid posteriors
     (out) and log f(X), S1, S2 (stdout)."""
-    site = parse_site_post(rst, "Bayes")
+    site = parse_site_post(rst, "Bayes", ncls)
     j0 = out.index("Posterior on the grid")
     rows = {}
     for ln in out[j0:].splitlines()[1:6]:

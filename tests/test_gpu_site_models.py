@@ -39,3 +39,21 @@ def test_site_model_fp64(name):
         gfd = fd_grad(pb, x, True)
         assert np.max(np.abs(g - gfd) / np.maximum(1.0, np.abs(gfd))) <= 1e-5
     lk.close()
+
+
+@pytest.mark.parametrize("name", [n for n in site_model_names() if n.startswith("msM2a")])
+def test_m2a_beb(name):
+    """gb_beb on the all-foreground tree is codeml's M2a BEB (class 2 = 2a + 2b;
+    the equivalence is pinned on the CPU): against codeml's printed output."""
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, x = as_model_a(fx, tree)
+    lk = api.Likelihood(t, z, fpatt, pi)
+    r = lk.beb_x(x)
+    post = np.stack([r["post"][0], r["post"][1], r["post"][2] + r["post"][3]])
+    g = fx["beb"]
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(g["site_post_5dp"]))) <= 5.01e-6
+    assert abs(r["lnfX"] - g["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])
+    lk.close()

@@ -31,3 +31,24 @@ def test_site_model_as_model_a_matches_codeml(name):
     assert abs(-v - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     ref = np.array(fx["lnf"])
     assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))
+
+
+@pytest.mark.parametrize("name", [n for n in site_model_names() if n.startswith("msM2a")])
+def test_m2a_beb_as_model_a(name):
+    """codeml's BEB for M2a (lfunNSsites_M2M8 codeml.c:6190-6415) has model
+    A's grid (ternary (p0, p1), w0 in (0, 1), w2 in (1, 11), 10 points each)
+    and prior; on the all-foreground tree model A's classes 2a and 2b both
+    carry w2, so M2a's class-2 posterior is their sum."""
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, x = as_model_a(fx, tree)
+    r = O.Problem(t, z, fpatt, pi, nthreads=4).beb(x)
+    post = np.stack([r["post"][0], r["post"][1], r["post"][2] + r["post"][3]])
+    g = fx["beb"]
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(g["site_post_5dp"]))) <= 5.01e-6
+    assert np.max(np.abs(r["grid"][2] - g["w0_post_3dp"])) <= 5.01e-4
+    assert np.max(np.abs(r["grid"][3] - g["w2_post_3dp"])) <= 5.01e-4
+    assert np.max(np.abs(r["p0p1"] - g["p0p1_post_3dp"])) <= 5.01e-4
+    assert abs(r["lnfX"] - g["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])

@@ -66,7 +66,8 @@ SIGNATURES = {
     "gb_eval": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, C.POINTER(Grad), _dp, _dp,
                           C.POINTER(Stats)]),
     "gb_beb": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)]),
-    "gb_beb_qf": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)]),
+    "gb_beb_qf": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
+                            C.POINTER(Stats)]),
     "gb_neb": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, _dp]),
     "gb_ng86": (C.c_int, [C.c_int, C.c_int, C.POINTER(C.c_ubyte), _dp, _dp, _dp, _dp]),
     "gb_se_opg": (C.c_int, [C.c_void_p, _ip, _dp, C.c_int, C.c_double, _dp, _dp, _dp, C.POINTER(Stats)]),

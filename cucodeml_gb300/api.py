@@ -255,7 +255,8 @@ class Likelihood:
 
     def beb_qf(self, blength, kappa, qfactor, want_lnfw: bool = False) -> dict:
         """beb() with the branch Qfactors given (gb_beb_qf): model B, or a
-        caller holding codeml's Qfactor_NS_branch."""
+        caller holding codeml's Qfactor_NS_branch.  Also returns wmean / wsd,
+        the posterior mean and SD of each pattern's w."""
         bl = np.ascontiguousarray(blength, dtype=np.float64)
         qf = np.ascontiguousarray(qfactor, dtype=np.float64)
         lnfw = np.zeros((121, self.npatt)) if want_lnfw else None
@@ -264,12 +265,14 @@ class Likelihood:
         p0p1 = np.zeros(100)
         fx = np.zeros(3)
         st = _lib.Stats()
+        wmean = np.zeros(self.npatt)
+        wsd = np.zeros(self.npatt)
         _lib.check(self._L.gb_beb_qf(self._h, _ptr(bl), float(kappa), _ptr(qf),
                                      _ptr(lnfw) if want_lnfw else None, _ptr(post), _ptr(grid), _ptr(p0p1),
-                                     _ptr(fx), C.byref(st)))
+                                     _ptr(fx), _ptr(wmean), _ptr(wsd), C.byref(st)))
         return {"post": post, "grid": grid, "p0p1": p0p1, "lnfX": float(fx[0]), "S1": float(fx[1]),
-                "S2": float(fx[2]), "lnfw": lnfw, "ms_device": st.ms_device, "ms_host": st.ms_host,
-                "kernels": st.kernels}
+                "S2": float(fx[2]), "lnfw": lnfw, "wmean": wmean, "wsd": wsd, "ms_device": st.ms_device,
+                "ms_host": st.ms_host, "kernels": st.kernels}
 
     def beb_x(self, x, lastround: bool = True, want_lnfw: bool = False) -> dict:
         """beb() from codeml's x vector."""

@@ -158,13 +158,65 @@ __global__ void __launch_bounds__(256) beb_post_kernel(const double *__restrict_
     }
 }
 
+// posterior mean and second moment of the site's w: sum_g w_g sum_k ratio_k w_k(g)
+// (and w_k(g)^2), w_k the class's w at grid point g -- w0_i, 1, and w2_j for
+// both 2a and 2b (the foreground w; on an all-foreground tree the w of M2a's
+// class 2).  codeml's lfunNSsites_M2M8 (codeml.c:6331-6374) drops terms with
+// ratio w_k below 1e-300.  Same layout as beb_post_kernel; wv: the 21 w values.
+__global__ void __launch_bounds__(256) beb_omega_kernel(const double *__restrict__ F,
+                                                        const double *__restrict__ pcl,
+                                                        const double2 *__restrict__ wt,
+                                                        const double *__restrict__ wv, int npatt, int npad,
+                                                        double *__restrict__ mom) {
+    __shared__ double fs[8][BNW + 7];
+    __shared__ double ps[BNT * 4];
+    __shared__ double ws[BNE];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int i = threadIdx.x; i < BNT * 4; i += blockDim.x) ps[i] = pcl[i];
+    if (threadIdx.x < BNE) ws[threadIdx.x] = wv[threadIdx.x];
+    const int h = blockIdx.x * 8 + warp;
+    if (h < npatt)
+        for (int k = lane; k < BNW; k += 32) fs[warp][k] = F[(size_t)k * npad + h];
+    __syncthreads();
+    if (h >= npatt) return;
+    const double *f = fs[warp];
+    double m1 = 0.0, m2 = 0.0;
+    for (int g = lane; g < BNG; g += 32) {
+        int t, s0, s2a, s2b;
+        beb_sets(g, t, s0, s2a, s2b);
+        const double w = wt[g].x;
+        const double f0 = ps[t * 4 + 0] * f[s0], f1 = ps[t * 4 + 1] * f[BD];
+        const double f2 = ps[t * 4 + 2] * f[s2a], f3 = ps[t * 4 + 3] * f[s2b];
+        const double inv = 1.0 / (((f0 + f1) + f2) + f3);
+        const double om[4] = {ws[s0], 1.0, ws[s2b - BD * BD], ws[s2b - BD * BD]};
+        const double r[4] = {f0 * inv, f1 * inv, f2 * inv, f3 * inv};
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const double a = r[k] * om[k];
+            if (a >= 1e-300) {
+                m1 = fma(a, w, m1);
+                m2 = fma(a * om[k], w, m2);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        m1 += __shfl_down_sync(0xffffffffu, m1, o);
+        m2 += __shfl_down_sync(0xffffffffu, m2, o);
+    }
+    if (lane == 0) {
+        mom[h] = m1;
+        mom[(size_t)npad + h] = m2;
+    }
+}
+
 // device scratch of one gb_beb call, freed on every exit
 struct BebBuffers {
     double *eig = nullptr, *lnfw = nullptr, *F = nullptr, *mrow = nullptr, *pcl = nullptr;
-    double *lnfXs = nullptr, *post = nullptr;
+    double *lnfXs = nullptr, *post = nullptr, *wv = nullptr, *mom = nullptr;
     double2 *wt = nullptr;
     ~BebBuffers() {
-        void *p[] = {eig, lnfw, F, mrow, pcl, lnfXs, post, wt};
+        void *p[] = {eig, lnfw, F, mrow, pcl, lnfXs, post, wt, wv, mom};
         for (void *q : p)
             if (q) cudaFree(q);
     }
@@ -238,11 +290,12 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw_out, double *post_ou
     int rc = derive_scalars(h->pi.data(), m, &Dv[0]);
     if (rc) return fail(rc, "model parameters out of range");
     return gb_beb_qf(h, prm->blength, prm->kappa, Dv[0].qf, lnfw_out, post_out, grid_out, p0p1_out, lnfX_out,
-                     stats);
+                     nullptr, nullptr, stats);
 }
 
 int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qfactor[2], double *lnfw_out,
-              double *post_out, double *grid_out, double *p0p1_out, double *lnfX_out, gb_stats *stats) {
+              double *post_out, double *grid_out, double *p0p1_out, double *lnfX_out, double *wmean_out,
+              double *wsd_out, gb_stats *stats) {
     if (!h) return fail(GB_ERR_STATE, "null handle");
     if (!blength || !qfactor) return fail(GB_ERR_ARG, "null argument");
     if (h->precision != GB_PREC_FP64) return fail(GB_ERR_STATE, "gb_beb needs a GB_PREC_FP64 handle");
@@ -290,7 +343,7 @@ int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qf
     if ((rc = dalloc(&B.eig, eig.size())) || (rc = dalloc(&B.lnfw, (size_t)BNW * npad)) ||
         (rc = dalloc(&B.F, (size_t)BNW * npad)) || (rc = dalloc(&B.mrow, npad)) ||
         (rc = dalloc(&B.pcl, BNT * 4)) || (rc = dalloc(&B.lnfXs, BNG)) || (rc = dalloc(&B.post, 4 * npad)) ||
-        (rc = dalloc(&B.wt, BNG)))
+        (rc = dalloc(&B.wt, BNG)) || (rc = dalloc(&B.wv, BNE)) || (rc = dalloc(&B.mom, 2 * npad)))
         return rc;
     std::vector<double> pcl(BNT * 4);
     for (int t = 0; t < BNT; t++) triangle_classes(t, &pcl[t * 4]);
@@ -390,13 +443,26 @@ int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qf
             for (int k = 0; k < BD; k++) grid_out[j * BD + k] = j < 2 ? -1.0 : pp[j][k] / fX;
     if (p0p1_out)
         for (int k = 0; k < BNT; k++) p0p1_out[k] = pq[k] / fX;
-    if (post_out) {
-        std::vector<double2> wt(BNG);
+    const bool want_w = wmean_out || wsd_out;
+    std::vector<double2> wt(BNG);
+    if (post_out || want_w) {
         for (int g = 0; g < BNG; g++) {
             const double lw = lnfXs[g] - lfX;
             wt[g] = make_double2(std::exp(lw), std::exp(-300 - lw));
         }
         CK(cudaMemcpyAsync(B.wt, wt.data(), sizeof(double2) * BNG, cudaMemcpyHostToDevice, st));
+    }
+    std::vector<double> mom;
+    if (want_w) {
+        CK(cudaMemcpyAsync(B.wv, wv, sizeof(double) * BNE, cudaMemcpyHostToDevice, st));
+        beb_omega_kernel<<<(npatt + 7) / 8, 256, 0, st>>>(B.F, B.pcl, B.wt, B.wv, npatt, (int)npad, B.mom);
+        kernels++;
+        CK(cudaGetLastError());
+        mom.resize((size_t)2 * npatt);
+        CK(cudaMemcpy2DAsync(mom.data(), sizeof(double) * npatt, B.mom, sizeof(double) * npad,
+                             sizeof(double) * npatt, 2, cudaMemcpyDeviceToHost, st));
+    }
+    if (post_out) {
         beb_post_kernel<<<(npatt + 7) / 8, 256, 0, st>>>(B.F, B.pcl, B.wt, npatt, (int)npad, B.post);
         kernels++;
         CK(cudaGetLastError());
@@ -406,6 +472,12 @@ int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qf
     CK(cudaEventRecord(h->ev1, st));
     CK(cudaStreamSynchronize(st));
     CK(cudaGetLastError());
+    // mean and standard deviation of w (codeml.c:6370-6374)
+    for (int hh = 0; want_w && hh < npatt; hh++) {
+        const double m1 = mom[hh], m2 = mom[(size_t)npatt + hh] - m1 * m1;
+        if (wmean_out) wmean_out[hh] = m1;
+        if (wsd_out) wsd_out[hh] = m2 > 0 ? std::sqrt(m2) : 0.0;
+    }
     if (stats) {
         float ms = 0;
         cudaEventElapsedTime(&ms, h->ev0, h->ev1);
@@ -414,7 +486,7 @@ int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qf
         stats->kernels = kernels;
         stats->nscale = h->nscale;
         stats->h2d_bytes = sizeof(double) * (eig.size() + pcl.size() + h->nnode) + sizeof(DevParams) +
-                           (post_out ? sizeof(double2) * BNG : 0);
+                           (post_out || want_w ? sizeof(double2) * BNG : 0);
         stats->d2h_bytes = sizeof(double) * (npatt + BNG + (lnfw_out ? (size_t)BNW * npatt : 0) +
                                              (post_out ? 4 * npatt : 0));
     }

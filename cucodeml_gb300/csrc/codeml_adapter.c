@@ -131,7 +131,7 @@ int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], 
     h = make_handle("GB_BEB (one gene, cleandata = 1, universal code only)");
     /* kappa from x, the Qfactors of the last SetParameters (at the MLE), as
        codeml's BEB reads them (GetPMatBranch treesub.c:7289-7301): models A and B */
-    rc = gb_beb_qf(h, bl, x[com.ntime], Qfactor_NS_branch, NULL, postSite, grid, p0p1, lnfX, NULL);
+    rc = gb_beb_qf(h, bl, x[com.ntime], Qfactor_NS_branch, NULL, postSite, grid, p0p1, lnfX, NULL, NULL, NULL);
     gb_destroy(h);
     free(bl);
     if (rc) gb_die("gb_beb", rc);

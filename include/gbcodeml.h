@@ -207,10 +207,15 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw, double *post, doubl
  * which its BEB reads at the MLE, GetPMatBranch treesub.c:7289-7301) instead
  * of derived from model A's parameters: the same analysis for branch-site
  * model B, whose Qfactors involve its free w1 (codeml runs model A's BEB grid
- * for it).  blength[nnode]: branch lengths by node.
+ * for it).  blength[nnode]: branch lengths by node.  wmean[npatt], wsd[npatt]
+ * (each may be NULL): the posterior mean and standard deviation of the site's
+ * w, taking w0_i, 1 and w2_j as the w of classes 0, 1 and 2a/2b -- on a tree
+ * with every branch in the foreground, the "post mean +- SE for w" codeml
+ * prints for M2a (lfunNSsites_M2M8 codeml.c:6331-6374).
  */
 int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qfactor[2], double *lnfw,
-              double *post, double *grid, double *p0p1, double *lnfX, gb_stats *stats);
+              double *post, double *grid, double *p0p1, double *lnfX, double *wmean, double *wsd,
+              gb_stats *stats);
 
 /*
  * Naive empirical Bayes (NEB) posteriors of the four site classes at prm, as

@@ -544,10 +544,14 @@ static void beb_omega_set(int iw, int *eb, int *ef) {
  *                    computed), w0, w2 (codeml's "Posterior on the grid")
  *   p0p1[100]        posterior over the ternary (p0, p1) triangles
  *   lnfX[3]          log f(X) as codeml prints it, and its scale terms S1, S2
+ *   wmean, wsd[npatt] posterior mean and SD of the site's w with classes 0,
+ *                    1, 2a, 2b at w0_i, 1, w2_j, w2_j (M2a's "post mean +- SE
+ *                    for w" on an all-foreground tree, lfunNSsites_M2M8
+ *                    codeml.c:6331-6374)
  * Returns 0, or -1 on a parameter error.
  */
 int oracle_beb(const oracle_problem *pb, const double *x, int lastround, double *lnfw_out,
-               double *post, double *grid, double *p0p1, double *lnfX) {
+               double *post, double *grid, double *p0p1, double *lnfX, double *wmean, double *wsd) {
     int n = NC, np = pb->npatt, nn = pb->nnode;
     params_t *P = (params_t *)malloc(sizeof(params_t));
     if (set_params(pb, x, lastround, P)) { free(P); return -1; }
@@ -684,6 +688,30 @@ int oracle_beb(const oracle_problem *pb, const double *x, int lastround, double 
                 }
             }
             for (int k = 0; k < 4; k++) post[k * np + h] = acc[k];
+        }
+    }
+    /* posterior mean and SD of w: terms exp(log(ratio w) + lnfXs - log f(X)),
+       skipped where ratio w < 1e-300 (codeml.c:6358-6374) */
+    if (wmean || wsd) {
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int h = 0; h < np; h++) {
+            double m1 = 0, m2 = 0;
+            for (int g = 0; g < BEB_NG; g++) {
+                int ip2 = (g / BEB_D) % BEB_D, ip3 = g % BEB_D;
+                double om[4] = {wv[ip2], 1, wv[BEB_D + 1 + ip3], wv[BEB_D + 1 + ip3]};
+                double fk[4], fh = 0;
+                for (int k = 0; k < 4; k++)
+                    fh += fk[k] = pcl[g * 4 + k] * F[(size_t)iwg[g * 4 + k] * np + h];
+                for (int k = 0; k < 4; k++) {
+                    double r = fk[k] / fh, a = r * om[k];
+                    if (!(a >= 1e-300)) continue;
+                    m1 += exp(log(a) + lnfXs[g] - lfX);
+                    m2 += exp(log(a * om[k]) + lnfXs[g] - lfX);
+                }
+            }
+            double v = m2 - m1 * m1;
+            if (wmean) wmean[h] = m1;
+            if (wsd) wsd[h] = v > 0 ? sqrt(v) : 0;
         }
     }
     free(P); free(U); free(V); free(R); free(Q); free(scale); free(tnode); free(Pall);

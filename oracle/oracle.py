@@ -58,7 +58,7 @@ def lib():
         L.oracle_pmat.argtypes = [dp, C.c_double, dp, dp, dp]
         L.oracle_max_threads.restype = C.c_int
         L.oracle_beb.restype = C.c_int
-        L.oracle_beb.argtypes = [C.POINTER(_Problem), dp, C.c_int, dp, dp, dp, dp, dp]
+        L.oracle_beb.argtypes = [C.POINTER(_Problem), dp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -152,14 +152,16 @@ class Problem:
         grid = np.zeros(40)
         p0p1 = np.zeros(100)
         fx = np.zeros(3)
+        wmean = np.zeros(self.npatt)
+        wsd = np.zeros(self.npatt)
         rc = lib().oracle_beb(C.byref(self._s), _dp(x), int(lastround),
                               _dp(lnfw) if lnfw is not None else None, _dp(post), _dp(grid),
-                              _dp(p0p1), _dp(fx))
+                              _dp(p0p1), _dp(fx), _dp(wmean), _dp(wsd))
         if rc:
             raise ValueError("parameter error")
         return {"lnfw": lnfw.reshape(121, self.npatt) if lnfw is not None else None,
                 "post": post.reshape(4, self.npatt), "grid": grid.reshape(4, 10), "p0p1": p0p1,
-                "lnfX": fx[0], "S1": fx[1], "S2": fx[2]}
+                "lnfX": fx[0], "S1": fx[1], "S2": fx[2], "wmean": wmean, "wsd": wsd}
 
 
     def neb(self, x, lastround: bool = True):

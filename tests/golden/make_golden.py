@@ -157,6 +157,7 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
         if site_model == "M2a":       # BEB of M2a (lfunNSsites_M2M8 codeml.c:6190-6415): 3 classes
             extra["beb"] = parse_beb(out, rst, r.stdout, ncls=3)
+            extra["beb"]["site_wmean_sd_3dp"] = parse_site_meanw(rst)
     elif model_b:
         extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns), "neb_site_post_5dp": parse_site_post(rst, "Naive"),
                  "beb": parse_beb(out, rst, r.stdout)}
@@ -222,6 +223,19 @@ def parse_site_post(rst: str, which: str, ncls: int = 4) -> list:
             break
         site.append([float(v) for v in parts[2:2 + ncls]])
     return site
+
+
+def parse_site_meanw(rst: str) -> list:
+    """The BEB block's per-site posterior mean and SD of w ("x +- y", 3 dp)
+    that codeml prints for the site models (PrintProbNSsites codeml.c:5000-5016)."""
+    i0 = rst.index("Bayes Empirical Bayes (BEB) probabilities")
+    out = []
+    for ln in rst[i0:].splitlines()[3:]:
+        m = re.search(r"\)\s+(-?\d+\.\d+)\s+\+-\s+(-?\d+\.\d+)", ln)
+        if not ln.split() or not ln.split()[0].isdigit() or not m:
+            break
+        out.append([float(m.group(1)), float(m.group(2))])
+    return out
 
 
 def parse_beb(out: str, rst: str, stdout: str, ncls: int = 4) -> dict:

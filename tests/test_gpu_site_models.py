@@ -49,11 +49,22 @@ def test_m2a_beb(name):
     fx, tree, codons = load_golden(name)
     z, fpatt, pi = O.patterns(codons)
     t, x = as_model_a(fx, tree)
+    pb = O.Problem(t, z, fpatt, pi, nthreads=4)
+    ref = pb.beb(x)
+    qf = pb.set_params(x)[3]
     lk = api.Likelihood(t, z, fpatt, pi)
-    r = lk.beb_x(x)
+    nb = t.nbranch
+    bl = np.zeros(t.nnode)
+    bl[t.branch_nodes()] = x[:nb]
+    r = lk.beb_qf(bl, x[nb], qf)
     post = np.stack([r["post"][0], r["post"][1], r["post"][2] + r["post"][3]])
     g = fx["beb"]
-    site = post[:, site_patterns(z, codons)].T
+    pose = site_patterns(z, codons)
+    site = post[:, pose].T
     assert np.max(np.abs(site - np.array(g["site_post_5dp"]))) <= 5.01e-6
     assert abs(r["lnfX"] - g["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])
+    assert np.max(np.abs(r["wmean"] - ref["wmean"])) <= 1e-8
+    assert np.max(np.abs(r["wsd"] - ref["wsd"])) <= 1e-6
+    ms = np.stack([r["wmean"], r["wsd"]])[:, pose].T
+    assert np.max(np.abs(ms - np.array(g["site_wmean_sd_3dp"]))) <= 5.01e-4
     lk.close()

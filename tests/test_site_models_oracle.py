@@ -52,3 +52,6 @@ def test_m2a_beb_as_model_a(name):
     assert np.max(np.abs(r["grid"][3] - g["w2_post_3dp"])) <= 5.01e-4
     assert np.max(np.abs(r["p0p1"] - g["p0p1_post_3dp"])) <= 5.01e-4
     assert abs(r["lnfX"] - g["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])
+    # the posterior mean and SD of w codeml prints beside them (3 dp)
+    ms = np.stack([r["wmean"], r["wsd"]])[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(ms - np.array(g["site_wmean_sd_3dp"]))) <= 5.01e-4

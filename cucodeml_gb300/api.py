@@ -147,6 +147,28 @@ class Likelihood:
                                        _ptr(lnf) if want_site else None, C.byref(st)))
         return EvalResult(f.value, fhK, lnf, None, st.ms_device, st.ms_host, st.kernels)
 
+    def clade_uvr(self, U, V, Root, qfactor, freqK, blength):
+        """Clade models C / D with two branch types from the host's eigen
+        solutions of (w0, w1, w2 background, w3 foreground) -- codeml's
+        _UU/_VV/_Root[0..3] and Qfactor_NS_branch.  Classes 0 and 1 are model
+        A's with slots (w0, w1, -), the third is model A's class 2a with
+        slots (w2, w1, w3): two gb_eval_uvr calls, then codeml's mixture of
+        the three classes (lfundG treesub.c:7342-7394).  Returns
+        (-lnL, fhK [3, npatt], lnf)."""
+        fk4 = np.full(4, 0.25)           # the calls' own mixture is not used
+        a = self.neg_lnL_uvr(U[:3], V[:3], Root[:3], qfactor, fk4, blength)
+        b = self.neg_lnL_uvr([U[2], U[1], U[3]], [V[2], V[1], V[3]], [Root[2], Root[1], Root[3]],
+                             qfactor, fk4, blength)
+        fhK = np.stack([a.fhK[0], a.fhK[1], b.fhK[2]])
+        fk = np.asarray(freqK, dtype=np.float64)[:3]
+        if self.nscale:
+            t = fhK.max(axis=0)
+            lnf = t + np.log((fk[:, None] * np.exp(fhK - t)).sum(axis=0))
+        else:
+            sm = (fk[:, None] * fhK).sum(axis=0)
+            lnf = np.log(np.where(sm <= 0, 1e-300, sm))
+        return -float((lnf * self._fpatt).sum()), fhK, lnf
+
     def evaluate(self, blength, kappa, omega0, omega2, p0, p1, grad: bool = False,
                  want_site: bool = False) -> EvalResult:
         bl = np.ascontiguousarray(blength, dtype=np.float64)

@@ -719,6 +719,48 @@ int oracle_beb(const oracle_problem *pb, const double *x, int lastround, double 
     return 0;
 }
 
+/*
+ * Per-class fhK (as oracle_lnL writes it) from given eigen solutions: U, V
+ * [3][61*61], Root [3][61] (model A's slots w0, w1, w2), Qfactors qf[2] and
+ * branch lengths by branch index (x[0..nb-1]); the classes follow model A's
+ * map (Set_UVR_BranchSite codeml.c:2555-2558).  Used to restate models whose
+ * classes are model-A classes of different eigen slots (clade model C: its
+ * third class is class 2a with slots (w2, -, w3)).  Returns nscale.
+ */
+int oracle_fhK_uvr(const oracle_problem *pb, const double *U, const double *V, const double *Root,
+                   const double *qf, const double *xb, double *fhK) {
+    int n = NC, np = pb->npatt, nn = pb->nnode;
+    params_t *P = (params_t *)malloc(sizeof(params_t));
+    for (int i = 0; i < 3; i++) {
+        memcpy(P->U[i], U + i * NC * NC, sizeof(double) * NC * NC);
+        memcpy(P->V[i], V + i * NC * NC, sizeof(double) * NC * NC);
+        memcpy(P->Root[i], Root + i * NC, sizeof(double) * NC);
+    }
+    P->qf[0] = qf[0];
+    P->qf[1] = qf[1];
+    char *scale = (char *)calloc(nn, 1);
+    int nscale = 0;
+    set_node_scale(pb, pb->root, scale, &nscale);
+    double *Pall = (double *)malloc(sizeof(double) * nn * n * n);
+    double *conP = (double *)malloc(sizeof(double) * (size_t)nn * np * n);
+    double *scaleF = (double *)calloc((size_t)nn * np, sizeof(double));
+    double *tnode = (double *)calloc(nn, sizeof(double));
+    double *lf = (double *)malloc(sizeof(double) * np);
+    for (int ib = 0; ib < nn - 1; ib++) tnode[pb->bnode[ib]] = xb[ib];
+    for (int ir = 0; ir < 4; ir++) {
+        for (int i = 0; i < nn; i++) {
+            if (i == pb->root) continue;
+            int lab = pb->label[i];
+            int iuvr = lab == 0 ? ir % 2 : (ir <= 1 ? ir : 2);
+            pmat(Pall + (size_t)i * n * n, tnode[i] * P->qf[lab], P->U[iuvr], P->V[iuvr], P->Root[iuvr]);
+        }
+        root_logf(pb, Pall, scale, conP, scaleF, lf);
+        for (int h = 0; h < np; h++) fhK[ir * np + h] = nscale ? lf[h] : exp(lf[h]);
+    }
+    free(P); free(scale); free(Pall); free(conP); free(scaleF); free(tnode); free(lf);
+    return nscale;
+}
+
 /* Model quantities codeml derives from x, for parity tests of the CUDA
    library's own host set-up: U,V,Root (3 sets, 61x61 row-major), qf[2],
    freqK[4]. */

@@ -57,6 +57,8 @@ def lib():
         L.oracle_pmat.restype = None
         L.oracle_pmat.argtypes = [dp, C.c_double, dp, dp, dp]
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_fhK_uvr.restype = C.c_int
+        L.oracle_fhK_uvr.argtypes = [C.POINTER(_Problem), dp, dp, dp, dp, dp, dp]
         L.oracle_beb.restype = C.c_int
         L.oracle_beb.argtypes = [C.POINTER(_Problem), dp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
         _lib = L
@@ -163,6 +165,48 @@ class Problem:
                 "post": post.reshape(4, self.npatt), "grid": grid.reshape(4, 10), "p0p1": p0p1,
                 "lnfX": fx[0], "S1": fx[1], "S2": fx[2], "wmean": wmean, "wsd": wsd}
 
+
+    def fhK_uvr(self, U, V, R, qf, xb):
+        """Per-class fhK (4, npatt) from given eigen slots, Qfactors and branch
+        lengths by branch index (oracle.c oracle_fhK_uvr); also nscale."""
+        U = np.ascontiguousarray(U, dtype=np.float64)
+        V = np.ascontiguousarray(V, dtype=np.float64)
+        R = np.ascontiguousarray(R, dtype=np.float64)
+        qf = np.ascontiguousarray(qf, dtype=np.float64)
+        xb = np.ascontiguousarray(xb, dtype=np.float64)
+        fhK = np.zeros(4 * self.npatt)
+        nsc = lib().oracle_fhK_uvr(C.byref(self._s), _dp(U), _dp(V), _dp(R), _dp(qf), _dp(xb), _dp(fhK))
+        return fhK.reshape(4, self.npatt), nsc
+
+    def clade_c(self, x):
+        """Clade model C (codeml model = 3, NSsites = 2, two branch types) at x =
+        [branch lengths, kappa, p0, p1, w0, w2 (background), w3 (foreground)]:
+        classes w0 and w1 = 1 on every branch and (w2, w3) by branch type,
+        Qfactor_NS_branch[b] = 1 / meanrate(Q(kappa, p0 w0 + p1 + p2 w_{2+b}))
+        (SetParametersNSsites codeml.c:2437-2446, 2522-2539).  Classes 0 and 1
+        are model A's with slots (w0, 1, -), the third is model A's class 2a
+        with slots (w2, -, w3).  Returns (-lnL, fhK [3, npatt], lnf)."""
+        x = np.asarray(x, dtype=np.float64)
+        nb = self.tree.nbranch
+        kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+        p2 = 1.0 - p0 - p1
+        Ua, Va, Ra, _, _ = self.set_params(np.concatenate([x[:nb], [kappa, p0, p1, w0, w2]]))
+        U3, V3, R3, _, _ = self.set_params(np.concatenate([x[:nb], [kappa, p0, p1, w0, w3]]))
+        qf = np.array([1.0 / build_q(self.pi, kappa, p0 * w0 + p1 + p2 * w)[1] for w in (w2, w3)])
+        fa, nsc = self.fhK_uvr(Ua, Va, Ra, qf, x[:nb])
+        Ub = np.stack([Ua[2], Ua[1], U3[2]])
+        Vb = np.stack([Va[2], Va[1], V3[2]])
+        Rb = np.stack([Ra[2], Ra[1], R3[2]])
+        fb, _ = self.fhK_uvr(Ub, Vb, Rb, qf, x[:nb])
+        fhK = np.stack([fa[0], fa[1], fb[0 + 2]])
+        fk = np.array([p0, p1, p2])
+        if nsc:
+            t = fhK.max(axis=0)
+            lnf = t + np.log((fk[:, None] * np.exp(fhK - t)).sum(axis=0))
+        else:
+            s = (fk[:, None] * fhK).sum(axis=0)
+            lnf = np.log(np.where(s <= 0, 1e-300, s))
+        return -float((lnf * self.fpatt).sum()), fhK, lnf
 
     def neb(self, x, lastround: bool = True):
         """NEB posteriors of the four site classes at x (lfunNSsites_rate

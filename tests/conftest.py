@@ -19,7 +19,7 @@ def pytest_configure(config):
 def golden_names():
     """Fixed-parameter model-A fixtures (codeml lnL and per-pattern log f at given x)."""
     return sorted(f[:-5] for f in os.listdir(GOLDEN)
-                  if f.endswith(".json") and not f.startswith(("mle_", "mb", "ms")))
+                  if f.endswith(".json") and not f.startswith(("mle_", "mb", "ms", "mc")))
 
 
 def site_model_names():
@@ -44,6 +44,11 @@ def as_model_a(fx, tree):
         kappa, p0, w0 = x[nb:nb + 3]
         x = np.concatenate([x[:nb], [kappa, p0, 1.0 - p0, w0, 1.0]])
     return t, x
+
+
+def clade_names():
+    """Fixed-parameter fixtures under clade model C (two branch types)."""
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("mc") and f.endswith(".json"))
 
 
 def model_b_names():

@@ -36,6 +36,8 @@ SEs are the square roots of the diagonal of its negated inverse
 codeml runs the same BEB for model B (lfunNSsites_ACD treats model = 2 as
 model A's grid, w1 = 1 in class 1, with model B's Qfactors), kept for the
 mb* fixtures too.
+The mcC* fixtures are clade model C (model = 3, NSsites = 2; branch types
+#1 and background; x ends p0, p1, w0, w2, w3), lnL, log f and NG86 only.
 The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
 x ends p0, p1, w0, w2 for M2a and p0, w0 for M1a): lnL, log f, NG86, and
 for M2a codeml's BEB (three classes).
@@ -122,7 +124,16 @@ CASES_SITE = [
 ]
 
 
-def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b=False, site_model=None):
+# clade model C (model = 3, NSsites = 2, two branch types: #1 and the rest):
+# evaluation params (kappa, p0, p1, w0, w2 background, w3 foreground)
+CASES_CLADE = [
+    ("mcC8x300_s12", 8, 300, 12, ModelA(), (2.0, 0.5, 0.3, 0.2, 0.8, 3.0), 1.0),
+    ("mcC24x400_s13", 24, 400, 13, ModelA(kappa=2.5, omega2=4.0), (2.4, 0.45, 0.35, 0.1, 1.5, 4.0), 1.0),
+]
+
+
+def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b=False, site_model=None,
+             clade=False):
     aln = simulate(ns, ncodon, seed=seed, model=model)
     tree = aln.tree
     if site_model:
@@ -142,18 +153,22 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         if site_model:
             ctl = CTL.replace("model = 2", "model = 0").replace(
                 "NSsites = 2", "NSsites = " + {"M1a": "1", "M2a": "2"}[site_model])
+        if clade:
+            ctl = CTL.replace("model = 2", "model = 3")
         with open(os.path.join(d, "codeml.ctl"), "w") as f:
             f.write(ctl)
         r = subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
         out = open(os.path.join(d, "out.txt")).read()
         lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
         rst = open(os.path.join(d, "rst")).read()
-        if not model_b and not site_model:
+        if not model_b and not site_model and not clade:
             with open(os.path.join(d, "codeml.ctl"), "w") as f:
                 f.write(CTL.replace("getSE = 0", "getSE = 1"))
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
-    if site_model:
+    if clade:
+        extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns)}
+    elif site_model:
         extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
         if site_model == "M2a":       # BEB of M2a (lfunNSsites_M2M8 codeml.c:6190-6415): 3 classes
             extra["beb"] = parse_beb(out, rst, r.stdout, ncls=3)
@@ -262,7 +277,8 @@ def main():
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
     codeml = os.path.join(ROOT, "oracle", "_ref", "codeml")
     outdir = os.path.dirname(os.path.abspath(__file__))
-    for case in CASES + [c + (True,) for c in CASES_B] + [c[:7] + (False, c[7]) for c in CASES_SITE]:
+    for case in (CASES + [c + (True,) for c in CASES_B] + [c[:7] + (False, c[7]) for c in CASES_SITE]
+                 + [c + (False, None, True) for c in CASES_CLADE]):
         fx = run_case(codeml, *case)
         with open(os.path.join(outdir, fx["name"] + ".json"), "w") as f:
             json.dump(fx, f, separators=(",", ":"))

@@ -1,0 +1,43 @@
+"""Clade model C on the GPU: two gb_eval_uvr calls (classes 0, 1 with eigen
+slots (w0, 1, -); class 2 as model A's class 2a with slots (w2, 1, w3)), the
+route codeml's adapter takes for model = 3, against the oracle's restatement
+(pinned to codeml in tests/test_clade_oracle.py) and codeml's printed lnL.
+
+Bars as for model A's gb_eval_uvr test: with the oracle's eigen solutions,
+lnL within 1e-12 relative and log f within 1e-11 of the oracle; 1e-9
+relative of codeml's lnL.
+"""
+import numpy as np
+import pytest
+
+from cucodeml_gb300 import api
+from oracle import oracle as O
+from tests.conftest import clade_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("name", clade_names())
+def test_clade_c_eval_uvr(name):
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+    p2 = 1 - p0 - p1
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=4)
+    v, fhK, lnf = pb.clade_c(x)
+    Ua, Va, Ra, _, _ = pb.set_params(np.concatenate([x[:nb], [kappa, p0, p1, w0, w2]]))
+    U3, V3, R3, _, _ = pb.set_params(np.concatenate([x[:nb], [kappa, p0, p1, w0, w3]]))
+    U = [Ua[0], Ua[1], Ua[2], U3[2]]
+    V = [Va[0], Va[1], Va[2], V3[2]]
+    R = [Ra[0], Ra[1], Ra[2], R3[2]]
+    qf = np.array([1.0 / O.build_q(pi, kappa, p0 * w0 + p1 + p2 * w)[1] for w in (w2, w3)])
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[:nb]
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    f, g_fhK, g_lnf = lk.clade_uvr(U, V, R, qf, [p0, p1, p2], bl)
+    assert abs(f - v) <= 1e-12 * abs(v)
+    assert np.max(np.abs(g_lnf - lnf)) <= 1e-11
+    assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+    lk.close()

@@ -13,6 +13,9 @@
  *                                  classes on the GPU from codeml's _UU/_VV/_Root,
  *                                  Qfactor_NS_branch and com.freqK; every call
  *                                  copies its class into com.fhK + ir*npatt.
+ *                                  Clade models C/D (model = 3, two branch
+ *                                  types): a second evaluation with slots
+ *                                  (w2, w1, w3) gives their third class.
  *   CUDA_FreeAll                   replaces cuda-codeml.cu:1162 (codeml.c:695).
  *   GB_dfun                        new: ming2's gradient hook
  *                                  (tools.c:6361-6363, `dfun`), the analytic

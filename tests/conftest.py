@@ -32,7 +32,8 @@ def as_model_a(fx, tree):
     it: every branch labelled foreground, so site classes 2a and 2b both carry
     w2 on every branch and together weigh 1 - p0 - p1 (M2a); M1a is that with
     p1 = 1 - p0 (no w2 class; w2 then carries no weight and is set to 1).
-    Returns (tree with labels, model-A x)."""
+    M3 with three classes (free w0, w1, w2) is model B on that tree, with x
+    unchanged (model B's layout).  Returns (tree with labels, x)."""
     import copy
 
     t = copy.deepcopy(tree)

@@ -39,8 +39,9 @@ mb* fixtures too.
 The mcC* fixtures are clade model C (model = 3, NSsites = 2; branch types
 #1 and background; x ends p0, p1, w0, w2, w3), lnL, log f and NG86 only.
 The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
-x ends p0, p1, w0, w2 for M2a and p0, w0 for M1a): lnL, log f, NG86, and
-for M2a codeml's BEB (three classes).
+x ends p0, p1, w0, w2 for M2a, p0, w0 for M1a, p0, p1, w0, w1, w2 for M3
+with three classes): lnL, log f, NG86, and for M2a codeml's BEB (three
+classes).
 The mb_* fixtures are the same evaluation under branch-site model B
 (NSsites = 3, ncatG = 3: w1 free; x ends w0, w1, w2), lnL and log f only.
 
@@ -121,6 +122,7 @@ CASES_SITE = [
     ("msM2a8x300_s9", 8, 300, 9, ModelA(), (2.0, 0.6, 0.3, 0.2, 2.5), 1.0, "M2a"),
     ("msM2a24x400_s10", 24, 400, 10, ModelA(omega2=4.0), (2.2, 0.5, 0.35, 0.15, 3.5), 1.0, "M2a"),
     ("msM1a12x300_s11", 12, 300, 11, ModelA(), (2.0, 0.7, 0.25), 1.0, "M1a"),
+    ("msM3k3x8x300_s14", 8, 300, 14, ModelA(), (2.0, 0.5, 0.3, 0.1, 0.6, 2.5), 1.0, "M3"),
 ]
 
 
@@ -152,7 +154,9 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         ctl = CTL.replace("NSsites = 2", "NSsites = 3").replace("ncatG = 4", "ncatG = 3") if model_b else CTL
         if site_model:
             ctl = CTL.replace("model = 2", "model = 0").replace(
-                "NSsites = 2", "NSsites = " + {"M1a": "1", "M2a": "2"}[site_model])
+                "NSsites = 2", "NSsites = " + {"M1a": "1", "M2a": "2", "M3": "3"}[site_model])
+            if site_model == "M3":
+                ctl = ctl.replace("ncatG = 4", "ncatG = 3")
         if clade:
             ctl = CTL.replace("model = 2", "model = 3")
         with open(os.path.join(d, "codeml.ctl"), "w") as f:

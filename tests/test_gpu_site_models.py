@@ -24,12 +24,17 @@ def test_site_model_fp64(name):
     fx, tree, codons = load_golden(name)
     z, fpatt, pi = O.patterns(codons)
     t, x = as_model_a(fx, tree)
-    pb = O.Problem(t, z, fpatt, pi, nthreads=4)
+    m3 = fx["model"] == "M3"
+    pb = O.Problem(t, z, fpatt, pi, nthreads=4, model_b=m3)
     lk = api.Likelihood(t, z, fpatt, pi)
     nb = t.nbranch
     bl = np.zeros(t.nnode)
     bl[t.branch_nodes()] = x[:nb]
-    r = lk.evaluate(bl, x[nb], x[nb + 3], x[nb + 4], x[nb + 1], x[nb + 2], want_site=True)
+    if m3:      # model B on the all-foreground tree: the drop-in's gb_eval_uvr
+        U, V, R, qf, fk = pb.set_params(x)
+        r = lk.neg_lnL_uvr(U, V, R, qf, fk, bl)
+    else:
+        r = lk.evaluate(bl, x[nb], x[nb + 3], x[nb + 4], x[nb + 1], x[nb + 2], want_site=True)
     assert abs(-r.neg_lnL - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     ref = np.array(fx["lnf"])
     assert np.all(np.abs(r.lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))

@@ -8,9 +8,10 @@ labelled #1 has the same mixture: classes 0 and 1 are w0 and 1 everywhere,
 classes 2a and 2b are both w2 everywhere with weights summing to p2, and the
 foreground Qfactor is the same mean-rate normalisation.  M1a is M2a with
 p2 = 0.  So the model-A machinery (oracle, FP64 drop-in, adjoint, split
-precision) evaluates them unchanged.  Pinned here: the oracle under that
-mapping against the reference codeml's own fixed-parameter runs of M2a and
-M1a (tests/golden/ms*.json).
+precision) evaluates them unchanged.  M3 with three classes (w0, w1, w2
+free) is, the same way, model B on the all-foreground tree.  Pinned here:
+the oracle under that mapping against the reference codeml's own
+fixed-parameter runs of M2a, M1a and M3 (tests/golden/ms*.json).
 """
 import numpy as np
 import pytest
@@ -25,7 +26,7 @@ def test_site_model_as_model_a_matches_codeml(name):
     assert np.all(tree.label == 0)
     z, fpatt, pi = O.patterns(codons)
     t, x = as_model_a(fx, tree)
-    pb = O.Problem(t, z, fpatt, pi, nthreads=2)
+    pb = O.Problem(t, z, fpatt, pi, nthreads=2, model_b=fx["model"] == "M3")
     v, fhK, lnf, nscale = pb.neg_lnL(x, lastround=True, want_fhK=True)
     assert abs(-v - fx["codeml_lnL"]) <= 5.1e-7 + 1e-12 * abs(v)
     assert abs(-v - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9

@@ -81,6 +81,11 @@ static gb_handle *make_handle(const char *who) {
 void CUDA_Init(double *x) {
     int i;
     (void)x;
+    /* the models whose site classes map onto the library's: branch-site A, B
+       (model = 2) and clade C, D with two branch types (model = 3); codeml's
+       other models never set up the per-class eigen slots this reads */
+    if (!((com.model == 2 || (com.model == 3 && com.nbtype == 2)) && (com.NSsites == 2 || com.NSsites == 3)))
+        gb_die("CUDA_Init (branch-site models A/B or clade models C/D with two branch types only)", GB_ERR_ARG);
     g_blen = (double *)malloc(sizeof(double) * tree.nnode);
     g_bnode = (int *)malloc(sizeof(int) * tree.nnode);
     g_fhK = (double *)malloc(sizeof(double) * 4 * com.npatt);

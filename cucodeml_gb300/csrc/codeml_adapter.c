@@ -144,6 +144,9 @@ int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], 
     gb_handle *h;
     double *bl;
     if (np < com.ntime + 1) gb_die("GB_BEB (parameter vector)", GB_ERR_ARG);
+    /* model A's grid (lfunNSsites_ACD uses it for model = 2, A and B); the
+       clade models' grids differ */
+    if (com.model != 2) gb_die("GB_BEB (branch-site models A and B only)", GB_ERR_ARG);
     bl = (double *)calloc(tree.nnode, sizeof(double));
     if (!bl) gb_die("GB_BEB (host memory)", GB_ERR_OOM);
     for (i = 0; i < tree.nnode; i++)

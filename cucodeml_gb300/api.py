@@ -147,6 +147,43 @@ class Likelihood:
                                        _ptr(lnf) if want_site else None, C.byref(st)))
         return EvalResult(f.value, fhK, lnf, None, st.ms_device, st.ms_host, st.kernels)
 
+    def site_model(self, blength, kappa, omegas, props):
+        """A site model with K classes (codeml model = 0: M1a, M2a, M3, M7,
+        M8, ...): class k has omegas[k] on every branch and weight props[k],
+        Qfactor_NS = 1 / meanrate(Q(kappa, sum props omegas))
+        (SetParametersNSsites codeml.c:2466-2487).  The handle's tree must
+        have every branch labelled foreground: each gb_eval_uvr call then
+        prunes three classes (eigen slots 0, 1, 2), so K classes take
+        ceil(K / 3) calls; the mixture follows codeml's lfundG.  Eigen
+        solutions from the library's host code.  Returns (-lnL, fhK [K,
+        npatt], lnf)."""
+        lab = np.asarray(self.tree.label).copy()
+        lab[self.tree.root] = 1
+        if not np.all(lab == 1):
+            raise ValueError("site_model needs every branch labelled foreground")
+        om = np.asarray(omegas, dtype=np.float64)
+        pr = np.asarray(props, dtype=np.float64)
+        U, V, R, _, _ = model_setup(self._pi, kappa, float(pr @ om), 1.0, 0.5, 0.3)
+        mr = -float(np.sum(self._pi * np.einsum("im,m,mi->i", U[0], R[0], V[0])))
+        qf = np.array([1.0 / mr, 1.0 / mr])
+        eig = [model_setup(self._pi, kappa, float(w), 1.0, 0.5, 0.3) for w in om]
+        fk4 = np.full(4, 0.25)
+        rows = []
+        for c in range(0, len(om), 3):
+            grp = list(range(c, min(c + 3, len(om))))
+            sl = grp + [grp[-1]] * (3 - len(grp))
+            r = self.neg_lnL_uvr([eig[k][0][0] for k in sl], [eig[k][1][0] for k in sl],
+                                 [eig[k][2][0] for k in sl], qf, fk4, blength)
+            rows += [r.fhK[0], r.fhK[1], r.fhK[2]][: len(grp)]
+        fhK = np.stack(rows)
+        if self.nscale:
+            t = fhK.max(axis=0)
+            lnf = t + np.log((pr[:, None] * np.exp(fhK - t)).sum(axis=0))
+        else:
+            sm = (pr[:, None] * fhK).sum(axis=0)
+            lnf = np.log(np.where(sm <= 0, 1e-300, sm))
+        return -float((lnf * self._fpatt).sum()), fhK, lnf
+
     def clade_uvr(self, U, V, Root, qfactor, freqK, blength):
         """Clade models C / D with two branch types from the host's eigen
         solutions of (w0, w1, w2 background, w3 foreground) -- codeml's

@@ -208,6 +208,32 @@ class Problem:
             lnf = np.log(np.where(s <= 0, 1e-300, s))
         return -float((lnf * self.fpatt).sum()), fhK, lnf
 
+    def site_classes(self, xb, kappa, omegas, props):
+        """A site model with K classes (codeml model = 0): class k has omega
+        omegas[k] on every branch and weight props[k]; Qfactor_NS =
+        1 / meanrate(Q(kappa, sum props omegas)) (SetParametersNSsites
+        codeml.c:2466-2487).  Needs every branch labelled foreground: each
+        oracle_fhK_uvr call then yields three classes (slots 0, 1 and 2).
+        Returns (-lnL, fhK [K, npatt], lnf)."""
+        om = np.asarray(omegas, dtype=np.float64)
+        pr = np.asarray(props, dtype=np.float64)
+        qns = 1.0 / build_q(self.pi, kappa, float(pr @ om))[1]
+        eig = Problem(self.tree, self.z, self.fpatt, self.pi, nthreads=1, model_b=True)
+        rows = []
+        for c in range(0, len(om), 3):
+            w = list(om[c:c + 3]) + [1.0] * (3 - len(om[c:c + 3]))
+            U, V, R, _, _ = eig.set_params(np.concatenate([xb, [kappa, 0.3, 0.3], w]))
+            f, nsc = self.fhK_uvr(U, V, R, [qns, qns], xb)
+            rows += [f[0], f[1], f[2]][: len(om[c:c + 3])]
+        fhK = np.stack(rows)
+        if nsc:
+            t = fhK.max(axis=0)
+            lnf = t + np.log((pr[:, None] * np.exp(fhK - t)).sum(axis=0))
+        else:
+            sm = (pr[:, None] * fhK).sum(axis=0)
+            lnf = np.log(np.where(sm <= 0, 1e-300, sm))
+        return -float((lnf * self.fpatt).sum()), fhK, lnf
+
     def neb(self, x, lastround: bool = True):
         """NEB posteriors of the four site classes at x (lfunNSsites_rate
         codeml.c:5079-5129): freqK_c f_c(h) normalised over c, from fhK (log
@@ -248,6 +274,14 @@ class Problem:
         dg = np.diag(V)
         se = np.where(dg > 0, np.sqrt(np.abs(dg)), -1.0)
         return g, H, se
+
+
+def beta_classes(p, q, K=10):
+    """M7's discrete beta: K equal-probability categories at their medians,
+    QuantileBeta((2j + 1) / (2K), p, q) (DiscreteNSsites codeml.c:2746-2752);
+    the inverse incomplete beta from scipy."""
+    from scipy.special import betaincinv
+    return np.array([betaincinv(p, q, (2 * j + 1) / (2.0 * K)) for j in range(K)]), np.full(K, 1.0 / K)
 
 
 def build_q(pi, kappa, omega):

@@ -33,7 +33,8 @@ def as_model_a(fx, tree):
     w2 on every branch and together weigh 1 - p0 - p1 (M2a); M1a is that with
     p1 = 1 - p0 (no w2 class; w2 then carries no weight and is set to 1).
     M3 with three classes (free w0, w1, w2) is model B on that tree, with x
-    unchanged (model B's layout).  Returns (tree with labels, x)."""
+    unchanged (model B's layout); M7 / M8 have no model-A form (x returned
+    as is; see site_model_classes).  Returns (tree with labels, x)."""
     import copy
 
     t = copy.deepcopy(tree)
@@ -50,6 +51,31 @@ def as_model_a(fx, tree):
 def clade_names():
     """Fixed-parameter fixtures under clade model C (two branch types)."""
     return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("mc") and f.endswith(".json"))
+
+
+def site_model_classes(fx, tree):
+    """(omegas, proportions) of a site-model fixture's classes at its x:
+    M2a / M1a / M3 directly, M7 / M8 by the discretised beta (ten categories
+    at their medians, DiscreteNSsites codeml.c:2728-2770)."""
+    from oracle import oracle as O
+
+    x = np.array(fx["x"], dtype=np.float64)
+    nb = tree.nbranch
+    m = fx["model"]
+    if m == "M7":
+        return O.beta_classes(x[nb + 1], x[nb + 2])
+    if m == "M8":
+        p0, p, q, ws = x[nb + 1:nb + 5]
+        om, pr = O.beta_classes(p, q)
+        return np.append(om, ws), np.append(pr * p0, 1 - p0)
+    if m == "M1a":
+        p0, w0 = x[nb + 1:nb + 3]
+        return np.array([w0, 1.0]), np.array([p0, 1 - p0])
+    if m == "M2a":
+        p0, p1, w0, w2 = x[nb + 1:nb + 5]
+        return np.array([w0, 1.0, w2]), np.array([p0, p1, 1 - p0 - p1])
+    p0, p1, w0, w1, w2 = x[nb + 1:nb + 6]          # M3, three classes
+    return np.array([w0, w1, w2]), np.array([p0, p1, 1 - p0 - p1])
 
 
 def model_b_names():

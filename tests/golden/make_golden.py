@@ -40,8 +40,8 @@ The mcC* fixtures are clade model C (model = 3, NSsites = 2; branch types
 #1 and background; x ends p0, p1, w0, w2, w3), lnL, log f and NG86 only.
 The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
 x ends p0, p1, w0, w2 for M2a, p0, w0 for M1a, p0, p1, w0, w1, w2 for M3
-with three classes): lnL, log f, NG86, and for M2a codeml's BEB (three
-classes).
+with three classes, p, q for M7, p0, p, q, ws for M8 with ten beta
+categories): lnL, log f, NG86, and for M2a codeml's BEB (three classes).
 The mb_* fixtures are the same evaluation under branch-site model B
 (NSsites = 3, ncatG = 3: w1 free; x ends w0, w1, w2), lnL and log f only.
 
@@ -123,6 +123,8 @@ CASES_SITE = [
     ("msM2a24x400_s10", 24, 400, 10, ModelA(omega2=4.0), (2.2, 0.5, 0.35, 0.15, 3.5), 1.0, "M2a"),
     ("msM1a12x300_s11", 12, 300, 11, ModelA(), (2.0, 0.7, 0.25), 1.0, "M1a"),
     ("msM3k3x8x300_s14", 8, 300, 14, ModelA(), (2.0, 0.5, 0.3, 0.1, 0.6, 2.5), 1.0, "M3"),
+    ("msM7x8x300_s15", 8, 300, 15, ModelA(), (2.0, 0.4, 1.3), 1.0, "M7"),
+    ("msM8x24x400_s16", 24, 400, 16, ModelA(), (2.2, 0.85, 0.5, 1.5, 3.0), 1.0, "M8"),
 ]
 
 
@@ -154,9 +156,11 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         ctl = CTL.replace("NSsites = 2", "NSsites = 3").replace("ncatG = 4", "ncatG = 3") if model_b else CTL
         if site_model:
             ctl = CTL.replace("model = 2", "model = 0").replace(
-                "NSsites = 2", "NSsites = " + {"M1a": "1", "M2a": "2", "M3": "3"}[site_model])
+                "NSsites = 2", "NSsites = " + {"M1a": "1", "M2a": "2", "M3": "3", "M7": "7", "M8": "8"}[site_model])
             if site_model == "M3":
                 ctl = ctl.replace("ncatG = 4", "ncatG = 3")
+            if site_model in ("M7", "M8"):
+                ctl = ctl.replace("ncatG = 4", "ncatG = 10")
         if clade:
             ctl = CTL.replace("model = 2", "model = 3")
         with open(os.path.join(d, "codeml.ctl"), "w") as f:

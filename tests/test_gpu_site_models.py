@@ -20,6 +20,28 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("name", site_model_names())
+def test_site_model_classes(name):
+    """Likelihood.site_model: K whole-tree classes, three per gb_eval_uvr
+    call, eigen solutions from the library; every site model including M7
+    and M8 (ten beta categories) against codeml's printed lnL and log f."""
+    from tests.conftest import site_model_classes
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, _ = as_model_a(fx, tree)
+    om, pr = site_model_classes(fx, tree)
+    x = np.array(fx["x"])
+    nb = t.nbranch
+    bl = np.zeros(t.nnode)
+    bl[t.branch_nodes()] = x[:nb]
+    lk = api.Likelihood(t, z, fpatt, pi)
+    f, fhK, lnf = lk.site_model(bl, x[nb], om, pr)
+    assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+    ref = np.array(fx["lnf"])
+    assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))
+    lk.close()
+
+
+@pytest.mark.parametrize("name", [n for n in site_model_names() if not n.startswith(("msM7", "msM8"))])
 def test_site_model_fp64(name):
     fx, tree, codons = load_golden(name)
     z, fpatt, pi = O.patterns(codons)

@@ -21,6 +21,24 @@ from tests.conftest import as_model_a, load_golden, site_model_names
 
 
 @pytest.mark.parametrize("name", site_model_names())
+def test_site_classes_match_codeml(name):
+    """Every site model as K whole-tree classes on the all-foreground tree
+    (three per evaluation of model A's class map), including M7 and M8 with
+    ten beta categories."""
+    from tests.conftest import site_model_classes
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, _ = as_model_a(fx, tree)
+    om, pr = site_model_classes(fx, tree)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    v, fhK, lnf = O.Problem(t, z, fpatt, pi, nthreads=2).site_classes(x[:nb], x[nb], om, pr)
+    assert abs(-v - fx["codeml_lnL"]) <= 5.1e-7 + 1e-12 * abs(v)
+    ref = np.array(fx["lnf"])
+    assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))
+
+
+@pytest.mark.parametrize("name", [n for n in site_model_names() if not n.startswith(("msM7", "msM8"))])
 def test_site_model_as_model_a_matches_codeml(name):
     fx, tree, codons = load_golden(name)
     assert np.all(tree.label == 0)

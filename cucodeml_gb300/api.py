@@ -61,6 +61,56 @@ def ng86(z: np.ndarray, fpatt: np.ndarray):
     return {"dS": dS, "dN": dN, "dN_dS": w, "dist": dist}
 
 
+def _ternary_classes():
+    """(p0, p1, p2) at the centroids of the 100 ternary triangles (GetIndexTernary tools.c:4441-4461)."""
+    t = np.arange(100)
+    ix = np.floor(np.sqrt(t)).astype(int)
+    iy = t - ix * ix
+    a = (1 + (iy // 2) * 3 + (iy % 2)) / 30.0
+    b = (1 + (9 - ix) * 3 + (iy % 2)) / 30.0
+    return np.stack([a, b, 1 - a - b], axis=1)
+
+
+def beb_clade_integrate(lnfw, fpatt):
+    """The grid integration of codeml's BEB under clade model C with two branch
+    types (lfunNSsites_ACD codeml.c:6700-6775 with modelACD = mC), host side,
+    from the 111 log f(x_h | w) tables: sets 0-9 (w0 in (0, 1) everywhere), 10
+    (w = 1), 11 + 10 i + j (w2_i background, w3_j foreground, both in (0, 3)).
+    Grid: 100 ternary (p0, p1) triangles x w0 x w2 x w3; classes (p0, p1, p2).
+    Returns post [3, npatt], grid [5, 10] (rows p0, p1 = -1), p0p1 [100], lnfX
+    as codeml prints it, S1."""
+    L = np.asarray(lnfw, dtype=np.float64)
+    fp = np.asarray(fpatt, dtype=np.float64)
+    m = L.max(axis=0)
+    F = np.exp(L - m)
+    S1 = float(m @ fp)
+    F0, F1, F2 = F[0:10], F[10], F[11:111]
+    tri = _ternary_classes()
+    lnfXs = np.empty((100, 10, 100))
+    for t in range(100):
+        for i0 in range(10):
+            fh = tri[t, 0] * F0[i0] + tri[t, 1] * F1 + tri[t, 2] * F2
+            lnfXs[t, i0] = np.where(fh < 1e-300, 0.0, np.log(np.maximum(fh, 1e-300))) @ fp
+    M = lnfXs.max()
+    lfX = M + np.log(np.exp(lnfXs - M).sum())
+    w = np.exp(lnfXs - lfX)                       # (t, i0, k = 10 i2 + i3)
+    post = np.zeros((3, L.shape[1]))
+    for t in range(100):
+        for i0 in range(10):
+            fh = tri[t, 0] * F0[i0] + tri[t, 1] * F1 + tri[t, 2] * F2
+            wk = w[t, i0][:, None] / fh
+            post[0] += tri[t, 0] * F0[i0] * wk.sum(axis=0)
+            post[1] += tri[t, 1] * F1 * wk.sum(axis=0)
+            post[2] += tri[t, 2] * (F2 * wk).sum(axis=0)
+    w5 = w.reshape(10, 10, 10, 10, 10)            # p-row index, p-col index, i0, i2, i3
+    grid = np.full((5, 10), -1.0)
+    grid[2] = w5.sum(axis=(0, 1, 3, 4))
+    grid[3] = w5.sum(axis=(0, 1, 2, 4))
+    grid[4] = w5.sum(axis=(0, 1, 2, 3))
+    p0p1 = w.sum(axis=(1, 2))
+    return {"post": post, "grid": grid, "p0p1": p0p1, "lnfX": float(lfX + S1 - 5 * np.log(10.0)), "S1": S1}
+
+
 def model_setup(pi, kappa, omega0, omega2, p0, p1):
     """(U [3,61,61], V [3,61,61], Root [3,61], qf [2], freqK [4]) computed by the library's host code."""
     L = _lib.load()
@@ -332,6 +382,30 @@ class Likelihood:
         return {"post": post, "grid": grid, "p0p1": p0p1, "lnfX": float(fx[0]), "S1": float(fx[1]),
                 "S2": float(fx[2]), "lnfw": lnfw, "wmean": wmean, "wsd": wsd, "ms_device": st.ms_device,
                 "ms_host": st.ms_host, "kernels": st.kernels}
+
+    def beb_tables(self, blength, kappa, qfactor, w_slot0, w_slot2):
+        """The 121 log f(x_h | w) tables with other omega grids (gb_beb_tables)."""
+        bl = np.ascontiguousarray(blength, dtype=np.float64)
+        qf = np.ascontiguousarray(qfactor, dtype=np.float64)
+        g0 = np.ascontiguousarray(w_slot0, dtype=np.float64)
+        g2 = np.ascontiguousarray(w_slot2, dtype=np.float64)
+        lnfw = np.zeros((121, self.npatt))
+        st = _lib.Stats()
+        _lib.check(self._L.gb_beb_tables(self._h, _ptr(bl), float(kappa), _ptr(qf), _ptr(g0), _ptr(g2),
+                                         _ptr(lnfw), C.byref(st)))
+        return lnfw
+
+    def beb_clade_c(self, blength, kappa, qfactor) -> dict:
+        """codeml's BEB under clade model C with two branch types at the MLE
+        (Qfactors qfactor of the two branch types): the 111 omega sets from two
+        gb_beb_tables calls on the device (w0 grid; then the (0, 3) grids of
+        w2 and w3 in eigen slots 0 and 2), the 10^5-point grid integration on
+        the host (beb_clade_integrate)."""
+        g01 = (np.arange(10) + 0.5) / 10
+        g03 = 0 + (np.arange(10) + 0.5) * (3 - 0) / 10
+        a = self.beb_tables(blength, kappa, qfactor, g01, g03)
+        b = self.beb_tables(blength, kappa, qfactor, g03, g03)
+        return beb_clade_integrate(np.concatenate([a[:11], b[11:111]]), self._fpatt)
 
     def beb_x(self, x, lastround: bool = True, want_lnfw: bool = False) -> dict:
         """beb() from codeml's x vector."""

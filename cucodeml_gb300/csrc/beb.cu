@@ -293,9 +293,14 @@ int gb_beb(gb_handle *h, const gb_params *prm, double *lnfw_out, double *post_ou
                      nullptr, nullptr, stats);
 }
 
-int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qfactor[2], double *lnfw_out,
-              double *post_out, double *grid_out, double *p0p1_out, double *lnfX_out, double *wmean_out,
-              double *wsd_out, gb_stats *stats) {
+namespace gb {
+namespace {
+// the BEB pipeline; wg0 / wg2 (both or neither): the omega grids of eigen
+// slots 0 and 2 in place of w0 in (0, 1) and w2 in (1, 11); tables_only:
+// stop after the 121 log f tables (no grid integration)
+int beb_run(gb_handle *h, const double *blength, double kappa, const double qfactor[2], const double *wg0,
+            const double *wg2, bool tables_only, double *lnfw_out, double *post_out, double *grid_out,
+            double *p0p1_out, double *lnfX_out, double *wmean_out, double *wsd_out, gb_stats *stats) {
     if (!h) return fail(GB_ERR_STATE, "null handle");
     if (!blength || !qfactor) return fail(GB_ERR_ARG, "null argument");
     if (h->precision != GB_PREC_FP64) return fail(GB_ERR_STATE, "gb_beb needs a GB_PREC_FP64 handle");
@@ -310,8 +315,9 @@ int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qf
     D.freqK[0] = D.freqK[1] = D.freqK[2] = D.freqK[3] = 0.25;   // the forward's mixture is not used
     double wv[BNE];
     for (int i = 0; i < BD; i++) {
-        wv[i] = (i + 0.5) / BD;                          // w0 in (0, 1)
-        wv[BD + 1 + i] = 1 + (i + 0.5) * (11 - 1) / BD;  // w2 in (1, 11)
+        wv[i] = wg0 ? wg0[i] : (i + 0.5) / BD;                          // w0 in (0, 1)
+        wv[BD + 1 + i] = wg2 ? wg2[i] : 1 + (i + 0.5) * (11 - 1) / BD;  // w2 in (1, 11)
+        if (!(wv[i] >= 0) || !(wv[BD + 1 + i] >= 0)) return fail(GB_ERR_PARAM, "omega grid");
     }
     wv[BD] = 1;
     std::vector<double> eig((size_t)BNE * EIG);
@@ -394,6 +400,27 @@ int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qf
     }
     beb_rescale_kernel<<<(npatt + 255) / 256, 256, 0, st>>>(B.lnfw, B.F, B.mrow, npatt, (int)npad,
                                                             h->nscale == 0);
+    if (tables_only) {
+        kernels++;
+        CK(cudaGetLastError());
+        if (lnfw_out)
+            CK(cudaMemcpy2DAsync(lnfw_out, sizeof(double) * npatt, B.lnfw, sizeof(double) * npad,
+                                 sizeof(double) * npatt, BNW, cudaMemcpyDeviceToHost, st));
+        CK(cudaEventRecord(h->ev1, st));
+        CK(cudaStreamSynchronize(st));
+        CK(cudaGetLastError());
+        if (stats) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+            stats->ms_device = ms;
+            stats->ms_host = now_ms() - t0;
+            stats->kernels = kernels;
+            stats->nscale = h->nscale;
+            stats->h2d_bytes = sizeof(double) * (eig.size() + pcl.size() + h->nnode) + sizeof(DevParams);
+            stats->d2h_bytes = lnfw_out ? sizeof(double) * (size_t)BNW * npatt : 0;
+        }
+        return GB_OK;
+    }
     beb_grid_kernel<<<BNG, 256, 0, st>>>(B.F, h->d_fpatt, B.pcl, npatt, (int)npad, B.lnfXs);
     kernels += 2;
     CK(cudaGetLastError());
@@ -491,4 +518,21 @@ int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qf
                                              (post_out ? 4 * npatt : 0));
     }
     return GB_OK;
+}
+}  // namespace
+}  // namespace gb
+
+int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qfactor[2], double *lnfw_out,
+              double *post_out, double *grid_out, double *p0p1_out, double *lnfX_out, double *wmean_out,
+              double *wsd_out, gb_stats *stats) {
+    return beb_run(h, blength, kappa, qfactor, nullptr, nullptr, false, lnfw_out, post_out, grid_out, p0p1_out,
+                   lnfX_out, wmean_out, wsd_out, stats);
+}
+
+int gb_beb_tables(gb_handle *h, const double *blength, double kappa, const double qfactor[2],
+                  const double w_slot0[GB_BEB_GRID], const double w_slot2[GB_BEB_GRID], double *lnfw,
+                  gb_stats *stats) {
+    if (!w_slot0 || !w_slot2 || !lnfw) return fail(GB_ERR_ARG, "null argument");
+    return beb_run(h, blength, kappa, qfactor, w_slot0, w_slot2, true, lnfw, nullptr, nullptr, nullptr, nullptr,
+                   nullptr, nullptr, stats);
 }

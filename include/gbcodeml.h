@@ -218,6 +218,18 @@ int gb_beb_qf(gb_handle *h, const double *blength, double kappa, const double qf
               gb_stats *stats);
 
 /*
+ * The 121 log f(x_h | w) tables of gb_beb_qf (lnfw[121*npatt], same set
+ * order) with other omega grids: w_slot0[10] in place of the w0 grid and
+ * w_slot2[10] in place of the w2 grid; no grid integration.  Serves BEB
+ * analyses on other grids, e.g. codeml's clade model C (w2, w3 in (0, 3),
+ * lfunNSsites_ACD codeml.c:6617-6826 with modelACD = mC): its third class's
+ * sets (w2_i background, w3_j foreground) are sets 11 + 10 i + j here.
+ */
+int gb_beb_tables(gb_handle *h, const double *blength, double kappa, const double qfactor[2],
+                  const double w_slot0[GB_BEB_GRID], const double w_slot2[GB_BEB_GRID], double *lnfw,
+                  gb_stats *stats);
+
+/*
  * Naive empirical Bayes (NEB) posteriors of the four site classes at prm, as
  * codeml's lfunNSsites_rate prints them ("Naive Empirical Bayes (NEB)
  * probabilities", codeml.c:5079-5129): post[c*npatt + h] = freqK_c f_c(h) /

@@ -720,6 +720,157 @@ int oracle_beb(const oracle_problem *pb, const double *x, int lastround, double 
 }
 
 /*
+ * Bayes empirical Bayes under clade model C with two branch types
+ * (lfunNSsites_ACD codeml.c:6617-6826 with modelACD = mC; grid set-up
+ * get_grid_para_like_ACD 6419-6470, classes get_pclassM_iw_ACD 6532-6615):
+ * x = [branch lengths, kappa, p0, p1, w0, w2 (background), w3 (foreground)].
+ * 111 omega sets: 10 (w0_i everywhere, w0 in (0, 1)), 1 (w = 1), and 100
+ * (w2_i on background, w3_j on foreground, both in (0, 3)) with set index
+ * 11 + 10 i + j; Qfactor_NS_branch of the two branch types fixed at x.  Grid:
+ * 100 ternary (p0, p1) triangles x w0 x w2 x w3 (10^5 points), classes
+ * (p0, p1, p2).  Outputs as oracle_beb: lnfw[111*npatt], post[3*npatt],
+ * grid[5*10] (rows p0, p1 = -1, w0, w2, w3), p0p1[100], lnfX[3].
+ */
+int oracle_beb_clade(const oracle_problem *pb, const double *x, double *lnfw_out, double *post,
+                     double *grid, double *p0p1, double *lnfX) {
+    const int D = BEB_D, NW = D + 1 + D * D, DIM = 5;
+    const long NG = (long)D * D * D * D * D;
+    int n = NC, np = pb->npatt, nn = pb->nnode, nb = nn - 1;
+    double kappa = x[nb], p0 = x[nb + 1], p1 = x[nb + 2], w0 = x[nb + 3], w2 = x[nb + 4], w3 = x[nb + 5];
+    double p2 = 1 - p0 - p1, Q[NC * NC];
+    double qf[2] = {1 / build_q(pb->pi, kappa, p0 * w0 + p1 + p2 * w2, Q),
+                    1 / build_q(pb->pi, kappa, p0 * w0 + p1 + p2 * w3, Q)};
+    /* omega values: 0..9 w0 grid, 10 = 1, 11..20 the (0, 3) grid of w2 and w3 */
+    double wv[2 * BEB_D + 1];
+    for (int i = 0; i < D; i++) {
+        wv[i] = (i + 0.5) / D;
+        wv[D + 1 + i] = 0 + (i + 0.5) * (3 - 0) / D;
+    }
+    wv[D] = 1;
+    int ne = 2 * D + 1;
+    double *U = (double *)malloc(sizeof(double) * ne * n * n), *V = (double *)malloc(sizeof(double) * ne * n * n);
+    double *R = (double *)malloc(sizeof(double) * ne * n);
+    for (int e = 0; e < ne; e++) {
+        build_q(pb->pi, kappa, wv[e], Q);
+        eigen_uvr(Q, pb->pi, U + (size_t)e * n * n, V + (size_t)e * n * n, R + (size_t)e * n);
+    }
+    char *scale = (char *)calloc(nn, 1);
+    int nscale = 0;
+    set_node_scale(pb, pb->root, scale, &nscale);
+    double *tnode = (double *)calloc(nn, sizeof(double));
+    for (int ib = 0; ib < nb; ib++) tnode[pb->bnode[ib]] = x[ib];
+    double *Pall = (double *)malloc(sizeof(double) * nn * n * n);
+    double *conP = (double *)malloc(sizeof(double) * (size_t)nn * np * n);
+    double *scaleF = (double *)calloc((size_t)nn * np, sizeof(double));
+    double *F = (double *)malloc(sizeof(double) * (size_t)NW * np);
+    for (int iw = 0; iw < NW; iw++) {
+        int eb, ef;
+        if (iw < D) eb = ef = iw;
+        else if (iw == D) eb = ef = D;
+        else { eb = D + 1 + (iw - D - 1) / D; ef = D + 1 + (iw - D - 1) % D; }
+        for (int i = 0; i < nn; i++) {
+            if (i == pb->root) continue;
+            int lab = pb->label[i], e = lab ? ef : eb;
+            pmat(Pall + (size_t)i * n * n, tnode[i] * qf[lab], U + (size_t)e * n * n, V + (size_t)e * n * n,
+                 R + (size_t)e * n);
+        }
+        root_logf(pb, Pall, scale, conP, scaleF, F + (size_t)iw * np);
+    }
+    if (lnfw_out) memcpy(lnfw_out, F, sizeof(double) * NW * np);
+    double S1 = 0;
+    for (int h = 0; h < np; h++) {
+        double m = F[h];
+        for (int k = 1; k < NW; k++)
+            if (F[(size_t)k * np + h] > m) m = F[(size_t)k * np + h];
+        for (int k = 0; k < NW; k++) F[(size_t)k * np + h] = exp(F[(size_t)k * np + h] - m);
+        S1 += m * pb->fpatt[h];
+    }
+    double tri[100][3];
+    for (int t = 0; t < 100; t++) {
+        int ix = (int)sqrt((double)t), iy = t - ix * ix;
+        tri[t][0] = (1 + (iy / 2) * 3 + (iy % 2)) / (3. * D);
+        tri[t][1] = (1 + (D - 1 - ix) * 3 + (iy % 2)) / (3. * D);
+        tri[t][2] = 1 - tri[t][0] - tri[t][1];
+    }
+    double *lnfXs = (double *)malloc(sizeof(double) * NG);
+#pragma omp parallel for schedule(static)
+    for (long g = 0; g < NG; g++) {
+        int ip[5];
+        long it = g;
+        for (int j = 4; j >= 0; j--) { ip[j] = (int)(it % D); it /= D; }
+        const double *pc = tri[ip[0] * D + ip[1]];
+        const double *f0 = F + (size_t)ip[2] * np, *f1 = F + (size_t)D * np;
+        const double *f2 = F + (size_t)(D + 1 + ip[3] * D + ip[4]) * np;
+        double sum = 0;
+        for (int h = 0; h < np; h++) {
+            double fh = pc[0] * f0[h] + pc[1] * f1[h] + pc[2] * f2[h];
+            if (fh < 1e-300) continue;
+            sum += log(fh) * pb->fpatt[h];
+        }
+        lnfXs[g] = sum;
+    }
+    double pp[5][BEB_D], pq[100];
+    memset(pp, 0, sizeof pp);
+    memset(pq, 0, sizeof pq);
+    double fX = 1, S2 = -1e300;
+    for (long g = 0; g < NG; g++) {
+        int ip[5];
+        long it = g;
+        for (int j = 4; j >= 0; j--) { ip[j] = (int)(it % D); it /= D; }
+        double t = lnfXs[g] - S2;
+        if (t > 10) {
+            t = t < 200 ? exp(-t) : 0;
+            fX = fX * t + 1;
+            for (int j = 0; j < DIM; j++)
+                for (int k = 0; k < D; k++) pp[j][k] *= t;
+            for (int k = 0; k < 100; k++) pq[k] *= t;
+            for (int j = 0; j < DIM; j++) pp[j][ip[j]] += 1;
+            pq[ip[0] * D + ip[1]] += 1;
+            S2 = lnfXs[g];
+        } else if (t > -200) {
+            t = exp(t);
+            fX += t;
+            for (int j = 0; j < DIM; j++) pp[j][ip[j]] += t;
+            pq[ip[0] * D + ip[1]] += t;
+        }
+    }
+    double lfX = log(fX) + S2;
+    if (lnfX) {
+        lnfX[0] = lfX + S1 - DIM * log((double)D);
+        lnfX[1] = S1;
+        lnfX[2] = S2;
+    }
+    if (grid)
+        for (int j = 0; j < DIM; j++)
+            for (int k = 0; k < D; k++) grid[j * D + k] = j < 2 ? -1 : pp[j][k] / fX;
+    if (p0p1)
+        for (int k = 0; k < 100; k++) p0p1[k] = pq[k] / fX;
+    if (post) {
+#pragma omp parallel for schedule(dynamic, 4)
+        for (int h = 0; h < np; h++) {
+            double acc[3] = {0, 0, 0};
+            for (long g = 0; g < NG; g++) {
+                int ip[5];
+                long it = g;
+                for (int j = 4; j >= 0; j--) { ip[j] = (int)(it % D); it /= D; }
+                const double *pc = tri[ip[0] * D + ip[1]];
+                double fk[3] = {pc[0] * F[(size_t)ip[2] * np + h], pc[1] * F[(size_t)D * np + h],
+                                pc[2] * F[(size_t)(D + 1 + ip[3] * D + ip[4]) * np + h]};
+                double fh = fk[0] + fk[1] + fk[2];
+                for (int k = 0; k < 3; k++) {
+                    double t = log(fk[k] / fh) + lnfXs[g] - lfX;
+                    if (t > -300) acc[k] += exp(t);
+                }
+            }
+            for (int k = 0; k < 3; k++) post[k * np + h] = acc[k];
+        }
+    }
+    free(U); free(V); free(R); free(scale); free(tnode); free(Pall); free(conP); free(scaleF); free(F);
+    free(lnfXs);
+    return 0;
+}
+
+/*
  * Per-class fhK (as oracle_lnL writes it) from given eigen solutions: U, V
  * [3][61*61], Root [3][61] (model A's slots w0, w1, w2), Qfactors qf[2] and
  * branch lengths by branch index (x[0..nb-1]); the classes follow model A's

@@ -57,6 +57,8 @@ def lib():
         L.oracle_pmat.restype = None
         L.oracle_pmat.argtypes = [dp, C.c_double, dp, dp, dp]
         L.oracle_max_threads.restype = C.c_int
+        L.oracle_beb_clade.restype = C.c_int
+        L.oracle_beb_clade.argtypes = [C.POINTER(_Problem), dp, dp, dp, dp, dp, dp]
         L.oracle_fhK_uvr.restype = C.c_int
         L.oracle_fhK_uvr.argtypes = [C.POINTER(_Problem), dp, dp, dp, dp, dp, dp]
         L.oracle_beb.restype = C.c_int
@@ -165,6 +167,22 @@ class Problem:
                 "post": post.reshape(4, self.npatt), "grid": grid.reshape(4, 10), "p0p1": p0p1,
                 "lnfX": fx[0], "S1": fx[1], "S2": fx[2], "wmean": wmean, "wsd": wsd}
 
+
+    def beb_clade(self, x, want_lnfw: bool = True):
+        """Bayes empirical Bayes under clade model C with two branch types
+        (oracle.c oracle_beb_clade): lnfw [111, npatt], post [3, npatt],
+        grid [5, 10], p0p1 [100], lnfX, S1, S2."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        lnfw = np.zeros(111 * self.npatt) if want_lnfw else None
+        post = np.zeros(3 * self.npatt)
+        grid = np.zeros(50)
+        p0p1 = np.zeros(100)
+        fx = np.zeros(3)
+        lib().oracle_beb_clade(C.byref(self._s), _dp(x), _dp(lnfw) if lnfw is not None else None, _dp(post),
+                               _dp(grid), _dp(p0p1), _dp(fx))
+        return {"lnfw": lnfw.reshape(111, self.npatt) if lnfw is not None else None,
+                "post": post.reshape(3, self.npatt), "grid": grid.reshape(5, 10), "p0p1": p0p1,
+                "lnfX": fx[0], "S1": fx[1], "S2": fx[2]}
 
     def fhK_uvr(self, U, V, R, qf, xb):
         """Per-class fhK (4, npatt) from given eigen slots, Qfactors and branch

@@ -37,7 +37,8 @@ codeml runs the same BEB for model B (lfunNSsites_ACD treats model = 2 as
 model A's grid, w1 = 1 in class 1, with model B's Qfactors), kept for the
 mb* fixtures too.
 The mcC* fixtures are clade model C (model = 3, NSsites = 2; branch types
-#1 and background; x ends p0, p1, w0, w2, w3), lnL, log f and NG86 only.
+#1 and background; x ends p0, p1, w0, w2, w3): lnL, log f, NG86 and codeml's
+clade-C BEB (three classes; grid w0, w2, w3).
 The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
 x ends p0, p1, w0, w2 for M2a, p0, w0 for M1a, p0, p1, w0, w1, w2 for M3
 with three classes, p, q for M7, p0, p, q, ws for M8 with ten beta
@@ -175,7 +176,7 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
     if clade:
-        extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns)}
+        extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3)}
     elif site_model:
         extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
         if site_model == "M2a":       # BEB of M2a (lfunNSsites_M2M8 codeml.c:6190-6415): 3 classes
@@ -267,16 +268,17 @@ def parse_beb(out: str, rst: str, stdout: str, ncls: int = 4) -> dict:
     site = parse_site_post(rst, "Bayes", ncls)
     j0 = out.index("Posterior on the grid")
     rows = {}
-    for ln in out[j0:].splitlines()[1:6]:
+    for ln in out[j0:].splitlines()[1:7]:
         parts = ln.split()
-        if parts and parts[0] in ("w0:", "w2:"):
+        if parts and parts[0] in ("w0:", "w2:", "w3:"):
             rows[parts[0][:2]] = [float(v) for v in parts[1:]]
     k0 = out.index("Posterior for p0-p1")
     k1 = out.index("sum of density on p0-p1")
     p0p1 = [float(v) for v in out[k0:k1].split("\n", 1)[1].split()]
     m = re.search(r"log\(fX\) =\s*(-?\d+\.\d+)\s+S =\s*(-?\d+\.\d+)\s+(-?\d+\.\d+)",
                   stdout.replace("\r", "\n"))
-    return {"site_post_5dp": site, "w0_post_3dp": rows["w0"], "w2_post_3dp": rows["w2"],
+    extra = {"w3_post_3dp": rows["w3"]} if "w3" in rows else {}
+    return {**extra, "site_post_5dp": site, "w0_post_3dp": rows["w0"], "w2_post_3dp": rows["w2"],
             "p0p1_post_3dp": p0p1, "lnfX_6dp": float(m.group(1)), "S1_6dp": float(m.group(2)),
             "S2_6dp": float(m.group(3))}
 

@@ -25,3 +25,28 @@ def test_clade_c_matches_codeml(name):
     assert abs(-v - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     ref = np.array(fx["lnf"])
     assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))
+
+
+@pytest.mark.parametrize("name", clade_names())
+def test_clade_c_beb_matches_codeml(name):
+    """codeml's BEB under clade C (lfunNSsites_ACD with modelACD = mC): the
+    oracle's restatement against codeml's printed posteriors, grid marginals
+    and log f(X); the library's host-side grid integration
+    (api.beb_clade_integrate) fed the oracle's 111 tables against the
+    oracle's own integration (1e-12)."""
+    from cucodeml_gb300 import api
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    r = O.Problem(tree, z, fpatt, pi, nthreads=4).beb_clade(np.array(fx["x"]))
+    g = fx["beb"]
+    site = r["post"][:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(g["site_post_5dp"]))) <= 5.01e-6
+    for row, key in ((2, "w0_post_3dp"), (3, "w2_post_3dp"), (4, "w3_post_3dp")):
+        assert np.max(np.abs(r["grid"][row] - g[key])) <= 5.01e-4
+    assert np.max(np.abs(r["p0p1"] - g["p0p1_post_3dp"])) <= 5.01e-4
+    assert abs(r["lnfX"] - g["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])
+    q = api.beb_clade_integrate(r["lnfw"], fpatt)
+    assert np.max(np.abs(q["post"] - r["post"])) <= 1e-12
+    assert np.max(np.abs(q["grid"] - r["grid"])) <= 1e-12
+    assert abs(q["lnfX"] - r["lnfX"]) <= 1e-12 * abs(r["lnfX"])

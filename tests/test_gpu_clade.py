@@ -41,3 +41,33 @@ def test_clade_c_eval_uvr(name):
     assert np.max(np.abs(g_lnf - lnf)) <= 1e-11
     assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     lk.close()
+
+
+@pytest.mark.parametrize("name", clade_names())
+def test_clade_c_beb(name):
+    """Likelihood.beb_clade_c: the 111 tables from two gb_beb_tables calls
+    against the oracle's (1e-10 + 2e-9 |log f|, as for model A's BEB), the
+    posteriors against codeml's printed clade-C BEB (print rounding)."""
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+    p2 = 1 - p0 - p1
+    ref = O.Problem(tree, z, fpatt, pi, nthreads=4).beb_clade(x)
+    qf = np.array([1.0 / O.build_q(pi, kappa, p0 * w0 + p1 + p2 * w)[1] for w in (w2, w3)])
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[:nb]
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    g01 = (np.arange(10) + 0.5) / 10
+    g03 = (np.arange(10) + 0.5) * 3 / 10
+    a = lk.beb_tables(bl, kappa, qf, g01, g03)
+    b = lk.beb_tables(bl, kappa, qf, g03, g03)
+    tab = np.concatenate([a[:11], b[11:111]])
+    assert np.all(np.abs(tab - ref["lnfw"]) <= 1e-10 + 2e-9 * np.abs(ref["lnfw"]))
+    r = lk.beb_clade_c(bl, kappa, qf)
+    site = r["post"][:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(fx["beb"]["site_post_5dp"]))) <= 5.01e-6
+    assert abs(r["lnfX"] - fx["beb"]["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])
+    lk.close()

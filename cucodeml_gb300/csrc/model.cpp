@@ -45,72 +45,81 @@ const CodeTables &tables() {
     return t;
 }
 
-// Householder reduction of the symmetric matrix a (row-major, n x n) to
-// tridiagonal form.  On return a holds the accumulated orthogonal transform,
-// d the diagonal and e[1..n-1] the sub-diagonal (e[0] = 0).
-void householder_tridiag(int n, double *a, double *d, double *e) {
-    for (int i = n - 1; i > 0; i--) {
-        int l = i - 1;
-        double h = 0;
-        if (l > 0) {
-            double scale = 0;
-            for (int k = 0; k <= l; k++) scale += std::fabs(a[i * n + k]);
-            if (scale == 0.0) {
-                e[i] = a[i * n + l];
-            } else {
-                for (int k = 0; k <= l; k++) {
-                    a[i * n + k] /= scale;
-                    h += a[i * n + k] * a[i * n + k];
-                }
-                double f = a[i * n + l];
-                double g = f >= 0 ? -std::sqrt(h) : std::sqrt(h);
-                e[i] = scale * g;
-                h -= f * g;
-                a[i * n + l] = f - g;
-                f = 0;
-                for (int j = 0; j <= l; j++) {
-                    a[j * n + i] = a[i * n + j] / h;
-                    double gg = 0;
-                    for (int k = 0; k <= j; k++) gg += a[j * n + k] * a[i * n + k];
-                    for (int k = j + 1; k <= l; k++) gg += a[k * n + j] * a[i * n + k];
-                    e[j] = gg / h;
-                    f += e[j] * a[i * n + j];
-                }
-                double hh = f / (h + h);
-                for (int j = 0; j <= l; j++) {
-                    double ff = a[i * n + j];
-                    double gg = e[j] - hh * ff;
-                    e[j] = gg;
-                    for (int k = 0; k <= j; k++) a[j * n + k] -= ff * e[k] + gg * a[i * n + k];
-                }
-            }
-        } else {
-            e[i] = a[i * n + l];
+// Reduction of a symmetric matrix to tridiagonal form by Householder
+// reflectors, column by column from the left (Golub & Van Loan, "Matrix
+// Computations", 4th ed., algorithm 8.3.1; the same scheme as LAPACK's
+// dsytd2 on the lower triangle followed by dorgtr).
+//
+// a: row-major n x n, full symmetric storage; overwritten.  Step k builds
+// H_k = I - tau_k v v^T, v = (1, v_1, .., v_{m-1}) over rows k+1..n-1, that
+// maps the column below the diagonal onto its first entry, and applies it to
+// the trailing block in the symmetric rank-2 form S <- S - v w^T - w v^T with
+// p = tau S v, w = p - (tau / 2)(p . v) v.  v_1.. are kept in column k under
+// the sub-diagonal.  On return d holds the diagonal, e[k] the entry that
+// couples k and k+1 (e[n-1] = 0), and q = H_0 H_1 .. H_{n-3} (row-major),
+// accumulated backwards, so that a_in = q T q^T.
+void tridiagonalize(int n, double *a, double *d, double *e, double *q) {
+    double tau[NC], v[NC], p[NC];
+    for (int k = 0; k + 2 < n; k++) {
+        const int m = n - k - 1;
+        double *S = a + (size_t)(k + 1) * n + (k + 1);      // S[r * n + c], r, c < m
+        auto x = [&](int i) -> double & { return a[(size_t)(k + 1 + i) * n + k]; };
+        d[k] = a[(size_t)k * n + k];
+        const double alpha = x(0);
+        double big = 0;
+        for (int i = 1; i < m; i++) big = std::fmax(big, std::fabs(x(i)));
+        if (big == 0.0) {                                    // already reduced
+            tau[k] = 0;
+            e[k] = alpha;
+            continue;
         }
-        d[i] = h;
+        double ss = 0;
+        for (int i = 1; i < m; i++) {
+            const double t = x(i) / big;
+            ss += t * t;
+        }
+        const double beta = -std::copysign(std::hypot(alpha, big * std::sqrt(ss)), alpha);
+        tau[k] = (beta - alpha) / beta;
+        const double inv = 1.0 / (alpha - beta);
+        v[0] = 1.0;
+        for (int i = 1; i < m; i++) v[i] = (x(i) *= inv);
+        e[k] = beta;
+        double pv = 0;
+        for (int r = 0; r < m; r++) {
+            double s = 0;
+            for (int c = 0; c < m; c++) s += S[(size_t)r * n + c] * v[c];
+            p[r] = tau[k] * s;
+            pv += p[r] * v[r];
+        }
+        const double half = 0.5 * tau[k] * pv;
+        for (int r = 0; r < m; r++) p[r] -= half * v[r];           // p is now w
+        for (int r = 0; r < m; r++)
+            for (int c = 0; c < m; c++) S[(size_t)r * n + c] -= v[r] * p[c] + p[r] * v[c];
     }
-    d[0] = 0;
-    e[0] = 0;
-    for (int i = 0; i < n; i++) {
-        int l = i - 1;
-        if (d[i] != 0.0) {
-            for (int j = 0; j <= l; j++) {
-                double g = 0;
-                for (int k = 0; k <= l; k++) g += a[i * n + k] * a[k * n + j];
-                for (int k = 0; k <= l; k++) a[k * n + j] -= g * a[k * n + i];
-            }
+    d[n - 2] = a[(size_t)(n - 2) * n + (n - 2)];
+    e[n - 2] = a[(size_t)(n - 1) * n + (n - 2)];
+    d[n - 1] = a[(size_t)(n - 1) * n + (n - 1)];
+    e[n - 1] = 0;
+    for (int i = 0; i < n * n; i++) q[i] = 0;
+    for (int i = 0; i < n; i++) q[(size_t)i * n + i] = 1;
+    for (int k = n - 3; k >= 0; k--) {
+        if (tau[k] == 0.0) continue;
+        const int m = n - k - 1;
+        v[0] = 1.0;
+        for (int i = 1; i < m; i++) v[i] = a[(size_t)(k + 1 + i) * n + k];
+        for (int c = k + 1; c < n; c++) {
+            double s = 0;
+            for (int r = 0; r < m; r++) s += v[r] * q[(size_t)(k + 1 + r) * n + c];
+            s *= tau[k];
+            for (int r = 0; r < m; r++) q[(size_t)(k + 1 + r) * n + c] -= s * v[r];
         }
-        d[i] = a[i * n + i];
-        a[i * n + i] = 1;
-        for (int j = 0; j <= l; j++) a[j * n + i] = a[i * n + j] = 0;
     }
 }
 
-// Implicit-shift QL on the tridiagonal (d, e); z accumulates the rotations
-// (eigenvectors in columns).  Returns 0, or -1 if an eigenvalue did not
-// converge in 60 iterations.
+// Implicit-shift QL on the tridiagonal (d, e), e[k] coupling k and k+1;
+// z accumulates the rotations (eigenvectors in columns).  Returns 0, or -1
+// if an eigenvalue did not converge in 60 iterations.
 int ql_implicit(int n, double *d, double *e, double *z) {
-    for (int i = 1; i < n; i++) e[i - 1] = e[i];
     e[n - 1] = 0;
     for (int l = 0; l < n; l++) {
         int iter = 0, m;
@@ -211,7 +220,7 @@ double build_q(const double *pi, double kappa, double omega, double *Q, double *
 }
 
 int eigen_qrev(const double *Q, const double *pi, double *U, double *V, double *Root) {
-    double a[NC * NC], e[NC], sq[NC];
+    double a[NC * NC], z[NC * NC], e[NC], sq[NC];
     for (int i = 0; i < NC; i++) {
         if (!(pi[i] > 0)) return -1;
         sq[i] = std::sqrt(pi[i]);
@@ -220,12 +229,12 @@ int eigen_qrev(const double *Q, const double *pi, double *U, double *V, double *
         a[i * NC + i] = Q[i * NC + i];
         for (int j = 0; j < i; j++) a[i * NC + j] = a[j * NC + i] = Q[i * NC + j] * sq[i] / sq[j];
     }
-    householder_tridiag(NC, a, Root, e);
-    if (ql_implicit(NC, Root, e, a)) return -1;
+    tridiagonalize(NC, a, Root, e, z);
+    if (ql_implicit(NC, Root, e, z)) return -1;
     for (int i = 0; i < NC; i++)
         for (int k = 0; k < NC; k++) {
-            U[i * NC + k] = a[i * NC + k] / sq[i];
-            V[k * NC + i] = a[i * NC + k] * sq[i];
+            U[i * NC + k] = z[i * NC + k] / sq[i];
+            V[k * NC + i] = z[i * NC + k] * sq[i];
         }
     return 0;
 }

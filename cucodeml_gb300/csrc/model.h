@@ -33,7 +33,8 @@ struct Derived {
 double build_q(const double *pi, double kappa, double omega, double *Q, double *dQk, double *dQw);
 
 // Symmetric eigen solution of a reversible Q: Q = U diag(Root) V, V = U^-1.
-// Householder tridiagonalisation + implicit QL.  Returns 0 or -1 (no convergence).
+// Householder tridiagonalisation (column-wise reflectors, Golub & Van Loan
+// alg. 8.3.1) + implicit QL.  Returns 0 or -1 (no convergence).
 int eigen_qrev(const double *Q, const double *pi, double *U, double *V, double *Root);
 
 // Fill everything a model-A evaluation needs; 0 or GB_ERR_PARAM.

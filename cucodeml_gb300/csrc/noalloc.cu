@@ -14,9 +14,18 @@
 //
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress and sets the kernels'
-// attributes; make that first call before any stream capture.  Calls share the
-// array and leave their contents in it; each call clears what must start at
-// zero.  Two calls whose work overlaps on the GPU race on the array.
+// attributes, and caches both for the rest of the process: do not use this
+// entry point across a cudaDeviceReset.  No call may be made while its stream
+// is being captured into a CUDA graph (it synchronises the stream and uploads
+// a host-side schedule that the next call overwrites); such a call returns
+// GB_ERR_STATE.  Calls share the array and leave their contents in it; each
+// call clears what must start at zero.  Two calls whose work overlaps on the
+// GPU race on the array.
+//
+// Codon ids are checked on the device before any kernel reads them: an id
+// outside 0..60 (codeml's ambiguity codes, or any stray byte) is replaced by
+// 0 in the scratch copy, flagged, and the call returns GB_ERR_ARG without
+// touching the caller's outputs.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -161,6 +170,20 @@ int build(Sched &s, int ns, int nn, int root, const int *father, const int *labe
 
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
+// Codon ids of the scratch copy of z (ns rows of npad, npatt used): an id
+// of 61 or more would index past the 61 rows of a transition matrix in the
+// pruning kernels, so it is replaced by 0 and flagged before they run.
+__global__ void noalloc_check_z(unsigned char *z, int ns, int npad, int npatt, unsigned *bad) {
+    const size_t n = (size_t)ns * npad;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        if ((int)(i % npad) >= npatt) continue;
+        if (z[i] >= 61) {
+            z[i] = 0;
+            atomicOr(bad, 1u);
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" int gb_lnL_noalloc(int ns, int nnode, int root, const int *father, const int *label,
@@ -170,6 +193,12 @@ extern "C" int gb_lnL_noalloc(int ns, int nnode, int root, const int *father, co
     using namespace gb;
     if (!d_z || !d_fpatt || !d_pi || !d_model || !d_blength || !d_neg_lnL)
         return fail(GB_ERR_ARG, "gb_lnL_noalloc: null device pointer");
+    {
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap));
+        if (cap != cudaStreamCaptureStatusNone)
+            return fail(GB_ERR_STATE, "gb_lnL_noalloc: not callable during stream capture");
+    }
     std::lock_guard<std::mutex> lock(g_mu);
     int dev = 0;
     CK(cudaGetDevice(&dev));
@@ -197,6 +226,8 @@ extern "C" int gb_lnL_noalloc(int ns, int nnode, int root, const int *father, co
     const size_t o_fhK = take(sizeof(double) * 4 * npad);
     const size_t o_part = take(sizeof(double) * (npad / 256 + 2));
     const size_t o_ticket = take(sizeof(unsigned));
+    const size_t o_bad = take(sizeof(unsigned));
+    const size_t o_lnL = take(sizeof(double));
     if (off > (size_t)GB_NOALLOC_SCRATCH_BYTES) {
         char msg[200];
         snprintf(msg, sizeof msg,
@@ -219,6 +250,8 @@ extern "C" int gb_lnL_noalloc(int ns, int nnode, int root, const int *father, co
     double *fhK = reinterpret_cast<double *>(base + o_fhK);
     double *part = reinterpret_cast<double *>(base + o_part);
     unsigned *ticket = reinterpret_cast<unsigned *>(base + o_ticket);
+    unsigned *bad = reinterpret_cast<unsigned *>(base + o_bad);
+    double *lnL = reinterpret_cast<double *>(base + o_lnL);
 
     CK(cudaMemcpyAsync(items, s.items, sizeof(Item) * s.nitems, cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(pairs, s.pairs, sizeof(PairDesc) * s.npair, cudaMemcpyHostToDevice, st));
@@ -228,6 +261,9 @@ extern "C" int gb_lnL_noalloc(int ns, int nnode, int root, const int *father, co
     CK(cudaMemsetAsync(z, 0, (size_t)s.ns * npad, st));
     CK(cudaMemcpy2DAsync(z, npad, d_z, s.npatt, s.npatt, s.ns, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemsetAsync(ticket, 0, sizeof(unsigned), st));
+    CK(cudaMemsetAsync(bad, 0, sizeof(unsigned), st));
+    noalloc_check_z<<<std::min<size_t>(1024, ((size_t)s.ns * npad + 255) / 256), 256, 0, st>>>(
+        z, s.ns, (int)npad, s.npatt, bad);
     const DevParams *prm = reinterpret_cast<const DevParams *>(d_model);
     launch_pmat_fp64(pairs, s.npair, lab, d_blength, prm, Pt, st);
     for (int L = 0; L < s.H; L++) {
@@ -236,11 +272,16 @@ extern "C" int gb_lnL_noalloc(int ns, int nnode, int root, const int *father, co
             launch_prune_fp64(items + s.level_off[L], n, s.ntile, s.npad, z, Pt, conP, nullptr, scaleF,
                               slist, s.nscale, d_pi, fbar, ssum, fhK, st);
     }
-    launch_mix(fhK, d_fpatt, prm, s.npatt, s.npad, s.nscale, nullptr, nullptr, part, ticket, d_neg_lnL, st);
+    launch_mix(fhK, d_fpatt, prm, s.npatt, s.npad, s.nscale, nullptr, nullptr, part, ticket, lnL, st);
+    unsigned flagged = 0;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(&flagged, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (flagged) return fail(GB_ERR_ARG, "gb_lnL_noalloc: codon ids must be 0..60 (sense codons)");
+    CK(cudaMemcpyAsync(d_neg_lnL, lnL, sizeof(double), cudaMemcpyDeviceToDevice, st));
     if (d_fhK)
         CK(cudaMemcpy2DAsync(d_fhK, sizeof(double) * s.npatt, fhK, sizeof(double) * npad,
                              sizeof(double) * s.npatt, 4, cudaMemcpyDeviceToDevice, st));
-    CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
     return GB_OK;
 }

@@ -405,9 +405,13 @@ int gb_model_setup(const double *pi, double kappa, double omega0, double omega2,
  *   and d_fhK [4*npatt] (may be NULL).
  *   stream: a cudaStream_t (NULL = legacy default stream); the call returns
  *   after that stream has finished the evaluation.
+ * Codon ids in d_z are checked on the device before any kernel uses them: an
+ * id outside 0..60 gives GB_ERR_ARG and leaves the outputs untouched.
  * The first call on a device (with it current) looks up the scratch array's
- * device address; make it before any stream capture.  All calls share the
- * array: calls that overlap on the GPU race, so serialise them.
+ * device address and caches it for the process: do not use this entry point
+ * across a cudaDeviceReset.  It cannot be called on a stream that is being
+ * captured into a CUDA graph (GB_ERR_STATE): it synchronises the stream.  All
+ * calls share the array: calls that overlap on the GPU race, so serialise them.
  */
 #define GB_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 #define GB_MODEL_DOUBLES (6 * 61 * 61 + 3 * 61 + 2 + 4)

@@ -81,3 +81,48 @@ def test_noalloc_rejects_too_large_problem():
                           None, None)
     assert rc == -1
     assert "GB_NOALLOC_SCRATCH_BYTES" in L.gb_last_error().decode()
+
+
+def test_noalloc_rejects_bad_codon_ids_before_pruning():
+    """A codon id of 61 (an ambiguity code, or any stray byte) would index
+    past a 61-row transition matrix: the entry point must catch it on the
+    device before any pruning kernel reads it, return GB_ERR_ARG, leave the
+    caller's output alone, and serve the next good call normally."""
+    import torch
+    fx, tree, codons = load_golden("c8x300_s1")
+    z, fpatt, pi = O.patterns(codons)
+    pb = O.Problem(tree, z, fpatt, pi)
+    x = np.array(fx["x"])
+    U, V, R, qf, fk = pb.set_params(x)
+    L = _lib.load()
+    dev = torch.device("cuda", 0)
+    model = torch.from_numpy(np.concatenate([U.ravel(), V.ravel(), R.ravel(), qf, fk])).to(dev)
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[: tree.nbranch]
+    d_bl = torch.from_numpy(bl).to(dev)
+    d_fp = torch.from_numpy(fpatt).to(dev)
+    d_pi = torch.from_numpy(pi).to(dev)
+    father = np.ascontiguousarray(tree.father, dtype=np.int32)
+    label = np.ascontiguousarray(tree.label, dtype=np.int32)
+    ip = C.POINTER(C.c_int)
+    for bad_id in (61, 255):
+        zb = np.ascontiguousarray(z).copy()
+        zb[tree.ns // 2, len(fpatt) // 3] = bad_id
+        d_z = torch.from_numpy(zb).to(dev)
+        d_out = torch.full((1,), 12345.0, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        rc = L.gb_lnL_noalloc(tree.ns, tree.nnode, tree.root, father.ctypes.data_as(ip),
+                              label.ctypes.data_as(ip), None, len(fpatt), d_z.data_ptr(),
+                              d_fp.data_ptr(), d_pi.data_ptr(), model.data_ptr(), d_bl.data_ptr(),
+                              d_out.data_ptr(), None, None)
+        assert rc == -1, rc
+        assert "0..60" in L.gb_last_error().decode()
+        assert float(d_out.cpu()[0]) == 12345.0
+    d_z = torch.from_numpy(np.ascontiguousarray(z)).to(dev)
+    rc = L.gb_lnL_noalloc(tree.ns, tree.nnode, tree.root, father.ctypes.data_as(ip),
+                          label.ctypes.data_as(ip), None, len(fpatt), d_z.data_ptr(),
+                          d_fp.data_ptr(), d_pi.data_ptr(), model.data_ptr(), d_bl.data_ptr(),
+                          d_out.data_ptr(), None, None)
+    _lib.check(rc)
+    ref = pb.neg_lnL(x)
+    assert abs(float(d_out.cpu()[0]) - ref) <= 1e-12 * abs(ref)

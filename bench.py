@@ -15,10 +15,14 @@ lengths, kappa, w0, w2, p0, p1.
             host model set-up, host->device parameter copy, device->host result
             and gradient copies inside the timed region).
 * roofline -- the dominant kernel class, algorithmic FLOPs / its measured time.
-* cpu_baseline -- the oracle (CPU restatement of codeml's lnfundG path) on the
-            host cores, a bounded sample of lnL evaluations; a CPU lnL+gradient
+* cpu_baseline -- the reference codeml itself (its CPU build from the staged
+            reference sources, oracle/Makefile) on all host cores, one process
+            per core, a bounded sample: one step of lfundG plus one forward-
+            difference gradient coordinate per process; a CPU lnL+gradient
             costs np+1 lnL evaluations (codeml's forward-difference gradientB).
---impl reference times that CPU implementation as the reference arm.
+            Where the reference cannot be built, the oracle port.
+--impl reference times the same reference codeml, K steps after W warm-ups,
+as the reference arm.
 Multi-GPU: replicas only (each rank evaluates its own copy); value sums ranks.
 """
 from __future__ import annotations
@@ -268,7 +272,7 @@ def beb_leg(args, dev, tree, z, fpatt, pi, bl0):
     return out
 
 
-def se_leg(args, dev, tree, z, fpatt, pi, cpu_lnL_s=None):
+def se_leg(args, dev, tree, z, fpatt, pi, cpu_lnL_s=None, cpu_kind="port"):
     """codeml's standard errors (getSE = 1: 2 np likelihood evaluations and
     the outer-product Hessian, gb_se_opg, FP64) at the bench parameters; the
     CPU figure is 2 np oracle lnL evaluations at the CPU leg's measured time."""
@@ -287,15 +291,99 @@ def se_leg(args, dev, tree, z, fpatt, pi, cpu_lnL_s=None):
            "ms_device": r["ms_device"], "ms_e2e": 1000.0 * e2e, "kernels": r["kernels"],
            "se_all_positive": bool(np.all(r["se"] > 0))}
     if cpu_lnL_s:
-        out["cpu_baseline"] = {"value_ms": 1000.0 * 2 * n * cpu_lnL_s, "kind": "port",
-                               "sample": f"2 np = {2 * n} oracle lnL evaluations at the CPU leg's "
-                                         f"{cpu_lnL_s:.3f} s each"}
+        out["cpu_baseline"] = {"value_ms": 1000.0 * 2 * n * cpu_lnL_s, "kind": cpu_kind,
+                               "sample": f"2 np = {2 * n} lnL evaluations at the CPU leg's measured "
+                                         f"{cpu_lnL_s:.3f} s per evaluation of the whole host"}
         out["e2e_speedup_vs_cpu"] = 2 * n * cpu_lnL_s / e2e
     return out
 
 
-def cpu_baseline(tree, z, fpatt, pi, threads: int, seconds: float = 12.0, min_evals: int = 2):
-    """Time the oracle's lnL on the host cores; lnL+gradient = (np+1) lnL evals."""
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def reference_codeml_binary():
+    """The reference codeml (CPU build, its own compiler flags) linked with
+    oracle/ref_harness.c, built from the staged reference sources by
+    oracle/Makefile; None when it cannot be built here."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "codeml_timed")
+    if not os.path.exists(exe):
+        r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "timed"],
+                           capture_output=True, text=True)
+        if r.returncode != 0 or not os.path.exists(exe):
+            return None
+    return exe
+
+
+def reference_cpu(ns: int, ncodon: int, steps: int, warmup: int, procs: int, seed: int = 2024,
+                  coords_per_proc: int = 1):
+    """The reference's own CPU path on the host cores: `procs` concurrent
+    codeml processes (codeml is single-threaded), each on the whole workload
+    alignment.  A step of one process is codeml's lfundG at x plus the
+    forward differences of `coords_per_proc` gradient coordinates (gradientB's
+    forward branch, tools.c:6342-6346), i.e. 1 + coords_per_proc full lnL
+    evaluations; the processes take disjoint coordinates.  A forward-difference
+    lnL + gradient costs np + 1 lnL evaluations (ming2's first gradient,
+    tools.c:6396-6409), so the host's throughput in lnL + gradient evaluations
+    per second is procs (1 + coords_per_proc) / (T (np + 1)), T the slowest
+    process's mean step time: the np + 1 evaluations spread perfectly over the
+    cores (a bound in the reference's favour)."""
+    from cucodeml_gb300.simulate import simulate
+    from oracle import refcodeml as R
+    exe = reference_codeml_binary()
+    if exe is None:
+        return None
+    aln = simulate(ns, ncodon, seed=seed)
+    tree = aln.tree
+    x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
+                                                  PARAMS["omega0"], PARAMS["omega2"]]])
+    rows = R.alignment_rows(aln)
+    np_ = tree.nbranch + 5
+    import tempfile
+    dirs, runs = [], []
+    t0 = time.perf_counter()
+    try:
+        for r in range(procs):
+            d = tempfile.mkdtemp(prefix="gbref_")
+            dirs.append(d)
+            R.write_case(d, tree.names, rows, tree.to_newick(), x)
+            first = (r * coords_per_proc) % max(1, np_ - coords_per_proc + 1)
+            env = dict(os.environ, GBREF_MODE="time", GBREF_STEPS=str(steps), GBREF_WARMUP=str(warmup),
+                       GBREF_COORDS=f"{first}:{coords_per_proc}")
+            runs.append(subprocess.Popen([exe, "codeml.ctl"], cwd=d, env=env, stdout=subprocess.PIPE,
+                                         stderr=subprocess.PIPE, text=True))
+        outs = []
+        for p in runs:
+            o, e = p.communicate()
+            if p.returncode != 0:
+                raise RuntimeError(f"reference codeml exited {p.returncode}: {e[-500:]}")
+            outs.append(R.parse(o))
+    finally:
+        import shutil
+        for d in dirs:
+            shutil.rmtree(d, ignore_errors=True)
+    wall = time.perf_counter() - t0
+    T = max(statistics.mean(o["step_s"]) for o in outs)
+    evals = 1 + coords_per_proc
+    value = procs * evals / (T * (np_ + 1))
+    return {"value": value, "unit": "evals/s", "cores": procs, "kind": "reference",
+            "sample": (f"{procs} concurrent reference codeml processes (CPU build, its own -O3 flags; codeml "
+                       f"is single-threaded) on the whole {ns} x {ncodon} alignment ({outs[0]['npatt']} "
+                       f"patterns); a step of each = codeml's lfundG + {coords_per_proc} forward-difference "
+                       f"gradient coordinate(s) = {evals} lnL evaluations, {T:.3f} s (slowest process, mean "
+                       f"of {steps}); lnL+gradient = np+1 = {np_ + 1} evaluations spread over the "
+                       f"{procs} processes"),
+            "step_s": T, "lnL_eval_s": T / evals, "neg_lnL": outs[0]["f0"], "wall_s": wall,
+            "npatt": outs[0]["npatt"], "np": np_}
+
+
+def port_cpu(tree, z, fpatt, pi, threads: int, seconds: float = 12.0, min_evals: int = 2):
+    """The oracle port (C restatement of codeml's lfundG, OpenMP over
+    patterns) on the host cores, where the reference codeml cannot be built;
+    lnL+gradient = (np+1) lnL evaluations."""
     from oracle import oracle as O
     pb = O.Problem(tree, z, fpatt, pi, nthreads=threads)
     x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
@@ -316,35 +404,50 @@ def cpu_baseline(tree, z, fpatt, pi, threads: int, seconds: float = 12.0, min_ev
             "lnL_eval_s": dt}
 
 
+def workload_config(ns: int, ncodon: int) -> dict:
+    """The config both arms report (identical dicts)."""
+    return {"workload": f"lnL+gradient, {ns} taxa x {ncodon} codons, branch-site model A "
+                        f"(seeded simulation, seed 2024)",
+            "l2": "working set per evaluation > L2 (no flush needed)"}
+
+
 def run_reference(args):
+    """The reference arm: the reference codeml's own CPU lnL + gradient
+    (lfundG, forward-difference gradientB) on all host cores; the oracle port
+    when the reference cannot be built on this machine."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return 0
-    tree, z, fpatt, pi = make_workload(args.ns, args.ncodon)
-    from oracle import oracle as O
-    threads = O.max_threads()
-    pb = O.Problem(tree, z, fpatt, pi, nthreads=threads)
-    x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
-                                                  PARAMS["omega0"], PARAMS["omega2"]]])
-    for _ in range(args.warmup):
-        pb.neg_lnL(x)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        pb.neg_lnL(x)
-    dt = (time.perf_counter() - t0) / args.steps
-    np_ = tree.nbranch + 5
-    value = 1.0 / ((np_ + 1) * dt)
+    procs = host_cores()
+    ref = reference_cpu(args.ns, args.ncodon, args.steps, args.warmup, procs)
+    if ref is None:
+        from cucodeml_gb300.simulate import simulate
+        from oracle import oracle as O
+        aln = simulate(args.ns, args.ncodon, seed=2024)
+        z, fpatt, pi = O.patterns(aln.codons)
+        tree = aln.tree
+        pb = O.Problem(tree, z, fpatt, pi, nthreads=procs)
+        x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
+                                                      PARAMS["omega0"], PARAMS["omega2"]]])
+        for _ in range(args.warmup):
+            pb.neg_lnL(x)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            pb.neg_lnL(x)
+        dt = (time.perf_counter() - t0) / args.steps
+        np_ = tree.nbranch + 5
+        ref = {"value": 1.0 / ((np_ + 1) * dt), "unit": "evals/s", "cores": procs, "kind": "port",
+               "sample": f"reference codeml not buildable here: the oracle port, one lnL evaluation per "
+                         f"step ({dt:.3f} s) on {procs} threads; lnL+gradient = np+1 = {np_ + 1} evaluations",
+               "step_s": dt}
+    value = ref["value"]
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 * (np_ + 1),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * ref["step_s"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded model-A simulation)",
-        "config": {"workload": f"lnL+gradient, {args.ns} taxa x {args.ncodon} codons, branch-site model A",
-                   "npatt": int(len(fpatt)), "np": np_},
-        "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.steps} lnL evaluations per run on {threads} threads "
-                                   f"({dt:.3f} s each); lnL+gradient = np+1 lnL evaluations "
-                                   "(codeml's forward-difference gradientB)"},
+        "data": "synthetic (seeded model-A simulation, seed 2024)",
+        "config": workload_config(args.ns, args.ncodon),
+        "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -475,11 +578,10 @@ def main():
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "f64+split",
         "data": "synthetic (seeded model-A simulation, seed 2024)",
-        "config": {"workload": f"lnL+gradient, {args.ns} taxa x {args.ncodon} codons, branch-site model A",
-                   "npatt": int(len(fpatt)), "np": tree.nbranch + 5, "precision": precision,
-                   "l2": "working set per evaluation > L2 (no flush needed)",
-                   "parallelism": f"replicas x{ws}", "flops_lnL_grad_alg": fl["flops_lnL_grad"],
-                   "flops_nominal_lnL": fl["flops_nominal_lnL"]},
+        "config": workload_config(args.ns, args.ncodon),
+        "workload_detail": {"npatt": int(len(fpatt)), "np": tree.nbranch + 5, "precision": precision,
+                            "parallelism": f"replicas x{ws}", "flops_lnL_grad_alg": fl["flops_lnL_grad"],
+                            "flops_nominal_lnL": fl["flops_nominal_lnL"]},
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": "evals/s", "h2d_bytes_per_step": h2d / args.steps,
                 "d2h_bytes_per_step": d2h / args.steps},
@@ -506,12 +608,24 @@ def main():
         line["batched"] = batched_leg(args, dev)
     if not args.no_beb:
         line["beb"] = secondary_leg(beb_leg, args, dev, tree, z, fpatt, pi, bl0)
+    cpu_lnL_s, cpu_kind = None, "port"
     if rank == 0 and not args.no_cpu:
-        from oracle import oracle as O
-        line["cpu_baseline"] = cpu_baseline(tree, z, fpatt, pi, O.max_threads())
+        procs = host_cores()
+        ref = reference_cpu(args.ns, args.ncodon, 1, 0, procs)
+        if ref is None:
+            from oracle import oracle as O
+            ref = port_cpu(tree, z, fpatt, pi, O.max_threads())
+            cpu_lnL_s = ref["lnL_eval_s"]
+        else:
+            cpu_lnL_s = ref["lnL_eval_s"] / procs      # evaluations spread over the processes
+            ref["abs_dlnL_vs_ours"] = abs(ref["neg_lnL"] - lk.evaluate(bl0, grad=False, **PARAMS).neg_lnL)
+        cpu_kind = ref["kind"]
+        line["cpu_baseline"] = {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")
+                                if k in ref}
+        if "abs_dlnL_vs_ours" in ref:
+            line["cpu_baseline"]["abs_dlnL_vs_ours"] = ref["abs_dlnL_vs_ours"]
     if not args.no_beb:
-        line["se"] = secondary_leg(se_leg, args, dev, tree, z, fpatt, pi,
-                                   line.get("cpu_baseline", {}).get("lnL_eval_s"))
+        line["se"] = secondary_leg(se_leg, args, dev, tree, z, fpatt, pi, cpu_lnL_s, cpu_kind)
     lk.close()
     if rank == 0:
         print(json.dumps(line))

@@ -1,41 +1,114 @@
-"""The drop-in boundary as codeml sees it: codeml.c (unmodified, built with
--DCUDA) linked against libgbcodeml.so through codeml_adapter.c instead of
-cuda-codeml.o.  Needs the reference sources, so it runs only where they are;
-without a GPU the run must get through CUDA_Init's marshalling of codeml's
-globals (tree, patterns, scale nodes all accepted by gb_create's checks) and
-stop at the device check with the library's status, not crash."""
+"""The drop-in boundary as codeml sees it.
+
+The reference codeml.c, built with -DCUDA from the staged reference sources
+(oracle/Makefile `dropin`), is linked against libgbcodeml.so through
+codeml_adapter.c in place of cuda-codeml.o, together with oracle/ref_harness.c,
+which wraps codeml's call of ming2 (codeml.c:683-692).  Inside one codeml
+process, after codeml has read the data, compressed the patterns and called
+CUDA_Init:
+
+* `eval`: codeml's CUDA objective CUDA_lfundG (treesub.c:7397-7450, whose
+  CUDA_fx_r calls the adapter's CUDA_ScheduleConditionalPNode per class) must
+  equal codeml's own CPU lfundG at the same x within 1e-9 relative, for
+  branch-site models A and B and clade model C; for model A the adapter's
+  GB_dfun must equal codeml's central-difference gradient (gradientB with
+  AlwaysCenter, tools.c:6326-6350) within its step error.
+* `dfun` / unchanged: codeml's whole model-A fit, ming2 driven by GB_dfun
+  (the one-argument change at codeml.c:688) or by its own finite differences
+  of CUDA_lfundG, must reach the maximum codeml's CPU build reached
+  (tests/golden/mle_*).
+
+Without a GPU the run must get through CUDA_Init's marshalling and stop at
+the device check with the library's status.  The tests need the staged
+reference sources (oracle/_ref/src, `make -C oracle stage`)."""
 import os
+import re
 import subprocess
 import tempfile
 
 import numpy as np
 import pytest
 
-from tests.conftest import ROOT, load_golden
+from oracle import refcodeml as R
+from tests.conftest import ROOT, clade_names, golden_names, load_golden, mle_names, model_b_names
 
-REF = "/root/reference"
+SRC = os.path.join(ROOT, "oracle", "_ref", "src")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF), reason="reference sources not present")
-def test_dropin_codeml_links_and_marshals():
-    import torch
+def dropin_binary():
+    if not os.path.isfile(os.path.join(SRC, "codeml.c")):
+        pytest.skip("reference sources not staged (make -C oracle stage)")
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "dropin"])
-    exe = os.path.join(ROOT, "oracle", "_ref", "codeml_gb")
-    from cucodeml_gb300.simulate import write_phylip
-    from tests.golden.make_golden import CTL
-    fx, tree, codons = load_golden("c24x400_s3")
-    with tempfile.TemporaryDirectory() as d:
-        from cucodeml_gb300 import codon
-        with open(os.path.join(d, "seq.phy"), "w") as f:
-            f.write(f"{fx['ns']} {3 * fx['ncodon']}\n")
-            for nm, row in zip(fx["names"], fx["codons"]):
-                f.write(f"{nm}    {row.replace(' ', '')}\n")
-        with open(os.path.join(d, "tree.nwk"), "w") as f:
-            f.write(f"{fx['ns']} 1\n{fx['newick']}\n")
-        with open(os.path.join(d, "codeml.ctl"), "w") as f:
-            f.write(CTL.replace("RateAncestor = -1", "RateAncestor = 0"))
-        r = subprocess.run([exe, "codeml.ctl"], cwd=d, capture_output=True, text=True, timeout=300)
+    return R.binary("codeml_gb")
+
+
+def fixture_case(d, fx, x=None, ctl=R.CTL):
+    rows = [row.replace(" ", "") for row in fx["codons"]]
+    R.write_case(d, fx["names"], rows, fx["newick"], fx["x"] if x is None else x, ctl)
+
+
+def ctl_for(name):
+    if name.startswith("mb"):
+        return R.CTL.replace("NSsites = 2", "NSsites = 3").replace("ncatG = 4", "ncatG = 3")
+    if name.startswith("mc"):
+        return R.CTL.replace("model = 2", "model = 3")
+    return R.CTL
+
+
+def test_dropin_links_and_stops_at_device_check_without_gpu():
+    import torch
     if torch.cuda.is_available():
-        pytest.skip("GPU present: the drop-in would run the optimisation")
+        pytest.skip("a GPU is present: the GPU tests below run the drop-in")
+    exe = dropin_binary()
+    fx, _, _ = load_golden("c24x400_s3")
+    with tempfile.TemporaryDirectory() as d:
+        fixture_case(d, fx)
+        r = subprocess.run([exe, "codeml.ctl"], cwd=d, capture_output=True, text=True, timeout=300)
     assert r.returncode != 0
     assert "gbcodeml: gb_create failed (-7)" in r.stderr, r.stderr[-2000:]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", golden_names() + model_b_names() + clade_names())
+def test_dropin_objective_matches_codeml_cpu(name):
+    exe = dropin_binary()
+    fx, _, _ = load_golden(name)
+    model_a = name.startswith("c")
+    with tempfile.TemporaryDirectory() as d:
+        fixture_case(d, fx, ctl=ctl_for(name))
+        r = R.run(exe, d, "eval", env={"GBREF_DFUN": "1" if model_a else "0"}, timeout=900)
+    print(f"{name}: GPU {r['f_fun']:.10f} codeml CPU {r['f_cpu']:.10f}")
+    assert abs(r["f_fun"] - r["f_cpu"]) <= 1e-9 * abs(r["f_cpu"])
+    if model_a:
+        ga, gc = np.array(r["grad_dfun"]), np.array(r["grad_cpu_central"])
+        assert abs(r["f_dfun"] - r["f_cpu"]) <= 1e-9 * abs(r["f_cpu"])
+        err = np.abs(ga - gc) / (1.0 + np.abs(gc))
+        print(f"{name}: max gradient deviation from codeml's gradientB {err.max():.2e}")
+        assert err.max() <= 1e-4
+
+
+def codeml_fit_lnL(exe, fx, mode):
+    with tempfile.TemporaryDirectory() as d:
+        rows = [row.replace(" ", "") for row in fx["codons"]]
+        R.write_case(d, fx["names"], rows, fx["newick"])
+        env = dict(os.environ)
+        env.pop("GBREF_MODE", None)
+        if mode:
+            env["GBREF_MODE"] = mode
+        r = subprocess.run([exe, "codeml.ctl"], cwd=d, capture_output=True, text=True, timeout=1800, env=env)
+        assert r.returncode == 0, r.stderr[-2000:]
+        out = open(os.path.join(d, "out.txt")).read()
+    m = re.search(r"lnL\(ntime:\s*\d+\s+np:\s*\d+\):\s*(-?\d+\.\d+)", out)
+    return float(m.group(1))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["dfun", None])
+def test_dropin_fit_reaches_codeml_maximum(mode):
+    exe = dropin_binary()
+    fx, _, _ = load_golden(mle_names()[0])
+    lnL = codeml_fit_lnL(exe, fx, mode)
+    print(f"codeml over the GPU drop-in ({mode or 'finite differences'}): lnL {lnL:.6f}, "
+          f"codeml CPU {fx['alt']['lnL']:.6f}")
+    assert lnL >= fx["alt"]["lnL"] - 1e-5
+    assert lnL - fx["alt"]["lnL"] <= 2e-3

@@ -338,8 +338,11 @@ def reference_cpu(ns: int, ncodon: int, steps: int, warmup: int, procs: int, see
         return None
     aln = simulate(ns, ncodon, seed=seed)
     tree = aln.tree
-    x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], PARAMS["p0"], PARAMS["p1"],
-                                                  PARAMS["omega0"], PARAMS["omega2"]]])
+    # codeml's own x space inside ming2 (LASTROUND = 0): p0, p1 through
+    # f_and_x (tools.c:1280-1305), p_i = e^{x_i} / (1 + e^{x_0} + e^{x_1})
+    p2 = 1.0 - PARAMS["p0"] - PARAMS["p1"]
+    x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], np.log(PARAMS["p0"] / p2),
+                                                  np.log(PARAMS["p1"] / p2), PARAMS["omega0"], PARAMS["omega2"]]])
     rows = R.alignment_rows(aln)
     np_ = tree.nbranch + 5
     import tempfile

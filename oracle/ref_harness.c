@@ -24,7 +24,8 @@
  *            wall times, then exits.
  *   eval     prints fun(x) and codeml's CPU objective com.plfun(x) at the
  *            same x, codeml's central-difference gradient of com.plfun
- *            (gradientB with AlwaysCenter), and with GBREF_DFUN=1 where the
+ *            (gradientB with AlwaysCenter), a five-point stencil of
+ *            com.plfun (step 1e-4 (|x_i| + 0.05)), and with GBREF_DFUN=1 where the
  *            adapter's GB_dfun is linked in (model A), its analytic gradient
  *            at x; then exits.
  *   dfun     runs ming2 with the adapter's GB_dfun as its gradient hook
@@ -113,25 +114,42 @@ static void mode_time(objective_t fun, double x[], int n) {
 static void mode_eval(objective_t fun, double x[], int n) {
     double *g = (double *)malloc(sizeof(double) * n), *tv = (double *)malloc(sizeof(double) * 2 * n);
     double *ga = (double *)malloc(sizeof(double) * n), f_fun, f_cpu, fa = 0;
+    double *g5 = (double *)malloc(sizeof(double) * n);
+    int i;
     int *xmark = (int *)calloc(n, sizeof(int)), have = GB_dfun != NULL && env_int("GBREF_DFUN", 0);
-    if (!g || !tv || !ga || !xmark) { fprintf(stderr, "ref_harness: out of memory\n"); exit(2); }
+    if (!g || !tv || !ga || !g5 || !xmark) { fprintf(stderr, "ref_harness: out of memory\n"); exit(2); }
     f_fun = fun(x, n);
     f_cpu = com.plfun(x, n);
     if (have) GB_dfun(x, &fa, ga, n);
     AlwaysCenter = 1;
     gradientB(n, x, f_cpu, g, com.plfun, tv, xmark);
+    /* a five-point stencil of the same CPU objective, step 1e-4 (|x_i| + 0.05):
+       truncation O(h^4), an accurate derivative of codeml's own lnL */
+    for (i = 0; i < n; i++) {
+        static const int k[4] = {-2, -1, 1, 2};
+        double f[4], h = 1e-4 * (fabs(x[i]) + 0.05), *x1 = tv + n;
+        int q;
+        for (q = 0; q < 4; q++) {
+            memcpy(x1, x, sizeof(double) * n);
+            x1[i] += k[q] * h;
+            f[q] = com.plfun(x1, n);
+        }
+        g5[i] = (f[0] - 8 * f[1] + 8 * f[2] - f[3]) / (12 * h);
+    }
     printf("\nGBREF {\"mode\": \"eval\", \"np\": %d, \"npatt\": %d, \"ns\": %d, \"f_fun\": %.17g, "
            "\"f_cpu\": %.17g, ", n, com.npatt, com.ns, f_fun, f_cpu);
     print_vec("x", x, n);
     printf(", ");
     print_vec("grad_cpu_central", g, n);
+    printf(", ");
+    print_vec("grad_cpu_5pt", g5, n);
     if (have) {
         printf(", \"f_dfun\": %.17g, ", fa);
         print_vec("grad_dfun", ga, n);
     }
     printf("}\n");
     fflush(stdout);
-    free(g); free(tv); free(ga); free(xmark);
+    free(g); free(tv); free(ga); free(g5); free(xmark);
 }
 
 int __wrap_ming2(FILE *fout, double *f, objective_t fun, gradient_t dfun, double x[], double xb[][2],

@@ -59,6 +59,9 @@ SIGNATURES = {
     "gb_version": (C.c_char_p, []),
     "gb_last_error": (C.c_char_p, []),
     "gb_create": (C.c_int, [C.POINTER(Problem), C.POINTER(C.c_void_p)]),
+    "gb_fault_inject": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "gb_create_unclean": (C.c_int, [C.POINTER(Problem), C.POINTER(C.c_ubyte), C.POINTER(C.c_ubyte),
+                                    C.POINTER(C.c_void_p)]),
     "gb_destroy": (C.c_int, [C.c_void_p]),
     "gb_nscale": (C.c_int, [C.c_void_p]),
     "gb_eval_uvr": (C.c_int, [C.c_void_p, _dp * 3, _dp * 3, _dp * 3, _dp, _dp, _dp, _dp, _dp, _dp,

@@ -137,7 +137,11 @@ class EvalResult:
 
 class Likelihood:
     def __init__(self, tree: Tree, z: np.ndarray, fpatt: np.ndarray, pi: np.ndarray,
-                 precision: str = "fp64", device: int = 0, node_scale=None, tuning: dict | None = None):
+                 precision: str = "fp64", device: int = 0, node_scale=None, tuning: dict | None = None,
+                 ambiguity=None):
+        """ambiguity: None for clean data, or codeml's (nChara[256],
+        CharaMap[256][64]) for tip codes z >= 61 (gaps and ambiguous codons,
+        cleandata = 0; FP64 only, gb_create_unclean)."""
         self._L = _lib.load()
         self.tree = tree
         self.ns, self.nnode = tree.ns, tree.nnode
@@ -158,7 +162,14 @@ class Likelihood:
                                   self._z.ctypes.data_as(C.POINTER(C.c_ubyte)), _ptr(self._fpatt),
                                   _ptr(self._pi), self._scale, prec, device)
         h = C.c_void_p()
-        _lib.check(self._L.gb_create(C.byref(self._prob), C.byref(h)))
+        if ambiguity is None:
+            _lib.check(self._L.gb_create(C.byref(self._prob), C.byref(h)))
+        else:
+            self._nch = np.ascontiguousarray(np.asarray(ambiguity[0]).reshape(256), dtype=np.uint8)
+            self._cmap = np.ascontiguousarray(np.asarray(ambiguity[1]).reshape(256 * 64), dtype=np.uint8)
+            ub = C.POINTER(C.c_ubyte)
+            _lib.check(self._L.gb_create_unclean(C.byref(self._prob), self._nch.ctypes.data_as(ub),
+                                                 self._cmap.ctypes.data_as(ub), C.byref(h)))
         self._h = h
         for knob, value in (tuning or {}).items():
             _lib.check(self._L.gb_tune(self._h, _lib.TUNE[knob], int(value)))

@@ -249,7 +249,8 @@ __global__ void __launch_bounds__(128) gradP_kernel(const Contrib *__restrict__ 
                                                     const double *__restrict__ Ebar,
                                                     const double *__restrict__ conP,
                                                     const unsigned char *__restrict__ z,
-                                                    double *__restrict__ Gpart, int nchunk) {
+                                                    double *__restrict__ Gpart, int nchunk,
+                                                    const unsigned char *__restrict__ amb) {
     extern __shared__ double smg[];
     double *Es = smg;                    // [32][65]
     double *Xs = smg + TILE64 * 65;      // [32][65]
@@ -292,7 +293,15 @@ __global__ void __launch_bounds__(128) gradP_kernel(const Contrib *__restrict__ 
             } else if (tid < 64) {
                 // tip: X is one-hot at z[h]; thread tid owns row j = tid of Gs
                 const unsigned char *zz = z + (size_t)cb.tip * npad + hb;
-                for (int hh = 0; hh < nh; hh++) Gs[tid * 65 + zz[hh]] += Es[hh * 65 + tid];
+                for (int hh = 0; hh < nh; hh++) {
+                    const int c = zz[hh];
+                    if (c < NCd || !amb) {
+                        Gs[tid * 65 + c] += Es[hh * 65 + tid];
+                    } else {   // ambiguous codon: X[h][k] = 1 for each sense codon k it stands for
+                        const unsigned char *map = amb + 256 + 64 * c;
+                        for (int q = 0; q < amb[c]; q++) Gs[tid * 65 + map[q]] += Es[hh * 65 + tid];
+                    }
+                }
             }
         }
     }
@@ -744,7 +753,7 @@ int record_backward(gb_handle *h) {
     }
     dim3 g2((unsigned)h->pairs.size(), a->nchunk);
     gradP_kernel<<<g2, 128, kGradPSmem, h->stream>>>(a->d_contrib, a->d_coff, h->npatt, h->npad, a->d_Ebar,
-                                            h->d_conP, h->d_z, a->d_Gpart, a->nchunk);
+                                            h->d_conP, h->d_z, a->d_Gpart, a->nchunk, h->d_amb);
     prof_mark(h, GB_K_GRADP);
     nk++;
     gradH_kernel<<<(unsigned)h->pairs.size(), 256, kGradHSmem, h->stream>>>(h->d_pairs, h->d_label, h->d_tnode,

@@ -251,7 +251,7 @@ int ensure_cls_graph(gb_handle *h, int mask) {
         if (n == 0) continue;
         launch_prune_fp64(h->d_items_cls[mask] + off[L], n, h->ntile, h->npad, h->d_z, h->d_Pt, h->d_conP,
                           nullptr, h->d_scaleF, h->d_scale_list, h->nscale, h->d_pi, h->d_fbar, h->d_ssum,
-                          h->d_fhK, h->stream);
+                          h->d_fhK, h->stream, h->d_amb);
         nk++;
     }
     CK(cudaStreamEndCapture(h->stream, &g));

@@ -40,8 +40,10 @@ static gb_handle *make_handle(const char *who) {
     char *scale = NULL;
     gb_problem p;
     gb_handle *h = NULL;
+    /* codeml itself runs no branch-site or clade model on several genes
+       (codeml.c:357); gaps and ambiguous codons (cleandata = 0) go to
+       gb_create_unclean with codeml's own nChara / CharaMap */
     if (com.ngene != 1) gb_die(who, GB_ERR_ARG);
-    if (!com.cleandata) gb_die(who, GB_ERR_ARG);
     if (com.ncode != GB_NCODE) gb_die(who, GB_ERR_ARG);
     z = (unsigned char *)malloc((size_t)com.ns * com.npatt);
     father = (int *)malloc(sizeof(int) * tree.nnode);
@@ -69,7 +71,8 @@ static gb_handle *make_handle(const char *who) {
         scale = (char *)calloc(tree.nnode, 1);
         p.node_scale = scale;
     }
-    rc = gb_create(&p, &h);
+    rc = com.cleandata ? gb_create(&p, &h)
+                       : gb_create_unclean(&p, (const unsigned char *)nChara, (const unsigned char *)CharaMap, &h);
     if (scale && scale != com.nodeScale) free(scale);
     free(z);
     free(father);
@@ -93,7 +96,7 @@ void CUDA_Init(double *x) {
     if (!g_blen || !g_bnode || !g_fhK || !g_fhK2) gb_die("CUDA_Init (host memory)", GB_ERR_OOM);
     for (i = 0; i < tree.nnode; i++)
         if (i != tree.root) g_bnode[nodes[i].ibranch] = i;
-    g_h = make_handle("CUDA_Init (one gene, cleandata = 1, universal code only)");
+    g_h = make_handle("CUDA_Init (one gene, universal code only)");
 }
 
 void CUDA_ScheduleConditionalPNode(int ir, int ig, double *x) {
@@ -151,7 +154,7 @@ int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], 
     if (!bl) gb_die("GB_BEB (host memory)", GB_ERR_OOM);
     for (i = 0; i < tree.nnode; i++)
         if (i != tree.root) bl[i] = x[nodes[i].ibranch];
-    h = make_handle("GB_BEB (one gene, cleandata = 1, universal code only)");
+    h = make_handle("GB_BEB (one gene, universal code only)");
     /* kappa from x, the Qfactors of the last SetParameters (at the MLE), as
        codeml's BEB reads them (GetPMatBranch treesub.c:7289-7301): models A and B */
     rc = gb_beb_qf(h, bl, x[com.ntime], Qfactor_NS_branch, NULL, postSite, grid, p0p1, lnfX, NULL, NULL, NULL);
@@ -172,7 +175,7 @@ int GB_HessianSKT2004(double xmle[], double lnLm, double g[], double H[]) {
     if (!bnode) gb_die("GB_HessianSKT2004 (host memory)", GB_ERR_OOM);
     for (ib = 0; ib < tree.nnode; ib++)
         if (ib != tree.root) bnode[nodes[ib].ibranch] = ib;
-    h = make_handle("GB_HessianSKT2004 (one gene, cleandata = 1, universal code only)");
+    h = make_handle("GB_HessianSKT2004 (one gene, universal code only)");
     rc = gb_se_opg(h, bnode, xmle, n, Small_Diff, g, H, NULL, NULL);
     gb_destroy(h);
     free(bnode);

@@ -561,6 +561,17 @@ int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap) 
     CK(cudaSetDevice(h->device));
     return persist_task_trace(&h->fast->plan, kernel, out, cap);
 }
+int fast_fault_inject(gb_handle *h, int wait_ms, int withhold) {
+    if (!h->fast || !h->fast->persist || !h->fast->plan.ctl)
+        return fail(GB_ERR_STATE, "gb_fault_inject: the handle's persistent kernels have not run yet");
+    if (wait_ms < 0 || wait_ms > 60000 || (withhold != 0 && withhold != 1))
+        return fail(GB_ERR_ARG, "gb_fault_inject: wait_ms in 0..60000, withhold 0 or 1");
+    CK(cudaSetDevice(h->device));
+    CK(cudaStreamSynchronize(h->stream));
+    const unsigned w[2] = {(unsigned)withhold, (unsigned)wait_ms};
+    CK(cudaMemcpy(h->fast->plan.ctl + CTL_SKEW, w, sizeof(w), cudaMemcpyHostToDevice));
+    return GB_OK;
+}
 int fast_ns(const gb_handle *h, bool adjoint) { return adjoint ? h->fast->nsb : h->fast->ns; }
 
 // one gene's whole evaluation with one launch per tree level (batches whose

@@ -22,7 +22,10 @@ struct Task {
 // control words of a persistent executor (device memory): the evaluation
 // epoch (ready flags hold the epoch of the evaluation that wrote them) and
 // the task counters of the three persistent kernels
-enum { CTL_EPOCH = 0, CTL_FWD = 1, CTL_BWD = 2, CTL_GRADP = 3, CTL_WORDS = 4 };
+// CTL_SKEW, CTL_WAIT_MS: the bounded flag waits compare against epoch + skew
+// (0: the current evaluation; gb_fault_inject sets 1, a value nothing writes)
+// and give up after CTL_WAIT_MS milliseconds (0: 2000)
+enum { CTL_EPOCH = 0, CTL_FWD = 1, CTL_BWD = 2, CTL_GRADP = 3, CTL_SKEW = 4, CTL_WAIT_MS = 5, CTL_WORDS = 6 };
 
 struct FastFwdArgs;
 struct FastBwdArgs;

@@ -93,6 +93,7 @@ struct gb_handle {
     gb::PairDesc *d_pairs = nullptr;
     int *d_label = nullptr, *d_scale_list = nullptr;
     unsigned char *d_z = nullptr;
+    unsigned char *d_amb = nullptr;   // unclean data: nChara[256] + CharaMap[256][64] (null: clean)
     double *d_fpatt = nullptr, *d_pi = nullptr, *d_tnode = nullptr;
     gb::DevParams *d_prm = nullptr;
     double *d_Pt = nullptr, *d_conP = nullptr, *d_E = nullptr, *d_scaleF = nullptr;
@@ -144,6 +145,7 @@ float2 *fast_groot(gb_handle *h);                               // adjoint root 
 PsliceArgs fast_pslice_args(gb_handle *h);                      // P digit-plane buffers (batched launches)
 void fast_swap_err(gb_handle *h, int *&d_err, int *&h_err);     // exchange the error word (batch staging)
 int fast_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);
+int fast_fault_inject(gb_handle *h, int wait_ms, int withhold);
 int persist_task_trace(PersistPlan *pp, int kernel, unsigned long long *out, int cap);
 int fast_ns(const gb_handle *h, bool adjoint);
 // persistent executors over one or many genes (fast.cu)

@@ -60,7 +60,7 @@ void launch_pmat_fp64(const PairDesc *pairs, int npair, const int *label, const 
 void launch_prune_fp64(const Item *items, int nitems, int ntile, int npad, const unsigned char *z,
                        const double *Pt, double *conP, double *E, double *scaleF,
                        const int *scale_list, int nscale, const double *pi, double *fbar,
-                       double *ssum, double *fhK, cudaStream_t st);
+                       double *ssum, double *fhK, cudaStream_t st, const unsigned char *amb = nullptr);
 void launch_mix(const double *fhK, const double *fpatt, const DevParams *prm, int npatt, int npad,
                 int nscale, double *lnf, double *post, double *partial, unsigned *ticket,
                 double *out, cudaStream_t st, const double *fbar = nullptr, float2 *groot = nullptr);

@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(128) prune_fp64_kernel(
     const double *__restrict__ Pt, double *__restrict__ conP, double *__restrict__ E,
     double *__restrict__ scaleF, const int *__restrict__ scale_list, int nscale,
     const double *__restrict__ pi, double *__restrict__ fbar, double *__restrict__ ssum,
-    double *__restrict__ fhK) {
+    double *__restrict__ fhK, const unsigned char *__restrict__ amb) {
     __shared__ double Ps[NC * 64];          // rows k < 61 of Pt
     __shared__ double Ls[TILE64 * 65];
     const Item it = items[blockIdx.y];
@@ -151,8 +151,19 @@ __global__ void __launch_bounds__(128) prune_fp64_kernel(
 #pragma unroll
             for (int r = 0; r < 4; r++) {
                 const int zz = zc[r];
+                if (zz < NC || !amb) {
 #pragma unroll
-                for (int c = 0; c < 4; c++) tmp[r][c] = Ps[zz * 64 + c0 + c];
+                    for (int c = 0; c < 4; c++) tmp[r][c] = Ps[zz * 64 + c0 + c];
+                } else {
+                    // an ambiguous codon: the sum over the sense codons it stands
+                    // for, in codeml's CharaMap order (codeml.c:3438-3445)
+                    const unsigned char *map = amb + 256 + 64 * zz;
+#pragma unroll
+                    for (int c = 0; c < 4; c++) tmp[r][c] = 0.0;
+                    for (int q = 0; q < amb[zz]; q++)
+#pragma unroll
+                        for (int c = 0; c < 4; c++) tmp[r][c] += Ps[map[q] * 64 + c0 + c];
+                }
             }
         } else {
             const double *L = conP + ((size_t)it.cslot[ci] * npad + h0) * 64;
@@ -385,10 +396,10 @@ void launch_pmat_fp64(const PairDesc *pairs, int npair, const int *label, const 
 void launch_prune_fp64(const Item *items, int nitems, int ntile, int npad, const unsigned char *z,
                        const double *Pt, double *conP, double *E, double *scaleF,
                        const int *scale_list, int nscale, const double *pi, double *fbar,
-                       double *ssum, double *fhK, cudaStream_t st) {
+                       double *ssum, double *fhK, cudaStream_t st, const unsigned char *amb) {
     dim3 grid(ntile, nitems);
     prune_fp64_kernel<<<grid, 128, 0, st>>>(items, npad, z, Pt, conP, E, scaleF, scale_list,
-                                            nscale, pi, fbar, ssum, fhK);
+                                            nscale, pi, fbar, ssum, fhK, amb);
 }
 
 void launch_mix(const double *fhK, const double *fpatt, const DevParams *prm, int npatt, int npad,

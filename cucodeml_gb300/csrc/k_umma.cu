@@ -107,19 +107,28 @@ __device__ __forceinline__ void stage(T *dst, const T *src) {
 
 // ---------------------------------------------------------------- cross-CTA flags
 
-// Wait until *flag == epoch (acquire).  Bounded: gives up after 2 s, or at
-// once when *err is set by another CTA.
-__device__ __forceinline__ bool wait_flag(const unsigned *flag, unsigned epoch, const int *err) {
+// Wait until *flag == epoch (acquire).  Bounded: gives up after limit_ns
+// (2 s unless the handle's wait limit says otherwise), or at once when *err is
+// set by another CTA.
+__device__ __forceinline__ bool wait_flag(const unsigned *flag, unsigned epoch, const int *err,
+                                          uint64_t limit_ns) {
     const uint64_t t0 = umma::global_ns();
     for (int i = 0; i < (1 << 26); i++) {
         unsigned v;
         asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(flag) : "memory");
         if (v == epoch) return true;
         if (*reinterpret_cast<const volatile int *>(err)) return false;
-        if (umma::global_ns() - t0 > 2000000000ull) return false;
+        if (umma::global_ns() - t0 > limit_ns) return false;
         __nanosleep(100);
     }
     return false;
+}
+
+// the epoch a consumer waits for and the wait limit, from the control words
+__device__ __forceinline__ unsigned wait_epoch(const unsigned *ctl) { return ctl[CTL_EPOCH] + ctl[CTL_SKEW]; }
+__device__ __forceinline__ uint64_t wait_limit(const unsigned *ctl) {
+    const unsigned ms = ctl[CTL_WAIT_MS];
+    return (ms ? ms : 2000u) * 1000000ull;
 }
 
 __device__ __forceinline__ void set_flag(unsigned *flag, unsigned epoch) {
@@ -567,7 +576,8 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
     Misc *m = reinterpret_cast<Misc *>(sm + USm<NS>::OFF_MISC);
     FastFwdArgs *a = reinterpret_cast<FastFwdArgs *>(sm + USm<NS>::OFF_ARGS);
     Item *it = reinterpret_cast<Item *>(sm + USm<NS>::OFF_ITEM);
-    const unsigned epoch = ctl[CTL_EPOCH];
+    const unsigned epoch = ctl[CTL_EPOCH], awaited = wait_epoch(ctl);
+    const uint64_t limit = wait_limit(ctl);
     tmem_setup(m);
     uint32_t phase = 0;
     for (;;) {
@@ -589,7 +599,7 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
                                       128 * 64 * sizeof(float2));
             for (int ci = 0; ci < it->nchild && good; ci++)
                 if (it->cslot[ci] >= 0)
-                    good = wait_flag(a->ready + (size_t)it->cslot[ci] * a->ntile + t.tile, epoch, a->err);
+                    good = wait_flag(a->ready + (size_t)it->cslot[ci] * a->ntile + t.tile, awaited, a->err, limit);
         }
         if (!__syncthreads_and(good)) {
             if (threadIdx.x == 0) atomicExch(a->err, 1);
@@ -779,7 +789,8 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
     Misc *m = reinterpret_cast<Misc *>(sm + USm<NS>::OFF_MISC);
     FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + USm<NS>::OFF_ARGS);
     BItem *it = reinterpret_cast<BItem *>(sm + USm<NS>::OFF_ITEM);
-    const unsigned epoch = ctl[CTL_EPOCH];
+    const unsigned epoch = ctl[CTL_EPOCH], awaited = wait_epoch(ctl);
+    const uint64_t limit = wait_limit(ctl);
     tmem_setup(m);
     uint32_t phase = 0;
     for (;;) {
@@ -806,7 +817,7 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
         }
         if (threadIdx.x == 0 && !it->is_root)
             for (int k = 0; k < it->ncls && good; k++)
-                good = wait_flag(a->ready + (size_t)it->pslot[k] * a->ntile + t.tile, epoch, a->err);
+                good = wait_flag(a->ready + (size_t)it->pslot[k] * a->ntile + t.tile, awaited, a->err, limit);
         if (!__syncthreads_and(good)) {
             if (threadIdx.x == 0) atomicExch(a->err, 1);
             break;

@@ -187,7 +187,8 @@ void free_all(gb_handle *h) {
     }
     void *dev[] = {h->d_items, h->d_pairs, h->d_label, h->d_scale_list, h->d_z, h->d_fpatt, h->d_pi,
                    h->d_tnode, h->d_prm, h->d_Pt, h->d_conP, h->d_E, h->d_scaleF, h->d_fbar,
-                   h->d_ssum, h->d_fhK, h->d_lnf, h->d_post, h->d_partial, h->d_out, h->d_ticket};
+                   h->d_ssum, h->d_fhK, h->d_lnf, h->d_post, h->d_partial, h->d_out, h->d_ticket,
+                   h->d_amb};
     for (void *p : dev)
         if (p) cudaFree(p);
     if (h->h_prm) cudaFreeHost(h->h_prm);
@@ -214,7 +215,7 @@ int record_forward(gb_handle *h, bool keepE) {
         if (n == 0) continue;
         launch_prune_fp64(h->d_items + h->level_off[L], n, h->ntile, h->npad, h->d_z, h->d_Pt,
                           h->d_conP, keepE ? h->d_E : nullptr, h->d_scaleF, h->d_scale_list,
-                          h->nscale, h->d_pi, h->d_fbar, h->d_ssum, h->d_fhK, h->stream);
+                          h->nscale, h->d_pi, h->d_fbar, h->d_ssum, h->d_fhK, h->stream, h->d_amb);
         prof_mark(h, GB_K_PRUNE);
         nk++;
     }
@@ -354,7 +355,10 @@ const char *gb_version(void) { return "gbcodeml 0.1 (sm_103a)"; }
 
 const char *gb_last_error(void) { return g_err.c_str(); }
 
-int gb_create(const gb_problem *prob, gb_handle **out) {
+namespace {
+// gb_create and gb_create_unclean: amb (nullable) is codeml's nChara[256]
+// followed by CharaMap[256][64]
+int create_handle(const gb_problem *prob, const unsigned char *amb, gb_handle **out) {
     if (!prob || !out) return fail(GB_ERR_ARG, "null argument");
     *out = nullptr;
     int prec = prob->precision, slices = 8;
@@ -370,8 +374,28 @@ int gb_create(const gb_problem *prob, gb_handle **out) {
     h->fast_slices = slices;
     int rc = build_schedule(h, prob);
     if (rc) { free_all(h); return rc; }
-    for (size_t i = 0; i < (size_t)prob->ns * prob->npatt; i++)
-        if (prob->z[i] >= 61) { free_all(h); return fail(GB_ERR_ARG, "z: codon id >= 61 (only clean data)"); }
+    bool unclean = false;
+    for (size_t i = 0; i < (size_t)prob->ns * prob->npatt; i++) {
+        const int c = prob->z[i];
+        if (c < 61) continue;
+        if (!amb) { free_all(h); return fail(GB_ERR_ARG, "z: codon id >= 61 (clean data; gb_create_unclean "
+                                                         "takes ambiguity codes)"); }
+        if (amb[c] < 1 || amb[c] > 61) {
+            free_all(h);
+            return fail(GB_ERR_ARG, "ambiguity code " + std::to_string(c) + " stands for no sense codon");
+        }
+        for (int q = 0; q < amb[c]; q++)
+            if (amb[256 + 64 * c + q] >= 61) {
+                free_all(h);
+                return fail(GB_ERR_ARG, "ambiguity code " + std::to_string(c) + " maps to a codon id >= 61");
+            }
+        unclean = true;
+    }
+    if (unclean && prec != GB_PREC_FP64) {
+        free_all(h);
+        return fail(GB_ERR_ARG, "ambiguous codons: GB_PREC_FP64 only (the split-precision kernels take "
+                                "clean data)");
+    }
     h->pi.assign(prob->pi, prob->pi + 61);
     h->fpatt.assign(prob->fpatt, prob->fpatt + prob->npatt);
     for (double v : h->pi)
@@ -421,8 +445,25 @@ int gb_create(const gb_problem *prob, gb_handle **out) {
         cudaMemset(h->d_post, 0, sizeof(double) * 4 * npad) || cudaMemset(h->d_fbar, 0, sizeof(double) * 4 * npad) ||
         cudaMemset(h->d_lnf, 0, sizeof(double) * npad) || init_fp64_kernels())
         return bad(fail(GB_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(cudaGetLastError())));
+    if (unclean) {
+        if ((rc = dalloc(&h->d_amb, (size_t)256 + 256 * 64))) return bad(rc);
+        if (cudaMemcpy(h->d_amb, amb, 256 + 256 * 64, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bad(fail(GB_ERR_CUDA, "upload of the ambiguity tables"));
+    }
     *out = h;
     return GB_OK;
+}
+}  // namespace
+
+int gb_create(const gb_problem *prob, gb_handle **out) { return create_handle(prob, nullptr, out); }
+
+int gb_create_unclean(const gb_problem *prob, const unsigned char *nchara, const unsigned char *charamap,
+                      gb_handle **out) {
+    if (!nchara || !charamap) return fail(GB_ERR_ARG, "null ambiguity tables");
+    std::vector<unsigned char> amb((size_t)256 + 256 * 64);
+    std::memcpy(amb.data(), nchara, 256);
+    std::memcpy(amb.data() + 256, charamap, 256 * 64);
+    return create_handle(prob, amb.data(), out);
 }
 
 int gb_destroy(gb_handle *h) {
@@ -615,6 +656,11 @@ int gb_tune(gb_handle *h, int knob, int value) {
 int gb_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap) {
     if (!h || cap < 0) return fail(GB_ERR_ARG, "gb_task_trace: bad arguments");
     return fast_task_trace(h, kernel, out, cap);
+}
+
+int gb_fault_inject(gb_handle *h, int wait_ms, int withhold) {
+    if (!h) return fail(GB_ERR_ARG, "gb_fault_inject: null handle");
+    return fast_fault_inject(h, wait_ms, withhold);
 }
 
 int gb_model_setup(const double *pi, double kappa, double omega0, double omega2, double p0, double p1,

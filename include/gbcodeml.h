@@ -143,6 +143,19 @@ const char *gb_last_error(void);
    change between evaluations.  Replaces CUDA_Init (cuda-codeml.cu:1106). */
 int gb_create(const gb_problem *prob, gb_handle **out);
 
+/* gb_create for data with gaps and ambiguous codons (codeml's cleandata = 0):
+   z may hold codes >= 61, each standing for the nchara[z] sense codons
+   charamap[64 * z + 0 .. nchara[z] - 1] (codeml's nChara[256] and
+   CharaMap[256][64] from SetMapAmbiguity treesub.c:1146-1200, as
+   EncodeSeqs treesub.c:1075-1143 numbers them).  A tip with such a code
+   contributes the sum of its transition probabilities over those codons, as
+   the reference's unclean tip kernels (cuda-codeml.cu:166-204) and
+   ConditionalPNode (codeml.c:3438-3445) do.  GB_PREC_FP64 only; the forward
+   evaluation, the adjoint gradient, BEB, NEB and standard errors all take
+   such data.  GB_ERR_ARG for a code that stands for no sense codon. */
+int gb_create_unclean(const gb_problem *prob, const unsigned char *nchara, const unsigned char *charamap,
+                      gb_handle **out);
+
 /* Free device memory and the handle.  Replaces CUDA_FreeAll (cuda-codeml.cu:1162). */
 int gb_destroy(gb_handle *h);
 
@@ -373,6 +386,21 @@ int gb_batch_tune(gb_batch *b, int knob, int value);
 int gb_task_trace(gb_handle *h, int kernel, unsigned long long *out, int cap);
 /* the same for a batch's persistent kernels (gene = index in the batch) */
 int gb_batch_task_trace(gb_batch *b, int kernel, unsigned long long *out, int cap);
+
+/*
+ * The persistent split-precision kernels' cross-CTA waits (a task waits for
+ * the ready flags of the tiles it reads) are bounded: after wait_ms
+ * milliseconds (0: the default, 2000) a waiting CTA sets the handle's error
+ * word, stops claiming tasks, frees its tensor memory and returns, and the
+ * evaluation returns GB_ERR_TIMEOUT.  withhold = 1 makes every such wait
+ * expect a flag value that no task writes, so the next evaluations end that
+ * way (a test of the error path that faults and hangs nothing); withhold = 0
+ * restores normal evaluations on the same handle.  Needs a GB_PREC_FAST
+ * handle whose persistent kernels have run (GB_ERR_STATE otherwise).  No
+ * counterpart in the reference, which exits on any CUDA error
+ * (cuda-codeml.cu:20-39).
+ */
+int gb_fault_inject(gb_handle *h, int wait_ms, int withhold);
 
 /*
  * Host-only model set-up (no GPU needed): for codon frequencies pi[61] and

@@ -20,7 +20,9 @@
  *   set_params        SetParametersNSsites codeml.c:2381-2414, 2488-2521 and
  *                     f_and_x tools.c:1280-1305
  *   pmat              PMatUVRoot tools.c:515-546
- *   cond_node         ConditionalPNode codeml.c:3402-3459
+ *   cond_node         ConditionalPNode codeml.c:3402-3459 (clean and unclean
+ *                     tips: codeml's nChara / CharaMap, SetMapAmbiguity
+ *                     treesub.c:1146-1200)
  *   node_scale        NodeScale treesub.c:6940-6975, SetNodeScale 6917-6937
  *   fx_r / lfundG     fx_r treesub.c:7485-7551, lfundG treesub.c:7342-7394
  *   gradientB         gradientB tools.c:6326-6350 (Small_Diff = 1e-6)
@@ -259,6 +261,9 @@ typedef struct {
     const double *pi;         /* [61] */
     int nthreads;             /* <=0: all available */
     int model_b;              /* branch-site model B (NSsites = 3): w1 free, x = [..., w0, w1, w2] */
+    const unsigned char *amb; /* NULL (clean data), or codeml's nChara[256] followed by
+                                 CharaMap[256][64]: a tip code z >= 61 stands for the
+                                 amb[z] sense codons amb[256 + 64 z + k] */
 } oracle_problem;
 
 typedef struct {
@@ -370,8 +375,20 @@ static void cond_node(walk_t *w, int inode, int pos0, int pos1) {
         const double *Pm = w->Pall + (size_t)s * n * n;
         if (pb->nson[s] < 1) {
             const unsigned char *zs = pb->z + (size_t)s * np;
-            for (int h = pos0; h < pos1; h++)
-                for (int j = 0; j < n; j++) cp[h * n + j] *= Pm[j * n + zs[h]];
+            for (int h = pos0; h < pos1; h++) {
+                if (zs[h] < NC || !pb->amb) {
+                    for (int j = 0; j < n; j++) cp[h * n + j] *= Pm[j * n + zs[h]];
+                } else {
+                    /* tip & unclean (ConditionalPNode codeml.c:3438-3445): the sum
+                       over the sense codons the ambiguity code stands for */
+                    const unsigned char *map = pb->amb + 256 + 64 * (size_t)zs[h];
+                    for (int j = 0; j < n; j++) {
+                        double t = 0;
+                        for (int k = 0; k < pb->amb[zs[h]]; k++) t += Pm[j * n + map[k]];
+                        cp[h * n + j] *= t;
+                    }
+                }
+            }
         } else {
             const double *cs = w->conP + (size_t)s * np * n;
             for (int h = pos0; h < pos1; h++)

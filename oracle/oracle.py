@@ -24,6 +24,7 @@ class _Problem(C.Structure):
         ("label", C.POINTER(C.c_int)), ("bnode", C.POINTER(C.c_int)),
         ("z", C.POINTER(C.c_ubyte)), ("fpatt", C.POINTER(C.c_double)),
         ("pi", C.POINTER(C.c_double)), ("nthreads", C.c_int), ("model_b", C.c_int),
+        ("amb", C.POINTER(C.c_ubyte)),
     ]
 
 
@@ -91,7 +92,9 @@ class Problem:
     """A tree + compressed patterns + codon frequencies, held for the C oracle."""
 
     def __init__(self, tree, z: np.ndarray, fpatt: np.ndarray, pi: np.ndarray, nthreads: int = 0,
-                 model_b: bool = False):
+                 model_b: bool = False, ambiguity=None):
+        """ambiguity: None (clean data), or codeml's (nChara[256], CharaMap[256][64])
+        for tip codes z >= 61."""
         self.tree = tree
         nn = tree.nnode
         self.nson = np.array([len(tree.sons[i]) for i in range(nn)], dtype=np.int32)
@@ -112,7 +115,12 @@ class Problem:
                            self.nson.ctypes.data_as(ip), self.sons.ctypes.data_as(ip),
                            self.label.ctypes.data_as(ip), self.bnode.ctypes.data_as(ip),
                            self.z.ctypes.data_as(C.POINTER(C.c_ubyte)), _dp(self.fpatt),
-                           _dp(self.pi), int(nthreads), int(model_b))
+                           _dp(self.pi), int(nthreads), int(model_b), None)
+        if ambiguity is not None:
+            nch, cmap = ambiguity
+            self.amb = np.concatenate([np.asarray(nch, dtype=np.uint8).reshape(256),
+                                       np.asarray(cmap, dtype=np.uint8).reshape(256 * 64)])
+            self._s.amb = self.amb.ctypes.data_as(C.POINTER(C.c_ubyte))
 
     def set_threads(self, n: int) -> None:
         self._s.nthreads = int(n)

@@ -28,6 +28,10 @@
  *            com.plfun (step 1e-4 (|x_i| + 0.05)), and with GBREF_DFUN=1 where the
  *            adapter's GB_dfun is linked in (model A), its analytic gradient
  *            at x; then exits.
+ *   dump     prints the data as codeml holds it after pattern compression
+ *            and encoding (com.z with its ambiguity codes, com.fpatt, com.pi,
+ *            nChara / CharaMap of SetMapAmbiguity treesub.c:1146-1200); then
+ *            exits.
  *   dfun     runs ming2 with the adapter's GB_dfun as its gradient hook
  *            (the one-argument change at codeml.c:688 that the drop-in
  *            enables), then codeml continues as usual.
@@ -152,6 +156,34 @@ static void mode_eval(objective_t fun, double x[], int n) {
     free(g); free(tv); free(ga); free(g5); free(xmark);
 }
 
+static void mode_dump(void) {
+    int j, h, c, k, maxcode = 0;
+    printf("\nGBREF {\"mode\": \"dump\", \"ns\": %d, \"npatt\": %d, \"cleandata\": %d, \"z\": [",
+           com.ns, com.npatt, (int)com.cleandata);
+    for (j = 0; j < com.ns; j++) {
+        printf("%s[", j ? ", " : "");
+        for (h = 0; h < com.npatt; h++) {
+            printf("%s%d", h ? ", " : "", (int)com.z[j][h]);
+            if ((int)com.z[j][h] > maxcode) maxcode = com.z[j][h];
+        }
+        printf("]");
+    }
+    printf("], ");
+    print_vec("fpatt", com.fpatt, com.npatt);
+    printf(", ");
+    print_vec("pi", com.pi, com.ncode);
+    printf(", \"nchara\": [");
+    for (c = 0; c <= maxcode; c++) printf("%s%d", c ? ", " : "", (int)nChara[c]);
+    printf("], \"charamap\": [");
+    for (c = 0; c <= maxcode; c++) {
+        printf("%s[", c ? ", " : "");
+        for (k = 0; k < nChara[c]; k++) printf("%s%d", k ? ", " : "", (int)CharaMap[c][k]);
+        printf("]");
+    }
+    printf("]}\n");
+    fflush(stdout);
+}
+
 int __wrap_ming2(FILE *fout, double *f, objective_t fun, gradient_t dfun, double x[], double xb[][2],
                  double space[], double e, int n) {
     const char *mode = getenv("GBREF_MODE");
@@ -161,6 +193,10 @@ int __wrap_ming2(FILE *fout, double *f, objective_t fun, gradient_t dfun, double
     }
     if (mode && !strcmp(mode, "eval")) {
         mode_eval(fun, x, n);
+        exit(0);
+    }
+    if (mode && !strcmp(mode, "dump")) {
+        mode_dump();
         exit(0);
     }
     if (mode && !strcmp(mode, "dfun")) {

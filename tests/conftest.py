@@ -19,7 +19,31 @@ def pytest_configure(config):
 def golden_names():
     """Fixed-parameter model-A fixtures (codeml lnL and per-pattern log f at given x)."""
     return sorted(f[:-5] for f in os.listdir(GOLDEN)
-                  if f.endswith(".json") and not f.startswith(("mle_", "mb", "ms", "mc")))
+                  if f.endswith(".json") and not f.startswith(("mle_", "mb", "ms", "mc", "u")))
+
+
+def unclean_names():
+    """Fixed-parameter model-A fixtures with gaps and ambiguous codons (cleandata = 0)."""
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("u") and f.endswith(".json"))
+
+
+def load_unclean(name):
+    """(fixture, tree, z, fpatt, pi, (nchara[256], charamap[256, 64])) with the
+    data as codeml encoded it."""
+    from cucodeml_gb300.tree import parse_newick
+
+    with open(os.path.join(GOLDEN, name + ".json")) as f:
+        fx = json.load(f)
+    tree = parse_newick(fx["newick"], fx["names"])
+    enc = fx["enc"]
+    z = np.array(enc["z"], dtype=np.uint8)
+    nch = np.zeros(256, dtype=np.uint8)
+    cmap = np.zeros((256, 64), dtype=np.uint8)
+    for c, (n, row) in enumerate(zip(enc["nchara"], enc["charamap"])):
+        nch[c] = n
+        cmap[c, :n] = row
+    return (fx, tree, z, np.array(enc["fpatt"], dtype=np.float64), np.array(enc["pi"], dtype=np.float64),
+            (nch, cmap))
 
 
 def site_model_names():

@@ -3,13 +3,14 @@
 * 64 taxa x 5000 codons, seed 2024, the bench parameters (the headline
   workload): FP64 drop-in and split precision against the oracle, lnL and
   per-pattern log f; the FP64 adjoint gradient (all 130 entries) against
-  central finite differences with h = 1e-6 and against codeml's own
-  numerical gradient (gradientB, central, restated in the oracle); the
-  split-precision gradient against the same.
+  central finite differences with h = 1e-6 and a five-point stencil of the
+  FP64 lnL, twelve entries against a five-point stencil of the oracle, and
+  all against codeml's own numerical gradient (gradientB, central, restated
+  in the oracle); the split-precision gradient against the same.
 * The batched workload's shape (taxa U{12..48}, codons log-uniform in
   [100, 3000], per-gene kappa, w0, w2): 32 genes through one batch, every
   gene's lnL against the oracle and, for eight of them, the gradient against
-  central differences of the oracle.
+  a five-point stencil of the oracle.
 
 Bars (written into each assertion): FP64 lnL 1e-11 relative, per-pattern
 log f 1e-11 + 2e-11 |log f| (the two eigensolvers differ by 1e-11 relative
@@ -88,62 +89,94 @@ def bench_gradients(bench_case):
     return out
 
 
-def test_gradient_vs_central_differences_h1e6_64x5000(bench_case, bench_gradients):
-    """All 130 entries against central differences with h = 1e-6 of the FP64
-    drop-in's lnL (itself equal to the oracle's to 1e-11 relative above), and
-    twelve entries (the five model parameters, the foreground branch and six
-    others) against central differences of the oracle itself."""
+def five_point(f, x, i):
+    """Five-point derivative of f along x_i, step 1e-4 (|x_i| + 0.05): truncation O(h^4)."""
+    e = 1e-4 * (abs(x[i]) + 0.05)
+    fs = []
+    for k in (-2, -1, 1, 2):
+        xk = x.copy()
+        xk[i] += k * e
+        fs.append(f(xk))
+    return (fs[0] - 8 * fs[1] + 8 * fs[2] - fs[3]) / (12 * e)
+
+
+@pytest.fixture(scope="module")
+def bench_fd(bench_case):
+    """Derivatives of the FP64 drop-in's lnL (itself equal to the oracle's to
+    1e-11 relative, test above) along all 130 coordinates: central
+    differences with h = 1e-6 and a five-point stencil."""
     tree, z, fpatt, pi, x, pb, v, lnf = bench_case
-    h = 1e-6
-    eps = np.finfo(float).eps
     lk = api.Likelihood(tree, z, fpatt, pi, precision="fp64")
 
     def f_gpu(xx):
         return lk.evaluate(*natural(tree, xx)).neg_lnL
 
+    h = 1e-6
     n = len(x)
-    fd = np.zeros(n)
+    c6, f5 = np.zeros(n), np.zeros(n)
     for i in range(n):
         xp, xm = x.copy(), x.copy()
         xp[i] += h
         xm[i] -= h
-        fd[i] = (f_gpu(xp) - f_gpu(xm)) / (2 * h)
+        c6[i] = (f_gpu(xp) - f_gpu(xm)) / (2 * h)
+        f5[i] = five_point(f_gpu, x, i)
     lk.close()
-    tol = 1e-5 * np.maximum(1.0, np.abs(fd)) + 4 * eps * abs(v) / h
-    fg = tree.label[tree.branch_nodes()].argmax()
-    sub = sorted({fg, 0, 17, 40, 77, 101, tree.nbranch - 1} | set(range(tree.nbranch, n)))
-    fdo = {}
-    for i in sub:
-        xp, xm = x.copy(), x.copy()
-        xp[i] += h
-        xm[i] -= h
-        fdo[i] = (pb.neg_lnL(xp) - pb.neg_lnL(xm)) / (2 * h)
-    for prec, g in bench_gradients.items():
-        err = np.abs(g - fd)
-        i = int(np.argmax(err / tol))
-        print(f"{prec}: max |g - fd_h1e-6| / tol = {(err / tol).max():.3f} at {i} (g {g[i]:.6f} fd {fd[i]:.6f})")
-        assert np.all(err <= tol), (prec, i, g[i], fd[i])
-        for k, ref in fdo.items():
-            assert abs(g[k] - ref) <= 1e-5 * max(1.0, abs(ref)) + 4 * eps * abs(v) / h, (prec, k, g[k], ref)
+    return c6, f5
 
 
-def test_gradient_vs_codeml_gradientB_64x5000(bench_case, bench_gradients):
-    """codeml's own numerical gradient (gradientB, central: step
-    (1e-6 (|x| + 1))^0.67, tools.c:6326-6350) of the oracle's lnL; its step
-    limits its accuracy to about 1e-6 relative."""
+def test_gradient_vs_central_differences_h1e6_64x5000(bench_case, bench_gradients, bench_fd):
+    """All 130 entries against central differences with h = 1e-6 (bar: 1e-5
+    relative plus the difference's own rounding error 4 eps |f| / h) and
+    against the five-point stencil (1e-5 relative)."""
     tree, z, fpatt, pi, x, pb, v, lnf = bench_case
-    gb = pb.gradientB(x, True, central=True)
+    c6, f5 = bench_fd
+    h = 1e-6
+    eps = np.finfo(float).eps
+    tol = 1e-5 * np.maximum(1.0, np.abs(c6)) + 4 * eps * abs(v) / h
     for prec, g in bench_gradients.items():
-        err = np.abs(g - gb) / np.maximum(1.0, np.abs(gb))
-        print(f"{prec}: max rel deviation from codeml's gradientB {err.max():.3e}")
-        assert err.max() <= 1e-4
+        err = np.abs(g - c6)
+        i = int(np.argmax(err / tol))
+        print(f"{prec}: max |g - fd_h1e-6| / tol = {(err / tol).max():.3f} at {i} (g {g[i]:.6f} fd {c6[i]:.6f})")
+        assert np.all(err <= tol), (prec, i, g[i], c6[i])
+        e5 = np.abs(g - f5) / np.maximum(1.0, np.abs(f5))
+        print(f"{prec}: max rel err vs five-point stencil {e5.max():.3e}")
+        assert e5.max() <= 1e-5
+
+
+def test_gradient_vs_oracle_differences_64x5000(bench_case, bench_gradients):
+    """Twelve entries (the five model parameters, the foreground branch and six
+    others) against a five-point stencil of the oracle's own lnL."""
+    tree, z, fpatt, pi, x, pb, v, lnf = bench_case
+    fg = int(tree.label[tree.branch_nodes()].argmax())
+    sub = sorted({fg, 0, 17, 40, 77, 101, tree.nbranch - 1} | set(range(tree.nbranch, len(x))))
+    ref = {i: five_point(pb.neg_lnL, x, i) for i in sub}
+    for prec, g in bench_gradients.items():
+        for i, r in ref.items():
+            assert abs(g[i] - r) <= 1e-5 * max(1.0, abs(r)), (prec, i, g[i], r)
+
+
+def test_gradient_vs_codeml_gradientB_64x5000(bench_case, bench_gradients, bench_fd):
+    """codeml's own numerical gradient (gradientB, central: step
+    (1e-6 (|x| + 1))^0.67, tools.c:6326-6350, restated in the oracle): the
+    analytic gradient is no farther from it than the accurate five-point
+    derivative is (gradientB's step error, large on the shortest branches),
+    plus 1e-5 relative."""
+    tree, z, fpatt, pi, x, pb, v, lnf = bench_case
+    gB = pb.gradientB(x, True, central=True)
+    c6, f5 = bench_fd
+    own = np.abs(f5 - gB)
+    for prec, g in bench_gradients.items():
+        dev = np.abs(g - gB)
+        print(f"{prec}: max rel deviation from codeml's gradientB {(dev / np.maximum(1.0, np.abs(gB))).max():.3e} "
+              f"(gradientB's own {(own / np.maximum(1.0, np.abs(gB))).max():.3e})")
+        assert np.all(dev <= own + 1e-5 * np.maximum(1.0, np.abs(gB)))
 
 
 def test_batch_shaped_workload_vs_oracle():
     """32 genes of the batched workload's distribution through one split-
     precision batch: each gene's lnL against the oracle (|dlnL| <= 1e-6), and
-    for every fourth gene the whole gradient against central differences of
-    the oracle (step 1e-5 (|x| + 0.05); relative error <= 1e-5 of max(1, |g|))."""
+    for every fourth gene the whole gradient against a five-point stencil of
+    the oracle (step 1e-4 (|x| + 0.05); relative error <= 1e-5 of max(1, |g|))."""
     alns = simulate_batch(32, seed=31, taxa=(12, 48), codons=(100, 3000))
     genes, prm, probs = [], [], []
     for a in alns:
@@ -169,13 +202,7 @@ def test_batch_shaped_workload_vs_oracle():
             continue
         gx = np.concatenate([g[i]["blength"][t.branch_nodes()],
                              [g[i]["kappa"], g[i]["p0"], g[i]["p1"], g[i]["omega0"], g[i]["omega2"]]])
-        fd = np.zeros(len(x))
-        for k in range(len(x)):
-            e = 1e-5 * (abs(x[k]) + 0.05)
-            xp, xm = x.copy(), x.copy()
-            xp[k] += e
-            xm[k] -= e
-            fd[k] = (pb.neg_lnL(xp) - pb.neg_lnL(xm)) / (2 * e)
+        fd = np.array([five_point(pb.neg_lnL, x, k) for k in range(len(x))])
         err = np.abs(gx - fd) / np.maximum(1.0, np.abs(fd))
         worst_g = max(worst_g, err.max())
         assert err.max() <= 1e-5, (i, int(np.argmax(err)))

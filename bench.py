@@ -198,20 +198,34 @@ def batched_leg(args, dev):
                            "candidates": [{"config": t["config"], "ms_per_batch": t.get("ms"),
                                            "agrees": t.get("agrees")} for t in tr["table"]]}
     for prec in ("fast", "fp64"):
-        b = api.Batch(genes, precision=prec, device=dev, tuning=tuning if prec == "fast" else None)
+        tn = tuning if prec == "fast" else None
+        b = api.Batch(genes, precision=prec, device=dev, tuning=tn)
         f, g, st = b.evaluate(prm, grad=True)
         f, g, st = b.evaluate(prm, grad=True)
         res[prec] = (f, g)
-        import time as _t
-        t0 = _t.perf_counter()
+        t0 = time.perf_counter()
         for _ in range(args.batch_steps):
             f, g, st = b.evaluate(prm, grad=True)
-        e2e = (_t.perf_counter() - t0) / args.batch_steps
+        e2e_serial = (time.perf_counter() - t0) / args.batch_steps
         ms = b.replay(args.batch_steps, True) / args.batch_steps
+        kernels = st.kernels
+        b.close()
+        # end to end with the genes in two halves whose host set-up and device
+        # work overlap (gb_batch_submit / gb_batch_collect), every step a whole
+        # lnL + gradient of all genes with its copies in and out
+        pb = api.PipelinedBatch(genes, precision=prec, device=dev, tuning=tn)
+        pb.evaluate_many([prm] * 2, grad=True)
+        t0 = time.perf_counter()
+        rp = pb.evaluate_many([prm] * args.batch_steps, grad=True)
+        e2e = (time.perf_counter() - t0) / args.batch_steps
+        pb.close()
+        assert np.max(np.abs(rp[-1][0] - f)) <= 1e-9 * np.max(np.abs(f))
         out[prec] = {"batch_evals_per_s": 1000.0 / ms, "gene_evals_per_s": args.batch * 1000.0 / ms,
                      "ms_per_batch": ms, "e2e_batch_evals_per_s": 1.0 / e2e,
-                     "e2e_gene_evals_per_s": args.batch / e2e, "kernels_per_batch": st.kernels}
-        b.close()
+                     "e2e_gene_evals_per_s": args.batch / e2e,
+                     "e2e_serial_batch_evals_per_s": 1.0 / e2e_serial, "kernels_per_batch": kernels,
+                     "e2e_note": "two half-batches, host set-up of one overlapping the device work of the "
+                                 "other (gb_batch_submit / gb_batch_collect); serial: gb_batch_eval"}
     out["speedup_vs_fp64"] = out["fast"]["batch_evals_per_s"] / out["fp64"]["batch_evals_per_s"]
     out["e2e_speedup_vs_fp64"] = out["fast"]["e2e_batch_evals_per_s"] / out["fp64"]["e2e_batch_evals_per_s"]
     out["max_abs_dlnL_vs_fp64"] = float(np.max(np.abs(res["fast"][0] - res["fp64"][0])))
@@ -407,6 +421,108 @@ def port_cpu(tree, z, fpatt, pi, threads: int, seconds: float = 12.0, min_evals:
             "lnL_eval_s": dt}
 
 
+def reference_gpu_leg(args, neg_lnL_ours):
+    """codeml's own CUDA objective CUDA_lfundG on this GPU, through two
+    builds of the reference codeml (oracle/Makefile): CuCodeML, the
+    reference's cuda-codeml.cu compiled for sm_103a (its kernels,
+    cuda-codeml.cu:112-742, schedule 1280-1406), and codeml over this
+    library's FP64 drop-in (codeml_adapter.c).  Each is timed inside codeml
+    (ref_harness.c, lnL only: codeml's host SetParameters, the four class
+    schedules and codeml's mixture included) at the bench point; codeml's
+    finite-difference lnL + gradient costs np + 1 of them."""
+    from cucodeml_gb300.simulate import simulate
+    from oracle import refcodeml as R
+    aln = simulate(args.ns, args.ncodon, seed=2024)
+    tree = aln.tree
+    p2 = 1.0 - PARAMS["p0"] - PARAMS["p1"]
+    x = np.concatenate([tree.x_branch_lengths(), [PARAMS["kappa"], np.log(PARAMS["p0"] / p2),
+                                                  np.log(PARAMS["p1"] / p2), PARAMS["omega0"], PARAMS["omega2"]]])
+    rows = R.alignment_rows(aln)
+    np_ = tree.nbranch + 5
+    out = {"workload": f"codeml's CUDA_lfundG (lnL only), {args.ns} taxa x {args.ncodon} codons, inside codeml"}
+    for key, exe in (("cucodeml_sm103a", "cucodeml"), ("codeml_over_fp64_dropin", "codeml_gb")):
+        path = os.path.join(ROOT, "oracle", "_ref", exe)
+        if not os.path.exists(path):
+            out[key] = {"unavailable": f"oracle/_ref/{exe} not built (reference sources not staged)"}
+            continue
+        r = R.time_steps(path, tree.names, rows, tree.to_newick(), x, steps=5, warmup=2,
+                         env={"GBREF_COORDS": "0:0"})
+        T = statistics.median(r["step_s"])
+        out[key] = {"lnL_ms": 1000.0 * T, "lnL_evals_per_s": 1.0 / T,
+                    "fd_lnL_grad_evals_per_s": 1.0 / ((np_ + 1) * T),
+                    "abs_dlnL_vs_ours": abs(r["f0"] - neg_lnL_ours)}
+    return out
+
+
+def checkpoint_leg(args, dev):
+    """Device memory of an FP64 lnL + gradient evaluation at 256 taxa x 20000
+    codons with the checkpointed adjoint off and on (GB_TUNE_CHECKPOINT:
+    edge messages recomputed per tree level in the reverse sweep), its time,
+    and that both give the same lnL and gradient."""
+    import torch
+    from cucodeml_gb300 import api
+    from cucodeml_gb300.simulate import simulate
+    aln = simulate(256, 20000, seed=2024)
+    z, fpatt, pi = api.patterns(aln.codons)
+    tree = aln.tree
+    out = {"workload": f"FP64 lnL+gradient, 256 taxa x 20000 codons ({len(fpatt)} patterns)"}
+    res = {}
+    for ck in (0, 1):
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        lk = api.Likelihood(tree, z, fpatt, pi, precision="fp64", device=dev, tuning={"checkpoint": ck})
+        r = lk.evaluate(tree.branch, grad=True, **PARAMS)
+        torch.cuda.synchronize()
+        used = free0 - torch.cuda.mem_get_info()[0]
+        ms = lk.replay(3, True) / 3
+        g = np.concatenate([r.grad["blength"], [r.grad[k] for k in ("kappa", "omega0", "omega2", "p0", "p1")]])
+        res[ck] = (r.neg_lnL, g)
+        out["on" if ck else "off"] = {"device_GB": used / 1e9, "ms_per_eval": ms}
+        lk.close()
+    out["bit_identical"] = bool(res[0][0] == res[1][0] and np.array_equal(res[0][1], res[1][1]))
+    out["memory_ratio"] = out["on"]["device_GB"] / out["off"]["device_GB"]
+    return out
+
+
+def alt_null_leg(args, dev):
+    """Model A against its null (w2 = 1) at 256 taxa x 20000 codons: both fits
+    by bounded L-BFGS-B driven by the split-precision path's lnL + adjoint
+    gradient (optimize.alt_null), then continued with the FP64 path from those
+    maxima; wall time, calls, lnL, LRT and the agreement of the two paths.
+    codeml's own route, ming2 with finite-difference gradients, costs np + 1
+    lnL evaluations per gradient: timed here per evaluation on the FP64 path
+    (the lnL codeml would get over the drop-in)."""
+    from cucodeml_gb300 import api, optimize
+    from cucodeml_gb300.simulate import simulate
+    aln = simulate(256, 20000, seed=2025)
+    z, fpatt, pi = api.patterns(aln.codons)
+    tree = aln.tree
+    out = {"workload": f"model A vs null, 256 taxa x 20000 codons ({len(fpatt)} patterns), seed 2025"}
+    t0 = time.perf_counter()
+    r = optimize.alt_null(tree, z, fpatt, pi, precision="fast")
+    t_fast = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    p = optimize.alt_null(tree, z, fpatt, pi, precision="fp64", x0_alt=r["alt"]["x"], x0_null=r["null"]["x"])
+    t_pol = time.perf_counter() - t0
+    for name, res, secs in (("split_precision", r, t_fast), ("fp64_continued", p, t_pol)):
+        out[name] = {"lnL_alt": res["alt"]["lnL"], "lnL_null": res["null"]["lnL"], "LRT": res["LRT"],
+                     "p_mixture": res["p_mixture"], "calls": res["alt"]["calls"] + res["null"]["calls"],
+                     "wall_s": secs, "omega2": res["alt"]["omega2"]}
+    out["abs_dlnL_alt_paths"] = abs(r["alt"]["lnL"] - p["alt"]["lnL"])
+    out["abs_dlnL_null_paths"] = abs(r["null"]["lnL"] - p["null"]["lnL"])
+    lk = api.Likelihood(tree, z, fpatt, pi, precision="fp64", device=dev)
+    x = np.asarray(p["alt"]["x"])
+    lk.evaluate_x(x, lastround=False)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        lk.evaluate_x(x, lastround=False)
+    per = (time.perf_counter() - t0) / 5
+    lk.close()
+    out["fd_gradient_on_this_gpu"] = {"lnL_eval_s": per, "np": len(x), "seconds_per_fd_gradient": per * (len(x) + 1),
+                                      "note": "codeml's forward-difference gradient = np + 1 FP64 lnL evaluations"}
+    return out
+
+
 def workload_config(ns: int, ncodon: int) -> dict:
     """The config both arms report (identical dicts)."""
     return {"workload": f"lnL+gradient, {ns} taxa x {ncodon} codons, branch-site model A "
@@ -471,6 +587,9 @@ def main():
     ap.add_argument("--batch", type=int, default=512, help="genes in the batched leg (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=3)
     ap.add_argument("--no-tune", action="store_true", help="batched leg: skip the autotuner (library defaults)")
+    ap.add_argument("--no-refgpu", action="store_true", help="skip the reference-GPU (CuCodeML) leg")
+    ap.add_argument("--no-ckpt", action="store_true", help="skip the checkpointed-adjoint memory leg")
+    ap.add_argument("--no-altnull", action="store_true", help="skip the 256 x 20000 model A vs null fits")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -629,6 +748,13 @@ def main():
             line["cpu_baseline"]["abs_dlnL_vs_ours"] = ref["abs_dlnL_vs_ours"]
     if not args.no_beb:
         line["se"] = secondary_leg(se_leg, args, dev, tree, z, fpatt, pi, cpu_lnL_s, cpu_kind)
+    if not args.no_altnull:
+        line["alt_null"] = secondary_leg(alt_null_leg, args, dev)
+    if not args.no_ckpt:
+        line["checkpoint"] = secondary_leg(checkpoint_leg, args, dev)
+    if not args.no_refgpu:
+        line["reference_gpu"] = secondary_leg(reference_gpu_leg, args,
+                                              lk.evaluate(bl0, grad=False, **PARAMS).neg_lnL)
     lk.close()
     if rank == 0:
         print(json.dumps(line))

@@ -17,7 +17,7 @@ GB_OK = 0
 GB_PREC_FP64 = 0
 GB_PREC_FAST = 1
 # gb_tune knobs (include/gbcodeml.h)
-TUNE = {"mma": 1, "persist": 2, "gchunk": 3, "order": 4, "grid": 5}
+TUNE = {"mma": 1, "persist": 2, "gchunk": 3, "order": 4, "grid": 5, "checkpoint": 6}
 ERRORS = {-1: "GB_ERR_ARG", -2: "GB_ERR_CUDA", -3: "GB_ERR_OOM", -4: "GB_ERR_PARAM",
           -5: "GB_ERR_TIMEOUT", -6: "GB_ERR_STATE", -7: "GB_ERR_NODEVICE"}
 
@@ -82,6 +82,8 @@ SIGNATURES = {
     "gb_batch_create": (C.c_int, [C.c_int, C.POINTER(Problem), C.POINTER(C.c_void_p)]),
     "gb_batch_size": (C.c_int, [C.c_void_p]),
     "gb_batch_eval": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, C.POINTER(Grad), C.POINTER(Stats)]),
+    "gb_batch_submit": (C.c_int, [C.c_void_p, C.POINTER(Params), C.c_int, C.c_void_p]),
+    "gb_batch_collect": (C.c_int, [C.c_void_p, _dp, C.POINTER(Grad), C.POINTER(Stats)]),
     "gb_batch_replay": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "gb_batch_destroy": (C.c_int, [C.c_void_p]),
     "gb_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),

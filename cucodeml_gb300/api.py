@@ -540,10 +540,85 @@ class Batch:
         return out, grads, EvalResult(float(out.sum()), None, None, None, st.ms_device, st.ms_host,
                                       st.kernels, st.h2d_bytes, st.d2h_bytes)
 
+    def submit(self, params, grad: bool = False, after: "Batch | None" = None) -> None:
+        """Host set-up and graph launch of one evaluation without waiting
+        (gb_batch_submit); after: another batch whose submitted evaluation the
+        device runs first.  collect() returns the results."""
+        n = self.n
+        pr = (_lib.Params * n)()
+        self._keep_bl = []
+        for i, p in enumerate(params):
+            bl = np.ascontiguousarray(p["blength"], dtype=np.float64)
+            self._keep_bl.append(bl)
+            pr[i] = _lib.Params(_ptr(bl), p["kappa"], p["omega0"], p["omega2"], p["p0"], p["p1"])
+        self._pending_grad = bool(grad)
+        _lib.check(self._L.gb_batch_submit(self._h, pr, int(grad), after._h if after is not None else None))
+
+    def collect(self):
+        """(neg_lnL [n], grads or None, EvalResult stats) of the submitted evaluation."""
+        n = self.n
+        out = np.zeros(n)
+        gr, dbl = None, []
+        if self._pending_grad:
+            gr = (_lib.Grad * n)()
+            for i in range(n):
+                d = np.zeros(self.trees[i].nnode)
+                dbl.append(d)
+                gr[i] = _lib.Grad(_ptr(d), 0, 0, 0, 0, 0)
+        st = _lib.Stats()
+        _lib.check(self._L.gb_batch_collect(self._h, _ptr(out), gr, C.byref(st)))
+        grads = None
+        if gr is not None:
+            grads = [{"blength": dbl[i], "kappa": gr[i].d_kappa, "omega0": gr[i].d_omega0,
+                      "omega2": gr[i].d_omega2, "p0": gr[i].d_p0, "p1": gr[i].d_p1} for i in range(n)]
+        return out, grads, EvalResult(float(out.sum()), None, None, None, st.ms_device, st.ms_host,
+                                      st.kernels, st.h2d_bytes, st.d2h_bytes)
+
     def replay(self, iters: int, with_grad: bool) -> float:
         ms = C.c_double(0)
         _lib.check(self._L.gb_batch_replay(self._h, int(iters), int(with_grad), C.byref(ms)))
         return ms.value
+
+
+class PipelinedBatch:
+    """The genes of a batch in two halves (two gb_batch objects), evaluated
+    alternately with gb_batch_submit / gb_batch_collect: while the device runs
+    one half's graph, the host sets up the other half (eigen solutions, chain
+    rule), so a stream of evaluations runs at the device's rate.  evaluate()
+    has Batch.evaluate's results; evaluate_many() pipelines a sequence of
+    parameter sets (independent evaluations, e.g. many starting points)."""
+
+    def __init__(self, genes, precision: str = "fast", device: int = 0, tuning: dict | None = None):
+        self.n = len(genes)
+        self.cut = (self.n + 1) // 2
+        self.half = [Batch(genes[:self.cut], precision, device, tuning),
+                     Batch(genes[self.cut:], precision, device, tuning)]
+
+    def close(self):
+        for b in self.half:
+            b.close()
+
+    def evaluate_many(self, param_sets, grad: bool = False):
+        """[(neg_lnL [n], grads or None)] for each parameter set, pipelined."""
+        A, B = self.half
+        out = []
+        prev_b = None
+        for prm in param_sets:
+            A.submit(prm[:self.cut], grad, after=B if prev_b is not None else None)
+            if prev_b is not None:
+                fb, gb_, _ = B.collect()
+                out[-1] = (np.concatenate([out[-1][0], fb]), (out[-1][1] + gb_) if grad else None)
+            B.submit(prm[self.cut:], grad, after=A)
+            fa, ga, _ = A.collect()
+            out.append((fa, ga if grad else None))
+            prev_b = True
+        if prev_b is not None:
+            fb, gb_, _ = B.collect()
+            out[-1] = (np.concatenate([out[-1][0], fb]), (out[-1][1] + gb_) if grad else None)
+        return out
+
+    def evaluate(self, params, grad: bool = False):
+        return self.evaluate_many([params], grad)[0]
 
     def task_trace(self, kernel: int) -> np.ndarray:
         """As Likelihood.task_trace, for the batch's persistent kernels."""

@@ -187,14 +187,14 @@ __global__ void __launch_bounds__(128) bwd_level_kernel(
                 for (int q = 0; q < 4; q++) Eb[k][r][q] = A[k][r][q];
             for (int i2 = 0; i2 < it.nchild; i2++) {
                 if (i2 == i) continue;
-                const double *e = E + ((size_t)(it.pslot[k] * MAXC + i2) * npad + h0 + r0) * 64 + c0;
+                const double *e = E + ((size_t)(it.eslot[k] + i2) * npad + h0 + r0) * 64 + c0;
 #pragma unroll
                 for (int r = 0; r < 4; r++) {
                     const double4 v = *reinterpret_cast<const double4 *>(e + r * 64);
                     Eb[k][r][0] *= v.x; Eb[k][r][1] *= v.y; Eb[k][r][2] *= v.z; Eb[k][r][3] *= v.w;
                 }
             }
-            double *eb = Ebar + ((size_t)(it.pslot[k] * MAXC + i) * npad + h0 + r0) * 64 + c0;
+            double *eb = Ebar + ((size_t)(it.eslot[k] + i) * npad + h0 + r0) * 64 + c0;
 #pragma unroll
             for (int r = 0; r < 4; r++)
                 *reinterpret_cast<double4 *>(eb + r * 64) = make_double4(Eb[k][r][0], Eb[k][r][1], Eb[k][r][2], Eb[k][r][3]);
@@ -250,12 +250,13 @@ __global__ void __launch_bounds__(128) gradP_kernel(const Contrib *__restrict__ 
                                                     const double *__restrict__ conP,
                                                     const unsigned char *__restrict__ z,
                                                     double *__restrict__ Gpart, int nchunk,
-                                                    const unsigned char *__restrict__ amb) {
+                                                    const unsigned char *__restrict__ amb,
+                                                    const int *__restrict__ plist) {
     extern __shared__ double smg[];
     double *Es = smg;                    // [32][65]
     double *Xs = smg + TILE64 * 65;      // [32][65]
     double *Gs = smg + 2 * TILE64 * 65;  // [64][65] tip scatter target
-    const int p = blockIdx.x, chunk = blockIdx.y;
+    const int p = plist ? plist[blockIdx.x] : (int)blockIdx.x, chunk = blockIdx.y;
     const int tid = threadIdx.x;
     // thread owns G rows j = 8*(tid/16) .. +7, cols k = 4*(tid%16) .. +3
     const int j0 = (tid >> 4) * 8, k0 = (tid & 15) * 4;
@@ -588,7 +589,7 @@ void adjoint_free(AdjointState *a) {
     if (!a) return;
     if (a->graph) cudaGraphExecDestroy(a->graph);
     void *dev[] = {a->d_bitems, a->d_contrib, a->d_coff, a->d_Ebar, a->d_Abar, a->d_Gpart,
-                   a->d_Dm, a->d_pout, a->d_fpart, a->d_gp, a->d_UVdf};
+                   a->d_Dm, a->d_pout, a->d_fpart, a->d_gp, a->d_UVdf, a->d_ritems, a->d_plist};
     for (void *p : dev)
         if (p) cudaFree(p);
     if (a->h_gp) cudaFreeHost(a->h_gp);
@@ -635,16 +636,51 @@ int adjoint_init(gb_handle *h) {
                     }
                     if (b.ncls == 1) { b.pidx[i][1] = b.pidx[i][0]; b.tslot[i][1] = b.tslot[i][0]; }
                 }
+                for (int k = 0; k < 2; k++) b.eslot[k] = b.pslot[k] >= 0 ? b.pslot[k] * MAXC : -1;
                 a->bitems.push_back(b);
             }
         }
     }
     a->blevel_off.push_back((int)a->bitems.size());
+    // checkpointed adjoint: E / Ebar rows numbered within each tree level
+    // (slot -> its index among the items of its level)
+    a->ckpt = h->precision == GB_PREC_FP64 && h->tune.checkpoint > 0;
+    std::vector<int> erow((size_t)h->nslot, -1);
+    for (int L = 0; L + 1 < (int)h->level_off.size(); L++)
+        for (int q = h->level_off[L]; q < h->level_off[L + 1]; q++) erow[h->items[q].slot] = q - h->level_off[L];
+    auto ebase = [&](int slot) { return a->ckpt ? erow[slot] * MAXC : slot * MAXC; };
+    if (a->ckpt) {
+        for (BItem &b : a->bitems)
+            for (int k = 0; k < 2; k++) b.eslot[k] = b.pslot[k] >= 0 ? ebase(b.pslot[k]) : -1;
+        a->ckpt_rows = 0;
+        a->ritems.clear();
+        a->rlevel_off.clear();
+        a->plist.clear();
+        a->plevel_off.clear();
+        std::vector<char> seen(h->pairs.size(), 0);
+        for (int L = (int)h->level_off.size() - 2; L >= 0; L--) {      // top-down, as the sweep
+            a->rlevel_off.push_back((int)a->ritems.size());
+            a->plevel_off.push_back((int)a->plist.size());
+            a->ckpt_rows = std::max(a->ckpt_rows, h->level_off[L + 1] - h->level_off[L]);
+            for (int q = h->level_off[L]; q < h->level_off[L + 1]; q++) {
+                Item it = h->items[q];
+                it.eslot = ebase(it.slot);
+                a->ritems.push_back(it);
+                for (int i = 0; i < it.nchild; i++)
+                    if (!seen[it.pidx[i]]) {
+                        seen[it.pidx[i]] = 1;
+                        a->plist.push_back(it.pidx[i]);
+                    }
+            }
+        }
+        a->rlevel_off.push_back((int)a->ritems.size());
+        a->plevel_off.push_back((int)a->plist.size());
+    }
     // dlnL/dP contributions per pair
     std::vector<std::vector<Contrib>> per((size_t)h->pairs.size());
     for (const Item &it : h->items)
         for (int i = 0; i < it.nchild; i++) {
-            Contrib cb{it.slot * MAXC + i, it.cslot[i], it.child[i]};
+            Contrib cb{ebase(it.slot) + i, it.cslot[i], it.child[i]};
             per[it.pidx[i]].push_back(cb);
         }
     a->coff.assign(h->pairs.size() + 1, 0);
@@ -673,7 +709,10 @@ int adjoint_init(gb_handle *h) {
     int rc;
     if ((rc = dalloc(&a->d_bitems, a->bitems.size())) || (rc = dalloc(&a->d_contrib, a->contrib.size())) ||
         (rc = dalloc(&a->d_coff, a->coff.size())) ||
-        (rc = dalloc(&a->d_Ebar, (size_t)h->nslot * MAXC * npad * 64)) ||
+        (rc = dalloc(&a->d_Ebar, (size_t)(a->ckpt ? a->ckpt_rows : h->nslot) * MAXC * npad * 64)) ||
+        (a->ckpt && !h->d_E && (rc = dalloc(&h->d_E, (size_t)a->ckpt_rows * MAXC * npad * 64))) ||
+        (a->ckpt && (rc = dalloc(&a->d_ritems, a->ritems.size()))) ||
+        (a->ckpt && (rc = dalloc(&a->d_plist, std::max<size_t>(a->plist.size(), 1)))) ||
         (rc = dalloc(&a->d_Abar, (size_t)h->nslot * npad * 64)) ||
         (rc = dalloc(&a->d_Gpart, h->pairs.size() * a->nchunk * 64 * 64)) ||
         (rc = dalloc(&a->d_Dm, DM_MATS * 64 * 64)) ||
@@ -687,6 +726,10 @@ int adjoint_init(gb_handle *h) {
     CK(cudaMemcpy(a->d_bitems, a->bitems.data(), sizeof(BItem) * a->bitems.size(), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(a->d_contrib, a->contrib.data(), sizeof(Contrib) * std::max<size_t>(a->contrib.size(), 1), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(a->d_coff, a->coff.data(), sizeof(int) * a->coff.size(), cudaMemcpyHostToDevice));
+    if (a->ckpt) {
+        CK(cudaMemcpy(a->d_ritems, a->ritems.data(), sizeof(Item) * a->ritems.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(a->d_plist, a->plist.data(), sizeof(int) * a->plist.size(), cudaMemcpyHostToDevice));
+    }
     // the Ebar rows of padded patterns must be zero for the dP reduction: they are
     // written by the sweep with g = 0 (fpatt = 0) at the root and products below
     CK(cudaMemset(a->d_Abar, 0, sizeof(double) * (size_t)h->nslot * npad * 64));
@@ -744,18 +787,43 @@ int record_backward(gb_handle *h) {
     for (size_t L = 0; L + 1 < a->blevel_off.size(); L++) {
         int n = a->blevel_off[L + 1] - a->blevel_off[L];
         if (!n) continue;
+        if (a->ckpt) {
+            // this level's edge messages again (the forward kept none): the
+            // level's items with level-local E rows; conditional likelihoods,
+            // scale factors and root sums are rewritten with the same values
+            const int nr = a->rlevel_off[L + 1] - a->rlevel_off[L];
+            launch_prune_fp64(a->d_ritems + a->rlevel_off[L], nr, h->ntile, h->npad, h->d_z, h->d_Pt, h->d_conP,
+                              h->d_E, h->d_scaleF, h->d_scale_list, h->nscale, h->d_pi, h->d_fbar, h->d_ssum,
+                              h->d_fhK, h->stream, h->d_amb);
+            prof_mark(h, GB_K_PRUNE);
+            nk++;
+        }
         dim3 grid(h->ntile, n);
         bwd_level_kernel<<<grid, 128, 0, h->stream>>>(a->d_bitems + a->blevel_off[L], h->npad, h->d_Pt,
                                                       h->d_E, a->d_Ebar, a->d_Abar, h->d_scaleF,
                                                       h->d_fpatt, h->d_post, h->d_fbar, h->d_pi);
         prof_mark(h, GB_K_BWD);
         nk++;
+        if (a->ckpt) {      // the level's pairs, while its Ebar rows are there
+            const int np = a->plevel_off[L + 1] - a->plevel_off[L];
+            if (np) {
+                dim3 g2((unsigned)np, a->nchunk);
+                gradP_kernel<<<g2, 128, kGradPSmem, h->stream>>>(a->d_contrib, a->d_coff, h->npatt, h->npad,
+                                                                 a->d_Ebar, h->d_conP, h->d_z, a->d_Gpart,
+                                                                 a->nchunk, h->d_amb, a->d_plist + a->plevel_off[L]);
+                prof_mark(h, GB_K_GRADP);
+                nk++;
+            }
+        }
     }
-    dim3 g2((unsigned)h->pairs.size(), a->nchunk);
-    gradP_kernel<<<g2, 128, kGradPSmem, h->stream>>>(a->d_contrib, a->d_coff, h->npatt, h->npad, a->d_Ebar,
-                                            h->d_conP, h->d_z, a->d_Gpart, a->nchunk, h->d_amb);
-    prof_mark(h, GB_K_GRADP);
-    nk++;
+    if (!a->ckpt) {
+        dim3 g2((unsigned)h->pairs.size(), a->nchunk);
+        gradP_kernel<<<g2, 128, kGradPSmem, h->stream>>>(a->d_contrib, a->d_coff, h->npatt, h->npad, a->d_Ebar,
+                                                         h->d_conP, h->d_z, a->d_Gpart, a->nchunk, h->d_amb,
+                                                         nullptr);
+        prof_mark(h, GB_K_GRADP);
+        nk++;
+    }
     gradH_kernel<<<(unsigned)h->pairs.size(), 256, kGradHSmem, h->stream>>>(h->d_pairs, h->d_label, h->d_tnode,
                                                                    h->d_prm, a->d_Gpart, a->nchunk,
                                                                    a->d_Dm, a->d_pout);

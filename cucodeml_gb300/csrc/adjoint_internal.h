@@ -26,6 +26,7 @@ constexpr int UVDF_DM = 3 * 2 * 61 * 64;   // offset of the double-float tables 
 struct BItem {                // backward work: (node, class family) of one level
     int node, ncls, is_root, nchild;
     int cls[2], pslot[2], sslot[2];
+    int eslot[2];             // first E / Ebar row block of the node's class k (FP64 path)
     int pidx[MAXC][2];        // pair of edge i under parent class k
     int tslot[MAXC][2];       // child slot receiving the adjoint (-1: tip)
     int child[MAXC];          // child node of edge i
@@ -60,6 +61,18 @@ struct AdjointState {
     double *h_pout = nullptr, *h_fpart = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graph_kernels = 0;
+    // checkpointed adjoint (FP64, gb_tune GB_TUNE_CHECKPOINT): conditional
+    // likelihoods kept at every internal node, the edge messages E and Ebar
+    // of one tree level at a time, recomputed level by level in the reverse
+    // sweep; per level: the forward items to recompute (E rows level-local),
+    // and the pairs whose dlnL/dP that level completes
+    bool ckpt = false;
+    int ckpt_rows = 0;               // E / Ebar slots of the widest level
+    std::vector<Item> ritems;        // forward items in the adjoint's level order
+    std::vector<int> rlevel_off;
+    std::vector<int> plist, plevel_off;
+    Item *d_ritems = nullptr;
+    int *d_plist = nullptr;
 };
 
 int adjoint_init(gb_handle *h);               // host structures and device buffers

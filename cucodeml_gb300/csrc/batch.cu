@@ -57,6 +57,10 @@ struct gb_batch {
         int2 *map = nullptr;
         int nblocks = 0;
     } l_pmat, l_pslice, l_mix, l_mixg, l_dmat, l_gradH, l_freq;   // l_mixg: with the adjoint's root seed
+    // an evaluation submitted and not yet collected (gb_batch_submit / _collect)
+    bool pending = false, pending_grad = false;
+    double pending_t0 = 0;
+    std::vector<std::vector<double>> pending_blength;
 };
 
 namespace {
@@ -409,9 +413,11 @@ int gb_batch_destroy(gb_batch *b) {
 
 int gb_batch_size(const gb_batch *b) { return b ? b->n : GB_ERR_STATE; }
 
-int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *grads, gb_stats *stats) {
-    if (!b || !prm || !neg_lnL) return fail(GB_ERR_ARG, "gb_batch_eval: bad arguments");
-    const bool grad = grads != nullptr;
+int gb_batch_submit(gb_batch *b, const gb_params *prm, int with_grad, const gb_batch *after) {
+    if (!b || !prm) return fail(GB_ERR_ARG, "gb_batch_submit: bad arguments");
+    if (b->pending) return fail(GB_ERR_STATE, "gb_batch_submit: the previous evaluation was not collected");
+    if (after && after->device != b->device) return fail(GB_ERR_ARG, "gb_batch_submit: batches on two devices");
+    const bool grad = with_grad != 0;
     CK(cudaSetDevice(b->device));
     const double t0 = now_ms();
     // host: model set-up of every gene, in parallel
@@ -431,27 +437,49 @@ int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *g
                 int rc = adjoint_init(b->h[i]);
                 if (rc) return rc;
             }
+        b->pending_blength.resize(b->n);
         parallel_for(b->n, b->nthreads, [&](int i) {
             std::memcpy(b->h[i]->adj->h_gp->dQk, b->D[i]->dQk, sizeof(b->D[i]->dQk));
             std::memcpy(b->h[i]->adj->h_gp->dQw, b->D[i]->dQw, sizeof(b->D[i]->dQw));
+            b->pending_blength[i].assign(prm[i].blength, prm[i].blength + b->h[i]->nnode);
         });
     }
     int rc = build_graph(b, grad);
     if (rc) return rc;
+    // another batch's evaluation first (its graph's end event), so that the
+    // device runs the two back to back while the host prepares the next
+    if (after && after->ev1) CK(cudaStreamWaitEvent(b->origin, after->ev1, 0));
     CK(cudaEventRecord(b->ev0, b->origin));
     CK(cudaGraphLaunch(b->graph[grad ? 1 : 0], b->origin));
     CK(cudaEventRecord(b->ev1, b->origin));
+    b->pending = true;
+    b->pending_grad = grad;
+    b->pending_t0 = t0;
+    return GB_OK;
+}
+
+int gb_batch_collect(gb_batch *b, double *neg_lnL, gb_grad *grads, gb_stats *stats) {
+    if (!b || !neg_lnL) return fail(GB_ERR_ARG, "gb_batch_collect: bad arguments");
+    if (!b->pending) return fail(GB_ERR_STATE, "gb_batch_collect: nothing submitted");
+    const bool grad = b->pending_grad;
+    if (grads && !grad) return fail(GB_ERR_ARG, "gb_batch_collect: the evaluation was submitted without gradient");
+    b->pending = false;
+    CK(cudaSetDevice(b->device));
     CK(cudaStreamSynchronize(b->origin));
     CK(cudaGetLastError());
+    int rc;
     for (int i = 0; i < b->n; i++)
         if (b->h[i]->precision == GB_PREC_FAST && (rc = fast_check_error(b->h[i]))) return rc;
     for (int i = 0; i < b->n; i++) neg_lnL[i] = b->h[i]->h_out[0];
-    if (grad) parallel_for(b->n, b->nthreads, [&](int i) { adjoint_chain(b->h[i], b->D[i], prm[i].blength, &grads[i]); });
+    if (grads)
+        parallel_for(b->n, b->nthreads, [&](int i) {
+            adjoint_chain(b->h[i], b->D[i], b->pending_blength[i].data(), &grads[i]);
+        });
     if (stats) {
         float ms = 0;
         cudaEventElapsedTime(&ms, b->ev0, b->ev1);
         stats->ms_device = ms;
-        stats->ms_host = now_ms() - t0;
+        stats->ms_host = now_ms() - b->pending_t0;
         stats->kernels = b->kernels[grad ? 1 : 0];
         stats->nscale = 0;
         double h2d = 0, d2h = 0;
@@ -464,6 +492,13 @@ int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *g
         stats->d2h_bytes = d2h;
     }
     return GB_OK;
+}
+
+int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *grads, gb_stats *stats) {
+    if (!b || !prm || !neg_lnL) return fail(GB_ERR_ARG, "gb_batch_eval: bad arguments");
+    int rc = gb_batch_submit(b, prm, grads != nullptr, nullptr);
+    if (rc) return rc;
+    return gb_batch_collect(b, neg_lnL, grads, stats);
 }
 
 int gb_batch_tune(gb_batch *b, int knob, int value) {

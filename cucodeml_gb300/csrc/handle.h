@@ -63,6 +63,7 @@ void fast_free(FastState *f);
 namespace gb {
 struct Tuning {                     // gb_tune knobs; -1 / 0: default
     int mma = -1, persist = -1, gchunk = 0, order = 0, grid = 0;
+    int checkpoint = 0;              // FP64 adjoint: edge messages recomputed per level
 };
 }  // namespace gb
 

@@ -56,9 +56,9 @@ const CodeTables &tables() {
 // the trailing block in the symmetric rank-2 form S <- S - v w^T - w v^T with
 // p = tau S v, w = p - (tau / 2)(p . v) v.  v_1.. are kept in column k under
 // the sub-diagonal.  On return d holds the diagonal, e[k] the entry that
-// couples k and k+1 (e[n-1] = 0), and q = H_0 H_1 .. H_{n-3} (row-major),
-// accumulated backwards, so that a_in = q T q^T.
-void tridiagonalize(int n, double *a, double *d, double *e, double *q) {
+// couples k and k+1 (e[n-1] = 0), and qt the transpose of q = H_0 H_1 ..
+// H_{n-3} (row-major), accumulated backwards, so that a_in = q T q^T.
+void tridiagonalize(int n, double *a, double *d, double *e, double *qt) {
     double tau[NC], v[NC], p[NC];
     for (int k = 0; k + 2 < n; k++) {
         const int m = n - k - 1;
@@ -100,26 +100,31 @@ void tridiagonalize(int n, double *a, double *d, double *e, double *q) {
     e[n - 2] = a[(size_t)(n - 1) * n + (n - 2)];
     d[n - 1] = a[(size_t)(n - 1) * n + (n - 1)];
     e[n - 1] = 0;
-    for (int i = 0; i < n * n; i++) q[i] = 0;
-    for (int i = 0; i < n; i++) q[(size_t)i * n + i] = 1;
+    // q^T, accumulated backwards: q^T <- q^T H_k on columns k+1.. (rows of q^T
+    // are the columns of q, contiguous)
+    for (int i = 0; i < n * n; i++) qt[i] = 0;
+    for (int i = 0; i < n; i++) qt[(size_t)i * n + i] = 1;
     for (int k = n - 3; k >= 0; k--) {
         if (tau[k] == 0.0) continue;
         const int m = n - k - 1;
         v[0] = 1.0;
         for (int i = 1; i < m; i++) v[i] = a[(size_t)(k + 1 + i) * n + k];
         for (int c = k + 1; c < n; c++) {
+            double *__restrict__ row = qt + (size_t)c * n + (k + 1);
             double s = 0;
-            for (int r = 0; r < m; r++) s += v[r] * q[(size_t)(k + 1 + r) * n + c];
+            for (int r = 0; r < m; r++) s += v[r] * row[r];
             s *= tau[k];
-            for (int r = 0; r < m; r++) q[(size_t)(k + 1 + r) * n + c] -= s * v[r];
+            for (int r = 0; r < m; r++) row[r] -= s * v[r];
         }
     }
 }
 
-// Implicit-shift QL on the tridiagonal (d, e), e[k] coupling k and k+1;
-// z accumulates the rotations (eigenvectors in columns).  Returns 0, or -1
-// if an eigenvalue did not converge in 60 iterations.
-int ql_implicit(int n, double *d, double *e, double *z) {
+// Implicit-shift QL on the tridiagonal (d, e), e[k] coupling k and k+1.
+// zt holds the transform transposed (row i = column i of the matrix the
+// rotations multiply from the right), so that each rotation combines two
+// contiguous rows; on return row i of zt is the eigenvector of d[i].  Returns
+// 0, or -1 if an eigenvalue did not converge in 60 iterations.
+int ql_implicit(int n, double *d, double *e, double *zt) {
     e[n - 1] = 0;
     for (int l = 0; l < n; l++) {
         int iter = 0, m;
@@ -153,10 +158,12 @@ int ql_implicit(int n, double *d, double *e, double *z) {
                     p = s * r;
                     d[i + 1] = g + p;
                     g = c * r - b;
+                    double *__restrict__ za = zt + (size_t)i * n;
+                    double *__restrict__ zb = zt + (size_t)(i + 1) * n;
                     for (int k = 0; k < n; k++) {
-                        double zf = z[k * n + i + 1];
-                        z[k * n + i + 1] = s * z[k * n + i] + c * zf;
-                        z[k * n + i] = c * z[k * n + i] - s * zf;
+                        const double zf = zb[k];
+                        zb[k] = s * za[k] + c * zf;
+                        za[k] = c * za[k] - s * zf;
                     }
                 }
                 if (underflow) continue;
@@ -231,10 +238,11 @@ int eigen_qrev(const double *Q, const double *pi, double *U, double *V, double *
     }
     tridiagonalize(NC, a, Root, e, z);
     if (ql_implicit(NC, Root, e, z)) return -1;
-    for (int i = 0; i < NC; i++)
-        for (int k = 0; k < NC; k++) {
-            U[i * NC + k] = z[i * NC + k] / sq[i];
-            V[k * NC + i] = z[i * NC + k] * sq[i];
+    // z row k = eigenvector k: U[i][k] = z[k][i] / sqrt(pi_i), V[k][i] = z[k][i] sqrt(pi_i)
+    for (int k = 0; k < NC; k++)
+        for (int i = 0; i < NC; i++) {
+            U[i * NC + k] = z[k * NC + i] / sq[i];
+            V[k * NC + i] = z[k * NC + i] * sq[i];
         }
     return 0;
 }

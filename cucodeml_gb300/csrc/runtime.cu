@@ -510,7 +510,8 @@ int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad, 
     if (h->precision == GB_PREC_FAST) {
         rc = fast_eval(h, D, prm->blength, &v, grad, fhK, lnf, stats);
     } else {
-        rc = upload_and_run(h, D, prm->blength, grad != nullptr, &v, fhK, lnf, stats);
+        // checkpointed adjoint: the forward keeps no edge messages
+        rc = upload_and_run(h, D, prm->blength, grad != nullptr && !h->tune.checkpoint, &v, fhK, lnf, stats);
         if (!rc && grad) rc = adjoint_run(h, D, m, prm->blength, grad, stats);
     }
     delete D;
@@ -581,7 +582,7 @@ int gb_dfun_x(gb_handle *h, const int *bnode, int lastround, const double *x, in
 int gb_replay(gb_handle *h, int iters, int with_grad, double *ms) {
     if (!h || !ms || iters < 1) return fail(GB_ERR_ARG, "gb_replay: bad arguments");
     if (h->precision == GB_PREC_FAST) return fast_replay(h, iters, with_grad, ms);
-    cudaGraphExec_t g = h->graph[with_grad ? 1 : 0];
+    cudaGraphExec_t g = h->graph[(with_grad && !h->tune.checkpoint) ? 1 : 0];
     if (!g || (with_grad && !adjoint_ready(h))) return fail(GB_ERR_STATE, "gb_replay: evaluate first");
     CK(cudaSetDevice(h->device));
     CK(cudaEventRecord(h->ev0, h->stream));
@@ -603,14 +604,14 @@ int gb_replay(gb_handle *h, int iters, int with_grad, double *ms) {
 int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches) {
     if (!h || !ms || !launches || iters < 1) return fail(GB_ERR_ARG, "gb_profile: bad arguments");
     if (h->precision == GB_PREC_FAST) return fast_profile(h, iters, with_grad, ms, launches);
-    if (!h->graph[with_grad ? 1 : 0] || (with_grad && !adjoint_ready(h)))
+    if (!h->graph[(with_grad && !h->tune.checkpoint) ? 1 : 0] || (with_grad && !adjoint_ready(h)))
         return fail(GB_ERR_STATE, "gb_profile: evaluate first");
     CK(cudaSetDevice(h->device));
     ProfRec rec;
     h->prof = &rec;
     prof_mark(h, -1);
     for (int i = 0; i < iters; i++) {
-        record_forward(h, with_grad != 0);
+        record_forward(h, with_grad != 0 && !h->tune.checkpoint);
         if (with_grad) adjoint_record(h);
     }
     h->prof = nullptr;
@@ -647,6 +648,12 @@ int gb_tune(gb_handle *h, int knob, int value) {
         case GB_TUNE_GRID:
             if (value < 0) return fail(GB_ERR_ARG, "gb_tune: grid must be >= 0");
             h->tune.grid = value;
+            return GB_OK;
+        case GB_TUNE_CHECKPOINT:
+            if (value != 0 && value != 1) return fail(GB_ERR_ARG, "gb_tune: value must be 0 or 1");
+            if (value && h->precision != GB_PREC_FP64)
+                return fail(GB_ERR_ARG, "gb_tune: the checkpointed adjoint is on the FP64 path");
+            h->tune.checkpoint = value;
             return GB_OK;
         default:
             return fail(GB_ERR_ARG, "gb_tune: unknown knob");

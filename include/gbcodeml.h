@@ -326,6 +326,19 @@ typedef struct gb_batch gb_batch;
 int gb_batch_create(int ngene, const gb_problem *probs, gb_batch **out);
 int gb_batch_size(const gb_batch *b);
 int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *grads, gb_stats *stats);
+/*
+ * gb_batch_eval in two halves, so that the host work of one batch overlaps
+ * the device work of another: gb_batch_submit runs the host model set-up
+ * and launches the batch's graph without waiting for it (after `after`'s
+ * last submitted graph when after != NULL, so that the device runs the two
+ * back to back); gb_batch_collect waits for it and fills neg_lnL (and grads,
+ * if the evaluation was submitted with with_grad).  One evaluation may be
+ * outstanding per batch (GB_ERR_STATE otherwise).  Two batches over two
+ * halves of a set of genes, submitted alternately, keep the device busy
+ * while the host prepares the other half.
+ */
+int gb_batch_submit(gb_batch *b, const gb_params *prm, int with_grad, const gb_batch *after);
+int gb_batch_collect(gb_batch *b, double *neg_lnL, gb_grad *grads, gb_stats *stats);
 int gb_batch_replay(gb_batch *b, int iters, int with_grad, double *ms);
 int gb_batch_destroy(gb_batch *b);
 
@@ -358,6 +371,17 @@ int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches
  *                    default), 1 gene by gene by tree level, 2 by tree level
  *                    across genes
  *   GB_TUNE_GRID     CTAs per persistent launch (0: one per SM, the default)
+ *   GB_TUNE_CHECKPOINT  FP64 handles, the adjoint's memory: 0 (default) keeps
+ *                    every edge message E = P L~ of the forward and every
+ *                    Ebar of the reverse sweep (3 + 3 blocks of the size of
+ *                    the conditional likelihoods); 1 keeps the conditional
+ *                    likelihoods of every internal node (the subtree roots
+ *                    of the sweep) and recomputes the edge messages of one
+ *                    tree level at a time during the reverse sweep, with the
+ *                    dlnL/dP of that level's branches, so E and Ebar hold one
+ *                    level (about half the device memory of a gradient
+ *                    evaluation, one more forward pass of work; the same
+ *                    arithmetic, so the same lnL and gradient bit for bit)
  * Environment defaults: GBCODEML_MMA=sync, GBCODEML_PERSIST=0.
  */
 #define GB_TUNE_MMA     1
@@ -365,6 +389,7 @@ int gb_profile(gb_handle *h, int iters, int with_grad, double *ms, int *launches
 #define GB_TUNE_GCHUNK  3
 #define GB_TUNE_ORDER   4
 #define GB_TUNE_GRID    5
+#define GB_TUNE_CHECKPOINT 6
 int gb_tune(gb_handle *h, int knob, int value);
 int gb_batch_tune(gb_batch *b, int knob, int value);
 

@@ -1,7 +1,8 @@
 """Generate golden fixtures by running the reference codeml (CPU build).
 
-Test infrastructure.  Needs the reference sources (REF, default
-/root/reference) to build oracle/_ref/codeml via `make -C oracle ref`; the
+Test infrastructure.  Needs the reference sources (GBCODEML_REFERENCE, or
+the staged copy of `make -C oracle stage`) to build oracle/_ref/codeml via
+`make -C oracle ref`; the
 fixtures it writes (tests/golden/*.json) are committed, so tests never need
 the reference at run time.
 

@@ -1,7 +1,8 @@
 """Golden maximum-likelihood fixtures from the reference codeml's own optimiser.
 
-Test infrastructure.  Needs the reference sources (REF, default
-/root/reference) to build oracle/_ref/codeml via `make -C oracle ref`; the
+Test infrastructure.  Needs the reference sources (GBCODEML_REFERENCE, or
+the staged copy of `make -C oracle stage`) to build oracle/_ref/codeml via
+`make -C oracle ref`; the
 fixtures it writes (tests/golden/mle_*.json) are committed.
 
 For each case a seeded model-A alignment is simulated and codeml optimises,

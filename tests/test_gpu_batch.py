@@ -97,3 +97,24 @@ def test_batch_task_orders_agree(genes):
         assert np.array_equal(f, out[0][0])
         for a, b2 in zip(g, out[0][1]):
             assert np.array_equal(a, b2)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fast"])
+def test_pipelined_halves_equal_one_batch(genes, precision):
+    """gb_batch_submit / gb_batch_collect over two half-batches, with the host
+    set-up of one overlapping the device work of the other, gives each gene
+    what one gb_batch_eval gives, for a sequence of parameter sets."""
+    gl = [(a.tree, z, fp, pi) for a, z, fp, pi in genes]
+    sets = [[params_of(a, s) for a, _, _, _ in genes] for s in (1.0, 1.1, 0.9)]
+    b = api.Batch(gl, precision=precision)
+    ref = [b.evaluate(p, grad=True)[:2] for p in sets]
+    b.close()
+    pb = api.PipelinedBatch(gl, precision=precision)
+    got = pb.evaluate_many(sets, grad=True)
+    pb.close()
+    for (f0, g0), (f1, g1) in zip(ref, got):
+        assert np.max(np.abs(f0 - f1) / np.abs(f0)) <= 1e-12
+        for a, c in zip(g0, g1):
+            assert np.allclose(a["blength"], c["blength"], rtol=1e-10, atol=1e-10)
+            for k in ("kappa", "omega0", "omega2", "p0", "p1"):
+                assert abs(a[k] - c[k]) <= 1e-10 * max(1.0, abs(a[k]))

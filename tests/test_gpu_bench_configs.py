@@ -6,7 +6,8 @@
   central finite differences with h = 1e-6 and a five-point stencil of the
   FP64 lnL, twelve entries against a five-point stencil of the oracle, and
   all against codeml's own numerical gradient (gradientB, central, restated
-  in the oracle); the split-precision gradient against the same.
+  in the oracle); the split-precision gradient and the FP64 gradient with
+  the checkpointed adjoint (GB_TUNE_CHECKPOINT) against the same.
 * The batched workload's shape (taxa U{12..48}, codons log-uniform in
   [100, 3000], per-gene kappa, w0, w2): 32 genes through one batch, every
   gene's lnL against the oracle and, for eight of them, the gradient against
@@ -81,11 +82,13 @@ def test_lnL_and_site_logf_vs_oracle_64x5000(bench_case, precision):
 def bench_gradients(bench_case):
     tree, z, fpatt, pi, x, pb, v, lnf = bench_case
     out = {}
-    for precision in ("fp64", "fast"):
-        lk = api.Likelihood(tree, z, fpatt, pi, precision=precision)
+    for name, precision, tuning in (("fp64", "fp64", None), ("fast", "fast", None),
+                                    ("fp64 checkpointed", "fp64", {"checkpoint": 1})):
+        lk = api.Likelihood(tree, z, fpatt, pi, precision=precision, tuning=tuning)
         lk.evaluate(*natural(tree, x), grad=True)
-        out[precision] = x_grad(tree, lk.evaluate(*natural(tree, x), grad=True))
+        out[name] = x_grad(tree, lk.evaluate(*natural(tree, x), grad=True))
         lk.close()
+    assert np.array_equal(out["fp64"], out["fp64 checkpointed"])
     return out
 
 

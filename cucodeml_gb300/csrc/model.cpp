@@ -2,7 +2,10 @@
 #include "model.h"
 
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <functional>
+#include <mutex>
 #include <thread>
 
 #include "gbcodeml.h"
@@ -176,6 +179,60 @@ int ql_implicit(int n, double *d, double *e, double *zt) {
     return 0;
 }
 
+// Two long-lived helper threads for the side-by-side eigen solutions of one
+// evaluation (starting threads per evaluation costs about as much as a
+// 61 x 61 eigen solution).  One caller at a time: a caller that finds the
+// helpers busy (another host thread's evaluation) runs its jobs itself.
+class Helpers {
+  public:
+    static Helpers &get() {     // never destroyed: its threads live until the process exits
+        static Helpers *h = new Helpers;
+        return *h;
+    }
+    // job(1) and job(2) on the helpers, job(0) on the caller; false if busy
+    bool run3(const std::function<void(int)> &job) {
+        std::unique_lock<std::mutex> use(use_, std::try_to_lock);
+        if (!use.owns_lock()) return false;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            job_ = &job;
+            left_ = 2;
+            gen_++;
+        }
+        cv_.notify_all();
+        job(0);
+        std::unique_lock<std::mutex> lk(mu_);
+        done_.wait(lk, [&] { return left_ == 0; });
+        job_ = nullptr;
+        return true;
+    }
+
+  private:
+    Helpers() {
+        for (int w = 1; w <= 2; w++) std::thread([this, w] { loop(w); }).detach();
+    }
+    void loop(int w) {
+        unsigned long seen = 0;
+        for (;;) {
+            const std::function<void(int)> *job;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return gen_ != seen; });
+                seen = gen_;
+                job = job_;
+            }
+            (*job)(w);
+            std::lock_guard<std::mutex> lk(mu_);
+            if (--left_ == 0) done_.notify_one();
+        }
+    }
+    std::mutex use_, mu_;
+    std::condition_variable cv_, done_;
+    const std::function<void(int)> *job_ = nullptr;
+    unsigned long gen_ = 0;
+    int left_ = 0;
+};
+
 double mean_rate_omega(const double *pi, double kappa, double omega) {
     double Q[NC * NC];
     return build_q(pi, kappa, omega, Q, nullptr, nullptr);
@@ -301,14 +358,9 @@ int derive(const double *pi, const ModelParams &m, bool want_grad, Derived *out,
     // the three eigen problems are independent: side by side for a single
     // alignment; one after the other when the caller is already parallel
     // over alignments (a batch)
-    if (threads) {
-        std::thread t1(one, 1), t2(one, 2);
-        one(0);
-        t1.join();
-        t2.join();
-    } else {
+    const std::function<void(int)> job = one;
+    if (!threads || !Helpers::get().run3(job))
         for (int i = 0; i < 3; i++) one(i);
-    }
     for (int i = 0; i < 3; i++)
         if (status[i]) return GB_ERR_PARAM;
     return 0;

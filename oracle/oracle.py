@@ -211,14 +211,22 @@ class Problem:
         Qfactor_NS_branch[b] = 1 / meanrate(Q(kappa, p0 w0 + p1 + p2 w_{2+b}))
         (SetParametersNSsites codeml.c:2437-2446, 2522-2539).  Classes 0 and 1
         are model A's with slots (w0, 1, -), the third is model A's class 2a
-        with slots (w2, -, w3).  Returns (-lnL, fhK [3, npatt], lnf)."""
+        with slots (w2, -, w3).  Clade model D (NSsites = 3, a Problem made
+        with model_b=True): the same with w1 free, x ending p0, p1, w0, w1,
+        w2, w3.  Returns (-lnL, fhK [3, npatt], lnf)."""
         x = np.asarray(x, dtype=np.float64)
         nb = self.tree.nbranch
-        kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+        if self._s.model_b:
+            # clade model D (NSsites = 3): w1 free as well, x ends p0, p1, w0, w1, w2, w3
+            kappa, p0, p1, w0, w1, w2, w3 = x[nb:nb + 7]
+            mid = [w0, w1]
+        else:
+            kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+            w1, mid = 1.0, [w0]
         p2 = 1.0 - p0 - p1
-        Ua, Va, Ra, _, _ = self.set_params(np.concatenate([x[:nb], [kappa, p0, p1, w0, w2]]))
-        U3, V3, R3, _, _ = self.set_params(np.concatenate([x[:nb], [kappa, p0, p1, w0, w3]]))
-        qf = np.array([1.0 / build_q(self.pi, kappa, p0 * w0 + p1 + p2 * w)[1] for w in (w2, w3)])
+        Ua, Va, Ra, _, _ = self.set_params(np.concatenate([x[:nb], [kappa, p0, p1], mid, [w2]]))
+        U3, V3, R3, _, _ = self.set_params(np.concatenate([x[:nb], [kappa, p0, p1], mid, [w3]]))
+        qf = np.array([1.0 / build_q(self.pi, kappa, p0 * w0 + p1 * w1 + p2 * w)[1] for w in (w2, w3)])
         fa, nsc = self.fhK_uvr(Ua, Va, Ra, qf, x[:nb])
         Ub = np.stack([Ua[2], Ua[1], U3[2]])
         Vb = np.stack([Va[2], Va[1], V3[2]])

@@ -74,7 +74,12 @@ def as_model_a(fx, tree):
 
 def clade_names():
     """Fixed-parameter fixtures under clade model C (two branch types)."""
-    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("mc") and f.endswith(".json"))
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("mcC") and f.endswith(".json"))
+
+
+def clade_d_names():
+    """Fixed-parameter fixtures under clade model D (two branch types, w1 free)."""
+    return sorted(f[:-5] for f in os.listdir(GOLDEN) if f.startswith("mcD") and f.endswith(".json"))
 
 
 def site_model_classes(fx, tree):

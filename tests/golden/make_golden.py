@@ -39,7 +39,9 @@ model A's grid, w1 = 1 in class 1, with model B's Qfactors), kept for the
 mb* fixtures too.
 The mcC* fixtures are clade model C (model = 3, NSsites = 2; branch types
 #1 and background; x ends p0, p1, w0, w2, w3): lnL, log f, NG86 and codeml's
-clade-C BEB (three classes; grid w0, w2, w3).
+clade-C BEB (three classes; grid w0, w2, w3).  The mcD* fixtures are clade
+model D (model = 3, NSsites = 3, ncatG = 3; x ends p0, p1, w0, w1, w2, w3):
+lnL, log f and NG86 (codeml runs no BEB for it).
 The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
 x ends p0, p1, w0, w2 for M2a, p0, w0 for M1a, p0, p1, w0, w1, w2 for M3
 with three classes, p, q for M7, p0, p, q, ws for M8 with ten beta
@@ -47,7 +49,7 @@ categories): lnL, log f, NG86, and for M2a codeml's BEB (three classes).
 The mb_* fixtures are the same evaluation under branch-site model B
 (NSsites = 3, ncatG = 3: w1 free; x ends w0, w1, w2), lnL and log f only.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name prefix]
 """
 from __future__ import annotations
 
@@ -139,7 +141,7 @@ CASES_CLADE = [
 
 
 def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b=False, site_model=None,
-             clade=False):
+             clade=False, clade_d=False):
     aln = simulate(ns, ncodon, seed=seed, model=model)
     tree = aln.tree
     if site_model:
@@ -165,6 +167,8 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
                 ctl = ctl.replace("ncatG = 4", "ncatG = 10")
         if clade:
             ctl = CTL.replace("model = 2", "model = 3")
+        if clade_d:
+            ctl = ctl.replace("NSsites = 2", "NSsites = 3").replace("ncatG = 4", "ncatG = 3")
         with open(os.path.join(d, "codeml.ctl"), "w") as f:
             f.write(ctl)
         r = subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
@@ -176,7 +180,9 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
                 f.write(CTL.replace("getSE = 0", "getSE = 1"))
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
-    if clade:
+    if clade_d:       # codeml runs no BEB for clade model D (NSsites = 3), only NEB
+        extra = {"model": "D", "ng86_4dp": parse_ng86(out, ns)}
+    elif clade:
         extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3)}
     elif site_model:
         extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
@@ -284,12 +290,23 @@ def parse_beb(out: str, rst: str, stdout: str, ncls: int = 4) -> dict:
             "S2_6dp": float(m.group(3))}
 
 
-def main():
+# clade model D (model = 3, NSsites = 3, ncatG = 3: w1 free as well):
+# evaluation params (kappa, p0, p1, w0, w1, w2 background, w3 foreground)
+CASES_CLADE_D = [
+    ("mcD8x300_s17", 8, 300, 17, ModelA(), (2.0, 0.5, 0.3, 0.1, 0.7, 1.5, 3.5), 1.0),
+    ("mcD24x400_s18", 24, 400, 18, ModelA(kappa=2.5, omega2=4.0), (2.4, 0.45, 0.35, 0.15, 0.9, 2.0, 4.5), 1.0),
+]
+
+
+def main(only: str | None = None):
     subprocess.check_call(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref"])
     codeml = os.path.join(ROOT, "oracle", "_ref", "codeml")
     outdir = os.path.dirname(os.path.abspath(__file__))
     for case in (CASES + [c + (True,) for c in CASES_B] + [c[:7] + (False, c[7]) for c in CASES_SITE]
-                 + [c + (False, None, True) for c in CASES_CLADE]):
+                 + [c + (False, None, True) for c in CASES_CLADE]
+                 + [c + (False, None, True, True) for c in CASES_CLADE_D]):
+        if only and not case[0].startswith(only):
+            continue
         fx = run_case(codeml, *case)
         with open(os.path.join(outdir, fx["name"] + ".json"), "w") as f:
             json.dump(fx, f, separators=(",", ":"))
@@ -297,4 +314,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1] if len(sys.argv) > 1 else None)

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from tests.conftest import clade_names, load_golden
+from tests.conftest import clade_d_names, clade_names, load_golden
 
 
 @pytest.mark.parametrize("name", clade_names())
@@ -50,3 +50,19 @@ def test_clade_c_beb_matches_codeml(name):
     assert np.max(np.abs(q["post"] - r["post"])) <= 1e-12
     assert np.max(np.abs(q["grid"] - r["grid"])) <= 1e-12
     assert abs(q["lnfX"] - r["lnfX"]) <= 1e-12 * abs(r["lnfX"])
+
+
+@pytest.mark.parametrize("name", clade_d_names())
+def test_clade_d_matches_codeml(name):
+    """Clade model D (NSsites = 3, ncatG = 3): clade C with w1 free
+    (SetParametersNSsites codeml.c:2427-2446, eigen slots w0, w1, w2, w3
+    codeml.c:2535-2539), against codeml's fixed-parameter runs."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=2, model_b=True)
+    x = np.array(fx["x"])
+    assert len(x) == fx["codeml_np"] == tree.nbranch + 7
+    v, fhK, lnf = pb.clade_c(x)
+    assert abs(-v - fx["codeml_lnL"]) <= 5.1e-7 + 1e-12 * abs(v)
+    ref = np.array(fx["lnf"])
+    assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))

@@ -30,7 +30,8 @@ import numpy as np
 import pytest
 
 from oracle import refcodeml as R
-from tests.conftest import ROOT, clade_names, golden_names, load_golden, mle_names, model_b_names, unclean_names
+from tests.conftest import (ROOT, clade_d_names, clade_names, golden_names, load_golden, mle_names, model_b_names,
+                            unclean_names)
 
 SRC = os.path.join(ROOT, "oracle", "_ref", "src")
 
@@ -58,6 +59,9 @@ def ctl_for(name):
         return R.CTL.replace("cleandata = 1", "cleandata = 0")
     if name.startswith("mb"):
         return R.CTL.replace("NSsites = 2", "NSsites = 3").replace("ncatG = 4", "ncatG = 3")
+    if name.startswith("mcD"):
+        return R.CTL.replace("model = 2", "model = 3").replace("NSsites = 2", "NSsites = 3").replace(
+            "ncatG = 4", "ncatG = 3")
     if name.startswith("mc"):
         return R.CTL.replace("model = 2", "model = 3")
     return R.CTL
@@ -77,7 +81,8 @@ def test_dropin_links_and_stops_at_device_check_without_gpu():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", golden_names() + unclean_names() + model_b_names() + clade_names())
+@pytest.mark.parametrize("name", golden_names() + unclean_names() + model_b_names() + clade_names()
+                         + clade_d_names())
 def test_dropin_objective_matches_codeml_cpu(name):
     exe = dropin_binary()
     fx = load_fixture(name)

@@ -12,7 +12,7 @@ import pytest
 
 from cucodeml_gb300 import api
 from oracle import oracle as O
-from tests.conftest import clade_names, load_golden
+from tests.conftest import clade_d_names, clade_names, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -70,4 +70,32 @@ def test_clade_c_beb(name):
     site = r["post"][:, site_patterns(z, codons)].T
     assert np.max(np.abs(site - np.array(fx["beb"]["site_post_5dp"]))) <= 5.01e-6
     assert abs(r["lnfX"] - fx["beb"]["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])
+    lk.close()
+
+
+@pytest.mark.parametrize("name", clade_d_names())
+def test_clade_d_eval_uvr(name):
+    """Clade model D (w1 free): the same two gb_eval_uvr calls with slot 1
+    holding w1, against the oracle and codeml's printed lnL."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    kappa, p0, p1, w0, w1, w2, w3 = x[nb:nb + 7]
+    p2 = 1 - p0 - p1
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=4, model_b=True)
+    v, fhK, lnf = pb.clade_c(x)
+    Ua, Va, Ra, _, _ = pb.set_params(np.concatenate([x[:nb], [kappa, p0, p1, w0, w1, w2]]))
+    U3, V3, R3, _, _ = pb.set_params(np.concatenate([x[:nb], [kappa, p0, p1, w0, w1, w3]]))
+    U = [Ua[0], Ua[1], Ua[2], U3[2]]
+    V = [Va[0], Va[1], Va[2], V3[2]]
+    R = [Ra[0], Ra[1], Ra[2], R3[2]]
+    qf = np.array([1.0 / O.build_q(pi, kappa, p0 * w0 + p1 * w1 + p2 * w)[1] for w in (w2, w3)])
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[:nb]
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    f, g_fhK, g_lnf = lk.clade_uvr(U, V, R, qf, [p0, p1, p2], bl)
+    assert abs(f - v) <= 1e-12 * abs(v)
+    assert np.max(np.abs(g_lnf - lnf)) <= 1e-11
+    assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     lk.close()

@@ -68,6 +68,8 @@ SIGNATURES = {
                               C.POINTER(Stats)]),
     "gb_eval": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, C.POINTER(Grad), _dp, _dp,
                           C.POINTER(Stats)]),
+    "gb_eval_b": (C.c_int, [C.c_void_p, C.POINTER(Params), C.c_double, _dp, C.POINTER(Grad), _dp, _dp, _dp,
+                            C.POINTER(Stats)]),
     "gb_beb": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)]),
     "gb_beb_tables": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, _dp, _dp, _dp, C.POINTER(Stats)]),
     "gb_beb_qf": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,

@@ -268,7 +268,9 @@ class Likelihood:
         return -float((lnf * self._fpatt).sum()), fhK, lnf
 
     def evaluate(self, blength, kappa, omega0, omega2, p0, p1, grad: bool = False,
-                 want_site: bool = False) -> EvalResult:
+                 want_site: bool = False, omega1: float | None = None) -> EvalResult:
+        """-lnL (and gradient) of branch-site model A, or with omega1 given of
+        model B (w1 free, gb_eval_b; the gradient then has "omega1" too)."""
         bl = np.ascontiguousarray(blength, dtype=np.float64)
         prm = _lib.Params(_ptr(bl), kappa, omega0, omega2, p0, p1)
         f = C.c_double(0)
@@ -280,13 +282,22 @@ class Likelihood:
             g = _lib.Grad(_ptr(dbl), 0, 0, 0, 0, 0)
         fhK = np.zeros((4, self.npatt)) if want_site else None
         lnf = np.zeros(self.npatt) if want_site else None
-        _lib.check(self._L.gb_eval(self._h, C.byref(prm), C.byref(f), C.byref(g) if grad else None,
-                                   _ptr(fhK) if want_site else None, _ptr(lnf) if want_site else None,
-                                   C.byref(st)))
+        dw1 = C.c_double(0)
+        if omega1 is None:
+            _lib.check(self._L.gb_eval(self._h, C.byref(prm), C.byref(f), C.byref(g) if grad else None,
+                                       _ptr(fhK) if want_site else None, _ptr(lnf) if want_site else None,
+                                       C.byref(st)))
+        else:
+            _lib.check(self._L.gb_eval_b(self._h, C.byref(prm), float(omega1), C.byref(f),
+                                         C.byref(g) if grad else None, C.byref(dw1),
+                                         _ptr(fhK) if want_site else None, _ptr(lnf) if want_site else None,
+                                         C.byref(st)))
         gd = None
         if grad:
             gd = {"blength": dbl, "kappa": g.d_kappa, "omega0": g.d_omega0, "omega2": g.d_omega2,
                   "p0": g.d_p0, "p1": g.d_p1}
+            if omega1 is not None:
+                gd["omega1"] = dw1.value
         return EvalResult(f.value, fhK, lnf, gd, st.ms_device, st.ms_host, st.kernels,
                           st.h2d_bytes, st.d2h_bytes)
 

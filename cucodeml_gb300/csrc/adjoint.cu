@@ -43,11 +43,12 @@ constexpr int kGradHSmem = (2 * 61 * 62 + 3 * 256 + 64) * sizeof(double);
 
 // ---------------------------------------------------------------- kernels
 
-// D matrices V dQ U for (kappa: w=0,1,2) and (omega: w=0,2), 64-padded, and
-// the inverse eigenvalue differences of each w (for Phi)
-// Block bid: derivative matrix which = bid / DM_RB (0,1,2: kappa for w; 3: omega
-// w0; 4: omega w2), output rows 16 (bid % DM_RB) .. + 15 of D = V dQ U; the
-// last 3 blocks: 1/(Root_m - Root_n) for w (and U, V^T as double-float).
+// D matrices V dQ U for (kappa: w=0,1,2) and (omega: w=0,2 and slot 1), 64-padded,
+// and the inverse eigenvalue differences of each w (for Phi)
+// Block bid: derivative d = bid / DM_RB (0,1,2: kappa for w; 3: omega w0; 4:
+// omega w2; 5: omega of slot 1, stored at DM_OMEGA1), output rows
+// 16 (bid % DM_RB) .. + 15 of D = V dQ U; the last 3 blocks:
+// 1/(Root_m - Root_n) for w (and U, V^T as double-float).
 // dQ has at most ~10 non-zeros per row (single-nucleotide neighbours and the
 // diagonal): T = dQ U runs over each row's non-zeros (dense past 16).
 __device__ __forceinline__ float2 df_of(double v) {
@@ -61,8 +62,8 @@ __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, con
     __shared__ int nzk[61][16];
     __shared__ double nzv[61][16];
     __shared__ int nnz[61];
-    if (bid >= 5 * DM_RB) {
-        const int w = bid - 5 * DM_RB, which = 5 + w;
+    if (bid >= DM_NDER * DM_RB) {
+        const int w = bid - DM_NDER * DM_RB, which = 5 + w;
         const double *R = prm->Root[w];
         double *out = Dm + (size_t)which * 64 * 64;
         for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
@@ -84,9 +85,10 @@ __device__ __forceinline__ void dmat_body(const DevParams *__restrict__ prm, con
         }
         return;
     }
-    const int which = bid / DM_RB, rb = bid % DM_RB;
-    const int w = which < 3 ? which : (which == 3 ? 0 : 2);
-    const double *dQ = which < 3 ? gp->dQk[w] : gp->dQw[w];
+    const int d = bid / DM_RB, rb = bid % DM_RB;
+    const int w = d < 3 ? d : (d == 3 ? 0 : (d == 4 ? 2 : 1));
+    const int which = d == 5 ? DM_OMEGA1 : d;
+    const double *dQ = d < 3 ? gp->dQk[w] : gp->dQw[w];
     const double *U = prm->U[w];
     const double *V = prm->V[w];
     if (threadIdx.x < 61) {               // non-zeros of row r of dQ
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(256) gradH_kernel(const PairDesc *__restrict__
     // H[m][n] = sum_j U[j][m] T[j][n]
     double sdt = 0, sk = 0, sw = 0;
     const double *Dk = Dm + (size_t)w * 64 * 64;
-    const double *Dw = w == 0 ? Dm + 3 * 64 * 64 : (w == 2 ? Dm + 4 * 64 * 64 : nullptr);
+    const double *Dw = Dm + (size_t)(w == 0 ? 3 : (w == 2 ? 4 : DM_OMEGA1)) * 64 * 64;
     const double *inv = Dm + (size_t)(5 + w) * 64 * 64;
     const double rtp = tp > 0.0 ? 1.0 / tp : 0.0;
     for (int i = threadIdx.x; i < 61 * 61; i += blockDim.x) {
@@ -487,7 +489,7 @@ __device__ __forceinline__ void gradH_df_body(const PairDesc *__restrict__ pairs
     float2 sdt = make_float2(0.f, 0.f), sk = sdt, sw = sdt;
     const float2 *Tdf = UVdf + UVDF_DM;
     const float2 *Dk = Tdf + (size_t)w * 64 * 64;
-    const float2 *Dw = w == 0 ? Tdf + 3 * 64 * 64 : (w == 2 ? Tdf + 4 * 64 * 64 : nullptr);
+    const float2 *Dw = Tdf + (size_t)(w == 0 ? 3 : (w == 2 ? 4 : DM_OMEGA1)) * 64 * 64;
     const float2 *inv = Tdf + (size_t)(5 + w) * 64 * 64;
     const double rtp = tp > 0.0 ? 1.0 / tp : 0.0;
     const float2 rtpd = df_of(rtp), tpd = df_of(tp);
@@ -903,12 +905,13 @@ void adjoint_chain(gb_handle *h, const Derived *D, const double *blength, gb_gra
     // chain rule on the host (all derivatives of lnL; negated at the end)
     const int nn = h->nnode;
     std::vector<double> dtp(nn, 0.0);    // dlnL/dt' per node
-    double dk = 0, dw0 = 0, dw2 = 0;
+    double dk = 0, dw0 = 0, dw1 = 0, dw2 = 0;
     for (size_t p = 0; p < np; p++) {
         const PairDesc &pd = h->pairs[p];
         dtp[pd.node] += a->h_pout[p * 3 + 0];
         dk += a->h_pout[p * 3 + 1];
         if (pd.w == 0) dw0 += a->h_pout[p * 3 + 2];
+        if (pd.w == 1) dw1 += a->h_pout[p * 3 + 2];     // model B's w1 (zero under model A)
         if (pd.w == 2) dw2 += a->h_pout[p * 3 + 2];
     }
     double dqf[2] = {0, 0};
@@ -923,14 +926,16 @@ void adjoint_chain(gb_handle *h, const Derived *D, const double *blength, gb_gra
     double dfk[4] = {0, 0, 0, 0};   // sum_h fpatt f_c / R
     for (int b = 0; b < a->nfreq_blocks; b++)
         for (int c = 0; c < 4; c++) dfk[c] += a->h_fpart[b * 4 + c];
-    double gk = dk, gw0 = dw0, gw2 = dw2, gp0 = 0, gp1 = 0;
+    double gk = dk, gw0 = dw0, gw1 = dw1, gw2 = dw2, gp0 = 0, gp1 = 0;
     for (int b = 0; b < 2; b++) {
         gk += dqf[b] * D->dqf[b][0];
         gw0 += dqf[b] * D->dqf[b][1];
         gw2 += dqf[b] * D->dqf[b][2];
         gp0 += dqf[b] * D->dqf[b][3];
         gp1 += dqf[b] * D->dqf[b][4];
+        gw1 += dqf[b] * D->dqf[b][5];
     }
+    a->d_omega1 = -gw1;
     for (int c = 0; c < 4; c++) {
         gp0 += dfk[c] * D->dfreqK[c][0];
         gp1 += dfk[c] * D->dfreqK[c][1];

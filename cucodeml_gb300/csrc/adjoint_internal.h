@@ -18,9 +18,15 @@ constexpr int GCHUNK = 512;   // patterns per partial of dlnL/dP (FP64 kernel)
 constexpr int GCHUNK_FAST = 2048;   // default of the split-precision kernels (measured fastest on a
                                     // single 64 x 5000 alignment and on a 512-gene batch; a single
                                     // small alignment halves it while its tasks are too few)
-constexpr int DM_MATS = 8;    // dP/dt buffer: 5 derivative matrices + 3 inverse-difference tables
+// dP/dt buffer: derivative matrices V dQ U at 0..4 (kappa for w0, w1, w2;
+// omega for w0, w2), the inverse-difference tables of w0, w1, w2 at 5..7, and
+// the omega derivative of slot 1 at 8 (branch-site model B's free w1; zero
+// under model A, where w1 = 1)
+constexpr int DM_MATS = 9;
 constexpr int DM_RB = 4;      // dP/dt kernel: row blocks per derivative matrix
-constexpr int DM_BLOCKS = 5 * DM_RB + 3;
+constexpr int DM_NDER = 6;    // derivative matrices formed
+constexpr int DM_BLOCKS = DM_NDER * DM_RB + 3;
+constexpr int DM_OMEGA1 = 8;  // index of the slot-1 omega derivative
 constexpr int UVDF_DM = 3 * 2 * 61 * 64;   // offset of the double-float tables in d_UVdf
 
 struct BItem {                // backward work: (node, class family) of one level
@@ -61,6 +67,7 @@ struct AdjointState {
     double *h_pout = nullptr, *h_fpart = nullptr;
     cudaGraphExec_t graph = nullptr;
     int graph_kernels = 0;
+    double d_omega1 = 0;             // d(-lnL)/d w1 of the last chain rule (model B)
     // checkpointed adjoint (FP64, gb_tune GB_TUNE_CHECKPOINT): conditional
     // likelihoods kept at every internal node, the edge messages E and Ebar
     // of one tree level at a time, recomputed level by level in the reverse

@@ -313,9 +313,12 @@ int derive_scalars(const double *pi, const ModelParams &m, Derived *out) {
     out->freqK[1] = m.p1;
     out->freqK[2] = (1 - s) * m.p0 / s;
     out->freqK[3] = (1 - s) * m.p1 / s;
-    // Qfactor_NS_branch: background mixes (w0, 1) by p/(p0+p1); foreground (w0, 1, w2) by (p0, p1, 1-s)
-    double wb = m.p0 / s * m.w0 + m.p1 / s * 1.0;
-    double wf = m.p0 * m.w0 + m.p1 * 1.0 + (1 - s) * m.w2;
+    // Qfactor_NS_branch: background mixes (w0, w1) by p/(p0+p1); foreground (w0, w1, w2) by
+    // (p0, p1, 1-s); w1 = 1 under model A
+    const double w1 = m.w1;
+    if (!(w1 >= 0)) return GB_ERR_PARAM;
+    double wb = m.p0 / s * m.w0 + m.p1 / s * w1;
+    double wf = m.p0 * m.w0 + m.p1 * w1 + (1 - s) * m.w2;
     double mr[2] = {mean_rate_omega(pi, m.kappa, wb), mean_rate_omega(pi, m.kappa, wf)};
     out->qf[0] = 1 / mr[0];
     out->qf[1] = 1 / mr[1];
@@ -323,17 +326,17 @@ int derive_scalars(const double *pi, const ModelParams &m, Derived *out) {
     double part[4];
     rate_parts(pi, part);
     double wbar[2] = {wb, wf};
-    // d wbar / d (w0, w2, p0, p1)
-    double dw[2][4] = {
-        {m.p0 / s, 0, m.p1 * (m.w0 - 1) / (s * s), m.p0 * (1 - m.w0) / (s * s)},
-        {m.p0, 1 - s, m.w0 - m.w2, 1 - m.w2},
+    // d wbar / d (w0, w2, p0, p1, w1)
+    double dw[2][5] = {
+        {m.p0 / s, 0, m.p1 * (m.w0 - w1) / (s * s), m.p0 * (w1 - m.w0) / (s * s), m.p1 / s},
+        {m.p0, 1 - s, m.w0 - m.w2, w1 - m.w2, m.p1},
     };
     for (int b = 0; b < 2; b++) {
         double q2 = -out->qf[b] * out->qf[b];
         double dmr_dk = part[1] + wbar[b] * part[3];
         double dmr_dw = part[2] + m.kappa * part[3];
         out->dqf[b][0] = q2 * dmr_dk;
-        for (int t = 0; t < 4; t++) out->dqf[b][1 + t] = q2 * dmr_dw * dw[b][t];
+        for (int t = 0; t < 5; t++) out->dqf[b][1 + t] = q2 * dmr_dw * dw[b][t];
     }
     double s2 = s * s;
     out->dfreqK[0][0] = 1; out->dfreqK[0][1] = 0;
@@ -346,14 +349,14 @@ int derive_scalars(const double *pi, const ModelParams &m, Derived *out) {
 int derive(const double *pi, const ModelParams &m, bool want_grad, Derived *out, bool threads) {
     int rc = derive_scalars(pi, m, out);
     if (rc) return rc;
-    const double w[3] = {m.w0, 1.0, m.w2};
+    const double w[3] = {m.w0, m.w1, m.w2};
     int status[3] = {0, 0, 0};
     auto one = [&](int i) {
         double Q[NC * NC];
         build_q(pi, m.kappa, w[i], Q, want_grad ? out->dQk[i] : nullptr,
                 want_grad ? out->dQw[i] : nullptr);
         status[i] = eigen_qrev(Q, pi, out->U[i], out->V[i], out->Root[i]);
-        if (want_grad && i == 1) std::memset(out->dQw[1], 0, sizeof(double) * NC * NC);
+        if (want_grad && i == 1 && !m.free_w1) std::memset(out->dQw[1], 0, sizeof(double) * NC * NC);
     };
     // the three eigen problems are independent: side by side for a single
     // alignment; one after the other when the caller is already parallel

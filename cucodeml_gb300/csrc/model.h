@@ -13,6 +13,8 @@ constexpr int NC = 61;
 
 struct ModelParams {
     double kappa, w0, w2, p0, p1;
+    double w1 = 1.0;         // site class 1's omega: 1 under model A, free under model B
+    bool free_w1 = false;    // branch-site model B: w1 is a parameter (its derivatives are kept)
 };
 
 struct Derived {
@@ -22,7 +24,7 @@ struct Derived {
     double freqK[4];     // p0, p1, p2a, p2b
     int sym = 1;         // V[m][k] = U[k][m] pi_k (true for eigen_qrev's solutions)
     // derivatives (filled when requested)
-    double dqf[2][5];    // d qf[b] / d (kappa, w0, w2, p0, p1)
+    double dqf[2][6];    // d qf[b] / d (kappa, w0, w2, p0, p1, w1)
     double dfreqK[4][2]; // d freqK[c] / d (p0, p1)
     double dQk[3][NC * NC];  // dQ_i/dkappa (row-major)
     double dQw[3][NC * NC];  // dQ_i/dw_i (zero matrix for w1 = 1)

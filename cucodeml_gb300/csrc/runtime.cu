@@ -497,13 +497,17 @@ int gb_eval_uvr(gb_handle *h, const double *const U[3], const double *const V[3]
     return rc;
 }
 
-int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad, double *fhK,
-            double *lnf, gb_stats *stats) {
+namespace {
+// gb_eval (model A: w1 = 1) and gb_eval_b (model B: w1 free)
+int eval_impl(gb_handle *h, const gb_params *prm, double w1, bool free_w1, double *neg_lnL, gb_grad *grad,
+              double *d_omega1, double *fhK, double *lnf, gb_stats *stats) {
     if (!h) return fail(GB_ERR_STATE, "null handle");
     if (!prm || !prm->blength) return fail(GB_ERR_ARG, "null argument");
     double t0 = now_ms();
     Derived *D = new Derived;
     ModelParams m{prm->kappa, prm->omega0, prm->omega2, prm->p0, prm->p1};
+    m.w1 = w1;
+    m.free_w1 = free_w1;
     int rc = derive(h->pi.data(), m, grad != nullptr, D);
     if (rc) { delete D; return fail(rc, "model parameters out of range"); }
     double v = 0;
@@ -517,8 +521,20 @@ int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad, 
     delete D;
     if (rc) return rc;
     if (neg_lnL) *neg_lnL = v;
+    if (grad && d_omega1) *d_omega1 = h->adj ? h->adj->d_omega1 : 0.0;
     if (stats) stats->ms_host = now_ms() - t0;
     return GB_OK;
+}
+}  // namespace
+
+int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad, double *fhK,
+            double *lnf, gb_stats *stats) {
+    return eval_impl(h, prm, 1.0, false, neg_lnL, grad, nullptr, fhK, lnf, stats);
+}
+
+int gb_eval_b(gb_handle *h, const gb_params *prm, double omega1, double *neg_lnL, gb_grad *grad,
+              double *d_omega1, double *fhK, double *lnf, gb_stats *stats) {
+    return eval_impl(h, prm, omega1, true, neg_lnL, grad, d_omega1, fhK, lnf, stats);
 }
 
 int gb_neb(gb_handle *h, const gb_params *prm, double *post, double *neg_lnL) {
@@ -544,13 +560,16 @@ int gb_dfun_x(gb_handle *h, const int *bnode, int lastround, const double *x, in
               double *dx) {
     if (!h) return fail(GB_ERR_STATE, "null handle");
     const int nb = h->nnode - 1;
-    if (!bnode || !x || !f || !dx || n != nb + 5) return fail(GB_ERR_ARG, "gb_dfun_x: bad arguments");
+    // model A: x ends kappa, p0', p1', w0, w2; model B (n = nb + 6): ..., w0, w1, w2
+    if (!bnode || !x || !f || !dx || (n != nb + 5 && n != nb + 6)) return fail(GB_ERR_ARG, "gb_dfun_x: bad arguments");
+    const bool model_b = n == nb + 6;
+    const int iw2 = model_b ? nb + 5 : nb + 4;
     std::vector<double> bl(h->nnode, 0.0), dbl(h->nnode, 0.0);
     for (int ib = 0; ib < nb; ib++) {
         if (bnode[ib] < 0 || bnode[ib] >= h->nnode || bnode[ib] == h->root) return fail(GB_ERR_ARG, "bnode");
         bl[bnode[ib]] = x[ib];
     }
-    gb_params p{bl.data(), x[nb], x[nb + 3], x[nb + 4], 0, 0};
+    gb_params p{bl.data(), x[nb], x[nb + 3], x[iw2], 0, 0};
     double e1 = 0, e2 = 0;
     if (!lastround) {   // codeml's f_and_x: p_i = e^{x_i} / (1 + e^{x_1} + e^{x_2})
         e1 = std::exp(x[nb + 1]);
@@ -563,7 +582,9 @@ int gb_dfun_x(gb_handle *h, const int *bnode, int lastround, const double *x, in
         p.p1 = x[nb + 2];
     }
     gb_grad g{dbl.data(), 0, 0, 0, 0, 0};
-    int rc = gb_eval(h, &p, f, &g, nullptr, nullptr, nullptr);
+    double dw1 = 0;
+    int rc = model_b ? gb_eval_b(h, &p, x[nb + 4], f, &g, &dw1, nullptr, nullptr, nullptr)
+                     : gb_eval(h, &p, f, &g, nullptr, nullptr, nullptr);
     if (rc) return rc;
     for (int ib = 0; ib < nb; ib++) dx[ib] = dbl[bnode[ib]];
     dx[nb] = g.d_kappa;
@@ -575,7 +596,8 @@ int gb_dfun_x(gb_handle *h, const int *bnode, int lastround, const double *x, in
         dx[nb + 2] = g.d_p1;
     }
     dx[nb + 3] = g.d_omega0;
-    dx[nb + 4] = g.d_omega2;
+    if (model_b) dx[nb + 4] = dw1;
+    dx[iw2] = g.d_omega2;
     return GB_OK;
 }
 

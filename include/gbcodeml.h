@@ -184,6 +184,17 @@ int gb_eval_uvr(gb_handle *h, const double *const U[3], const double *const V[3]
 int gb_eval(gb_handle *h, const gb_params *prm, double *neg_lnL, gb_grad *grad,
             double *fhK, double *lnf, gb_stats *stats);
 
+/* gb_eval for branch-site model B (codeml NSsites = 3, ncatG = 3), whose
+   site class 1 has a free omega1 where model A fixes it at 1: the second
+   eigen solution is Q(kappa, omega1) and omega1 enters both branch types'
+   mean rates behind the Qfactors (SetParametersNSsites codeml.c:2427-2436,
+   2488-2521); classes, their omega map and the pruning are model A's.  Any
+   precision.  With grad, *d_omega1 (may be NULL) receives d(-lnL)/d omega1
+   beside the other derivatives.  gb_dfun_x takes model B's x (branch lengths,
+   kappa, p0, p1, w0, w1, w2) when n = nbranch + 6. */
+int gb_eval_b(gb_handle *h, const gb_params *prm, double omega1, double *neg_lnL, gb_grad *grad,
+              double *d_omega1, double *fhK, double *lnf, gb_stats *stats);
+
 /*
  * Bayes empirical Bayes (BEB) analysis of branch-site model A at prm
  * (normally the MLE), as codeml's lfunNSsites_ACD (codeml.c:6617-6826, with

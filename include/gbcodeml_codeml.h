@@ -19,7 +19,8 @@
  *   CUDA_FreeAll                   replaces cuda-codeml.cu:1162 (codeml.c:695).
  *   GB_dfun                        new: ming2's gradient hook
  *                                  (tools.c:6361-6363, `dfun`), the analytic
- *                                  gradient of -lnL in codeml's x space; pass it
+ *                                  gradient of -lnL in codeml's x space
+ *                                  (branch-site models A and B); pass it
  *                                  instead of NULL at codeml.c:688.
  *   GB_BEB                         new: the Bayes empirical Bayes analysis of
  *                                  models A and B on the GPU at codeml's final

@@ -86,7 +86,7 @@ def test_dropin_links_and_stops_at_device_check_without_gpu():
 def test_dropin_objective_matches_codeml_cpu(name):
     exe = dropin_binary()
     fx = load_fixture(name)
-    model_a = name.startswith(("c", "u"))
+    model_a = name.startswith(("c", "u", "mb"))      # GB_dfun: models A and B
     with tempfile.TemporaryDirectory() as d:
         fixture_case(d, fx, ctl=ctl_for(name))
         r = R.run(exe, d, "eval", env={"GBREF_DFUN": "1" if model_a else "0"}, timeout=900)

@@ -192,6 +192,79 @@ class Problem:
                 "post": post.reshape(3, self.npatt), "grid": grid.reshape(5, 10), "p0p1": p0p1,
                 "lnfX": fx[0], "S1": fx[1], "S2": fx[2]}
 
+    def beb_clade_d(self, x):
+        """Bayes empirical Bayes under clade model D with two branch types
+        (lfunNSsites_ACD codeml.c:6617-6826 with modelACD = mD; grid and sets
+        get_grid_para_like_ACD 6419-6530), in numpy over this oracle's
+        pruning.  x = [branch lengths, kappa, p0, p1, w0, w1, w2, w3] (p0,
+        p1 untransformed).  Sets: 10 w0 values in (0, 0.5) and 10 w1 values
+        in (0.5, 1.5) on every branch, then (w2_i background, w3_j
+        foreground) for w2, w3 in (0, 3), set 20 + 10 i + j; P from each
+        omega's unscaled Q with the MLE's Qfactors applied to t.  Grid: 100
+        ternary (p0, p1) triangles x w0 x w1 x w2 x w3 (10^6 points, uniform).
+        Returns lnfw [120, npatt], post [3, npatt], grid rows w0, w1, w2, w3
+        [4, 10], p0p1 [100], lnfX (as codeml prints it), S1."""
+        x = np.asarray(x, dtype=np.float64)
+        nb = self.tree.nbranch
+        kappa, p0, p1, w0, w1, w2, w3 = x[nb:nb + 7]
+        p2 = 1.0 - p0 - p1
+        qf = np.array([1.0 / build_q(self.pi, kappa, p0 * w0 + p1 * w1 + p2 * w)[1] for w in (w2, w3)])
+        sq = np.sqrt(self.pi)
+
+        def eig(w):      # eigenQREV's symmetrisation, solved by LAPACK (numpy)
+            Q = build_q(self.pi, kappa, w)[0]
+            lam, E = np.linalg.eigh(sq[:, None] * Q / sq[None, :])
+            return E / sq[:, None], E.T * sq[None, :], lam
+
+        def classes(wa, wc):     # fhK of model A's classes with slots (wa, 1, wc) as log f
+            e = [eig(wa), eig(1.0), eig(wc)]
+            fh, nsc = self.fhK_uvr(np.stack([q[0] for q in e]), np.stack([q[1] for q in e]),
+                                   np.stack([q[2] for q in e]), qf, x[:nb])
+            return fh if nsc else np.log(np.where(fh <= 0, 1e-300, fh))
+
+        g0 = 0.5 * (np.arange(10) + 0.5) / 10
+        g1 = 0.5 + (np.arange(10) + 0.5) / 10
+        g2 = 3.0 * (np.arange(10) + 0.5) / 10
+        lnfw = np.empty((120, self.npatt))
+        for i in range(10):
+            lnfw[i] = classes(g0[i], 1.0)[0]
+            lnfw[10 + i] = classes(g1[i], 1.0)[0]
+            for j in range(10):
+                lnfw[20 + 10 * i + j] = classes(g2[i], g2[j])[2]
+        m = lnfw.max(axis=0)
+        F = np.exp(lnfw - m)
+        S1 = float(m @ self.fpatt)
+        t = np.arange(100)
+        ix = np.floor(np.sqrt(t)).astype(int)
+        iy = t - ix * ix
+        pa = (1 + (iy // 2) * 3 + (iy % 2)) / 30.0          # GetIndexTernary tools.c:4441-4461
+        pb = (1 + (9 - ix) * 3 + (iy % 2)) / 30.0
+        P3 = np.stack([pa, pb, 1 - pa - pb], axis=1)
+        F0, F1, F2 = F[0:10], F[10:20], F[20:120]
+        lnfXs = np.empty((100, 10, 10, 100))
+        for a in range(100):
+            for i0 in range(10):
+                for i1 in range(10):
+                    fh = P3[a, 0] * F0[i0] + P3[a, 1] * F1[i1] + P3[a, 2] * F2
+                    lnfXs[a, i0, i1] = np.where(fh < 1e-300, 0.0, np.log(np.maximum(fh, 1e-300))) @ self.fpatt
+        M = lnfXs.max()
+        lfX = M + np.log(np.exp(lnfXs - M).sum())
+        w = np.exp(lnfXs - lfX)
+        post = np.zeros((3, self.npatt))
+        for a in range(100):
+            for i0 in range(10):
+                for i1 in range(10):
+                    fh = P3[a, 0] * F0[i0] + P3[a, 1] * F1[i1] + P3[a, 2] * F2
+                    wk = w[a, i0, i1][:, None] / fh
+                    post[0] += P3[a, 0] * F0[i0] * wk.sum(axis=0)
+                    post[1] += P3[a, 1] * F1[i1] * wk.sum(axis=0)
+                    post[2] += P3[a, 2] * (F2 * wk).sum(axis=0)
+        w6 = w.reshape(100, 10, 10, 10, 10)
+        grid = np.stack([w6.sum(axis=(0, 2, 3, 4)), w6.sum(axis=(0, 1, 3, 4)), w6.sum(axis=(0, 1, 2, 4)),
+                         w6.sum(axis=(0, 1, 2, 3))])
+        return {"lnfw": lnfw, "post": post, "grid": grid, "p0p1": w.sum(axis=(1, 2, 3)),
+                "lnfX": float(lfX + S1 - 6 * np.log(10.0)), "S1": S1}
+
     def fhK_uvr(self, U, V, R, qf, xb):
         """Per-class fhK (4, npatt) from given eigen slots, Qfactors and branch
         lengths by branch index (oracle.c oracle_fhK_uvr); also nscale."""

@@ -41,7 +41,8 @@ The mcC* fixtures are clade model C (model = 3, NSsites = 2; branch types
 #1 and background; x ends p0, p1, w0, w2, w3): lnL, log f, NG86 and codeml's
 clade-C BEB (three classes; grid w0, w2, w3).  The mcD* fixtures are clade
 model D (model = 3, NSsites = 3, ncatG = 3; x ends p0, p1, w0, w1, w2, w3):
-lnL, log f and NG86 (codeml runs no BEB for it).
+lnL, log f, NG86 and codeml's clade-D BEB (three classes; grid w0, w1, w2,
+w3: 10^6 points).
 The ms* fixtures are site models M2a and M1a (model = 0, no branch labels;
 x ends p0, p1, w0, w2 for M2a, p0, w0 for M1a, p0, p1, w0, w1, w2 for M3
 with three classes, p, q for M7, p0, p, q, ws for M8 with ten beta
@@ -180,8 +181,8 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
                 f.write(CTL.replace("getSE = 0", "getSE = 1"))
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
-    if clade_d:       # codeml runs no BEB for clade model D (NSsites = 3), only NEB
-        extra = {"model": "D", "ng86_4dp": parse_ng86(out, ns)}
+    if clade_d:       # clade-D BEB: grid w0 in (0, 0.5), w1 in (0.5, 1.5), w2, w3 in (0, 3)
+        extra = {"model": "D", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3)}
     elif clade:
         extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3)}
     elif site_model:
@@ -277,7 +278,7 @@ def parse_beb(out: str, rst: str, stdout: str, ncls: int = 4) -> dict:
     rows = {}
     for ln in out[j0:].splitlines()[1:7]:
         parts = ln.split()
-        if parts and parts[0] in ("w0:", "w2:", "w3:"):
+        if parts and parts[0] in ("w0:", "w1:", "w2:", "w3:"):
             rows[parts[0][:2]] = [float(v) for v in parts[1:]]
     k0 = out.index("Posterior for p0-p1")
     k1 = out.index("sum of density on p0-p1")
@@ -285,6 +286,8 @@ def parse_beb(out: str, rst: str, stdout: str, ncls: int = 4) -> dict:
     m = re.search(r"log\(fX\) =\s*(-?\d+\.\d+)\s+S =\s*(-?\d+\.\d+)\s+(-?\d+\.\d+)",
                   stdout.replace("\r", "\n"))
     extra = {"w3_post_3dp": rows["w3"]} if "w3" in rows else {}
+    if "w1" in rows:
+        extra["w1_post_3dp"] = rows["w1"]
     return {**extra, "site_post_5dp": site, "w0_post_3dp": rows["w0"], "w2_post_3dp": rows["w2"],
             "p0p1_post_3dp": p0p1, "lnfX_6dp": float(m.group(1)), "S1_6dp": float(m.group(2)),
             "S2_6dp": float(m.group(3))}

@@ -66,3 +66,25 @@ def test_clade_d_matches_codeml(name):
     assert abs(-v - fx["codeml_lnL"]) <= 5.1e-7 + 1e-12 * abs(v)
     ref = np.array(fx["lnf"])
     assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))
+
+
+@pytest.mark.parametrize("name", clade_d_names())
+def test_clade_d_beb_matches_codeml(name):
+    """codeml's BEB under clade model D (lfunNSsites_ACD with modelACD = mD:
+    120 omega sets, 10^6-point grid over the (p0, p1) triangles, w0, w1, w2,
+    w3), restated in numpy over the oracle's pruning, against codeml's
+    printed site posteriors (rst, 5 dp), grid posteriors and (p0, p1)
+    posterior (out, 3 dp) and log f(X), S1 (stdout, 6 dp)."""
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    r = O.Problem(tree, z, fpatt, pi, nthreads=O.max_threads(), model_b=True).beb_clade_d(np.array(fx["x"]))
+    b = fx["beb"]
+    assert abs(r["lnfX"] - b["lnfX_6dp"]) <= 1e-6 + 1e-12 * abs(b["lnfX_6dp"])
+    assert abs(r["S1"] - b["S1_6dp"]) <= 1e-6 + 1e-12 * abs(b["S1_6dp"])
+    site = r["post"][:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(b["site_post_5dp"]))) <= 5.01e-6
+    for row, key in enumerate(("w0_post_3dp", "w1_post_3dp", "w2_post_3dp", "w3_post_3dp")):
+        assert np.max(np.abs(r["grid"][row] - np.array(b[key]))) <= 5.01e-4
+    assert np.max(np.abs(r["p0p1"] - np.array(b["p0p1_post_3dp"]))) <= 5.01e-4
+    assert np.allclose(r["post"].sum(axis=0), 1.0, atol=1e-12)

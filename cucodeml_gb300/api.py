@@ -71,46 +71,6 @@ def _ternary_classes():
     return np.stack([a, b, 1 - a - b], axis=1)
 
 
-def beb_clade_integrate(lnfw, fpatt):
-    """The grid integration of codeml's BEB under clade model C with two branch
-    types (lfunNSsites_ACD codeml.c:6700-6775 with modelACD = mC), host side,
-    from the 111 log f(x_h | w) tables: sets 0-9 (w0 in (0, 1) everywhere), 10
-    (w = 1), 11 + 10 i + j (w2_i background, w3_j foreground, both in (0, 3)).
-    Grid: 100 ternary (p0, p1) triangles x w0 x w2 x w3; classes (p0, p1, p2).
-    Returns post [3, npatt], grid [5, 10] (rows p0, p1 = -1), p0p1 [100], lnfX
-    as codeml prints it, S1."""
-    L = np.asarray(lnfw, dtype=np.float64)
-    fp = np.asarray(fpatt, dtype=np.float64)
-    m = L.max(axis=0)
-    F = np.exp(L - m)
-    S1 = float(m @ fp)
-    F0, F1, F2 = F[0:10], F[10], F[11:111]
-    tri = _ternary_classes()
-    lnfXs = np.empty((100, 10, 100))
-    for t in range(100):
-        for i0 in range(10):
-            fh = tri[t, 0] * F0[i0] + tri[t, 1] * F1 + tri[t, 2] * F2
-            lnfXs[t, i0] = np.where(fh < 1e-300, 0.0, np.log(np.maximum(fh, 1e-300))) @ fp
-    M = lnfXs.max()
-    lfX = M + np.log(np.exp(lnfXs - M).sum())
-    w = np.exp(lnfXs - lfX)                       # (t, i0, k = 10 i2 + i3)
-    post = np.zeros((3, L.shape[1]))
-    for t in range(100):
-        for i0 in range(10):
-            fh = tri[t, 0] * F0[i0] + tri[t, 1] * F1 + tri[t, 2] * F2
-            wk = w[t, i0][:, None] / fh
-            post[0] += tri[t, 0] * F0[i0] * wk.sum(axis=0)
-            post[1] += tri[t, 1] * F1 * wk.sum(axis=0)
-            post[2] += tri[t, 2] * (F2 * wk).sum(axis=0)
-    w5 = w.reshape(10, 10, 10, 10, 10)            # p-row index, p-col index, i0, i2, i3
-    grid = np.full((5, 10), -1.0)
-    grid[2] = w5.sum(axis=(0, 1, 3, 4))
-    grid[3] = w5.sum(axis=(0, 1, 2, 4))
-    grid[4] = w5.sum(axis=(0, 1, 2, 3))
-    p0p1 = w.sum(axis=(1, 2))
-    return {"post": post, "grid": grid, "p0p1": p0p1, "lnfX": float(lfX + S1 - 5 * np.log(10.0)), "S1": S1}
-
-
 def model_setup(pi, kappa, omega0, omega2, p0, p1):
     """(U [3,61,61], V [3,61,61], Root [3,61], qf [2], freqK [4]) computed by the library's host code."""
     L = _lib.load()
@@ -417,17 +377,46 @@ class Likelihood:
                                          _ptr(lnfw), C.byref(st)))
         return lnfw
 
+    def beb_clade(self, lnfw, model_d: bool = False) -> dict:
+        """The grid integral of codeml's BEB under clade model C (111 log f
+        tables) or D (model_d: 120 tables) on the device (gb_beb_clade):
+        post [3, npatt], grid [4, 10] (rows w0, w1 (-1 under C), w2, w3), p0p1
+        [100], lnfX as codeml prints it, S1, S2, ms_device."""
+        L = np.ascontiguousarray(lnfw, dtype=np.float64)
+        assert L.shape == ((120 if model_d else 111), self.npatt)
+        post = np.zeros((3, self.npatt))
+        grid = np.zeros((4, 10))
+        p0p1 = np.zeros(100)
+        fx = np.zeros(3)
+        st = _lib.Stats()
+        _lib.check(self._L.gb_beb_clade(self._h, int(bool(model_d)), _ptr(L), _ptr(post), _ptr(grid), _ptr(p0p1),
+                                        _ptr(fx), C.byref(st)))
+        return {"post": post, "grid": grid, "p0p1": p0p1, "lnfX": float(fx[0]), "S1": float(fx[1]),
+                "S2": float(fx[2]), "ms_device": st.ms_device}
+
     def beb_clade_c(self, blength, kappa, qfactor) -> dict:
         """codeml's BEB under clade model C with two branch types at the MLE
         (Qfactors qfactor of the two branch types): the 111 omega sets from two
-        gb_beb_tables calls on the device (w0 grid; then the (0, 3) grids of
-        w2 and w3 in eigen slots 0 and 2), the 10^5-point grid integration on
-        the host (beb_clade_integrate)."""
+        gb_beb_tables calls (w0 grid in (0, 1); then the (0, 3) grids of w2 and
+        w3 in eigen slots 0 and 2) and the 10^5-point grid integral, all on the
+        device."""
         g01 = (np.arange(10) + 0.5) / 10
         g03 = 0 + (np.arange(10) + 0.5) * (3 - 0) / 10
         a = self.beb_tables(blength, kappa, qfactor, g01, g03)
         b = self.beb_tables(blength, kappa, qfactor, g03, g03)
-        return beb_clade_integrate(np.concatenate([a[:11], b[11:111]]), self._fpatt)
+        return self.beb_clade(np.concatenate([a[:11], b[11:111]]), model_d=False)
+
+    def beb_clade_d(self, blength, kappa, qfactor) -> dict:
+        """codeml's BEB under clade model D with two branch types at the MLE:
+        120 omega sets (w0 in (0, 0.5), w1 in (0.5, 1.5) on every branch; w2, w3
+        in (0, 3) by branch type; get_grid_para_like_ACD codeml.c:6457-6473)
+        from three gb_beb_tables calls, and the 10^6-point grid integral, on
+        the device."""
+        g = (np.arange(10) + 0.5) / 10
+        a = self.beb_tables(blength, kappa, qfactor, 0.5 * g, 3 * g)
+        b = self.beb_tables(blength, kappa, qfactor, 0.5 + g, 3 * g)
+        c = self.beb_tables(blength, kappa, qfactor, 3 * g, 3 * g)
+        return self.beb_clade(np.concatenate([a[:10], b[:10], c[11:111]]), model_d=True)
 
     def beb_x(self, x, lastround: bool = True, want_lnfw: bool = False) -> dict:
         """beb() from codeml's x vector."""

@@ -254,6 +254,26 @@ int gb_beb_tables(gb_handle *h, const double *blength, double kappa, const doubl
                   gb_stats *stats);
 
 /*
+ * The grid integral of codeml's BEB under the clade models with two branch
+ * types (lfunNSsites_ACD codeml.c:6617-6826, modelACD = mC / mD), on the
+ * device, from host tables lnfw [nsets][npatt] of log f(x_h | w):
+ *   model_d = 0 (clade C): 111 sets -- 0..9 w0 (grid in (0, 1)) on every
+ *     branch, 10 w = 1 on every branch, 11 + 10 i + j w2_i background and
+ *     w3_j foreground (grids in (0, 3)); 10^5 grid points;
+ *   model_d = 1 (clade D): 120 sets -- 0..9 w0 (grid in (0, 0.5)), 10..19 w1
+ *     (grid in (0.5, 1.5)) on every branch, 20 + 10 i + j as above; 10^6
+ *     grid points.
+ * (gb_beb_tables computes such tables with its two eigen slots on these
+ * grids.)  Outputs (each may be NULL): post [3*npatt] site-class posteriors,
+ * grid [4*10] posterior on the w0, w1 (-1 under C), w2 and w3 grids, p0p1
+ * [100] posterior of the (p0, p1) triangles, lnfX [3] = log f(X) as codeml
+ * prints it, S1, S2.  No counterpart in the reference's GPU code (codeml
+ * integrates on one CPU core).
+ */
+int gb_beb_clade(gb_handle *h, int model_d, const double *lnfw, double *post, double *grid, double *p0p1,
+                 double *lnfX, gb_stats *stats);
+
+/*
  * Naive empirical Bayes (NEB) posteriors of the four site classes at prm, as
  * codeml's lfunNSsites_rate prints them ("Naive Empirical Bayes (NEB)
  * probabilities", codeml.c:5079-5129): post[c*npatt + h] = freqK_c f_c(h) /

@@ -99,3 +99,57 @@ def test_clade_d_eval_uvr(name):
     assert np.max(np.abs(g_lnf - lnf)) <= 1e-11
     assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     lk.close()
+
+
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+def test_clade_beb_integral_on_device_matches_oracle(name):
+    """gb_beb_clade, fed the oracle's own log f(x_h | w) tables (111 for clade
+    C, 120 for clade D), against the oracle's grid integration of the same
+    tables: posteriors and grid marginals within 1e-12, log f(X) within 1e-12
+    relative (the device sums patterns in another order)."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    d = name.startswith("mcD")
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=O.max_threads(), model_b=d)
+    ref = pb.beb_clade_d(x) if d else pb.beb_clade(x)
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    r = lk.beb_clade(ref["lnfw"], model_d=d)
+    lk.close()
+    assert np.max(np.abs(r["post"] - ref["post"])) <= 1e-12
+    rows = ref["grid"] if d else ref["grid"][[2, 3, 4]]
+    got = r["grid"] if d else r["grid"][[0, 2, 3]]
+    assert np.max(np.abs(got - rows)) <= 1e-12
+    assert np.max(np.abs(r["p0p1"] - ref["p0p1"])) <= 1e-12
+    assert abs(r["lnfX"] - ref["lnfX"]) <= 1e-12 * abs(ref["lnfX"])
+    if not d:
+        assert np.all(r["grid"][1] == -1.0)
+    print(f"{name}: device grid integral {r['ms_device']:.1f} ms, lnfX {r['lnfX']:.6f}")
+
+
+@pytest.mark.parametrize("name", clade_d_names())
+def test_clade_d_beb(name):
+    """Likelihood.beb_clade_d: the 120 tables from three gb_beb_tables calls
+    and the 10^6-point integral on the device, against codeml's printed
+    clade-D BEB: site posteriors (5 dp), grid and (p0, p1) posteriors (3 dp),
+    log f(X) (6 dp)."""
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    kappa, p0, p1, w0, w1, w2, w3 = x[nb:nb + 7]
+    p2 = 1 - p0 - p1
+    qf = np.array([1.0 / O.build_q(pi, kappa, p0 * w0 + p1 * w1 + p2 * w)[1] for w in (w2, w3)])
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[:nb]
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    r = lk.beb_clade_d(bl, kappa, qf)
+    lk.close()
+    b = fx["beb"]
+    site = r["post"][:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(b["site_post_5dp"]))) <= 5.01e-6
+    for row, key in enumerate(("w0_post_3dp", "w1_post_3dp", "w2_post_3dp", "w3_post_3dp")):
+        assert np.max(np.abs(r["grid"][row] - np.array(b[key]))) <= 5.01e-4
+    assert np.max(np.abs(r["p0p1"] - np.array(b["p0p1_post_3dp"]))) <= 5.01e-4
+    assert abs(r["lnfX"] - b["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])

@@ -95,3 +95,27 @@ def test_m2a_beb(name):
     ms = np.stack([r["wmean"], r["wsd"]])[:, pose].T
     assert np.max(np.abs(ms - np.array(g["site_wmean_sd_3dp"]))) <= 5.01e-4
     lk.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fast"])
+def test_m3_gradient_through_model_b(precision):
+    """M3 with three classes (w0, w1, w2 free on every branch, proportions
+    p0, p1, p2, Qfactor from p0 w0 + p1 w1 + p2 w2) is branch-site model B
+    on the all-foreground tree, so gb_eval_b and its adjoint serve it: lnL
+    against codeml's printed value, and the gradient in codeml's x (branch
+    lengths, kappa, p0, p1, w0, w1, w2) against five-point differences of
+    the oracle's model B on that tree (1e-5)."""
+    name = "msM3k3x8x300_s14"
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, x = as_model_a(fx, tree)
+    nb = t.nbranch
+    lk = api.Likelihood(t, z, fpatt, pi, precision=precision)
+    f, g = lk.dfun_x(x, True)
+    assert abs(-f - fx["codeml_lnL"]) <= (1e-9 * abs(f) if precision == "fp64" else 1e-6) + 5.1e-7
+    pb = O.Problem(t, z, fpatt, pi, nthreads=4, model_b=True)
+    ref = fd_grad(pb, x, True)
+    err = np.abs(g - ref) / np.maximum(1.0, np.abs(ref))
+    print(f"M3 via model B ({precision}): max rel err {err.max():.2e}")
+    assert err.max() <= 1e-5
+    lk.close()

@@ -58,11 +58,10 @@ template <int NS>
 struct USm {
     static constexpr int OFF_B = NS * A_PLANE;
     static constexpr int OFF_MISC = OFF_B + NS * B_PLANE;
-    static constexpr int OFF_RMAX = OFF_MISC + 64;            // float [2][NCG][128]
-    static constexpr int OFF_RSUM = OFF_RMAX + 2 * NCG * 128 * 4;   // double [NCG][128]
-    static constexpr int OFF_ARGS = OFF_RSUM + NCG * 128 * 8;
-    static constexpr int OFF_ITEM = OFF_ARGS + ARGS_BYTES;
-    static constexpr int NEED = OFF_ITEM + ITEM_BYTES;
+    static constexpr int OFF_REXP = OFF_MISC + 64;            // int [128] row exponents of a staged tile
+    static constexpr int OFF_ARGS = OFF_REXP + 128 * 4;
+    static constexpr int OFF_ITEM = OFF_ARGS + 2 * ARGS_BYTES;       // two of each: current and next task
+    static constexpr int NEED = OFF_ITEM + 2 * ITEM_BYTES;
     static constexpr int BYTES = NEED > MIN_SMEM ? NEED : MIN_SMEM;
 };
 
@@ -332,39 +331,48 @@ __device__ __forceinline__ bool slice_contract(const float2 *__restrict__ src, u
 }
 
 
-__device__ __forceinline__ void load_row32(const float2 *p, float2 (&v)[NCOL]) {
+// Staged tile: after a contraction's MMAs have completed, the plane area
+// (free until the next contraction's cut) holds a 128 x 64 double-float tile
+// that the read-out wrote thread-per-row, so that the epilogue can run in the
+// warp-row layout of tip_rows / ebar_rows (warp w rows 8w..8w+7, lane l states
+// 2l, 2l+1): coalesced 512-byte row stores and loads, row maxima by warp
+// shuffles.  Rows are padded to TROW float2 (528 B): the 32 rows a read-out
+// warp writes at once fall in distinct bank groups, and a staged row is read
+// as 512 contiguous bytes.
+constexpr int TROW = 66;
+constexpr int STAGED_BYTES = 128 * TROW * 8;
+
+__device__ __forceinline__ void stage_rows(unsigned char *sm, const float2 (&v)[NCOL]) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4 *d = reinterpret_cast<float4 *>(reinterpret_cast<float2 *>(sm) + (32 * (warp & 3) + lane) * TROW +
+                                           NCOL * (warp >> 2));
 #pragma unroll
-    for (int c = 0; c < NCOL / 2; c++) {
-        const float4 x = __ldcg(reinterpret_cast<const float4 *>(p) + c);
-        v[2 * c] = make_float2(x.x, x.y);
-        v[2 * c + 1] = make_float2(x.z, x.w);
-    }
+    for (int q = 0; q < NCOL / 2; q++) d[q] = make_float4(v[2 * q].x, v[2 * q].y, v[2 * q + 1].x, v[2 * q + 1].y);
 }
 
-__device__ __forceinline__ void store_row32(float2 *p, const float2 (&v)[NCOL]) {
-#pragma unroll
-    for (int c = 0; c < NCOL / 2; c++)
-        reinterpret_cast<float4 *>(p)[c] = make_float4(v[2 * c].x, v[2 * c].y, v[2 * c + 1].x, v[2 * c + 1].y);
+// staged row r: this lane's states 2 lane, 2 lane + 1
+__device__ __forceinline__ float4 staged_row(const unsigned char *sm, int r) {
+    return reinterpret_cast<const float4 *>(reinterpret_cast<const float2 *>(sm) + r * TROW)[threadIdx.x & 31];
 }
 
-// row maximum over the valid states of the NCG threads sharing a row (in
-// NCG warps): one barrier, two alternating buffers (a buffer is rewritten
-// only after the next call's barrier, which every reader of the previous
-// call has passed)
-__device__ __forceinline__ float row_max(const float2 (&v)[NCOL], int col0, float *rmax, int row, int ch,
-                                         int &par) {
-    float m = 0.f;
+__device__ __forceinline__ float4 df_mul4(float4 x, float4 e) {
+    const float2 x0 = df_mul(make_float2(x.x, x.y), make_float2(e.x, e.y));
+    const float2 x1 = df_mul(make_float2(x.z, x.w), make_float2(e.z, e.w));
+    return make_float4(x0.x, x0.y, x1.x, x1.y);
+}
+
+// warp-row: maximum of a row over the valid states (all lanes get it)
+__device__ __forceinline__ float row_max_w(float4 x) {
+    const int lane = threadIdx.x & 31;
+    float m = fmaxf(2 * lane < NC ? x.x : 0.f, 2 * lane + 1 < NC ? x.z : 0.f);
 #pragma unroll
-    for (int c = 0; c < NCOL; c++)
-        if (col0 + c < NC) m = fmaxf(m, v[c].x);
-    float *buf = rmax + par * (NCG * 128);
-    buf[ch * 128 + row] = m;
-    __syncthreads();
-    m = buf[row];
-#pragma unroll
-    for (int g = 1; g < NCG; g++) m = fmaxf(m, buf[g * 128 + row]);
-    par ^= 1;
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     return m;
+}
+
+__device__ __forceinline__ float4 df_scale4(float4 x, int e) {
+    const float2 x0 = df_scale(make_float2(x.x, x.y), e), x1 = df_scale(make_float2(x.z, x.w), e);
+    return make_float4(x0.x, x0.y, x1.x, x1.y);
 }
 
 // ---------------------------------------------------------------- forward
@@ -448,17 +456,18 @@ __device__ __forceinline__ void tip_rows(const FastFwdArgs &a, const Item &it, i
 }
 
 // One (node, class) item on one 128-pattern tile.  Needs TMEM when the item
-// has an internal child.  Returns the block-uniform success flag.
+// has an internal child.  The children's product runs in the warp-row layout
+// (tip_rows): tip children's rows of P gathered row by row, each internal
+// child's contraction read out thread-per-row into the staged tile and taken
+// from there row by row.  Returns the block-uniform success flag.
 template <int NS>
 __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsigned char *sm, Misc *m,
                            uint32_t &phase, unsigned long long *tr = nullptr, int tidx = 0) {
-    float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_RMAX);
-    double *rsum = reinterpret_cast<double *>(sm + USm<NS>::OFF_RSUM);
+    static_assert(STAGED_BYTES <= USm<NS>::OFF_MISC, "staged tile in the plane area");
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ch = warp >> 2;
-    const int row = 32 * (warp & 3) + lane, c0 = NCOL * ch;
     const size_t npad = a.npad;
-    const size_t h0 = (size_t)tile * 128, h = h0 + row;
+    const size_t h0 = (size_t)tile * 128, r0 = h0 + 8 * warp;
+    const size_t hl = r0 + (lane & 7);                 // the row of this lane's scalars
     bool ok = true;
     if (!it.is_root) {
         bool all_tips = true;
@@ -468,22 +477,21 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
             return true;
         }
     }
-    float2 prod[NCOL];
-    int expo = 0;
+    float4 X[8];
     bool have = false;
-    // tip children first: their codons, then their rows of P (a tip's edge
+    int expo = 0;                                      // lanes 0..7: row hl's exponent
+    // tip children first: their rows of P for their codons (a tip's edge
     // message, not stored: the adjoint gathers it again)
-    int zc[MAXC];
+#pragma unroll 1
+    for (int ci = 0; ci < it.nchild; ci++) {
+        if (it.cslot[ci] >= 0) continue;
+        const int zl = a.z[(size_t)it.child[ci] * npad + hl];
+        const float4 *P = reinterpret_cast<const float4 *>(a.Pdf + (size_t)it.pidx[ci] * 4096) + lane;
+        float4 E[8];
 #pragma unroll
-    for (int ci = 0; ci < MAXC; ci++)
-        zc[ci] = (ci < it.nchild && it.cslot[ci] < 0) ? a.z[(size_t)it.child[ci] * npad + h] : 0;
+        for (int j = 0; j < 8; j++) E[j] = __ldg(P + 32 * __shfl_sync(0xffffffffu, zl, j));
 #pragma unroll
-    for (int ci = 0; ci < MAXC; ci++) {
-        if (ci >= it.nchild || it.cslot[ci] >= 0) continue;
-        float2 E[NCOL];
-        load_row32(a.Pdf + (size_t)it.pidx[ci] * 4096 + zc[ci] * 64 + c0, E);
-#pragma unroll
-        for (int c = 0; c < NCOL; c++) prod[c] = have ? df_mul(prod[c], E[c]) : E[c];
+        for (int j = 0; j < 8; j++) X[j] = have ? df_mul4(X[j], E[j]) : E[j];
         have = true;
     }
     trace_put(tr, tidx, TR_P0, umma::global_ns());
@@ -491,8 +499,7 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
     for (int ci = 0; ci < it.nchild && ok; ci++) {
         const int cs = it.cslot[ci];
         if (cs < 0) continue;
-        float2 E[NCOL];
-        __syncthreads();                                   // the previous contraction's planes are free
+        __syncthreads();                  // the previous contraction's planes and staged tile are free
         start_B<NS>(a.Bf + (size_t)it.pidx[ci] * NS * 4096, sm + USm<NS>::OFF_B, &m->mbar_b);
         unsigned long long t_cut = 0;
         ok = slice_contract<NS>(a.conP + ((size_t)cs * npad + h0) * 64, sm, m, phase, USm<NS>::OFF_B, true,
@@ -500,46 +507,61 @@ __device__ bool prune_tile(const FastFwdArgs &a, const Item &it, int tile, unsig
         if (first) trace_put(tr, tidx, TR_SLICED, t_cut);
         if (!ok) break;
         if (first) trace_put(tr, tidx, TR_MMA, umma::global_ns());
-        readout<NS>(m, E, true, 0, 0);
+        {
+            float2 E[NCOL];
+            readout<NS>(m, E, true, 0, 0);
+            stage_rows(sm, E);
+        }
         if (first) trace_put(tr, tidx, TR_READOUT, umma::global_ns());
         first = false;
-        expo += __ldcg(a.expo + (size_t)cs * npad + h);
+        if (lane < 8) expo += __ldcg(a.expo + (size_t)cs * npad + hl);
+        __syncthreads();                                   // the tile is staged
         // edge messages of internal children are kept for the adjoint
-        if (a.E) store_row32(a.E + ((size_t)(it.eslot + ci) * npad + h) * 64 + c0, E);
+        float4 *dE = a.E ? reinterpret_cast<float4 *>(a.E + ((size_t)(it.eslot + ci) * npad + r0) * 64) + lane
+                         : nullptr;
 #pragma unroll
-        for (int c = 0; c < NCOL; c++) prod[c] = have ? df_mul(prod[c], E[c]) : E[c];
+        for (int j = 0; j < 8; j++) {
+            const float4 e = staged_row(sm, 8 * warp + j);
+            if (dE) dE[32 * j] = e;
+            X[j] = have ? df_mul4(X[j], e) : e;
+        }
         have = true;
     }
     if (!ok) {
         on_failure(a.err, m, phase, true);
         return false;
     }
-    int par = 0;
-    const float mx = row_max(prod, c0, rmax, row, ch, par);
-    const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
-    expo += sh;
+    // per row: renormalise by a power of two; store, or at the root sum pi L~
+    int shl = 0;
+    double fl = 0.0;
+    float4 *dst = it.is_root ? nullptr : reinterpret_cast<float4 *>(a.conP + ((size_t)it.slot * npad + r0) * 64) + lane;
+    const double pi0 = 2 * lane < NC ? a.pi[2 * lane] : 0.0, pi1 = 2 * lane + 1 < NC ? a.pi[2 * lane + 1] : 0.0;
 #pragma unroll
-    for (int c = 0; c < NCOL; c++) prod[c] = df_scale(prod[c], -sh);
-    if (!it.is_root) {
-        store_row32(a.conP + ((size_t)it.slot * npad + h) * 64 + c0, prod);
-        if (ch == 0) a.expo[(size_t)it.slot * npad + h] = expo;
-    } else {
-        double f = 0.0;
+    for (int j = 0; j < 8; j++) {
+        const float mx = row_max_w(X[j]);
+        const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
+        const float4 x = df_scale4(X[j], -sh);
+        if (dst) {
+            dst[32 * j] = x;
+        } else {
+            double f = fma(pi1, (double)x.z + (double)x.w, pi0 * ((double)x.x + (double)x.y));
 #pragma unroll
-        for (int c = 0; c < NCOL; c++)
-            if (c0 + c < NC) f = fma(a.pi[c0 + c], (double)prod[c].x + (double)prod[c].y, f);
-        rsum[ch * 128 + row] = f;
-        __syncthreads();
-        if (ch == 0) {
-            f = rsum[row];
-#pragma unroll
-            for (int g = 1; g < NCG; g++) f += rsum[g * 128 + row];
-            if (f <= 0.0) f = 1e-300;
+            for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
+            if ((lane & 7) == j) fl = f;
+        }
+        if ((lane & 7) == j) shl = sh;
+    }
+    if (lane < 8) {
+        expo += shl;
+        if (!it.is_root) {
+            a.expo[(size_t)it.slot * npad + hl] = expo;
+        } else {
+            const double f = fl <= 0.0 ? 1e-300 : fl;
             const double sl = (double)expo * 0.69314718055994530942;
-            a.fbar[(size_t)it.cls * npad + h] = f;
-            a.ssum[(size_t)it.cls * npad + h] = sl;
-            a.fhK[(size_t)it.cls * npad + h] = log(f) + sl;
-            a.expo_root[(size_t)it.cls * npad + h] = expo;
+            a.fbar[(size_t)it.cls * npad + hl] = f;
+            a.ssum[(size_t)it.cls * npad + hl] = sl;
+            a.fhK[(size_t)it.cls * npad + hl] = log(f) + sl;
+            a.expo_root[(size_t)it.cls * npad + hl] = expo;
         }
     }
     return true;
@@ -574,20 +596,25 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
                                                               unsigned *ctl, unsigned long long *trace) {
     extern __shared__ __align__(1024) unsigned char sm[];
     Misc *m = reinterpret_cast<Misc *>(sm + USm<NS>::OFF_MISC);
-    FastFwdArgs *a = reinterpret_cast<FastFwdArgs *>(sm + USm<NS>::OFF_ARGS);
-    Item *it = reinterpret_cast<Item *>(sm + USm<NS>::OFF_ITEM);
     const unsigned epoch = ctl[CTL_EPOCH], awaited = wait_epoch(ctl);
     const uint64_t limit = wait_limit(ctl);
     tmem_setup(m);
     uint32_t phase = 0;
-    for (;;) {
-        const int idx = claim(ctl + CTL_FWD, m);
+    int idx = claim(ctl + CTL_FWD, m);
+    for (int par = 0;; par ^= 1) {
         if (idx >= ntask) break;
+        // the following task is claimed now and taken up after this one (its
+        // index is posted at this task's last barrier); the task's arguments
+        // and item are staged in alternating buffers, so that thread 0 still
+        // reads this task's while the others stage the next
+        unsigned nxt = 0;
+        if (threadIdx.x == 0) nxt = atomicAdd(ctl + CTL_FWD, 1u);
+        FastFwdArgs *a = reinterpret_cast<FastFwdArgs *>(sm + USm<NS>::OFF_ARGS + par * ARGS_BYTES);
+        Item *it = reinterpret_cast<Item *>(sm + USm<NS>::OFF_ITEM + par * ITEM_BYTES);
         trace_put(trace, idx, TR_CLAIM, umma::global_ns());
         const Task t = tasks[idx];
         stage(a, genes + t.gene);
-        __syncthreads();
-        stage(it, a->items + t.item);
+        stage(it, genes[t.gene].items + t.item);
         __syncthreads();
         int good = 1;
         if (threadIdx.x == 0) {
@@ -607,10 +634,12 @@ __global__ void __launch_bounds__(NT, 1) prune_persist_kernel(const FastFwdArgs 
         }
         trace_put(trace, idx, TR_READY, umma::global_ns());
         if (!prune_tile<NS>(*a, *it, t.tile, sm, m, phase, trace, idx)) break;
+        if (threadIdx.x == 0) m->task = (int)nxt;
         __syncthreads();                                   // the tile's rows are written
         trace_put(trace, idx, TR_END, umma::global_ns());
         trace_put(trace, idx, TR_SM, smid());
         if (threadIdx.x == 0 && !it->is_root) set_flag(a->ready + (size_t)it->slot * a->ntile + t.tile, epoch);
+        idx = m->task;
     }
     tmem_teardown(m);
 }
@@ -700,16 +729,14 @@ __device__ __forceinline__ void ebar_rows(const FastBwdArgs &a, const BItem &it,
 template <int NS>
 __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsigned char *sm, Misc *m,
                          uint32_t &phase, unsigned long long *tr = nullptr, int tidx = 0, int only = -1) {
+    static_assert(STAGED_BYTES <= USm<NS>::OFF_MISC, "staged tile in the plane area");
     bool first = true;
-    float *rmax = reinterpret_cast<float *>(sm + USm<NS>::OFF_RMAX);
+    int *rexp = reinterpret_cast<int *>(sm + USm<NS>::OFF_REXP);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int ch = warp >> 2;
-    const int row = 32 * (warp & 3) + lane, c0 = NCOL * ch;
+    const int row = 32 * (warp & 3) + lane;
     const size_t npad = a.npad;
-    const size_t h0 = (size_t)tile * 128, h = h0 + row;
+    const size_t h0 = (size_t)tile * 128, h = h0 + row, r0 = h0 + 8 * warp;
     bool ok = true;
-
-    int par = 0;           // row_max buffer parity
 
     for (int i = 0; i < it.nchild && ok; i++) {
         if (only >= 0 && i != only) continue;
@@ -745,13 +772,30 @@ __device__ bool bwd_tile(const FastBwdArgs &a, const BItem &it, int tile, unsign
                 first = false;
             }
             if (!ok) break;
-            const float mx = row_max(acc, c0, rmax, row, ch, par);
-            const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
-#pragma unroll
-            for (int q = 0; q < NCOL; q++) acc[q] = df_scale(acc[q], -sh);
+            // renormalise and store the child's upper partial in the warp-row
+            // layout, from the staged tile
+            stage_rows(sm, acc);
+            if (warp < 4) rexp[row] = eacc;
+            __syncthreads();
             const int ts = it.tslot[i][tg];
-            store_row32(a.Abar + ((size_t)ts * npad + h) * 64 + c0, acc);
-            if (ch == 0) a.aexp[(size_t)ts * npad + h] = (!(mx > 0.f) || eacc == ZERO_EXP) ? ZERO_EXP : eacc + sh;
+            float4 *dst = reinterpret_cast<float4 *>(a.Abar + ((size_t)ts * npad + r0) * 64) + lane;
+            int shl = 0;
+            float mxl = 0.f;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const float4 x = staged_row(sm, 8 * warp + j);
+                const float mx = row_max_w(x);
+                const int sh = mx > 0.f ? ilogbf(mx) + 1 : 0;
+                dst[32 * j] = df_scale4(x, -sh);
+                if ((lane & 7) == j) {
+                    shl = sh;
+                    mxl = mx;
+                }
+            }
+            if (lane < 8) {
+                const int ea = rexp[8 * warp + lane];
+                a.aexp[(size_t)ts * npad + r0 + lane] = (!(mxl > 0.f) || ea == ZERO_EXP) ? ZERO_EXP : ea + shl;
+            }
         }
     }
     if (!ok) {
@@ -787,20 +831,22 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
                                                             unsigned *ctl, unsigned long long *trace) {
     extern __shared__ __align__(1024) unsigned char sm[];
     Misc *m = reinterpret_cast<Misc *>(sm + USm<NS>::OFF_MISC);
-    FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + USm<NS>::OFF_ARGS);
-    BItem *it = reinterpret_cast<BItem *>(sm + USm<NS>::OFF_ITEM);
     const unsigned epoch = ctl[CTL_EPOCH], awaited = wait_epoch(ctl);
     const uint64_t limit = wait_limit(ctl);
     tmem_setup(m);
     uint32_t phase = 0;
-    for (;;) {
-        const int idx = claim(ctl + CTL_BWD, m);
+    int idx = claim(ctl + CTL_BWD, m);
+    for (int par = 0;; par ^= 1) {
         if (idx >= ntask) break;
+        // claimed ahead, alternating staging buffers: as in prune_persist_kernel
+        unsigned nxt = 0;
+        if (threadIdx.x == 0) nxt = atomicAdd(ctl + CTL_BWD, 1u);
+        FastBwdArgs *a = reinterpret_cast<FastBwdArgs *>(sm + USm<NS>::OFF_ARGS + par * ARGS_BYTES);
+        BItem *it = reinterpret_cast<BItem *>(sm + USm<NS>::OFF_ITEM + par * ITEM_BYTES);
         trace_put(trace, idx, TR_CLAIM, umma::global_ns());
         const Task t = tasks[idx];
         stage(a, genes + t.gene);
-        __syncthreads();
-        stage(it, a->bitems + t.item);
+        stage(it, genes[t.gene].bitems + t.item);
         __syncthreads();
         int good = 1;
         if (threadIdx.x == 0) {
@@ -824,12 +870,13 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
         }
         trace_put(trace, idx, TR_READY, umma::global_ns());
         if (!bwd_tile<NS>(*a, *it, t.tile, sm, m, phase, trace, idx, t.edge)) break;
+        if (threadIdx.x == 0) m->task = (int)nxt;
         __syncthreads();
         trace_put(trace, idx, TR_END, umma::global_ns());
         trace_put(trace, idx, TR_SM, smid());
-        // publish the children's slots that received an upper partial; the
-        // staged item and arguments are not rewritten before the next claim's
-        // barrier, which thread 0 reaches only after this
+        // publish the children's slots that received an upper partial (this
+        // task's item and arguments stay in their buffers until the task after
+        // the next is staged, past barriers that thread 0 reaches after this)
         if (threadIdx.x == 0)
             for (int i = 0; i < it->nchild; i++) {
                 if (it->tslot[i][0] < 0 || (t.edge >= 0 && i != t.edge)) continue;
@@ -837,6 +884,7 @@ __global__ void __launch_bounds__(NT, 1) bwd_persist_kernel(const FastBwdArgs *_
                 if (it->ncls == 2 && it->tslot[i][1] != it->tslot[i][0])
                     set_flag(a->ready + (size_t)it->tslot[i][1] * a->ntile + t.tile, epoch);
             }
+        idx = m->task;
     }
     tmem_teardown(m);
 }

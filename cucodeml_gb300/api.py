@@ -82,6 +82,17 @@ def model_setup(pi, kappa, omega0, omega2, p0, p1):
     return U, V, R, qf, fk
 
 
+def beta_classes(p, q, K: int = 10):
+    """(omegas [K], proportions [K]) of codeml's discretised beta under M7 /
+    M8: K equal-probability categories at their medians (DiscreteNSsites
+    codeml.c:2728-2770), from the library's host code."""
+    L = _lib.load()
+    om = np.zeros(K)
+    pr = np.zeros(K)
+    _lib.check(L.gb_beta_classes(float(p), float(q), int(K), _ptr(om), _ptr(pr)))
+    return om, pr
+
+
 @dataclass
 class EvalResult:
     neg_lnL: float
@@ -116,6 +127,8 @@ class Likelihood:
             self._scale = np.ascontiguousarray(node_scale, dtype=np.int8).tobytes()
         prec = precision if isinstance(precision, int) else \
             {"fp64": _lib.GB_PREC_FP64, "fast": _lib.GB_PREC_FAST}[precision]
+        self._fp64 = prec == _lib.GB_PREC_FP64
+        self.last_ms = 0.0
         ip = C.POINTER(C.c_int)
         self._prob = _lib.Problem(self.ns, self.nnode, tree.root, self._father.ctypes.data_as(ip),
                                   self._label.ctypes.data_as(ip), self.npatt,
@@ -168,6 +181,19 @@ class Likelihood:
                                        _ptr(lnf) if want_site else None, C.byref(st)))
         return EvalResult(f.value, fhK, lnf, None, st.ms_device, st.ms_host, st.kernels)
 
+    def m7(self, blength, kappa, p, q, K: int = 10):
+        """Site model M7 (beta, K categories) on a tree with every branch
+        labelled foreground: (-lnL, fhK [K, npatt], lnf)."""
+        om, pr = beta_classes(p, q, K)
+        return self.site_model(blength, kappa, om, pr)
+
+    def m8(self, blength, kappa, p0, p, q, ws, K: int = 10):
+        """Site model M8 (beta with weight p0, K categories, and omega_s with
+        1 - p0) on a tree with every branch labelled foreground: (-lnL, fhK
+        [K + 1, npatt], lnf)."""
+        om, pr = beta_classes(p, q, K)
+        return self.site_model(blength, kappa, np.append(om, ws), np.append(pr * p0, 1 - p0))
+
     def site_model(self, blength, kappa, omegas, props):
         """A site model with K classes (codeml model = 0: M1a, M2a, M3, M7,
         M8, ...): class k has omegas[k] on every branch and weight props[k],
@@ -205,18 +231,39 @@ class Likelihood:
             lnf = np.log(np.where(sm <= 0, 1e-300, sm))
         return -float((lnf * self._fpatt).sum()), fhK, lnf
 
-    def clade_uvr(self, U, V, Root, qfactor, freqK, blength):
+    def clade_uvr(self, U, V, Root, qfactor, freqK, blength, two_calls: bool = False):
         """Clade models C / D with two branch types from the host's eigen
         solutions of (w0, w1, w2 background, w3 foreground) -- codeml's
-        _UU/_VV/_Root[0..3] and Qfactor_NS_branch.  Classes 0 and 1 are model
-        A's with slots (w0, w1, -), the third is model A's class 2a with
-        slots (w2, w1, w3): two gb_eval_uvr calls, then codeml's mixture of
-        the three classes (lfundG treesub.c:7342-7394).  Returns
-        (-lnL, fhK [3, npatt], lnf)."""
+        _UU/_VV/_Root[0..3] and Qfactor_NS_branch -- and the three class
+        weights.  FP64 handles: one gb_eval_clade_uvr call (three classes at
+        every internal node).  Split-precision handles, or two_calls: two
+        gb_eval_uvr calls (classes 0 and 1 are model A's with slots (w0, w1,
+        -), the third is model A's class 2a with slots (w2, w1, w3)), then
+        codeml's mixture of the three classes (lfundG treesub.c:7342-7394).
+        Returns (-lnL, fhK [3, npatt], lnf) and keeps the call's device time
+        in self.last_ms."""
+        if self._fp64 and not two_calls:
+            arr4 = _dp * 4
+            U = [np.ascontiguousarray(u, dtype=np.float64) for u in U]
+            V = [np.ascontiguousarray(v, dtype=np.float64) for v in V]
+            R = [np.ascontiguousarray(r, dtype=np.float64) for r in Root]
+            qf = np.ascontiguousarray(qfactor, dtype=np.float64)
+            fk = np.ascontiguousarray(np.asarray(freqK, dtype=np.float64)[:3])
+            bl = np.ascontiguousarray(blength, dtype=np.float64)
+            f = C.c_double(0)
+            fhK = np.zeros((3, self.npatt))
+            lnf = np.zeros(self.npatt)
+            st = _lib.Stats()
+            _lib.check(self._L.gb_eval_clade_uvr(self._h, arr4(*[_ptr(u) for u in U]), arr4(*[_ptr(v) for v in V]),
+                                                 arr4(*[_ptr(r) for r in R]), _ptr(qf), _ptr(fk), _ptr(bl),
+                                                 C.byref(f), _ptr(fhK), _ptr(lnf), C.byref(st)))
+            self.last_ms = st.ms_device
+            return f.value, fhK, lnf
         fk4 = np.full(4, 0.25)           # the calls' own mixture is not used
         a = self.neg_lnL_uvr(U[:3], V[:3], Root[:3], qfactor, fk4, blength)
         b = self.neg_lnL_uvr([U[2], U[1], U[3]], [V[2], V[1], V[3]], [Root[2], Root[1], Root[3]],
                              qfactor, fk4, blength)
+        self.last_ms = a.ms_device + b.ms_device
         fhK = np.stack([a.fhK[0], a.fhK[1], b.fhK[2]])
         fk = np.asarray(freqK, dtype=np.float64)[:3]
         if self.nscale:

@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libgbcodeml.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["runtime.cu", "batch.cu", "k_fp64.cu", "adjoint.cu", "fast.cu", "k_fast.cu", "k_fast_bwd.cu", "k_umma.cu", "noalloc.cu", "beb.cu", "beb_clade.cu", "se.cu", "model.cpp", "patterns.cpp", "ng86.cpp"]
+SOURCES = ["runtime.cu", "batch.cu", "k_fp64.cu", "adjoint.cu", "fast.cu", "k_fast.cu", "k_fast_bwd.cu", "k_umma.cu", "noalloc.cu", "beb.cu", "beb_clade.cu", "clade.cu", "se.cu", "model.cpp", "patterns.cpp", "ng86.cpp", "betaw.cpp"]
 
 
 def nvcc() -> str:

@@ -23,7 +23,6 @@ extern double Small_Diff;
 
 static gb_handle *g_h = NULL;
 static double *g_fhK = NULL;      /* [4*npatt] all classes of the current evaluation */
-static double *g_fhK2 = NULL;     /* [4*npatt] clade models: the evaluation whose class 2a is their class 2 */
 static double *g_blen = NULL;     /* [nnode] */
 static int *g_bnode = NULL;       /* [nbranch] node of x[ib] */
 
@@ -92,15 +91,13 @@ void CUDA_Init(double *x) {
     g_blen = (double *)malloc(sizeof(double) * tree.nnode);
     g_bnode = (int *)malloc(sizeof(int) * tree.nnode);
     g_fhK = (double *)malloc(sizeof(double) * 4 * com.npatt);
-    g_fhK2 = (double *)malloc(sizeof(double) * 4 * com.npatt);
-    if (!g_blen || !g_bnode || !g_fhK || !g_fhK2) gb_die("CUDA_Init (host memory)", GB_ERR_OOM);
+    if (!g_blen || !g_bnode || !g_fhK) gb_die("CUDA_Init (host memory)", GB_ERR_OOM);
     for (i = 0; i < tree.nnode; i++)
         if (i != tree.root) g_bnode[nodes[i].ibranch] = i;
     g_h = make_handle("CUDA_Init (one gene, universal code only)");
 }
 
 void CUDA_ScheduleConditionalPNode(int ir, int ig, double *x) {
-    static const double fk4[4] = {0.25, 0.25, 0.25, 0.25};
     int i, rc;
     const int clade = com.model == 3;    /* clade models C / D (NSbranch3) */
     (void)x;
@@ -108,31 +105,30 @@ void CUDA_ScheduleConditionalPNode(int ir, int ig, double *x) {
         if (clade && (com.nbtype != 2 || com.ncatG != 3)) gb_die("clade model (two branch types only)", GB_ERR_ARG);
         for (i = 0; i < tree.nnode; i++)
             g_blen[i] = (i == tree.root) ? 0 : nodes[i].branch * com.rgene[ig];
-        rc = gb_eval_uvr(g_h, (const double *const *)_UU, (const double *const *)_VV,
-                         (const double *const *)_Root, Qfactor_NS_branch, clade ? fk4 : com.freqK, g_blen,
-                         NULL, g_fhK, NULL, NULL);
-        if (rc) gb_die("gb_eval_uvr", rc);
         if (clade) {
-            /* class 2 (w2 background, w3 foreground, Set_UVR_BranchSite codeml.c:2561-2563)
-               is model A's class 2a with slots (w2, w1, w3) */
-            const double *U2[3] = {_UU[2], _UU[1], _UU[3]}, *V2[3] = {_VV[2], _VV[1], _VV[3]};
-            const double *R2[3] = {_Root[2], _Root[1], _Root[3]};
-            rc = gb_eval_uvr(g_h, U2, V2, R2, Qfactor_NS_branch, fk4, g_blen, NULL, g_fhK2, NULL, NULL);
+            /* three classes, four eigen solutions: class 2 takes w2 on branch
+               type 0 and w3 on type 1 (Set_UVR_BranchSite codeml.c:2561-2563) */
+            rc = gb_eval_clade_uvr(g_h, (const double *const *)_UU, (const double *const *)_VV,
+                                   (const double *const *)_Root, Qfactor_NS_branch, com.freqK, g_blen, NULL, g_fhK,
+                                   NULL, NULL);
+            if (rc) gb_die("gb_eval_clade_uvr", rc);
+        } else {
+            rc = gb_eval_uvr(g_h, (const double *const *)_UU, (const double *const *)_VV,
+                             (const double *const *)_Root, Qfactor_NS_branch, com.freqK, g_blen, NULL, g_fhK,
+                             NULL, NULL);
             if (rc) gb_die("gb_eval_uvr", rc);
         }
     }
-    memcpy(com.fhK + (size_t)ir * com.npatt, (clade && ir == 2 ? g_fhK2 : g_fhK) + (size_t)ir * com.npatt,
-           sizeof(double) * com.npatt);
+    memcpy(com.fhK + (size_t)ir * com.npatt, g_fhK + (size_t)ir * com.npatt, sizeof(double) * com.npatt);
 }
 
 void CUDA_FreeAll(void) {
     if (g_h) gb_destroy(g_h);
     g_h = NULL;
     free(g_fhK);
-    free(g_fhK2);
     free(g_blen);
     free(g_bnode);
-    g_fhK = g_fhK2 = g_blen = NULL;
+    g_fhK = g_blen = NULL;
     g_bnode = NULL;
 }
 

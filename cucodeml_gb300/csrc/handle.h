@@ -15,6 +15,7 @@
 namespace gb {
 
 struct AdjointState;
+struct CladeState;
 struct FastState;
 struct PersistPlan;
 
@@ -52,6 +53,7 @@ struct ProfRec {
 };
 void prof_mark(gb_handle *h, int cls);
 void adjoint_free(AdjointState *a);
+void clade_free(CladeState *c);
 int fast_eval(gb_handle *h, const Derived *D, const double *blength, double *neg_lnL, gb_grad *grad,
               double *fhK, double *lnf, gb_stats *stats);
 int fast_replay(gb_handle *h, int iters, int with_grad, double *ms);
@@ -118,6 +120,7 @@ struct gb_handle {
 
     gb::AdjointState *adj = nullptr;
     gb::FastState *fast = nullptr;
+    gb::CladeState *clade = nullptr;    // clade models C / D in one evaluation (clade.cu)
     int kernels_last = 0;
     gb::ProfRec *prof = nullptr;
 };

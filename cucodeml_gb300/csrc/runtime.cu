@@ -199,6 +199,7 @@ void free_all(gb_handle *h) {
     if (h->stream) cudaStreamDestroy(h->stream);
     adjoint_free(h->adj);
     fast_free(h->fast);
+    clade_free(h->clade);
     delete h;
 }
 

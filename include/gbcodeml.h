@@ -178,6 +178,24 @@ int gb_eval_uvr(gb_handle *h, const double *const U[3], const double *const V[3]
                 gb_stats *stats);
 
 /*
+ * Clade models C and D with two branch types (codeml model = 3, NSsites = 2
+ * or 3, ncatG = 3) in one evaluation: the eigen solutions of w0, w1, w2
+ * (branch type 0's third class) and w3 (branch type 1's) as codeml's
+ * _UU/_VV/_Root[0..3], the two branch types' Qfactors and the three class
+ * weights (SetParametersNSsites codeml.c:2437-2446, 2522-2539;
+ * Set_UVR_BranchSite codeml.c:2545-2568).  Branch labels 0 / 1 of gb_problem
+ * are the branch types.  fhK (may be NULL) receives codeml's fhK of the three
+ * classes [3][npatt]; -lnL is codeml's mixture of them (lfundG).  Replaces the
+ * clade route of CUDA_ScheduleConditionalPNode (CUDA_fx_r treesub.c:7554-7595
+ * with com.model = 3).  FP64 handles; the first call builds the three-class
+ * schedule (its own conditional likelihoods and transition matrices).
+ */
+int gb_eval_clade_uvr(gb_handle *h, const double *const U[4], const double *const V[4],
+                      const double *const Root[4], const double qfactor[2], const double freqK[3],
+                      const double *blength, double *neg_lnL, double *fhK, double *lnf,
+                      gb_stats *stats);
+
+/*
  * Evaluate -lnL from natural parameters; if grad != NULL also the analytic
  * gradient of -lnL (adjoint sweep).  fhK / lnf / stats may be NULL.
  */
@@ -457,6 +475,13 @@ int gb_batch_task_trace(gb_batch *b, int kernel, unsigned long long *out, int ca
  * (cuda-codeml.cu:20-39).
  */
 int gb_fault_inject(gb_handle *h, int wait_ms, int withhold);
+
+/* Site models M7 (beta) and M8 (beta & omega_s): codeml's discretised
+   beta, K equal-probability categories at their medians, omegas[j] =
+   QuantileBeta((2j + 1) / (2K), p, q), props[j] = 1 / K (DiscreteNSsites
+   codeml.c:2728-2770; M8 then scales props by p0 and adds omega_s with
+   1 - p0).  Host only. */
+int gb_beta_classes(double p, double q, int K, double *omegas, double *props);
 
 /*
  * Host-only model set-up (no GPU needed): for codon frequencies pi[61] and

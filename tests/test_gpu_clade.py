@@ -153,3 +153,71 @@ def test_clade_d_beb(name):
         assert np.max(np.abs(r["grid"][row] - np.array(b[key]))) <= 5.01e-4
     assert np.max(np.abs(r["p0p1"] - np.array(b["p0p1_post_3dp"]))) <= 5.01e-4
     assert abs(r["lnfX"] - b["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(r["lnfX"])
+
+
+def _clade_inputs(pb, x, nb, model_d):
+    """codeml's four eigen solutions (w0, w1, w2, w3), Qfactors and class
+    weights of clade model C (model_d False: w1 = 1) or D at x."""
+    if model_d:
+        kappa, p0, p1, w0, w1, w2, w3 = x[nb:nb + 7]
+        head = [kappa, p0, p1, w0, w1]
+    else:
+        kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+        w1 = 1.0
+        head = [kappa, p0, p1, w0]
+    p2 = 1 - p0 - p1
+    Ua, Va, Ra, _, _ = pb.set_params(np.concatenate([x[:nb], head, [w2]]))
+    U3, V3, R3, _, _ = pb.set_params(np.concatenate([x[:nb], head, [w3]]))
+    qf = np.array([1.0 / O.build_q(pb.pi, kappa, p0 * w0 + p1 * w1 + p2 * w)[1] for w in (w2, w3)])
+    return ([Ua[0], Ua[1], Ua[2], U3[2]], [Va[0], Va[1], Va[2], V3[2]], [Ra[0], Ra[1], Ra[2], R3[2]], qf,
+            [p0, p1, p2])
+
+
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+def test_clade_one_evaluation_matches_two_calls(name):
+    """gb_eval_clade_uvr (three classes at every internal node, four eigen
+    solutions, one graph) against the composition of two gb_eval_uvr calls:
+    the same FP64 kernels on the same matrices, so fhK agrees to rounding of
+    the mixture (1e-13) and -lnL to 1e-12 relative."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=2, model_b=name.startswith("mcD"))
+    U, V, R, qf, fk = _clade_inputs(pb, x, nb, name.startswith("mcD"))
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[:nb]
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    f1, fhK1, lnf1 = lk.clade_uvr(U, V, R, qf, fk, bl)
+    f2, fhK2, lnf2 = lk.clade_uvr(U, V, R, qf, fk, bl, two_calls=True)
+    f1b, fhK1b, _ = lk.clade_uvr(U, V, R, qf, fk, bl)        # the graph replayed
+    lk.close()
+    assert np.max(np.abs(fhK1 - fhK2)) <= 1e-13 * np.max(np.abs(fhK2))
+    assert np.max(np.abs(lnf1 - lnf2)) <= 1e-13 * np.max(np.abs(lnf2))
+    assert abs(f1 - f2) <= 1e-12 * abs(f2)
+    assert f1b == f1 and np.array_equal(fhK1b, fhK1)
+    assert abs(-f1 - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+
+
+def test_clade_one_evaluation_time():
+    """64 taxa x 2000 codons with a foreground clade: one clade evaluation
+    against the two model-A-shaped calls it replaces (times printed; the
+    single evaluation prunes 3 classes per internal node where the pair
+    prunes 2 + 2 at every node and 2 more at the clade's nodes twice)."""
+    from cucodeml_gb300.simulate import simulate
+    a = simulate(64, 2000, seed=2024)
+    z, fpatt, pi = api.patterns(a.codons)
+    nb = a.tree.nbranch
+    pb = O.Problem(a.tree, z, fpatt, pi, nthreads=2)
+    x = np.concatenate([a.tree.branch[a.tree.branch_nodes()], [2.0, 0.5, 0.3, 0.3, 2.5, 4.0]])
+    U, V, R, qf, fk = _clade_inputs(pb, x, nb, False)
+    lk = api.Likelihood(a.tree, z, fpatt, pi)
+    t1, t2 = [], []
+    for _ in range(5):
+        f1, _, _ = lk.clade_uvr(U, V, R, qf, fk, a.tree.branch)
+        t1.append(lk.last_ms)
+        f2, _, _ = lk.clade_uvr(U, V, R, qf, fk, a.tree.branch, two_calls=True)
+        t2.append(lk.last_ms)
+    lk.close()
+    assert abs(f1 - f2) <= 1e-12 * abs(f2)
+    print(f"clade C 64x2000 ({len(fpatt)} patterns): one evaluation {min(t1):.2f} ms, two calls {min(t2):.2f} ms")

@@ -23,7 +23,9 @@ pytestmark = pytest.mark.gpu
 def test_site_model_classes(name):
     """Likelihood.site_model: K whole-tree classes, three per gb_eval_uvr
     call, eigen solutions from the library; every site model including M7
-    and M8 (ten beta categories) against codeml's printed lnL and log f."""
+    and M8 (ten beta categories) against codeml's printed lnL and log f, and
+    for M7 / M8 Likelihood.m7 / m8 (the library's discretised beta) against
+    the same classes from the oracle's quantiles."""
     from tests.conftest import site_model_classes
     fx, tree, codons = load_golden(name)
     z, fpatt, pi = O.patterns(codons)
@@ -35,6 +37,10 @@ def test_site_model_classes(name):
     bl[t.branch_nodes()] = x[:nb]
     lk = api.Likelihood(t, z, fpatt, pi)
     f, fhK, lnf = lk.site_model(bl, x[nb], om, pr)
+    if fx["model"] in ("M7", "M8"):          # the library's own discretised beta
+        g = lk.m7(bl, x[nb], *x[nb + 1:nb + 3]) if fx["model"] == "M7" else lk.m8(bl, x[nb], *x[nb + 1:nb + 5])
+        assert abs(g[0] - f) <= 1e-11 * abs(f)
+        assert np.max(np.abs(g[2] - lnf)) <= 1e-11
     assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     ref = np.array(fx["lnf"])
     assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))

@@ -109,3 +109,30 @@ def test_create_without_gpu_fails_loudly():
     with pytest.raises(_lib.GBError) as e:
         api.Likelihood(tree, z, fpatt, pi)
     assert e.value.code in (-7, -2)
+
+
+def test_beta_classes_match_the_inverse_incomplete_beta():
+    """gb_beta_classes (M7 / M8's discretised beta, DiscreteNSsites
+    codeml.c:2728-2770) against the oracle's scipy-based quantiles over the
+    range codeml allows for p and q (0.005 .. 99): 3e-11 relative (the
+    extreme corners reach quantiles of 1e-263; 1e-12 inside [0.05, 99])."""
+    from cucodeml_gb300 import api
+    from oracle import oracle as O
+    grid = [0.005, 0.01, 0.05, 0.1, 0.3, 0.5, 0.9, 1.0, 1.5, 2.0, 5.0, 20.0, 99.0]
+    for p in grid:
+        for q in grid:
+            om, pr = api.beta_classes(p, q)
+            ref, rpr = O.beta_classes(p, q)
+            tol = 1e-12 if min(p, q) >= 0.05 else 3e-11
+            assert np.all(np.abs(om - ref) <= tol * ref), (p, q)
+            assert np.all(pr == rpr)
+            assert np.all(np.diff(om) >= -4 * np.finfo(float).eps)        # ascending, to rounding near 1
+
+
+def test_beta_classes_reject_bad_parameters():
+    from cucodeml_gb300 import _lib, api
+    for p, q in ((0.0, 1.0), (1.0, -2.0), (float("nan"), 1.0), (1.0, float("inf"))):
+        with pytest.raises(Exception):
+            api.beta_classes(p, q)
+    L = _lib.load()
+    assert L.gb_beta_classes(1.0, 1.0, 0, None, None) == -1          # GB_ERR_ARG

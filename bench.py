@@ -120,7 +120,7 @@ def make_workload(ns: int, ncodon: int, seed: int = 2024):
 # kernels from one ncu capture at 32 taxa x 2000 codons (1974 patterns, 62
 # contractions, 910811496 contraction FLOPs), profiles/fast_kernels_32x2000.md;
 # scaled to another workload by its contraction FLOPs
-NCU_TRAFFIC_SMALL = {"prune": 27.39e6 + 70.80e6, "bwd": 85.18e6 + 136.97e6, "gradP": 193.28e6 + 10.13e6}
+NCU_TRAFFIC_SMALL = {"prune": 29.09e6 + 68.11e6, "bwd": 87.62e6 + 137.58e6, "gradP": 193.19e6 + 10.66e6}
 NCU_FLOPS_SMALL = 910811496.0
 
 

@@ -181,6 +181,22 @@ class Likelihood:
                                        _ptr(lnf) if want_site else None, C.byref(st)))
         return EvalResult(f.value, fhK, lnf, None, st.ms_device, st.ms_host, st.kernels)
 
+    def clade(self, blength, kappa, p0, p1, w0, w2, w3, w1: float = 1.0):
+        """Clade model C (w1 = 1) or D (w1 free) with two branch types from
+        its parameters (gb_eval_clade: the library's eigen solutions and
+        Qfactors; w2 on branch type 0, w3 on type 1).  FP64 handles.
+        Returns (-lnL, fhK [3, npatt], lnf)."""
+        bl = np.ascontiguousarray(blength, dtype=np.float64)
+        om = np.ascontiguousarray([w0, w1, w2, w3], dtype=np.float64)
+        f = C.c_double(0)
+        fhK = np.zeros((3, self.npatt))
+        lnf = np.zeros(self.npatt)
+        st = _lib.Stats()
+        _lib.check(self._L.gb_eval_clade(self._h, _ptr(bl), float(kappa), float(p0), float(p1), _ptr(om),
+                                         C.byref(f), _ptr(fhK), _ptr(lnf), C.byref(st)))
+        self.last_ms = st.ms_device
+        return f.value, fhK, lnf
+
     def m7(self, blength, kappa, p, q, K: int = 10):
         """Site model M7 (beta, K categories) on a tree with every branch
         labelled foreground: (-lnL, fhK [K, npatt], lnf)."""

@@ -187,15 +187,12 @@ int clade_init(gb_handle *h) {
 
 using namespace gb;
 
-extern "C" int gb_eval_clade_uvr(gb_handle *h, const double *const U[4], const double *const V[4],
-                                 const double *const Root[4], const double qfactor[2], const double freqK[3],
-                                 const double *blength, double *neg_lnL, double *fhK, double *lnf,
-                                 gb_stats *stats) {
-    if (!h) return fail(GB_ERR_STATE, "null handle");
-    if (!U || !V || !Root || !qfactor || !freqK || !blength) return fail(GB_ERR_ARG, "null argument");
-    for (int i = 0; i < 4; i++)
-        if (!U[i] || !V[i] || !Root[i]) return fail(GB_ERR_ARG, "null U/V/Root");
-    if (h->precision != GB_PREC_FP64) return fail(GB_ERR_ARG, "gb_eval_clade_uvr: FP64 handles only");
+namespace {
+// one evaluation from the four eigen solutions (host arrays), Qfactors, class weights
+int eval_clade(gb_handle *h, const double *const U[4], const double *const V[4], const double *const Root[4],
+               const double qfactor[2], const double freqK[3], const double *blength, double *neg_lnL, double *fhK,
+               double *lnf, gb_stats *stats) {
+    if (h->precision != GB_PREC_FP64) return fail(GB_ERR_ARG, "clade models: FP64 handles only");
     CK(cudaSetDevice(h->device));
     const double t0 = now_ms();
     for (int n = 0; n < h->nnode; n++) {
@@ -246,4 +243,50 @@ extern "C" int gb_eval_clade_uvr(gb_handle *h, const double *const U[4], const d
         stats->d2h_bytes = sizeof(double) * (1 + (fhK ? 3 * h->npatt : 0) + (lnf ? h->npatt : 0));
     }
     return GB_OK;
+}
+}  // namespace
+
+extern "C" int gb_eval_clade_uvr(gb_handle *h, const double *const U[4], const double *const V[4],
+                                 const double *const Root[4], const double qfactor[2], const double freqK[3],
+                                 const double *blength, double *neg_lnL, double *fhK, double *lnf,
+                                 gb_stats *stats) {
+    if (!h) return fail(GB_ERR_STATE, "null handle");
+    if (!U || !V || !Root || !qfactor || !freqK || !blength) return fail(GB_ERR_ARG, "null argument");
+    for (int i = 0; i < 4; i++)
+        if (!U[i] || !V[i] || !Root[i]) return fail(GB_ERR_ARG, "null U/V/Root");
+    return eval_clade(h, U, V, Root, qfactor, freqK, blength, neg_lnL, fhK, lnf, stats);
+}
+
+// Clade models C / D from their parameters (SetParametersNSsites
+// codeml.c:2522-2539): branch type b's Qfactor is 1 / meanrate(Q(kappa,
+// p0 w0 + p1 w1 + p2 w_{2+b})) and the eigen solutions are those of Q(kappa,
+// w) for w0, w1, w2, w3, from the library's host code.
+extern "C" int gb_eval_clade(gb_handle *h, const double *blength, double kappa, double p0, double p1,
+                             const double omega[4], double *neg_lnL, double *fhK, double *lnf, gb_stats *stats) {
+    if (!h) return fail(GB_ERR_STATE, "null handle");
+    if (!blength || !omega) return fail(GB_ERR_ARG, "null argument");
+    const double p2 = 1.0 - p0 - p1;
+    if (!(kappa > 0.0) || !(p0 >= 0.0) || !(p1 >= 0.0) || !(p2 >= -1e-12) || !std::isfinite(kappa))
+        return fail(GB_ERR_PARAM, "clade model parameters out of range");
+    for (int i = 0; i < 4; i++)
+        if (!(omega[i] >= 0.0) || !std::isfinite(omega[i])) return fail(GB_ERR_PARAM, "omega out of range");
+    const double *pi = h->pi.data();
+    std::vector<double> buf((size_t)4 * (2 * 61 * 61 + 61));
+    double *U[4], *V[4], *R[4];
+    for (int i = 0; i < 4; i++) {
+        U[i] = buf.data() + (size_t)i * (2 * 61 * 61 + 61);
+        V[i] = U[i] + 61 * 61;
+        R[i] = V[i] + 61 * 61;
+        std::vector<double> Q(61 * 61);
+        build_q(pi, kappa, omega[i], Q.data(), nullptr, nullptr);
+        if (eigen_qrev(Q.data(), pi, U[i], V[i], R[i])) return fail(GB_ERR_PARAM, "eigen solution failed");
+    }
+    const double fk[3] = {p0, p1, p2 > 0.0 ? p2 : 0.0};
+    double qf[2];
+    for (int b = 0; b < 2; b++) {
+        std::vector<double> Q(61 * 61);
+        qf[b] = 1.0 / build_q(pi, kappa, p0 * omega[0] + p1 * omega[1] + fk[2] * omega[2 + b], Q.data(), nullptr,
+                              nullptr);
+    }
+    return eval_clade(h, U, V, R, qf, fk, blength, neg_lnL, fhK, lnf, stats);
 }

@@ -195,6 +195,14 @@ int gb_eval_clade_uvr(gb_handle *h, const double *const U[4], const double *cons
                       const double *blength, double *neg_lnL, double *fhK, double *lnf,
                       gb_stats *stats);
 
+/* gb_eval_clade_uvr from the clade model's parameters, set up by the
+   library: kappa, the class weights p0, p1 (p2 = 1 - p0 - p1) and omega[4] =
+   (w0, w1, w2, w3) -- w1 = 1 under clade model C, free under D; w2 is the
+   third class's omega on branch type 0, w3 on branch type 1 (codeml.c:
+   2522-2539).  blength in node order.  FP64 handles. */
+int gb_eval_clade(gb_handle *h, const double *blength, double kappa, double p0, double p1,
+                  const double omega[4], double *neg_lnL, double *fhK, double *lnf, gb_stats *stats);
+
 /*
  * Evaluate -lnL from natural parameters; if grad != NULL also the analytic
  * gradient of -lnL (adjoint sweep).  fhK / lnf / stats may be NULL.

@@ -221,3 +221,35 @@ def test_clade_one_evaluation_time():
     lk.close()
     assert abs(f1 - f2) <= 1e-12 * abs(f2)
     print(f"clade C 64x2000 ({len(fpatt)} patterns): one evaluation {min(t1):.2f} ms, two calls {min(t2):.2f} ms")
+
+
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+def test_clade_own_setup_matches_codeml(name):
+    """gb_eval_clade: the clade model from its parameters with the library's
+    eigen solutions and Qfactors, against codeml's printed lnL and log f and
+    against the same evaluation from the oracle's eigen solutions (the two
+    eigensolvers agree to rounding: 1e-11 relative in lnL)."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    d = name.startswith("mcD")
+    if d:
+        kappa, p0, p1, w0, w1, w2, w3 = x[nb:nb + 7]
+    else:
+        kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+        w1 = 1.0
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[:nb]
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=2, model_b=d)
+    U, V, R, qf, fk = _clade_inputs(pb, x, nb, d)
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    f, fhK, lnf = lk.clade(bl, kappa, p0, p1, w0, w2, w3, w1=w1)
+    f2, _, _ = lk.clade_uvr(U, V, R, qf, fk, bl)
+    with pytest.raises(Exception):
+        lk.clade(bl, kappa, 0.7, 0.6, w0, w2, w3)              # p0 + p1 > 1
+    lk.close()
+    assert abs(f - f2) <= 1e-11 * abs(f2)
+    assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+    ref = np.array(fx["lnf"])
+    assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))

@@ -67,8 +67,9 @@ SIGNATURES = {
     "gb_eval_uvr": (C.c_int, [C.c_void_p, _dp * 3, _dp * 3, _dp * 3, _dp, _dp, _dp, _dp, _dp, _dp,
                               C.POINTER(Stats)]),
     "gb_beta_classes": (C.c_int, [C.c_double, C.c_double, C.c_int, _dp, _dp]),
-    "gb_eval_clade": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, _dp,
+    "gb_eval_clade": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp,
                                 C.POINTER(Stats)]),
+    "gb_dfun_clade_x": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_int, _dp, C.c_int, _dp, _dp]),
     "gb_eval_clade_uvr": (C.c_int, [C.c_void_p, _dp * 4, _dp * 4, _dp * 4, _dp, _dp, _dp, _dp, _dp, _dp,
                                     C.POINTER(Stats)]),
     "gb_eval": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, C.POINTER(Grad), _dp, _dp,

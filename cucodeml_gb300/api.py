@@ -181,21 +181,40 @@ class Likelihood:
                                        _ptr(lnf) if want_site else None, C.byref(st)))
         return EvalResult(f.value, fhK, lnf, None, st.ms_device, st.ms_host, st.kernels)
 
-    def clade(self, blength, kappa, p0, p1, w0, w2, w3, w1: float = 1.0):
+    def clade(self, blength, kappa, p0, p1, w0, w2, w3, w1: float = 1.0, grad: bool = False):
         """Clade model C (w1 = 1) or D (w1 free) with two branch types from
         its parameters (gb_eval_clade: the library's eigen solutions and
         Qfactors; w2 on branch type 0, w3 on type 1).  FP64 handles.
-        Returns (-lnL, fhK [3, npatt], lnf)."""
+        Returns (-lnL, fhK [3, npatt], lnf), with grad a fourth item: the
+        gradient of -lnL as a dict (blength in node order, kappa, p0, p1, w0,
+        w1, w2, w3)."""
         bl = np.ascontiguousarray(blength, dtype=np.float64)
         om = np.ascontiguousarray([w0, w1, w2, w3], dtype=np.float64)
         f = C.c_double(0)
         fhK = np.zeros((3, self.npatt))
         lnf = np.zeros(self.npatt)
+        g = np.zeros(self.nnode + 7) if grad else None
         st = _lib.Stats()
         _lib.check(self._L.gb_eval_clade(self._h, _ptr(bl), float(kappa), float(p0), float(p1), _ptr(om),
-                                         C.byref(f), _ptr(fhK), _ptr(lnf), C.byref(st)))
+                                         C.byref(f), _ptr(g) if grad else None, _ptr(fhK), _ptr(lnf), C.byref(st)))
         self.last_ms = st.ms_device
-        return f.value, fhK, lnf
+        if not grad:
+            return f.value, fhK, lnf
+        nn = self.nnode
+        names = ("kappa", "p0", "p1", "omega0", "omega1", "omega2", "omega3")
+        gd = {"blength": g[:nn].copy(), **{k: float(g[nn + i]) for i, k in enumerate(names)}}
+        return f.value, fhK, lnf, gd
+
+    def dfun_clade_x(self, x, lastround: bool = True, model_d: bool = False):
+        """(-lnL, gradient) of a clade model in codeml's x space (gb_dfun_clade_x:
+        branch lengths, kappa, p0, p1, w0, [w1 under clade D], w2, w3)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        dx = np.zeros_like(x)
+        f = C.c_double(0)
+        bn = np.ascontiguousarray(self.bnode, dtype=np.int32)
+        _lib.check(self._L.gb_dfun_clade_x(self._h, bn.ctypes.data_as(C.POINTER(C.c_int)), int(lastround),
+                                           int(model_d), _ptr(x), len(x), C.byref(f), _ptr(dx)))
+        return f.value, dx
 
     def m7(self, blength, kappa, p, q, K: int = 10):
         """Site model M7 (beta, K categories) on a tree with every branch

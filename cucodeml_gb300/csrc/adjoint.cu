@@ -772,6 +772,43 @@ void launch_freq_batched(const FreqArgs *args, const int2 *map, int nblocks, cud
     if (nblocks > 0) freq_batched_kernel<<<nblocks, 256, 0, st>>>(args, map);
 }
 
+// the FP64 gradient kernels on explicit buffers (clade models, clade.cu)
+cudaError_t init_fp64_adjoint_kernels() {
+    cudaError_t e = cudaFuncSetAttribute(gradP_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradPSmem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(gradH_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kGradHSmem);
+}
+
+void launch_dmat_fp64(const DevParams *prm, const GradParams *gp, double *Dm, cudaStream_t st) {
+    dmat_kernel<<<DM_BLOCKS, 256, 0, st>>>(prm, gp, Dm, nullptr);
+}
+
+void launch_bwd_level_fp64(const BItem *bitems, int nitems, int ntile, int npad, const double *Pt, const double *E,
+                           double *Ebar, double *Abar, const double *scaleF, const double *fpatt, const double *post,
+                           const double *fbar, const double *pi, cudaStream_t st) {
+    dim3 grid(ntile, nitems);
+    bwd_level_kernel<<<grid, 128, 0, st>>>(bitems, npad, Pt, E, Ebar, Abar, scaleF, fpatt, post, fbar, pi);
+}
+
+void launch_gradP_fp64(const Contrib *contrib, const int *coff, int npair, int nchunk, int npatt, int npad,
+                       const double *Ebar, const double *conP, const unsigned char *z, double *Gpart,
+                       const unsigned char *amb, cudaStream_t st) {
+    dim3 grid((unsigned)npair, nchunk);
+    gradP_kernel<<<grid, 128, kGradPSmem, st>>>(contrib, coff, npatt, npad, Ebar, conP, z, Gpart, nchunk, amb,
+                                                nullptr);
+}
+
+void launch_gradH_fp64(const PairDesc *pairs, int npair, const int *label, const double *tnode, const DevParams *prm,
+                       const double *Gpart, int nchunk, const double *Dm, double *pout, cudaStream_t st) {
+    if (npair > 0)
+        gradH_kernel<<<(unsigned)npair, 256, kGradHSmem, st>>>(pairs, label, tnode, prm, Gpart, nchunk, Dm, pout);
+}
+
+void launch_freq_fp64(const double *fhK, const double *lnf, const double *fpatt, int npatt, int npad, int nscale,
+                      double *fpart, cudaStream_t st) {
+    freq_kernel<<<(npatt + 255) / 256, 256, 0, st>>>(fhK, lnf, fpatt, npatt, npad, nscale, fpart);
+}
+
 void launch_freq(gb_handle *h, int nscale) {
     AdjointState *a = h->adj;
     freq_kernel<<<a->nfreq_blocks, 256, 0, h->stream>>>(h->d_fhK, h->d_lnf, h->d_fpatt, h->npatt, h->npad,

@@ -89,5 +89,21 @@ void launch_gradH_df(gb_handle *h);      // split-precision path: double-float p
 void launch_freq(gb_handle *h, int nscale);
 void adjoint_chain(gb_handle *h, const Derived *D, const double *blength, gb_grad *grad);
 int adjoint_fetch(gb_handle *h);              // D2H of per-pair and class-weight sums (async)
+// the FP64 gradient kernels on explicit buffers (clade models): attributes
+// (before any capture), dP/dt matrices of one parameter block, one backward
+// level, dlnL/dP partials of every pair, per-pair sums (dt', kappa, omega of
+// the pair's eigen slot), class-weight sums ((npatt + 255) / 256 blocks of 4)
+cudaError_t init_fp64_adjoint_kernels();
+void launch_dmat_fp64(const DevParams *prm, const GradParams *gp, double *Dm, cudaStream_t st);
+void launch_bwd_level_fp64(const BItem *bitems, int nitems, int ntile, int npad, const double *Pt, const double *E,
+                           double *Ebar, double *Abar, const double *scaleF, const double *fpatt, const double *post,
+                           const double *fbar, const double *pi, cudaStream_t st);
+void launch_gradP_fp64(const Contrib *contrib, const int *coff, int npair, int nchunk, int npatt, int npad,
+                       const double *Ebar, const double *conP, const unsigned char *z, double *Gpart,
+                       const unsigned char *amb, cudaStream_t st);
+void launch_gradH_fp64(const PairDesc *pairs, int npair, const int *label, const double *tnode, const DevParams *prm,
+                       const double *Gpart, int nchunk, const double *Dm, double *pout, cudaStream_t st);
+void launch_freq_fp64(const double *fhK, const double *lnf, const double *fpatt, int npatt, int npad, int nscale,
+                      double *fpart, cudaStream_t st);
 
 }  // namespace gb

@@ -133,7 +133,13 @@ void CUDA_FreeAll(void) {
 }
 
 int GB_dfun(double x[], double *f, double dx[], int n) {
-    int rc = gb_dfun_x(g_h, g_bnode, LASTROUND, x, n, f, dx);
+    int rc;
+    if (com.model == 3) {      /* clade models C (NSsites = 2) and D (NSsites = 3) */
+        rc = gb_dfun_clade_x(g_h, g_bnode, LASTROUND, com.NSsites == 3, x, n, f, dx);
+        if (rc) gb_die("gb_dfun_clade_x", rc);
+        return 0;
+    }
+    rc = gb_dfun_x(g_h, g_bnode, LASTROUND, x, n, f, dx);
     if (rc) gb_die("gb_dfun_x", rc);
     return 0;
 }

@@ -252,6 +252,8 @@ void rate_parts(const double *pi, double part[4]) {
 
 }  // namespace
 
+void mean_rate_parts(const double *pi, double part[4]) { rate_parts(pi, part); }
+
 double build_q(const double *pi, double kappa, double omega, double *Q, double *dQk, double *dQw) {
     const CodeTables &T = tables();
     for (int i = 0; i < NC * NC; i++) Q[i] = 0;

@@ -34,6 +34,9 @@ struct Derived {
 // -sum_i pi_i Q_ii.  dQk/dQw (nullable) receive dQ/dkappa and dQ/domega.
 double build_q(const double *pi, double kappa, double omega, double *Q, double *dQk, double *dQw);
 
+// GY94's mean rate as part[0] + kappa part[1] + omega part[2] + kappa omega part[3]
+void mean_rate_parts(const double *pi, double part[4]);
+
 // Symmetric eigen solution of a reversible Q: Q = U diag(Root) V, V = U^-1.
 // Householder tridiagonalisation (column-wise reflectors, Golub & Van Loan
 // alg. 8.3.1) + implicit QL.  Returns 0 or -1 (no convergence).

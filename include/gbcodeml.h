@@ -199,9 +199,19 @@ int gb_eval_clade_uvr(gb_handle *h, const double *const U[4], const double *cons
    library: kappa, the class weights p0, p1 (p2 = 1 - p0 - p1) and omega[4] =
    (w0, w1, w2, w3) -- w1 = 1 under clade model C, free under D; w2 is the
    third class's omega on branch type 0, w3 on branch type 1 (codeml.c:
-   2522-2539).  blength in node order.  FP64 handles. */
+   2522-2539).  blength in node order.  grad (may be NULL): the analytic
+   gradient of -lnL, [nnode] by branch length (node order, 0 at the root) then
+   kappa, p0, p1, w0, w1, w2, w3 (the adjoint of the FP64 path).  FP64 handles. */
 int gb_eval_clade(gb_handle *h, const double *blength, double kappa, double p0, double p1,
-                  const double omega[4], double *neg_lnL, double *fhK, double *lnf, gb_stats *stats);
+                  const double omega[4], double *neg_lnL, double *grad, double *fhK, double *lnf,
+                  gb_stats *stats);
+
+/* gb_eval_clade in codeml's x space for ming2's dfun under clade models:
+   x = branch lengths (bnode[i] = node of x[i]), kappa, p0, p1 (codeml's
+   transformed proportions unless lastround), w0, [w1 when model_d], w2, w3;
+   n = nbranch + 6 (clade C) or + 7 (clade D).  f = -lnL, dx = its gradient. */
+int gb_dfun_clade_x(gb_handle *h, const int *bnode, int lastround, int model_d, const double *x, int n,
+                    double *f, double *dx);
 
 /*
  * Evaluate -lnL from natural parameters; if grad != NULL also the analytic

@@ -14,14 +14,16 @@
  *                                  Qfactor_NS_branch and com.freqK; every call
  *                                  copies its class into com.fhK + ir*npatt.
  *                                  Clade models C/D (model = 3, two branch
- *                                  types): a second evaluation with slots
- *                                  (w2, w1, w3) gives their third class.
+ *                                  types): their three classes in one
+ *                                  evaluation from _UU/_VV/_Root[0..3]
+ *                                  (gb_eval_clade_uvr).
  *   CUDA_FreeAll                   replaces cuda-codeml.cu:1162 (codeml.c:695).
  *   GB_dfun                        new: ming2's gradient hook
  *                                  (tools.c:6361-6363, `dfun`), the analytic
  *                                  gradient of -lnL in codeml's x space
- *                                  (branch-site models A and B); pass it
- *                                  instead of NULL at codeml.c:688.
+ *                                  (branch-site models A and B, clade models
+ *                                  C and D); pass it instead of NULL at
+ *                                  codeml.c:688.
  *   GB_BEB                         new: the Bayes empirical Bayes analysis of
  *                                  models A and B on the GPU at codeml's final
  *                                  x (kappa and branch lengths; the Qfactors

@@ -10,8 +10,8 @@ CUDA_Init:
 * `eval`: codeml's CUDA objective CUDA_lfundG (treesub.c:7397-7450, whose
   CUDA_fx_r calls the adapter's CUDA_ScheduleConditionalPNode per class) must
   equal codeml's own CPU lfundG at the same x within 1e-9 relative, for
-  branch-site models A and B and clade model C; for model A the adapter's
-  GB_dfun must equal codeml's central-difference gradient (gradientB with
+  branch-site models A and B and clade models C and D; the adapter's GB_dfun
+  must equal codeml's central-difference gradient (gradientB with
   AlwaysCenter, tools.c:6326-6350) within its step error.
 * `dfun` / unchanged: codeml's whole model-A fit, ming2 driven by GB_dfun
   (the one-argument change at codeml.c:688) or by its own finite differences
@@ -86,7 +86,7 @@ def test_dropin_links_and_stops_at_device_check_without_gpu():
 def test_dropin_objective_matches_codeml_cpu(name):
     exe = dropin_binary()
     fx = load_fixture(name)
-    model_a = name.startswith(("c", "u", "mb"))      # GB_dfun: models A and B
+    model_a = name.startswith(("c", "u", "mb", "mc"))      # GB_dfun: models A, B and clade models C, D
     with tempfile.TemporaryDirectory() as d:
         fixture_case(d, fx, ctl=ctl_for(name))
         r = R.run(exe, d, "eval", env={"GBREF_DFUN": "1" if model_a else "0"}, timeout=900)

@@ -253,3 +253,77 @@ def test_clade_own_setup_matches_codeml(name):
     assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     ref = np.array(fx["lnf"])
     assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))
+
+
+def _clade_neg_lnL(pb, x, nb, lastround):
+    """The oracle's clade -lnL at codeml's x, proportions transformed as
+    codeml's f_and_x does unless lastround."""
+    x = np.array(x, dtype=np.float64)
+    if not lastround:
+        e1, e2 = np.exp(x[nb + 1]), np.exp(x[nb + 2])
+        x[nb + 1], x[nb + 2] = e1 / (1 + e1 + e2), e2 / (1 + e1 + e2)
+    return pb.clade_c(x)[0]
+
+
+def _fd5(f, x, h=1e-4):
+    g = np.zeros(len(x))
+    for i in range(len(x)):
+        e = h * (abs(x[i]) + 0.05)
+        v = []
+        for k in (-2, -1, 1, 2):
+            xk = x.copy()
+            xk[i] += k * e
+            v.append(f(xk))
+        g[i] = (v[0] - 8 * v[1] + 8 * v[2] - v[3]) / (12 * e)
+    return g
+
+
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+@pytest.mark.parametrize("lastround", [True, False])
+def test_clade_gradient_matches_fd(name, lastround):
+    """The clade models' analytic gradient (gb_dfun_clade_x: the FP64 adjoint
+    over the three-class schedule, the chain rule through both branch types'
+    Qfactors and the class weights) against five-point differences of the
+    oracle's clade -lnL in codeml's x space, both of codeml's proportion
+    spaces: 1e-5 relative, as for model A."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    d = name.startswith("mcD")
+    nb = tree.nbranch
+    x = np.array(fx["x"])
+    if not lastround:
+        p0, p1 = x[nb + 1], x[nb + 2]
+        p2 = 1 - p0 - p1
+        x[nb + 1], x[nb + 2] = np.log(p0 / p2), np.log(p1 / p2)
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=O.max_threads(), model_b=d)
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    f, g = lk.dfun_clade_x(x, lastround, model_d=d)
+    lk.close()
+    f0 = _clade_neg_lnL(pb, x, nb, lastround)
+    assert abs(f - f0) <= 1e-12 * abs(f0)
+    gfd = _fd5(lambda xx: _clade_neg_lnL(pb, xx, nb, lastround), x)
+    err = np.abs(g - gfd) / np.maximum(1.0, np.abs(gfd))
+    print(f"{name} lastround={lastround}: max rel err {err.max():.2e}")
+    assert err.max() <= 1e-5
+
+
+def test_clade_gradient_natural_parameters():
+    """Likelihood.clade(grad=True) against the x-space entry: the same
+    adjoint, branch lengths in node order and (kappa, p0, p1, w0, w2, w3)."""
+    name = clade_names()[0]
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    nb = tree.nbranch
+    x = np.array(fx["x"])
+    kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[:nb]
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    f, _, _, g = lk.clade(bl, kappa, p0, p1, w0, w2, w3, grad=True)
+    f2, gx = lk.dfun_clade_x(x, True)
+    f3, _, _ = lk.clade(bl, kappa, p0, p1, w0, w2, w3)
+    lk.close()
+    assert f == f2 == f3
+    assert np.allclose(g["blength"][tree.branch_nodes()], gx[:nb], rtol=1e-13, atol=0)
+    assert np.allclose([g["kappa"], g["p0"], g["p1"], g["omega0"], g["omega2"], g["omega3"]], gx[nb:],
+                       rtol=1e-13, atol=0)

@@ -30,6 +30,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import re
 import statistics
 import subprocess
 import sys
@@ -454,6 +455,63 @@ def reference_gpu_leg(args, neg_lnL_ours):
     return out
 
 
+def codeml_fit_leg(args):
+    """codeml's own model-A fit (ming2, codeml.c:683-692) on this GPU from one
+    fixed starting point (in.codeml: the simulation's branch lengths x 0.8,
+    kappa 1.5, p0 0.6, p1 0.2, w0 0.5, w2 2; codeml's own starting values are
+    randomised), three ways: ming2 with finite-difference gradients
+    (gradientB, tools.c:6326-6350) of CuCodeML's CUDA_lfundG (the reference's
+    GPU path, cuda-codeml.cu for sm_103a); the same over this library's FP64
+    drop-in; and ming2 driven by the drop-in's analytic gradient (GB_dfun, the
+    one-argument change at codeml.c:688).  Per run: ming2's own wall time,
+    rounds and lnL calls (ref_harness.c), the lnL reached and the whole
+    codeml run's wall time (reading, initial estimates, NEB / BEB output
+    included)."""
+    import tempfile
+    from cucodeml_gb300.simulate import simulate
+    from oracle import refcodeml as R
+    aln = simulate(args.fit_ns, args.fit_ncodon, seed=2024)
+    tree = aln.tree
+    rows = R.alignment_rows(aln)
+    p0, p1 = 0.6, 0.2
+    x0 = np.concatenate([tree.x_branch_lengths() * 0.8, [1.5, np.log(p0 / (1 - p0 - p1)),
+                                                        np.log(p1 / (1 - p0 - p1)), 0.5, 2.0]])
+    out = {"workload": f"codeml model-A fit (ming2), {args.fit_ns} taxa x {args.fit_ncodon} codons, seed 2024, "
+                       "fixed start"}
+    for key, exe, mode in (("cucodeml_fd", "cucodeml", None), ("dropin_fd", "codeml_gb", None),
+                           ("dropin_dfun", "codeml_gb", "dfun")):
+        path = os.path.join(ROOT, "oracle", "_ref", exe)
+        if not os.path.exists(path):
+            out[key] = {"unavailable": f"oracle/_ref/{exe} not built (reference sources not staged)"}
+            continue
+        env = {k: v for k, v in os.environ.items() if not k.startswith("GBREF_")}
+        if mode:
+            env["GBREF_MODE"] = mode
+        with tempfile.TemporaryDirectory() as d:
+            R.write_case(d, tree.names, rows, tree.to_newick(), x0)
+            t0 = time.perf_counter()
+            r = subprocess.run([path, "codeml.ctl"], cwd=d, capture_output=True, text=True, env=env,
+                               timeout=args.fit_timeout)
+            wall = time.perf_counter() - t0
+            if r.returncode != 0:
+                out[key] = {"error": f"exit {r.returncode}: {r.stderr[-300:]}"}
+                continue
+            with open(os.path.join(d, "out.txt")) as f:
+                txt = f.read()
+        m = re.search(r"lnL\(ntime:\s*\d+\s+np:\s*(\d+)\):\s*(-?\d+\.\d+)", txt)
+        g = re.search(r"GBREF_MING2 (\S+) (\d+) (\d+)", r.stderr)
+        rounds = int(g.group(2)) if g else None
+        out[key] = {"ming2_s": float(g.group(1)) if g else None,
+                    # ming2 sets its round counter to maxround (10000) when it stops on line-search failure
+                    "ming2_rounds": rounds if rounds is not None and rounds < 10000 else "stopped on line-search failure",
+                    "lnL_calls": int(g.group(3)) if g else None, "lnL": float(m.group(2)) if m else None,
+                    "np": int(m.group(1)) if m else None, "codeml_wall_s": wall}
+    a, b = out.get("cucodeml_fd", {}), out.get("dropin_dfun", {})
+    if a.get("ming2_s") and b.get("ming2_s"):
+        out["ming2_speedup_dfun_vs_cucodeml_fd"] = a["ming2_s"] / b["ming2_s"]
+    return out
+
+
 def checkpoint_leg(args, dev):
     """Device memory of an FP64 lnL + gradient evaluation at 256 taxa x 20000
     codons with the checkpointed adjoint off and on (GB_TUNE_CHECKPOINT:
@@ -590,6 +648,11 @@ def main():
     ap.add_argument("--no-refgpu", action="store_true", help="skip the reference-GPU (CuCodeML) leg")
     ap.add_argument("--no-ckpt", action="store_true", help="skip the checkpointed-adjoint memory leg")
     ap.add_argument("--no-altnull", action="store_true", help="skip the 256 x 20000 model A vs null fits")
+    ap.add_argument("--no-fit", action="store_true",
+                    help="skip codeml's own fit over CuCodeML and over the drop-in (finite differences / GB_dfun)")
+    ap.add_argument("--fit-ns", type=int, default=24)
+    ap.add_argument("--fit-ncodon", type=int, default=600)
+    ap.add_argument("--fit-timeout", type=float, default=900.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -755,6 +818,8 @@ def main():
     if not args.no_refgpu:
         line["reference_gpu"] = secondary_leg(reference_gpu_leg, args,
                                               lk.evaluate(bl0, grad=False, **PARAMS).neg_lnL)
+    if not args.no_fit:
+        line["codeml_fit"] = secondary_leg(codeml_fit_leg, args)
     lk.close()
     if rank == 0:
         print(json.dumps(line))

@@ -199,9 +199,19 @@ int __wrap_ming2(FILE *fout, double *f, objective_t fun, gradient_t dfun, double
         mode_dump();
         exit(0);
     }
+    /* a full fit: ming2 as codeml calls it (finite differences) or with
+       GB_dfun; on stderr its wall time, iterations and lnL calls
+       ("GBREF_MING2 seconds rounds calls") */
     if (mode && !strcmp(mode, "dfun")) {
         if (!GB_dfun) { fprintf(stderr, "ref_harness: GBREF_MODE=dfun needs the drop-in adapter\n"); exit(2); }
-        return __real_ming2(fout, f, fun, GB_dfun, x, xb, space, e, n);
+        dfun = GB_dfun;
     }
-    return __real_ming2(fout, f, fun, dfun, x, xb, space, e, n);
+    {
+        extern int Iround, NFunCall;
+        const double t0 = now_s();
+        const int calls0 = NFunCall;
+        const int rc = __real_ming2(fout, f, fun, dfun, x, xb, space, e, n);
+        fprintf(stderr, "GBREF_MING2 %.6f %d %d\n", now_s() - t0, Iround, NFunCall - calls0);
+        return rc;
+    }
 }

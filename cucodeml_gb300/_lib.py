@@ -93,6 +93,8 @@ SIGNATURES = {
     "gb_batch_eval": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, C.POINTER(Grad), C.POINTER(Stats)]),
     "gb_batch_submit": (C.c_int, [C.c_void_p, C.POINTER(Params), C.c_int, C.c_void_p]),
     "gb_batch_collect": (C.c_int, [C.c_void_p, _dp, C.POINTER(Grad), C.POINTER(Stats)]),
+    "gb_batch_submit_b": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, C.c_int, C.c_void_p]),
+    "gb_batch_omega1_grad": (C.c_int, [C.c_void_p, _dp]),
     "gb_batch_replay": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "gb_batch_destroy": (C.c_int, [C.c_void_p]),
     "gb_profile": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp, _ip]),

@@ -595,8 +595,13 @@ class Batch:
             pass
 
     def evaluate(self, params, grad: bool = False):
-        """params: list of dicts (blength, kappa, omega0, omega2, p0, p1) per gene.
-        Returns (neg_lnL [n], grads list or None, EvalResult stats)."""
+        """params: list of dicts (blength, kappa, omega0, omega2, p0, p1) per gene,
+        each with omega1 as well for branch-site model B (gb_batch_submit_b;
+        its gradient then has "omega1").  Returns (neg_lnL [n], grads list or
+        None, EvalResult stats)."""
+        if any("omega1" in p for p in params):
+            self.submit(params, grad)
+            return self.collect()
         n = self.n
         pr = (_lib.Params * n)()
         keep = []
@@ -634,7 +639,13 @@ class Batch:
             self._keep_bl.append(bl)
             pr[i] = _lib.Params(_ptr(bl), p["kappa"], p["omega0"], p["omega2"], p["p0"], p["p1"])
         self._pending_grad = bool(grad)
-        _lib.check(self._L.gb_batch_submit(self._h, pr, int(grad), after._h if after is not None else None))
+        self._pending_b = any("omega1" in p for p in params)
+        ah = after._h if after is not None else None
+        if self._pending_b:
+            self._omega1 = np.ascontiguousarray([p.get("omega1", 1.0) for p in params], dtype=np.float64)
+            _lib.check(self._L.gb_batch_submit_b(self._h, pr, _ptr(self._omega1), int(grad), ah))
+        else:
+            _lib.check(self._L.gb_batch_submit(self._h, pr, int(grad), ah))
 
     def collect(self):
         """(neg_lnL [n], grads or None, EvalResult stats) of the submitted evaluation."""
@@ -653,6 +664,11 @@ class Batch:
         if gr is not None:
             grads = [{"blength": dbl[i], "kappa": gr[i].d_kappa, "omega0": gr[i].d_omega0,
                       "omega2": gr[i].d_omega2, "p0": gr[i].d_p0, "p1": gr[i].d_p1} for i in range(n)]
+            if getattr(self, "_pending_b", False):
+                dw1 = np.zeros(n)
+                _lib.check(self._L.gb_batch_omega1_grad(self._h, _ptr(dw1)))
+                for i in range(n):
+                    grads[i]["omega1"] = float(dw1[i])
         return out, grads, EvalResult(float(out.sum()), None, None, None, st.ms_device, st.ms_host,
                                       st.kernels, st.h2d_bytes, st.d2h_bytes)
 

@@ -413,7 +413,10 @@ int gb_batch_destroy(gb_batch *b) {
 
 int gb_batch_size(const gb_batch *b) { return b ? b->n : GB_ERR_STATE; }
 
-int gb_batch_submit(gb_batch *b, const gb_params *prm, int with_grad, const gb_batch *after) {
+namespace {
+// gb_batch_submit and gb_batch_submit_b: omega1 (nullable) gives each gene
+// branch-site model B's free w1 (model A: w1 = 1)
+int batch_submit(gb_batch *b, const gb_params *prm, const double *omega1, int with_grad, const gb_batch *after) {
     if (!b || !prm) return fail(GB_ERR_ARG, "gb_batch_submit: bad arguments");
     if (b->pending) return fail(GB_ERR_STATE, "gb_batch_submit: the previous evaluation was not collected");
     if (after && after->device != b->device) return fail(GB_ERR_ARG, "gb_batch_submit: batches on two devices");
@@ -425,6 +428,10 @@ int gb_batch_submit(gb_batch *b, const gb_params *prm, int with_grad, const gb_b
     parallel_for(b->n, b->nthreads, [&](int i) {
         gb_handle *h = b->h[i];
         ModelParams m{prm[i].kappa, prm[i].omega0, prm[i].omega2, prm[i].p0, prm[i].p1};
+        if (omega1) {
+            m.w1 = omega1[i];
+            m.free_w1 = true;
+        }
         int rc = prm[i].blength ? derive(h->pi.data(), m, grad, b->D[i], false) : GB_ERR_ARG;
         if (!rc) rc = stage_params(h, b->D[i], prm[i].blength);
         status[i] = rc;
@@ -456,6 +463,17 @@ int gb_batch_submit(gb_batch *b, const gb_params *prm, int with_grad, const gb_b
     b->pending_grad = grad;
     b->pending_t0 = t0;
     return GB_OK;
+}
+}  // namespace
+
+int gb_batch_submit(gb_batch *b, const gb_params *prm, int with_grad, const gb_batch *after) {
+    return batch_submit(b, prm, nullptr, with_grad, after);
+}
+
+int gb_batch_submit_b(gb_batch *b, const gb_params *prm, const double *omega1, int with_grad,
+                      const gb_batch *after) {
+    if (!omega1) return fail(GB_ERR_ARG, "gb_batch_submit_b: null omega1");
+    return batch_submit(b, prm, omega1, with_grad, after);
 }
 
 int gb_batch_collect(gb_batch *b, double *neg_lnL, gb_grad *grads, gb_stats *stats) {
@@ -490,6 +508,15 @@ int gb_batch_collect(gb_batch *b, double *neg_lnL, gb_grad *grads, gb_stats *sta
         }
         stats->h2d_bytes = h2d;
         stats->d2h_bytes = d2h;
+    }
+    return GB_OK;
+}
+
+int gb_batch_omega1_grad(const gb_batch *b, double *d_omega1) {
+    if (!b || !d_omega1) return fail(GB_ERR_ARG, "gb_batch_omega1_grad: bad arguments");
+    for (int i = 0; i < b->n; i++) {
+        if (!b->h[i]->adj) return fail(GB_ERR_STATE, "gb_batch_omega1_grad: no gradient collected");
+        d_omega1[i] = b->h[i]->adj->d_omega1;
     }
     return GB_OK;
 }

@@ -406,6 +406,13 @@ int gb_batch_eval(gb_batch *b, const gb_params *prm, double *neg_lnL, gb_grad *g
  */
 int gb_batch_submit(gb_batch *b, const gb_params *prm, int with_grad, const gb_batch *after);
 int gb_batch_collect(gb_batch *b, double *neg_lnL, gb_grad *grads, gb_stats *stats);
+/* Branch-site model B over a batch (gb_eval_b per gene, codeml NSsites = 3):
+   gb_batch_submit with each gene's free omega1[i]; after gb_batch_collect
+   of an evaluation submitted with gradient, gb_batch_omega1_grad gives each
+   gene's d(-lnL)/d omega1 (the other derivatives are in grads). */
+int gb_batch_submit_b(gb_batch *b, const gb_params *prm, const double *omega1, int with_grad,
+                      const gb_batch *after);
+int gb_batch_omega1_grad(const gb_batch *b, double *d_omega1);
 int gb_batch_replay(gb_batch *b, int iters, int with_grad, double *ms);
 int gb_batch_destroy(gb_batch *b);
 

@@ -118,3 +118,32 @@ def test_pipelined_halves_equal_one_batch(genes, precision):
             assert np.allclose(a["blength"], c["blength"], rtol=1e-10, atol=1e-10)
             for k in ("kappa", "omega0", "omega2", "p0", "p1"):
                 assert abs(a[k] - c[k]) <= 1e-10 * max(1.0, abs(a[k]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fast"])
+def test_batch_model_b_equals_single(genes, precision):
+    """Branch-site model B over a batch (gb_batch_submit_b, each gene's own
+    free w1) against per-gene gb_eval_b: lnL to 1e-12, gradient including
+    d/dw1 to 1e-10; then model A again on the same batch object (w1 = 1)."""
+    b = api.Batch([(a.tree, z, fp, pi) for a, z, fp, pi in genes], precision=precision)
+    prm = [dict(params_of(a), omega1=0.6 + 0.05 * i) for i, (a, _, _, _) in enumerate(genes)]
+    f, g, _ = b.evaluate(prm, grad=True)
+    for i, (a, z, fp, pi) in enumerate(genes):
+        lk = api.Likelihood(a.tree, z, fp, pi, precision=precision)
+        p = prm[i]
+        r = lk.evaluate(p["blength"], p["kappa"], p["omega0"], p["omega2"], p["p0"], p["p1"], grad=True,
+                        omega1=p["omega1"])
+        assert abs(f[i] - r.neg_lnL) <= 1e-12 * abs(r.neg_lnL), i
+        assert np.allclose(g[i]["blength"], r.grad["blength"], rtol=1e-10, atol=1e-10)
+        for k in ("kappa", "omega0", "omega1", "omega2", "p0", "p1"):
+            assert abs(g[i][k] - r.grad[k]) <= 1e-10 * max(1.0, abs(r.grad[k])), (i, k)
+        lk.close()
+    fa, ga, _ = b.evaluate([params_of(a) for a, _, _, _ in genes], grad=True)
+    assert "omega1" not in ga[0]
+    for i, (a, z, fp, pi) in enumerate(genes):
+        lk = api.Likelihood(a.tree, z, fp, pi, precision=precision)
+        p = params_of(a)
+        r = lk.evaluate(p["blength"], p["kappa"], p["omega0"], p["omega2"], p["p0"], p["p1"])
+        assert abs(fa[i] - r.neg_lnL) <= 1e-12 * abs(r.neg_lnL), i
+        lk.close()
+    b.close()

@@ -205,6 +205,17 @@ class Likelihood:
         gd = {"blength": g[:nn].copy(), **{k: float(g[nn + i]) for i, k in enumerate(names)}}
         return f.value, fhK, lnf, gd
 
+    def neb_clade(self, blength, kappa, p0, p1, w0, w2, w3, w1: float = 1.0):
+        """codeml's NEB site-class posteriors under clade model C / D
+        (gb_neb_clade): (post [3, npatt], -lnL)."""
+        bl = np.ascontiguousarray(blength, dtype=np.float64)
+        om = np.ascontiguousarray([w0, w1, w2, w3], dtype=np.float64)
+        post = np.zeros((3, self.npatt))
+        f = C.c_double(0)
+        _lib.check(self._L.gb_neb_clade(self._h, _ptr(bl), float(kappa), float(p0), float(p1), _ptr(om),
+                                        _ptr(post), C.byref(f)))
+        return post, f.value
+
     def dfun_clade_x(self, x, lastround: bool = True, model_d: bool = False):
         """(-lnL, gradient) of a clade model in codeml's x space (gb_dfun_clade_x:
         branch lengths, kappa, p0, p1, w0, [w1 under clade D], w2, w3)."""

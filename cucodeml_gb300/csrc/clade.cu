@@ -572,3 +572,17 @@ extern "C" int gb_dfun_clade_x(gb_handle *h, const int *bnode, int lastround, in
     dx[n - 1] = g[nn + 6];
     return GB_OK;
 }
+
+// codeml's NEB under the clade models (lfunNSsites_rate codeml.c:5079-5129:
+// freqK_c f_c / sum over the three classes at the parameters): the mixture
+// kernel's class posteriors of one gb_eval_clade evaluation, [3][npatt].
+extern "C" int gb_neb_clade(gb_handle *h, const double *blength, double kappa, double p0, double p1,
+                            const double omega[4], double *post, double *neg_lnL) {
+    if (!h) return fail(GB_ERR_STATE, "null handle");
+    if (!post) return fail(GB_ERR_ARG, "null argument");
+    const int rc = gb_eval_clade(h, blength, kappa, p0, p1, omega, neg_lnL, nullptr, nullptr, nullptr, nullptr);
+    if (rc) return rc;
+    CK(cudaMemcpy2D(post, sizeof(double) * h->npatt, h->d_post, sizeof(double) * h->npad,
+                    sizeof(double) * h->npatt, 3, cudaMemcpyDeviceToHost));
+    return GB_OK;
+}

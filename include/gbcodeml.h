@@ -206,6 +206,13 @@ int gb_eval_clade(gb_handle *h, const double *blength, double kappa, double p0, 
                   const double omega[4], double *neg_lnL, double *grad, double *fhK, double *lnf,
                   gb_stats *stats);
 
+/* codeml's naive empirical Bayes (NEB) site-class posteriors under the
+   clade models (lfunNSsites_rate codeml.c:5079-5129) at gb_eval_clade's
+   parameters: post [3][npatt] (pattern order), -lnL in *neg_lnL (may be
+   NULL).  FP64 handles. */
+int gb_neb_clade(gb_handle *h, const double *blength, double kappa, double p0, double p1,
+                 const double omega[4], double *post, double *neg_lnL);
+
 /* gb_eval_clade in codeml's x space for ming2's dfun under clade models:
    x = branch lengths (bnode[i] = node of x[i]), kappa, p0, p1 (codeml's
    transformed proportions unless lastround), w0, [w1 when model_d], w2, w3;

@@ -182,9 +182,11 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
     if clade_d:       # clade-D BEB: grid w0 in (0, 0.5), w1 in (0.5, 1.5), w2, w3 in (0, 3)
-        extra = {"model": "D", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3)}
+        extra = {"model": "D", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3),
+                 "neb_site_post_5dp": parse_site_post(rst, "Naive", ncls=3)}
     elif clade:
-        extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3)}
+        extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3),
+                 "neb_site_post_5dp": parse_site_post(rst, "Naive", ncls=3)}
     elif site_model:
         extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
         if site_model == "M2a":       # BEB of M2a (lfunNSsites_M2M8 codeml.c:6190-6415): 3 classes

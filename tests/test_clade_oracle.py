@@ -82,3 +82,26 @@ def test_clade_d_beb_matches_codeml(name):
         assert np.max(np.abs(r["grid"][row] - np.array(b[key]))) <= 5.01e-4
     assert np.max(np.abs(r["p0p1"] - np.array(b["p0p1_post_3dp"]))) <= 5.01e-4
     assert np.allclose(r["post"].sum(axis=0), 1.0, atol=1e-12)
+
+
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+def test_clade_neb_matches_codeml(name):
+    """codeml's NEB under the clade models (lfunNSsites_rate
+    codeml.c:5079-5129: freqK_c f_c normalised over the three classes),
+    from the oracle's clade evaluation, against codeml's rst (5 dp)."""
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    d = name.startswith("mcD")
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=2, model_b=d)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    v, fhK, lnf = pb.clade_c(x)
+    p0, p1 = x[nb + 1], x[nb + 2]
+    fk = np.array([p0, p1, 1 - p0 - p1])
+    scaled = bool(np.any(fhK < 0))      # with scaled nodes fhK holds log f (f itself otherwise)
+    f = np.exp(fhK - fhK.max(axis=0)) if scaled else fhK
+    q = fk[:, None] * f
+    post = q / q.sum(axis=0)
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6

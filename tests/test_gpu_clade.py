@@ -327,3 +327,28 @@ def test_clade_gradient_natural_parameters():
     assert np.allclose(g["blength"][tree.branch_nodes()], gx[:nb], rtol=1e-13, atol=0)
     assert np.allclose([g["kappa"], g["p0"], g["p1"], g["omega0"], g["omega2"], g["omega3"]], gx[nb:],
                        rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+def test_clade_neb_matches_codeml(name):
+    """gb_neb_clade: the mixture kernel's class posteriors of one clade
+    evaluation against codeml's NEB (rst, 5 dp); they sum to 1."""
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    if name.startswith("mcD"):
+        kappa, p0, p1, w0, w1, w2, w3 = x[nb:nb + 7]
+    else:
+        kappa, p0, p1, w0, w2, w3 = x[nb:nb + 6]
+        w1 = 1.0
+    bl = np.zeros(tree.nnode)
+    bl[tree.branch_nodes()] = x[:nb]
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    post, f = lk.neb_clade(bl, kappa, p0, p1, w0, w2, w3, w1=w1)
+    lk.close()
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6
+    assert np.allclose(post.sum(axis=0), 1.0, atol=1e-13)
+    assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9

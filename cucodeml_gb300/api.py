@@ -277,6 +277,17 @@ class Likelihood:
             lnf = np.log(np.where(sm <= 0, 1e-300, sm))
         return -float((lnf * self._fpatt).sum()), fhK, lnf
 
+    def site_neb(self, fhK, props):
+        """codeml's NEB posteriors of a site model's classes (lfunNSsites_rate
+        codeml.c:5079-5129: props_k f_k normalised over k, from site_model's
+        fhK; log values shifted by their maximum when nodes are scaled):
+        [K, npatt]."""
+        fhK = np.asarray(fhK, dtype=np.float64)
+        pr = np.asarray(props, dtype=np.float64)
+        f = np.exp(fhK - fhK.max(axis=0)) if self.nscale else fhK
+        q = pr[:, None] * f
+        return q / q.sum(axis=0)
+
     def clade_uvr(self, U, V, Root, qfactor, freqK, blength, two_calls: bool = False):
         """Clade models C / D with two branch types from the host's eigen
         solutions of (w0, w1, w2 background, w3 foreground) -- codeml's

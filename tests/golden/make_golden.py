@@ -188,7 +188,9 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3),
                  "neb_site_post_5dp": parse_site_post(rst, "Naive", ncls=3)}
     elif site_model:
-        extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns)}
+        ncat = {"M1a": 2, "M2a": 3, "M3": 3, "M7": 10, "M8": 11}[site_model]
+        extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns),
+                 "neb_site_post_5dp": parse_site_post(rst, "Naive", ncls=ncat)}
         if site_model == "M2a":       # BEB of M2a (lfunNSsites_M2M8 codeml.c:6190-6415): 3 classes
             extra["beb"] = parse_beb(out, rst, r.stdout, ncls=3)
             extra["beb"]["site_wmean_sd_3dp"] = parse_site_meanw(rst)

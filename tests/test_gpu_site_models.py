@@ -25,7 +25,8 @@ def test_site_model_classes(name):
     call, eigen solutions from the library; every site model including M7
     and M8 (ten beta categories) against codeml's printed lnL and log f, and
     for M7 / M8 Likelihood.m7 / m8 (the library's discretised beta) against
-    the same classes from the oracle's quantiles."""
+    the same classes from the oracle's quantiles; codeml's NEB over the K
+    classes (Likelihood.site_neb)."""
     from tests.conftest import site_model_classes
     fx, tree, codons = load_golden(name)
     z, fpatt, pi = O.patterns(codons)
@@ -44,6 +45,11 @@ def test_site_model_classes(name):
     assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
     ref = np.array(fx["lnf"])
     assert np.all(np.abs(lnf - ref) <= 5.1e-11 + 2e-11 * np.abs(ref))
+    # codeml's NEB over the K classes (rst, 5 dp)
+    from tests.test_beb_oracle import site_patterns
+    post = lk.site_neb(fhK, pr)
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6
     lk.close()
 
 

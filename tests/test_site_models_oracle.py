@@ -74,3 +74,26 @@ def test_m2a_beb_as_model_a(name):
     # the posterior mean and SD of w codeml prints beside them (3 dp)
     ms = np.stack([r["wmean"], r["wsd"]])[:, site_patterns(z, codons)].T
     assert np.max(np.abs(ms - np.array(g["site_wmean_sd_3dp"]))) <= 5.01e-4
+
+
+@pytest.mark.parametrize("name", site_model_names())
+def test_site_model_neb_matches_codeml(name):
+    """codeml's NEB under the site models (lfunNSsites_rate codeml.c:5079-5129:
+    props_k f_k normalised over the K classes; M7 / M8 over the ten beta
+    categories and w_s), from the oracle's K whole-tree classes, against
+    codeml's rst (5 dp)."""
+    from tests.conftest import site_model_classes
+    from tests.test_beb_oracle import site_patterns
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, _ = as_model_a(fx, tree)
+    om, pr = site_model_classes(fx, tree)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    v, fhK, lnf = O.Problem(t, z, fpatt, pi, nthreads=2).site_classes(x[:nb], x[nb], om, pr)
+    scaled = bool(np.any(fhK < 0))      # with scaled nodes fhK holds log f
+    f = np.exp(fhK - fhK.max(axis=0)) if scaled else fhK
+    q = np.asarray(pr)[:, None] * f
+    post = q / q.sum(axis=0)
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6

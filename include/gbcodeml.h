@@ -1,6 +1,7 @@
 /*
  * gbcodeml.h -- C ABI of libgbcodeml.so, a GB300 (sm_103a) implementation of
- * PAML codeml's branch-site model A likelihood hot path.
+ * PAML codeml's branch-site model A likelihood hot path (and, on the same
+ * kernels, model B, the clade models C / D and the site models).
  *
  * Everything here is plain C: pointers, sizes and status codes.  No call
  * exits the process; every entry point returns GB_OK (0) or a negative
@@ -48,6 +49,19 @@
  *                            lfunNSsites_ACD (codeml.c:6617-6826): 121 full
  *                            prunings over an omega grid and the integration
  *                            over a 10^4-point parameter grid, on the device.
+ *   gb_eval_b                branch-site model B (NSsites = 3, codeml.c:
+ *                            2427-2436): model A with a free w1, with gradient.
+ *   gb_eval_clade_uvr /      clade models C and D with two branch types
+ *   gb_eval_clade /          (model = 3, codeml.c:2437-2446, 2522-2539) in one
+ *   gb_dfun_clade_x /        evaluation, from codeml's four eigen solutions or
+ *   gb_neb_clade             the library's own set-up; gradient, ming2's dfun
+ *                            and the NEB posteriors.
+ *   gb_beb_tables /          f(x_h | w) on other omega grids and the clade-C /
+ *   gb_beb_clade             clade-D BEB grid integrals (10^5 / 10^6 points).
+ *   gb_beta_classes          M7 / M8's discretised beta (DiscreteNSsites
+ *                            codeml.c:2728-2770).
+ *   gb_batch_*               many alignments in one graph launch per
+ *                            evaluation (models A and B).
  *
  * The five symbols codeml.c itself calls (CUDA_Init, CUDA_lfundG, CUDA_fx_r,
  * CUDA_ScheduleConditionalPNode, CUDA_FreeAll; codeml.h:67-85) are provided

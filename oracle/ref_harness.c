@@ -32,6 +32,9 @@
  *            and encoding (com.z with its ambiguity codes, com.fpatt, com.pi,
  *            nChara / CharaMap of SetMapAmbiguity treesub.c:1146-1200); then
  *            exits.
+ *   sites    at x as final values (LASTROUND = 1), the adapter's GB_BEB and
+ *            GB_HessianSKT2004 with codeml's SE arithmetic after it; prints
+ *            the BEB arrays, log f(X) and the SEs, then exits.
  *   dfun     runs ming2 with the adapter's GB_dfun as its gradient hook
  *            (the one-argument change at codeml.c:688 that the drop-in
  *            enables), then codeml continues as usual.
@@ -59,6 +62,11 @@ extern double Small_Diff;
 
 /* present only when the drop-in adapter is linked in */
 extern int GB_dfun(double x[], double *f, double dx[], int n) __attribute__((weak));
+extern int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], double lnfX[])
+    __attribute__((weak));
+extern int GB_HessianSKT2004(double xmle[], double lnLm, double g[], double H[]) __attribute__((weak));
+extern int LASTROUND;
+int matinv(double x[], int n, int m, double space[]);
 
 static double now_s(void) {
     struct timespec t;
@@ -118,7 +126,7 @@ static void mode_time(objective_t fun, double x[], int n) {
 static void mode_eval(objective_t fun, double x[], int n) {
     double *g = (double *)malloc(sizeof(double) * n), *tv = (double *)malloc(sizeof(double) * 2 * n);
     double *ga = (double *)malloc(sizeof(double) * n), f_fun, f_cpu, fa = 0;
-    double *g5 = (double *)malloc(sizeof(double) * n);
+    double *g5 = (double *)calloc(n, sizeof(double));
     int i;
     int *xmark = (int *)calloc(n, sizeof(int)), have = GB_dfun != NULL && env_int("GBREF_DFUN", 0);
     if (!g || !tv || !ga || !g5 || !xmark) { fprintf(stderr, "ref_harness: out of memory\n"); exit(2); }
@@ -154,6 +162,44 @@ static void mode_eval(objective_t fun, double x[], int n) {
     printf("}\n");
     fflush(stdout);
     free(g); free(tv); free(ga); free(g5); free(xmark);
+}
+
+/* what codeml computes after a model-A fit, through the adapter: at x taken
+   as final values (LASTROUND = 1, so that SetParameters leaves Qfactor_NS_branch
+   as codeml's BEB reads it), GB_BEB (the lfunNSsites_ACD arrays,
+   codeml.c:6697-6775) and GB_HessianSKT2004 (codeml.c:764) followed by
+   codeml's own SE arithmetic (H negated, matinv, sqrt of the diagonal,
+   codeml.c:778-782) */
+static void mode_sites(objective_t fun, double x[], int n) {
+    const int np4 = 4 * com.npatt;
+    double *post = (double *)malloc(sizeof(double) * np4), grid[40], p0p1[100], lnfX[3];
+    double *g = (double *)malloc(sizeof(double) * n), *H = (double *)malloc(sizeof(double) * (2 * n * n + n));
+    double f, se;
+    int i;
+    if (!GB_BEB || !GB_HessianSKT2004) { fprintf(stderr, "ref_harness: GBREF_MODE=sites needs the drop-in adapter\n"); exit(2); }
+    if (!post || !g || !H) { fprintf(stderr, "ref_harness: out of memory\n"); exit(2); }
+    LASTROUND = 1;
+    f = fun(x, n);
+    GB_BEB(x, n, post, grid, p0p1, lnfX);
+    GB_HessianSKT2004(x, -f, g, H);
+    for (i = 0; i < n * n; i++) H[i] *= -1;
+    matinv(H, n, n, H + n * n);
+    printf("\nGBREF {\"mode\": \"sites\", \"np\": %d, \"npatt\": %d, \"f\": %.17g, ", n, com.npatt, f);
+    print_vec("post", post, np4);
+    printf(", ");
+    print_vec("grid", grid, 40);
+    printf(", ");
+    print_vec("p0p1", p0p1, 100);
+    printf(", ");
+    print_vec("lnfX", lnfX, 3);
+    printf(", \"se\": [");
+    for (i = 0; i < n; i++) {
+        se = H[i * n + i] > 0. ? sqrt(H[i * n + i]) : -1;
+        printf("%s%.17g", i ? ", " : "", se);
+    }
+    printf("]}\n");
+    fflush(stdout);
+    free(post); free(g); free(H);
 }
 
 static void mode_dump(void) {
@@ -197,6 +243,10 @@ int __wrap_ming2(FILE *fout, double *f, objective_t fun, gradient_t dfun, double
     }
     if (mode && !strcmp(mode, "dump")) {
         mode_dump();
+        exit(0);
+    }
+    if (mode && !strcmp(mode, "sites")) {
+        mode_sites(fun, x, n);
         exit(0);
     }
     /* a full fit: ming2 as codeml calls it (finite differences) or with

@@ -13,6 +13,8 @@ CUDA_Init:
   branch-site models A and B and clade models C and D; the adapter's GB_dfun
   must equal codeml's central-difference gradient (gradientB with
   AlwaysCenter, tools.c:6326-6350) within its step error.
+* `sites`: the adapter's GB_BEB and GB_HessianSKT2004 inside codeml at the
+  fixture's x must give the BEB and the SEs the reference codeml printed.
 * `dfun` / unchanged: codeml's whole model-A fit, ming2 driven by GB_dfun
   (the one-argument change at codeml.c:688) or by its own finite differences
   of CUDA_lfundG, must reach the maximum codeml's CPU build reached
@@ -161,3 +163,40 @@ def test_codeml_itself_rejects_branch_site_models_on_partitioned_data():
                            timeout=300)
     assert r.returncode != 0
     assert "NSbranchsites with ngene" in r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", [n for n in golden_names() if not n.startswith("c5x120")])
+def test_dropin_beb_and_se_inside_codeml(name):
+    """The adapter's GB_BEB and GB_HessianSKT2004 inside codeml (harness mode
+    `sites`, at the fixture's x as final values): the BEB arrays codeml
+    prints from (lfunNSsites_ACD's postSite, the w0 / w2 grid posteriors,
+    postp0p1, log f(X); codeml.c:6697-6775) and the SEs from codeml's own
+    arithmetic after HessianSKT2004 (codeml.c:764-782), against what the
+    reference codeml printed for the same x (rst / out, print precision).
+    Not c5x120_s5: its zero-length branch is an initial value below codeml's
+    lower bound, which codeml moves to the bound before ming2 (the fixture's
+    own run fixed x with in.codeml's -1, where no bound applies)."""
+    from tests.test_beb_oracle import site_patterns
+    exe = dropin_binary()
+    fx, tree, codons = load_golden(name)
+    with tempfile.TemporaryDirectory() as d:
+        fixture_case(d, fx)
+        r = R.run(exe, d, "sites", timeout=900)
+    from oracle import oracle as O
+    z, fpatt, pi = O.patterns(codons)
+    assert r["npatt"] == len(fpatt)
+    assert abs(-r["f"] - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+    b = fx["beb"]
+    post = np.array(r["post"]).reshape(4, -1)
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(b["site_post_5dp"]))) <= 5.01e-6
+    grid = np.array(r["grid"])
+    assert np.max(np.abs(grid[20:30] - b["w0_post_3dp"])) <= 5.01e-4
+    assert np.max(np.abs(grid[30:40] - b["w2_post_3dp"])) <= 5.01e-4
+    assert np.max(np.abs(np.array(r["p0p1"]) - b["p0p1_post_3dp"])) <= 5.01e-4
+    assert abs(r["lnfX"][0] - b["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(b["lnfX_6dp"])
+    ref = np.array(fx["se_6dp"])
+    se = np.array(r["se"])
+    print(f"{name}: SE max rel diff {np.max(np.abs(se - ref) / np.abs(ref)):.1e}")
+    assert np.all(np.abs(se - ref) <= 5.01e-7 + 1e-4 * np.abs(ref))

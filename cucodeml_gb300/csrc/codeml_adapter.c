@@ -172,7 +172,8 @@ int GB_HessianSKT2004(double xmle[], double lnLm, double g[], double H[]) {
     gb_handle *h;
     const int n = com.np;
     (void)lnLm;
-    if (n != com.ntime + 5) gb_die("GB_HessianSKT2004 (model A parameter vector)", GB_ERR_ARG);
+    if (com.model != 2 || (n != com.ntime + 5 && n != com.ntime + 6))
+        gb_die("GB_HessianSKT2004 (branch-site models A and B)", GB_ERR_ARG);
     bnode = (int *)malloc(sizeof(int) * tree.nnode);
     if (!bnode) gb_die("GB_HessianSKT2004 (host memory)", GB_ERR_OOM);
     for (ib = 0; ib < tree.nnode; ib++)

@@ -141,17 +141,25 @@ int gb_se_opg(gb_handle *h, const int *bnode, const double *x, int n, double sma
     if (!h) return fail(GB_ERR_STATE, "null handle");
     if (h->precision != GB_PREC_FP64) return fail(GB_ERR_STATE, "gb_se_opg needs a GB_PREC_FP64 handle");
     const int nb = h->nnode - 1;
-    if (!bnode || !x || n != nb + 5 || !(small_diff > 0)) return fail(GB_ERR_ARG, "gb_se_opg: bad arguments");
+    // model A: x ends kappa, p0, p1, w0, w2; model B (n = nb + 6): ..., w0, w1, w2
+    if (!bnode || !x || (n != nb + 5 && n != nb + 6) || !(small_diff > 0))
+        return fail(GB_ERR_ARG, "gb_se_opg: bad arguments");
+    const int nm = n - nb;             // model parameters
+    const bool model_b = nm == 6;
     for (int ib = 0; ib < nb; ib++)
         if (bnode[ib] < 0 || bnode[ib] >= h->nnode || bnode[ib] == h->root) return fail(GB_ERR_ARG, "bnode");
     const double t0 = now_ms();
     std::vector<double> eh(n);
     for (int i = 0; i < n; i++) eh[i] = small_diff * 2 * (std::fabs(x[i]) + 1);
     // parameter blocks: [0] at x, [1 + 2 q + bf] with model parameter q moved by -eh (bf 0) / +eh (bf 1)
-    std::vector<DevParams> P(11);
+    std::vector<DevParams> P(1 + 2 * nm);
     std::vector<Derived> Dv(1);
     auto model_at = [&](const double *xv, DevParams *out) -> int {
-        ModelParams m{xv[nb], xv[nb + 3], xv[nb + 4], xv[nb + 1], xv[nb + 2]};
+        ModelParams m{xv[nb], xv[nb + 3], xv[n - 1], xv[nb + 1], xv[nb + 2]};
+        if (model_b) {
+            m.w1 = xv[nb + 4];
+            m.free_w1 = true;
+        }
         int rc = derive(h->pi.data(), m, false, &Dv[0]);
         if (rc) return fail(rc, "model parameters out of range");
         to_devparams(Dv[0], out);
@@ -160,7 +168,7 @@ int gb_se_opg(gb_handle *h, const int *bnode, const double *x, int n, double sma
     int rc = model_at(x, &P[0]);
     if (rc) return rc;
     std::vector<double> xs(x, x + n);
-    for (int q = 0; q < 5; q++)
+    for (int q = 0; q < nm; q++)
         for (int bf = 0; bf < 2; bf++) {
             xs[nb + q] = x[nb + q] + (bf ? eh[nb + q] : -eh[nb + q]);
             rc = model_at(xs.data(), &P[1 + 2 * q + bf]);
@@ -243,7 +251,8 @@ int gb_se_opg(gb_handle *h, const int *bnode, const double *x, int n, double sma
 int gb_hessian_x(gb_handle *h, const int *bnode, int lastround, const double *x, int n, double rel_step,
                  double *H, double *se) {
     if (!h) return fail(GB_ERR_STATE, "null handle");
-    if (!bnode || !x || !H || n != h->nnode - 1 + 5) return fail(GB_ERR_ARG, "gb_hessian_x: bad arguments");
+    if (!bnode || !x || !H || (n != h->nnode - 1 + 5 && n != h->nnode - 1 + 6))
+        return fail(GB_ERR_ARG, "gb_hessian_x: bad arguments");
     if (!(rel_step > 0)) rel_step = 1e-5;
     std::vector<double> xs(x, x + n), gp(n), gm(n);
     double f = 0;

@@ -348,7 +348,8 @@ int gb_neb(gb_handle *h, const gb_params *prm, double *post, double *neg_lnL);
  *   x[n]: codeml's parameter vector as Forestry leaves it after the fit
  *         (codeml.c:713-729): branch lengths by branch index (bnode[ib] is the
  *         node of branch ib), kappa, p0, p1, w0, w2 (p0, p1 untransformed);
- *         n = nnode - 1 + 5.  small_diff: codeml's Small_Diff.
+ *         n = nnode - 1 + 5; branch-site model B: ..., w0, w1, w2 with
+ *         n = nnode - 1 + 6.  small_diff: codeml's Small_Diff.
  * Outputs (each may be NULL): g[n] = dlnL/dx from the same 2n evaluations,
  * H[n*n] (before codeml negates it), se[n].  The 2n FP64 evaluations run on
  * the device back to back.  Needs a GB_PREC_FP64 handle.  Returns

@@ -176,9 +176,9 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         out = open(os.path.join(d, "out.txt")).read()
         lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
         rst = open(os.path.join(d, "rst")).read()
-        if not model_b and not site_model and not clade:
+        if not site_model and not clade:
             with open(os.path.join(d, "codeml.ctl"), "w") as f:
-                f.write(CTL.replace("getSE = 0", "getSE = 1"))
+                f.write(ctl.replace("getSE = 0", "getSE = 1"))
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
     if clade_d:       # clade-D BEB: grid w0 in (0, 0.5), w1 in (0.5, 1.5), w2, w3 in (0, 3)
@@ -195,8 +195,10 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
             extra["beb"] = parse_beb(out, rst, r.stdout, ncls=3)
             extra["beb"]["site_wmean_sd_3dp"] = parse_site_meanw(rst)
     elif model_b:
+        k = out_se.index("SEs for parameters:")
         extra = {"model": "B", "ng86_4dp": parse_ng86(out, ns), "neb_site_post_5dp": parse_site_post(rst, "Naive"),
-                 "beb": parse_beb(out, rst, r.stdout)}
+                 "beb": parse_beb(out, rst, r.stdout),
+                 "se_6dp": [float(v) for v in out_se[k:].splitlines()[1].split()], "small_diff": 1e-6}
     else:
         k = out_se.index("SEs for parameters:")
         extra = {"beb": parse_beb(out, rst, r.stdout), "ng86_4dp": parse_ng86(out, ns),

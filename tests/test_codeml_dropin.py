@@ -166,7 +166,7 @@ def test_codeml_itself_rejects_branch_site_models_on_partitioned_data():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", [n for n in golden_names() if not n.startswith("c5x120")])
+@pytest.mark.parametrize("name", [n for n in golden_names() if not n.startswith("c5x120")] + model_b_names())
 def test_dropin_beb_and_se_inside_codeml(name):
     """The adapter's GB_BEB and GB_HessianSKT2004 inside codeml (harness mode
     `sites`, at the fixture's x as final values): the BEB arrays codeml
@@ -181,7 +181,7 @@ def test_dropin_beb_and_se_inside_codeml(name):
     exe = dropin_binary()
     fx, tree, codons = load_golden(name)
     with tempfile.TemporaryDirectory() as d:
-        fixture_case(d, fx)
+        fixture_case(d, fx, ctl=ctl_for(name))
         r = R.run(exe, d, "sites", timeout=900)
     from oracle import oracle as O
     z, fpatt, pi = O.patterns(codons)

@@ -18,17 +18,19 @@ import pytest
 
 from cucodeml_gb300 import api
 from oracle import oracle as O
-from tests.conftest import golden_names, load_golden
+from tests.conftest import golden_names, load_golden, model_b_names
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names() + model_b_names())
 def test_se_opg_matches_oracle_and_codeml(name):
+    """Models A and B (gb_se_opg takes model B's x, n = nbranch + 6)."""
     fx, tree, codons = load_golden(name)
     z, fpatt, pi = O.patterns(codons)
     x = np.array(fx["x"])
-    go, Ho, seo = O.Problem(tree, z, fpatt, pi, nthreads=4).opg_se(x, small_diff=fx["small_diff"])
+    go, Ho, seo = O.Problem(tree, z, fpatt, pi, nthreads=4,
+                            model_b=name.startswith("mb")).opg_se(x, small_diff=fx["small_diff"])
     lk = api.Likelihood(tree, z, fpatt, pi)
     r = lk.se_opg(x, small_diff=fx["small_diff"])
     assert np.array_equal(r["H"], r["H"].T)

@@ -23,3 +23,20 @@ def test_opg_se_matches_codeml(golden):
     assert np.all(np.abs(se - ref) <= 5.01e-7 + 5e-5 * np.abs(ref))
     assert np.array_equal(H, H.T)
     assert np.all(np.linalg.eigvalsh(-H) > -1e-8 * np.max(np.abs(H)))   # -H is a Gram matrix
+
+
+import pytest
+
+from tests.conftest import load_golden, model_b_names
+
+
+@pytest.mark.parametrize("name", model_b_names())
+def test_opg_se_matches_codeml_model_b(name):
+    """The same estimator under branch-site model B (x ends w0, w1, w2)."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=4, model_b=True)
+    g, H, se = pb.opg_se(np.array(fx["x"]), small_diff=fx["small_diff"])
+    ref = np.array(fx["se_6dp"])
+    assert se.shape == ref.shape
+    assert np.all(np.abs(se - ref) <= 5.01e-7 + 5e-5 * np.abs(ref))

@@ -40,7 +40,8 @@
  *                                  H at codeml's x, H before codeml negates
  *                                  it), its 2 np likelihood evaluations on the
  *                                  GPU; call it in place of HessianSKT2004 at
- *                                  codeml.c:764 for getSE = 1.
+ *                                  codeml.c:764 for getSE = 1 (branch-site
+ *                                  models A and B).
  *
  * CUDA_lfundG and CUDA_fx_r stay codeml's own (treesub.c:7397, 7554).  On any
  * library error these functions print the library's message and exit(-1), as

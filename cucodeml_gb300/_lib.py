@@ -79,6 +79,8 @@ SIGNATURES = {
                             C.POINTER(Stats)]),
     "gb_beb": (C.c_int, [C.c_void_p, C.POINTER(Params), _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)]),
     "gb_beb_clade": (C.c_int, [C.c_void_p, C.c_int, _dp, _dp, _dp, _dp, _dp, C.POINTER(Stats)]),
+    "gb_beb_clade_bl": (C.c_int, [C.c_void_p, C.c_int, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp,
+                                  C.POINTER(Stats)]),
     "gb_beb_tables": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, _dp, _dp, _dp, C.POINTER(Stats)]),
     "gb_beb_qf": (C.c_int, [C.c_void_p, _dp, C.c_double, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _dp,
                             C.POINTER(Stats)]),

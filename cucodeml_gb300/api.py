@@ -500,15 +500,24 @@ class Likelihood:
 
     def beb_clade_c(self, blength, kappa, qfactor) -> dict:
         """codeml's BEB under clade model C with two branch types at the MLE
-        (Qfactors qfactor of the two branch types): the 111 omega sets from two
-        gb_beb_tables calls (w0 grid in (0, 1); then the (0, 3) grids of w2 and
-        w3 in eigen slots 0 and 2) and the 10^5-point grid integral, all on the
-        device."""
-        g01 = (np.arange(10) + 0.5) / 10
-        g03 = 0 + (np.arange(10) + 0.5) * (3 - 0) / 10
-        a = self.beb_tables(blength, kappa, qfactor, g01, g03)
-        b = self.beb_tables(blength, kappa, qfactor, g03, g03)
-        return self.beb_clade(np.concatenate([a[:11], b[11:111]]), model_d=False)
+        (Qfactors qfactor of the two branch types; gb_beb_clade_bl): the 111
+        omega sets from two gb_beb_tables calls (w0 grid in (0, 1); then the
+        (0, 3) grids of w2 and w3 in eigen slots 0 and 2) and the 10^5-point
+        grid integral, all on the device."""
+        return self._beb_clade_bl(blength, kappa, qfactor, False)
+
+    def _beb_clade_bl(self, blength, kappa, qfactor, model_d):
+        bl = np.ascontiguousarray(blength, dtype=np.float64)
+        qf = np.ascontiguousarray(qfactor, dtype=np.float64)
+        post = np.zeros((3, self.npatt))
+        grid = np.zeros((4, 10))
+        p0p1 = np.zeros(100)
+        fx = np.zeros(3)
+        st = _lib.Stats()
+        _lib.check(self._L.gb_beb_clade_bl(self._h, int(bool(model_d)), _ptr(bl), float(kappa), _ptr(qf),
+                                           _ptr(post), _ptr(grid), _ptr(p0p1), _ptr(fx), C.byref(st)))
+        return {"post": post, "grid": grid, "p0p1": p0p1, "lnfX": float(fx[0]), "S1": float(fx[1]),
+                "S2": float(fx[2]), "ms_device": st.ms_device}
 
     def beb_clade_d(self, blength, kappa, qfactor) -> dict:
         """codeml's BEB under clade model D with two branch types at the MLE:
@@ -516,11 +525,7 @@ class Likelihood:
         in (0, 3) by branch type; get_grid_para_like_ACD codeml.c:6457-6473)
         from three gb_beb_tables calls, and the 10^6-point grid integral, on
         the device."""
-        g = (np.arange(10) + 0.5) / 10
-        a = self.beb_tables(blength, kappa, qfactor, 0.5 * g, 3 * g)
-        b = self.beb_tables(blength, kappa, qfactor, 0.5 + g, 3 * g)
-        c = self.beb_tables(blength, kappa, qfactor, 3 * g, 3 * g)
-        return self.beb_clade(np.concatenate([a[:10], b[:10], c[11:111]]), model_d=True)
+        return self._beb_clade_bl(blength, kappa, qfactor, True)
 
     def beb_x(self, x, lastround: bool = True, want_lnfw: bool = False) -> dict:
         """beb() from codeml's x vector."""

@@ -27,6 +27,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <vector>
 
 #include "gbcodeml.h"
@@ -265,4 +266,42 @@ int gb_beb_clade(gb_handle *h, int model_d, const double *lnfw, double *post_out
         stats->d2h_bytes = sizeof(double) * ((double)npatt + c.ngrid + (post_out ? 3.0 * npatt : 0));
     }
     return GB_OK;
+}
+
+// The whole clade BEB from the branch lengths, kappa and the branch types'
+// Qfactors at the MLE (as codeml's lfunNSsites_ACD reads them): the log f
+// tables from gb_beb_tables on the clade grids (get_grid_para_like_ACD
+// codeml.c:6457-6473) -- clade C: sets 0..10 from w0 in (0, 1) and w = 1,
+// 11..110 from the (0, 3) grids of w2 and w3; clade D: w0 in (0, 0.5), w1 in
+// (0.5, 1.5), then the (0, 3) pairs -- followed by gb_beb_clade.
+int gb_beb_clade_bl(gb_handle *h, int model_d, const double *blength, double kappa, const double qfactor[2],
+                    double *post, double *grid, double *p0p1, double *lnfX, gb_stats *stats) {
+    using namespace gb;
+    if (!h) return fail(GB_ERR_STATE, "null handle");
+    if (!blength || !qfactor) return fail(GB_ERR_ARG, "null argument");
+    const size_t np = (size_t)h->npatt;
+    const int nsets = model_d ? 120 : 111;
+    std::vector<double> t((size_t)121 * np), L((size_t)nsets * np);
+    double g[GB_BEB_GRID], ga[GB_BEB_GRID], gb3[GB_BEB_GRID];
+    for (int k = 0; k < GB_BEB_GRID; k++) {
+        g[k] = (k + 0.5) / GB_BEB_GRID;
+        gb3[k] = 3.0 * g[k];
+    }
+    // rows [r0, r1) of one gb_beb_tables call into L from row dst
+    auto tables = [&](const double *w0, const double *w2, int r0, int r1, int dst) -> int {
+        const int rc = gb_beb_tables(h, blength, kappa, qfactor, w0, w2, t.data(), nullptr);
+        if (rc) return rc;
+        std::copy(t.begin() + (size_t)r0 * np, t.begin() + (size_t)r1 * np, L.begin() + (size_t)dst * np);
+        return 0;
+    };
+    int rc;
+    if (!model_d) {
+        if ((rc = tables(g, gb3, 0, 11, 0)) || (rc = tables(gb3, gb3, 11, 111, 11))) return rc;
+    } else {
+        for (int k = 0; k < GB_BEB_GRID; k++) ga[k] = 0.5 * g[k];
+        if ((rc = tables(ga, gb3, 0, 10, 0))) return rc;
+        for (int k = 0; k < GB_BEB_GRID; k++) ga[k] = 0.5 + g[k];
+        if ((rc = tables(ga, gb3, 0, 10, 10)) || (rc = tables(gb3, gb3, 11, 111, 20))) return rc;
+    }
+    return gb_beb_clade(h, model_d, L.data(), post, grid, p0p1, lnfX, stats);
 }

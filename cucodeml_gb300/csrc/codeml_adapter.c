@@ -149,17 +149,31 @@ int GB_BEB(double x[], int np, double postSite[], double grid[], double p0p1[], 
     gb_handle *h;
     double *bl;
     if (np < com.ntime + 1) gb_die("GB_BEB (parameter vector)", GB_ERR_ARG);
-    /* model A's grid (lfunNSsites_ACD uses it for model = 2, A and B); the
-       clade models' grids differ */
-    if (com.model != 2) gb_die("GB_BEB (branch-site models A and B only)", GB_ERR_ARG);
+    if (!(com.model == 2 || (com.model == 3 && com.nbtype == 2)))
+        gb_die("GB_BEB (branch-site models A and B, clade models C and D with two branch types)", GB_ERR_ARG);
     bl = (double *)calloc(tree.nnode, sizeof(double));
     if (!bl) gb_die("GB_BEB (host memory)", GB_ERR_OOM);
     for (i = 0; i < tree.nnode; i++)
         if (i != tree.root) bl[i] = x[nodes[i].ibranch];
     h = make_handle("GB_BEB (one gene, universal code only)");
     /* kappa from x, the Qfactors of the last SetParameters (at the MLE), as
-       codeml's BEB reads them (GetPMatBranch treesub.c:7289-7301): models A and B */
-    rc = gb_beb_qf(h, bl, x[com.ntime], Qfactor_NS_branch, NULL, postSite, grid, p0p1, lnfX, NULL, NULL, NULL);
+       codeml's BEB reads them (GetPMatBranch treesub.c:7289-7301) */
+    if (com.model == 2) {
+        /* models A and B: model A's grid; postSite[4*npatt], grid rows w0, w2 at [20..39] */
+        rc = gb_beb_qf(h, bl, x[com.ntime], Qfactor_NS_branch, NULL, postSite, grid, p0p1, lnfX, NULL, NULL, NULL);
+    } else {
+        /* clade models C and D: postSite[3*npatt]; grid as lfunNSsites_ACD's
+           postpara rows (dim x 10): p0, p1 (-1, ternary), w0, [w1 under D], w2, w3 */
+        const int d = com.NSsites == 3, dim = 5 + d;
+        double g4[40];
+        int k, r;
+        rc = gb_beb_clade_bl(h, d, bl, x[com.ntime], Qfactor_NS_branch, postSite, g4, p0p1, lnfX, NULL);
+        for (r = 0; r < dim; r++)
+            for (k = 0; k < 10; k++) {
+                const int src = r < 2 ? -1 : (r == 2 ? 0 : (d && r == 3 ? 1 : r - 3 - d + 2));
+                grid[r * 10 + k] = src < 0 ? -1.0 : g4[src * 10 + k];
+            }
+    }
     gb_destroy(h);
     free(bl);
     if (rc) gb_die("gb_beb", rc);

@@ -330,6 +330,13 @@ int gb_beb_tables(gb_handle *h, const double *blength, double kappa, const doubl
 int gb_beb_clade(gb_handle *h, int model_d, const double *lnfw, double *post, double *grid, double *p0p1,
                  double *lnfX, gb_stats *stats);
 
+/* The whole clade-C / clade-D BEB at the MLE: the log f tables of
+   gb_beb_clade from gb_beb_tables on the clade grids (branch lengths in
+   node order, kappa and the branch types' Qfactors as codeml's
+   lfunNSsites_ACD reads them), then gb_beb_clade; outputs as there. */
+int gb_beb_clade_bl(gb_handle *h, int model_d, const double *blength, double kappa, const double qfactor[2],
+                    double *post, double *grid, double *p0p1, double *lnfX, gb_stats *stats);
+
 /*
  * Naive empirical Bayes (NEB) posteriors of the four site classes at prm, as
  * codeml's lfunNSsites_rate prints them ("Naive Empirical Bayes (NEB)

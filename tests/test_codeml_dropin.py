@@ -200,3 +200,33 @@ def test_dropin_beb_and_se_inside_codeml(name):
     se = np.array(r["se"])
     print(f"{name}: SE max rel diff {np.max(np.abs(se - ref) / np.abs(ref)):.1e}")
     assert np.all(np.abs(se - ref) <= 5.01e-7 + 1e-4 * np.abs(ref))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+def test_dropin_clade_beb_inside_codeml(name):
+    """The adapter's GB_BEB under clade models C and D inside codeml (harness
+    mode `sites`): the three-class site posteriors, the w0 / (w1) / w2 / w3
+    rows of lfunNSsites_ACD's postpara, postp0p1 and log f(X) against what the
+    reference codeml printed for the same x."""
+    from tests.test_beb_oracle import site_patterns
+    exe = dropin_binary()
+    fx, tree, codons = load_golden(name)
+    with tempfile.TemporaryDirectory() as d:
+        fixture_case(d, fx, ctl=ctl_for(name))
+        r = R.run(exe, d, "sites", timeout=900)
+    from oracle import oracle as O
+    z, fpatt, pi = O.patterns(codons)
+    assert r["ncls"] == 3
+    assert abs(-r["f"] - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+    b = fx["beb"]
+    post = np.array(r["post"]).reshape(3, -1)
+    site = post[:, site_patterns(z, codons)].T
+    assert np.max(np.abs(site - np.array(b["site_post_5dp"]))) <= 5.01e-6
+    grid = np.array(r["grid"]).reshape(-1, 10)
+    assert np.all(grid[:2] == -1.0)
+    rows = ["w0_post_3dp"] + (["w1_post_3dp"] if name.startswith("mcD") else []) + ["w2_post_3dp", "w3_post_3dp"]
+    for i, key in enumerate(rows):
+        assert np.max(np.abs(grid[2 + i] - b[key])) <= 5.01e-4, key
+    assert np.max(np.abs(np.array(r["p0p1"]) - b["p0p1_post_3dp"])) <= 5.01e-4
+    assert abs(r["lnfX"][0] - b["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(b["lnfX_6dp"])

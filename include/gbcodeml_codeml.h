@@ -25,7 +25,10 @@
  *                                  C and D); pass it instead of NULL at
  *                                  codeml.c:688.
  *   GB_BEB                         new: the Bayes empirical Bayes analysis of
- *                                  models A and B on the GPU at codeml's final
+ *                                  models A and B (and of the clade models C
+ *                                  and D: postSite[3*npatt], grid = the
+ *                                  postpara rows p0, p1 (-1), w0, [w1], w2,
+ *                                  w3) on the GPU at codeml's final
  *                                  x (kappa and branch lengths; the Qfactors
  *                                  are codeml's Qfactor_NS_branch, as its BEB
  *                                  reads them): fills

@@ -69,6 +69,8 @@ SIGNATURES = {
     "gb_beta_classes": (C.c_int, [C.c_double, C.c_double, C.c_int, _dp, _dp]),
     "gb_eval_clade": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp, _dp, _dp,
                                 C.POINTER(Stats)]),
+    "gb_se_opg_clade": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, _dp, C.c_int, C.c_double, _dp, _dp,
+                                  _dp]),
     "gb_neb_clade": (C.c_int, [C.c_void_p, _dp, C.c_double, C.c_double, C.c_double, _dp, _dp, _dp]),
     "gb_dfun_clade_x": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.c_int, C.c_int, _dp, C.c_int, _dp, _dp]),
     "gb_eval_clade_uvr": (C.c_int, [C.c_void_p, _dp * 4, _dp * 4, _dp * 4, _dp, _dp, _dp, _dp, _dp, _dp,

@@ -556,6 +556,18 @@ class Likelihood:
         return {"g": g, "H": H, "se": se, "ms_device": st.ms_device, "ms_host": st.ms_host,
                 "kernels": st.kernels}
 
+    def se_opg_clade(self, x, model_d: bool = False, small_diff: float = 1e-6) -> dict:
+        """codeml's standard errors under clade model C / D at codeml's x
+        (untransformed p0, p1; gb_se_opg_clade): g, H (before negation), se."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        n = len(x)
+        g = np.zeros(n)
+        H = np.zeros((n, n))
+        se = np.zeros(n)
+        _lib.check(self._L.gb_se_opg_clade(self._h, self.bnode.ctypes.data_as(C.POINTER(C.c_int)), int(model_d),
+                                           _ptr(x), n, float(small_diff), _ptr(g), _ptr(H), _ptr(se)))
+        return {"g": g, "H": H, "se": se}
+
     def hessian_x(self, x, lastround: bool = True, rel_step: float = 0.0):
         """(H, se): the Hessian of -lnL over codeml's x by central differences
         of the analytic gradient (gb_hessian_x) and the SEs from its inverse."""

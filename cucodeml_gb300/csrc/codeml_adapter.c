@@ -186,14 +186,17 @@ int GB_HessianSKT2004(double xmle[], double lnLm, double g[], double H[]) {
     gb_handle *h;
     const int n = com.np;
     (void)lnLm;
-    if (com.model != 2 || (n != com.ntime + 5 && n != com.ntime + 6))
-        gb_die("GB_HessianSKT2004 (branch-site models A and B)", GB_ERR_ARG);
+    const int clade = com.model == 3;
+    if (!((com.model == 2 && (n == com.ntime + 5 || n == com.ntime + 6)) ||
+          (clade && com.nbtype == 2 && n == com.ntime + (com.NSsites == 3 ? 7 : 6))))
+        gb_die("GB_HessianSKT2004 (branch-site models A and B, clade models C and D)", GB_ERR_ARG);
     bnode = (int *)malloc(sizeof(int) * tree.nnode);
     if (!bnode) gb_die("GB_HessianSKT2004 (host memory)", GB_ERR_OOM);
     for (ib = 0; ib < tree.nnode; ib++)
         if (ib != tree.root) bnode[nodes[ib].ibranch] = ib;
     h = make_handle("GB_HessianSKT2004 (one gene, universal code only)");
-    rc = gb_se_opg(h, bnode, xmle, n, Small_Diff, g, H, NULL, NULL);
+    rc = clade ? gb_se_opg_clade(h, bnode, com.NSsites == 3, xmle, n, Small_Diff, g, H, NULL)
+               : gb_se_opg(h, bnode, xmle, n, Small_Diff, g, H, NULL, NULL);
     gb_destroy(h);
     free(bnode);
     if (rc) gb_die("gb_se_opg", rc);

@@ -274,3 +274,50 @@ int gb_hessian_x(gb_handle *h, const int *bnode, int lastround, const double *x,
         }
     return se ? standard_errors(H, n, se) : 0;
 }
+
+// codeml's getSE = 1 estimator under the clade models C and D: x = branch
+// lengths (codeml's branch order), kappa, p0, p1 (untransformed), w0, [w1
+// under D], w2, w3.  The 2n evaluations are gb_eval_clade calls (one graph
+// each), their per-pattern log f copied back; the scores and the outer
+// product on the host (n^2 npatt operations).
+int gb_se_opg_clade(gb_handle *h, const int *bnode, int model_d, const double *x, int n, double small_diff,
+                    double *g, double *H_out, double *se) {
+    if (!h) return fail(GB_ERR_STATE, "null handle");
+    const int nb = h->nnode - 1;
+    if (!bnode || !x || n != nb + (model_d ? 7 : 6) || !(small_diff > 0))
+        return fail(GB_ERR_ARG, "gb_se_opg_clade: bad arguments");
+    const int np = h->npatt;
+    std::vector<double> eh(n), xs(x, x + n), bl(h->nnode, 0.0), lnf(np);
+    std::vector<double> D((size_t)n * np), lnL(2 * n);
+    for (int i = 0; i < n; i++) eh[i] = small_diff * 2 * (std::fabs(x[i]) + 1);
+    for (int i = 0; i < n; i++)
+        for (int bf = 0; bf < 2; bf++) {
+            xs[i] = x[i] + (bf ? eh[i] : -eh[i]);
+            for (int ib = 0; ib < nb; ib++) {
+                if (bnode[ib] < 0 || bnode[ib] >= h->nnode || bnode[ib] == h->root) return fail(GB_ERR_ARG, "bnode");
+                bl[bnode[ib]] = xs[ib] > 0.0 ? xs[ib] : 0.0;     // a length moved below zero acts as zero
+            }
+            const double om[4] = {xs[nb + 3], model_d ? xs[nb + 4] : 1.0, xs[n - 2], xs[n - 1]};
+            double f = 0;
+            const int rc = gb_eval_clade(h, bl.data(), xs[nb], xs[nb + 1], xs[nb + 2], om, &f, nullptr, nullptr,
+                                         lnf.data(), nullptr);
+            xs[i] = x[i];
+            if (rc) return rc;
+            lnL[bf * n + i] = -f;
+            for (int hh = 0; hh < np; hh++) D[(size_t)i * np + hh] += (bf ? lnf[hh] : -lnf[hh]) / (2 * eh[i]);
+        }
+    std::vector<double> H((size_t)n * n);
+    const double *fp = h->fpatt.data();
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j <= i; j++) {
+            double s = 0;
+            for (int hh = 0; hh < np; hh++) s += fp[hh] * D[(size_t)i * np + hh] * D[(size_t)j * np + hh];
+            H[(size_t)i * n + j] = H[(size_t)j * n + i] = -s;
+        }
+    if (g)
+        for (int i = 0; i < n; i++) g[i] = (lnL[n + i] - lnL[i]) / (2 * eh[i]);
+    if (H_out) std::memcpy(H_out, H.data(), sizeof(double) * H.size());
+    if (!se) return GB_OK;
+    for (double &v : H) v = -v;
+    return standard_errors(H.data(), n, se);
+}

@@ -365,6 +365,13 @@ int gb_neb(gb_handle *h, const gb_params *prm, double *post, double *neg_lnL);
 int gb_se_opg(gb_handle *h, const int *bnode, const double *x, int n, double small_diff, double *g,
               double *H, double *se, gb_stats *stats);
 
+/* gb_se_opg under the clade models C (model_d = 0) and D: x = branch
+   lengths (bnode as there), kappa, p0, p1 (untransformed), w0, [w1 under D],
+   w2, w3; n = nnode - 1 + 6 (C) or + 7 (D).  The 2n evaluations are
+   gb_eval_clade calls.  FP64 handles. */
+int gb_se_opg_clade(gb_handle *h, const int *bnode, int model_d, const double *x, int n, double small_diff,
+                    double *g, double *H, double *se);
+
 /*
  * The Hessian of -lnL over codeml's x (the layout and p0/p1 convention of
  * gb_dfun_x) by central differences of the analytic gradient, step

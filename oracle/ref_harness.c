@@ -33,9 +33,8 @@
  *            nChara / CharaMap of SetMapAmbiguity treesub.c:1146-1200); then
  *            exits.
  *   sites    at x as final values (LASTROUND = 1), the adapter's GB_BEB and
- *            (models A, B) GB_HessianSKT2004 with codeml's SE arithmetic
- *            after it; prints the BEB arrays, log f(X) and the SEs, then
- *            exits.
+ *            GB_HessianSKT2004 with codeml's SE arithmetic after it; prints
+ *            the BEB arrays, log f(X) and the SEs, then exits.
  *   dfun     runs ming2 with the adapter's GB_dfun as its gradient hook
  *            (the one-argument change at codeml.c:688 that the drop-in
  *            enables), then codeml continues as usual.
@@ -172,7 +171,7 @@ static void mode_eval(objective_t fun, double x[], int n) {
    codeml's own SE arithmetic (H negated, matinv, sqrt of the diagonal,
    codeml.c:778-782) */
 static void mode_sites(objective_t fun, double x[], int n) {
-    /* clade models (model = 3): three classes, grid rows p0, p1, w0, [w1], w2, w3; no SEs */
+    /* clade models (model = 3): three classes, grid rows p0, p1, w0, [w1], w2, w3 */
     const int clade = com.model == 3, ncls = clade ? 3 : 4, ngrid = clade ? 10 * (5 + (com.NSsites == 3)) : 40;
     const int np4 = ncls * com.npatt;
     double *post = (double *)malloc(sizeof(double) * 4 * com.npatt), grid[60], p0p1[100], lnfX[3];
@@ -184,11 +183,9 @@ static void mode_sites(objective_t fun, double x[], int n) {
     LASTROUND = 1;
     f = fun(x, n);
     GB_BEB(x, n, post, grid, p0p1, lnfX);
-    if (!clade) {
-        GB_HessianSKT2004(x, -f, g, H);
-        for (i = 0; i < n * n; i++) H[i] *= -1;
-        matinv(H, n, n, H + n * n);
-    }
+    GB_HessianSKT2004(x, -f, g, H);
+    for (i = 0; i < n * n; i++) H[i] *= -1;
+    matinv(H, n, n, H + n * n);
     printf("\nGBREF {\"mode\": \"sites\", \"np\": %d, \"npatt\": %d, \"ncls\": %d, \"f\": %.17g, ", n,
            com.npatt, ncls, f);
     print_vec("post", post, np4);
@@ -199,7 +196,7 @@ static void mode_sites(objective_t fun, double x[], int n) {
     printf(", ");
     print_vec("lnfX", lnfX, 3);
     printf(", \"se\": [");
-    for (i = 0; i < (clade ? 0 : n); i++) {
+    for (i = 0; i < n; i++) {
         se = H[i * n + i] > 0. ? sqrt(H[i * n + i]) : -1;
         printf("%s%.17g", i ? ", " : "", se);
     }

@@ -176,17 +176,20 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         out = open(os.path.join(d, "out.txt")).read()
         lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
         rst = open(os.path.join(d, "rst")).read()
-        if not site_model and not clade:
+        if not site_model:
             with open(os.path.join(d, "codeml.ctl"), "w") as f:
                 f.write(ctl.replace("getSE = 0", "getSE = 1"))
             subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
             out_se = open(os.path.join(d, "out.txt")).read()
+    if clade:
+        k = out_se.index("SEs for parameters:")
+        se = {"se_6dp": [float(v) for v in out_se[k:].splitlines()[1].split()], "small_diff": 1e-6}
     if clade_d:       # clade-D BEB: grid w0 in (0, 0.5), w1 in (0.5, 1.5), w2, w3 in (0, 3)
         extra = {"model": "D", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3),
-                 "neb_site_post_5dp": parse_site_post(rst, "Naive", ncls=3)}
+                 "neb_site_post_5dp": parse_site_post(rst, "Naive", ncls=3), **se}
     elif clade:
         extra = {"model": "C", "ng86_4dp": parse_ng86(out, ns), "beb": parse_beb(out, rst, r.stdout, ncls=3),
-                 "neb_site_post_5dp": parse_site_post(rst, "Naive", ncls=3)}
+                 "neb_site_post_5dp": parse_site_post(rst, "Naive", ncls=3), **se}
     elif site_model:
         ncat = {"M1a": 2, "M2a": 3, "M3": 3, "M7": 10, "M8": 11}[site_model]
         extra = {"model": site_model, "ng86_4dp": parse_ng86(out, ns),

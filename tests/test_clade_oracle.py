@@ -105,3 +105,37 @@ def test_clade_neb_matches_codeml(name):
     post = q / q.sum(axis=0)
     site = post[:, site_patterns(z, codons)].T
     assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6
+
+
+def clade_opg_se(pb, x, small_diff):
+    """codeml's getSE = 1 estimator (HessianSKT2004 treesub.c:6979-7048) over
+    the oracle's clade evaluation: per-pattern scores from central
+    differences of log f_h, step 2 small_diff (|x_i| + 1)."""
+    n = len(x)
+    eh = 2 * small_diff * (np.abs(x) + 1)
+    D = []
+    for i in range(n):
+        f = []
+        for s in (-1, 1):
+            x1 = x.copy()
+            x1[i] += s * eh[i]
+            f.append(pb.clade_c(x1)[2])
+        D.append((f[1] - f[0]) / (2 * eh[i]))
+    D = np.array(D)
+    H = -(D * pb.fpatt[None, :]) @ D.T
+    V = np.linalg.inv(-0.5 * (H + H.T))
+    dg = np.diag(V)
+    return np.where(dg > 0, np.sqrt(np.abs(dg)), -1.0)
+
+
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+def test_clade_se_matches_codeml(name):
+    """codeml's SEs under the clade models (getSE = 1), restated over the
+    oracle's clade evaluation: print rounding plus 5e-5 of the value."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    pb = O.Problem(tree, z, fpatt, pi, nthreads=2, model_b=name.startswith("mcD"))
+    se = clade_opg_se(pb, np.array(fx["x"]), fx["small_diff"])
+    ref = np.array(fx["se_6dp"])
+    assert se.shape == ref.shape
+    assert np.all(np.abs(se - ref) <= 5.01e-7 + 5e-5 * np.abs(ref))

@@ -205,10 +205,10 @@ def test_dropin_beb_and_se_inside_codeml(name):
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", clade_names() + clade_d_names())
 def test_dropin_clade_beb_inside_codeml(name):
-    """The adapter's GB_BEB under clade models C and D inside codeml (harness
-    mode `sites`): the three-class site posteriors, the w0 / (w1) / w2 / w3
-    rows of lfunNSsites_ACD's postpara, postp0p1 and log f(X) against what the
-    reference codeml printed for the same x."""
+    """The adapter's GB_BEB and GB_HessianSKT2004 under clade models C and D
+    inside codeml (harness mode `sites`): the three-class site posteriors, the
+    w0 / (w1) / w2 / w3 rows of lfunNSsites_ACD's postpara, postp0p1, log f(X)
+    and the SEs against what the reference codeml printed for the same x."""
     from tests.test_beb_oracle import site_patterns
     exe = dropin_binary()
     fx, tree, codons = load_golden(name)
@@ -230,3 +230,5 @@ def test_dropin_clade_beb_inside_codeml(name):
         assert np.max(np.abs(grid[2 + i] - b[key])) <= 5.01e-4, key
     assert np.max(np.abs(np.array(r["p0p1"]) - b["p0p1_post_3dp"])) <= 5.01e-4
     assert abs(r["lnfX"][0] - b["lnfX_6dp"]) <= 5.01e-7 + 1e-12 * abs(b["lnfX_6dp"])
+    ref = np.array(fx["se_6dp"])
+    assert np.all(np.abs(np.array(r["se"]) - ref) <= 5.01e-7 + 1e-4 * np.abs(ref))

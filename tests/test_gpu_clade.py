@@ -352,3 +352,18 @@ def test_clade_neb_matches_codeml(name):
     assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6
     assert np.allclose(post.sum(axis=0), 1.0, atol=1e-13)
     assert abs(-f - fx["codeml_lnL"]) / abs(fx["codeml_lnL"]) <= 1e-9
+
+
+@pytest.mark.parametrize("name", clade_names() + clade_d_names())
+def test_clade_se_matches_codeml(name):
+    """gb_se_opg_clade (codeml's getSE = 1 estimator over 2 np clade
+    evaluations) against codeml's printed SEs: print rounding plus 1e-4 of
+    the value, as for model A."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    lk = api.Likelihood(tree, z, fpatt, pi)
+    r = lk.se_opg_clade(np.array(fx["x"]), model_d=name.startswith("mcD"), small_diff=fx["small_diff"])
+    lk.close()
+    ref = np.array(fx["se_6dp"])
+    assert np.array_equal(r["H"], r["H"].T)
+    assert np.all(np.abs(r["se"] - ref) <= 5.01e-7 + 1e-4 * np.abs(ref))

@@ -131,3 +131,17 @@ def test_m3_gradient_through_model_b(precision):
     print(f"M3 via model B ({precision}): max rel err {err.max():.2e}")
     assert err.max() <= 1e-5
     lk.close()
+
+
+@pytest.mark.parametrize("name", [n for n in site_model_names() if n.startswith(("msM2a", "msM3"))])
+def test_site_model_se_matches_codeml(name):
+    """gb_se_opg on the all-foreground tree gives codeml's SEs under M2a
+    (model A's x) and M3 (model B's x): print rounding plus 1e-4."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, x = as_model_a(fx, tree)
+    lk = api.Likelihood(t, z, fpatt, pi)
+    r = lk.se_opg(x, small_diff=fx["small_diff"])
+    lk.close()
+    ref = np.array(fx["se_6dp"])
+    assert np.all(np.abs(r["se"] - ref) <= 5.01e-7 + 1e-4 * np.abs(ref))

@@ -97,3 +97,17 @@ def test_site_model_neb_matches_codeml(name):
     post = q / q.sum(axis=0)
     site = post[:, site_patterns(z, codons)].T
     assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6
+
+
+@pytest.mark.parametrize("name", [n for n in site_model_names() if n.startswith(("msM2a", "msM3"))])
+def test_site_model_se_matches_codeml(name):
+    """codeml's SEs (getSE = 1) under M2a and M3: their x is model A's /
+    model B's on the all-foreground tree, so the model-A / model-B estimator
+    gives them (print rounding plus 5e-5 of the value)."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, x = as_model_a(fx, tree)
+    pb = O.Problem(t, z, fpatt, pi, nthreads=4, model_b=fx["model"] == "M3")
+    g, H, se = pb.opg_se(x, small_diff=fx["small_diff"])
+    ref = np.array(fx["se_6dp"])
+    assert np.all(np.abs(se - ref) <= 5.01e-7 + 5e-5 * np.abs(ref))

@@ -277,6 +277,65 @@ class Likelihood:
             lnf = np.log(np.where(sm <= 0, 1e-300, sm))
         return -float((lnf * self._fpatt).sum()), fhK, lnf
 
+    def site_classes_x(self, x, model: str):
+        """(blength in node order, kappa, omegas, props) of a site model at
+        codeml's x (branch lengths in codeml's branch order, then M1a: kappa,
+        p0, w0; M2a: kappa, p0, p1, w0, w2; M3 (three classes): kappa, p0,
+        p1, w0, w1, w2; M7: kappa, p, q; M8: kappa, p0, p, q, ws)."""
+        x = np.asarray(x, dtype=np.float64)
+        nb = self.nnode - 1
+        bl = np.zeros(self.nnode)
+        bl[self.bnode] = x[:nb]
+        k, r = x[nb], x[nb + 1:]
+        if model == "M1a":
+            om, pr = np.array([r[1], 1.0]), np.array([r[0], 1 - r[0]])
+        elif model == "M2a":
+            om, pr = np.array([r[2], 1.0, r[3]]), np.array([r[0], r[1], 1 - r[0] - r[1]])
+        elif model == "M3":
+            om, pr = np.array(r[2:5]), np.array([r[0], r[1], 1 - r[0] - r[1]])
+        elif model == "M7":
+            om, pr = beta_classes(r[0], r[1])
+        elif model == "M8":
+            om, pr = beta_classes(r[1], r[2])
+            om, pr = np.append(om, r[3]), np.append(pr * r[0], 1 - r[0])
+        else:
+            raise ValueError("site model: M1a, M2a, M3, M7 or M8")
+        return bl, k, om, pr
+
+    def se_opg_site(self, x, model: str, small_diff: float = 1e-6) -> dict:
+        """codeml's standard errors (getSE = 1, HessianSKT2004 treesub.c:
+        6979-7048) under a site model at codeml's x (site_classes_x; the
+        proportions untransformed): per-pattern scores from central
+        differences of log f_h, step 2 small_diff (|x_i| + 1), over 2 n
+        site_model evaluations on the device; H = -sum_h fpatt_h s_h s_h^T,
+        SE_i = sqrt([(-H)^-1]_ii) (-1 where not positive).  Needs the
+        all-foreground tree of site_model."""
+        x = np.asarray(x, dtype=np.float64)
+        n = len(x)
+        nb = self.nnode - 1
+        eh = 2 * small_diff * (np.abs(x) + 1)
+        D = np.zeros((n, self.npatt))
+        lnL = np.zeros((2, n))
+        for i in range(n):
+            for bf, sgn in enumerate((-1.0, 1.0)):
+                x1 = x.copy()
+                x1[i] += sgn * eh[i]
+                if i < nb:
+                    x1[i] = max(x1[i], 0.0)        # a length moved below zero acts as zero
+                f, _, lnf = self.site_model(*self.site_classes_x(x1, model))
+                lnL[bf, i] = -f
+                D[i] += sgn * lnf / (2 * eh[i])
+        H = -(D * self._fpatt[None, :]) @ D.T
+        H = 0.5 * (H + H.T)
+        g = (lnL[1] - lnL[0]) / (2 * eh)
+        try:
+            V = np.linalg.inv(-H)
+            dg = np.diag(V)
+            se = np.where(dg > 0, np.sqrt(np.abs(dg)), -1.0)
+        except np.linalg.LinAlgError:
+            se = np.full(n, -1.0)
+        return {"g": g, "H": H, "se": se}
+
     def site_neb(self, fhK, props):
         """codeml's NEB posteriors of a site model's classes (lfunNSsites_rate
         codeml.c:5079-5129: props_k f_k normalised over k, from site_model's

@@ -176,11 +176,11 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         out = open(os.path.join(d, "out.txt")).read()
         lnf_lines = open(os.path.join(d, "lnf")).read().splitlines()
         rst = open(os.path.join(d, "rst")).read()
-        if not site_model or site_model in ("M2a", "M3"):
-            with open(os.path.join(d, "codeml.ctl"), "w") as f:
-                f.write(ctl.replace("getSE = 0", "getSE = 1"))
-            subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
-            out_se = open(os.path.join(d, "out.txt")).read()
+        # a second run with getSE = 1 for codeml's standard errors
+        with open(os.path.join(d, "codeml.ctl"), "w") as f:
+            f.write(ctl.replace("getSE = 0", "getSE = 1"))
+        subprocess.run([codeml, "codeml.ctl"], cwd=d, check=True, capture_output=True, text=True)
+        out_se = open(os.path.join(d, "out.txt")).read()
     if clade:
         k = out_se.index("SEs for parameters:")
         se = {"se_6dp": [float(v) for v in out_se[k:].splitlines()[1].split()], "small_diff": 1e-6}
@@ -197,7 +197,7 @@ def run_case(codeml: str, name, ns, ncodon, seed, model, params, bscale, model_b
         if site_model == "M2a":       # BEB of M2a (lfunNSsites_M2M8 codeml.c:6190-6415): 3 classes
             extra["beb"] = parse_beb(out, rst, r.stdout, ncls=3)
             extra["beb"]["site_wmean_sd_3dp"] = parse_site_meanw(rst)
-        if site_model in ("M2a", "M3"):   # their x is model A's / model B's: SEs as for those
+        if site_model:                    # codeml's getSE = 1 SEs
             k = out_se.index("SEs for parameters:")
             extra["se_6dp"] = [float(v) for v in out_se[k:].splitlines()[1].split()]
             extra["small_diff"] = 1e-6

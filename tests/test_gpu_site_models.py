@@ -145,3 +145,19 @@ def test_site_model_se_matches_codeml(name):
     lk.close()
     ref = np.array(fx["se_6dp"])
     assert np.all(np.abs(r["se"] - ref) <= 5.01e-7 + 1e-4 * np.abs(ref))
+
+
+@pytest.mark.parametrize("name", site_model_names())
+def test_site_model_se_opg_site(name):
+    """Likelihood.se_opg_site: codeml's getSE = 1 estimator under any site
+    model from 2 n site_model evaluations on the device (the library's own
+    beta categories for M7 / M8), against codeml's printed SEs: print
+    rounding plus 1e-4 of the value."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, _ = as_model_a(fx, tree)
+    lk = api.Likelihood(t, z, fpatt, pi)
+    r = lk.se_opg_site(np.array(fx["x"]), fx["model"], small_diff=fx["small_diff"])
+    lk.close()
+    ref = np.array(fx["se_6dp"])
+    assert np.all(np.abs(r["se"] - ref) <= 5.01e-7 + 1e-4 * np.abs(ref))

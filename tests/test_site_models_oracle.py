@@ -111,3 +111,45 @@ def test_site_model_se_matches_codeml(name):
     g, H, se = pb.opg_se(x, small_diff=fx["small_diff"])
     ref = np.array(fx["se_6dp"])
     assert np.all(np.abs(se - ref) <= 5.01e-7 + 5e-5 * np.abs(ref))
+
+
+def _site_x_classes(x, nb, model):
+    """(omegas, props) of a site model at codeml's x (oracle's quantiles)."""
+    r = x[nb + 1:]
+    if model == "M1a":
+        return np.array([r[1], 1.0]), np.array([r[0], 1 - r[0]])
+    if model == "M2a":
+        return np.array([r[2], 1.0, r[3]]), np.array([r[0], r[1], 1 - r[0] - r[1]])
+    if model == "M3":
+        return np.array(r[2:5]), np.array([r[0], r[1], 1 - r[0] - r[1]])
+    if model == "M7":
+        return O.beta_classes(r[0], r[1])
+    om, pr = O.beta_classes(r[1], r[2])
+    return np.append(om, r[3]), np.append(pr * r[0], 1 - r[0])
+
+
+@pytest.mark.parametrize("name", site_model_names())
+def test_site_model_se_generic_matches_codeml(name):
+    """codeml's getSE = 1 SEs under every site model (M1a, M2a, M3, M7, M8),
+    by the estimator over the oracle's K whole-tree classes at the perturbed
+    x: print rounding plus 5e-5 of the value."""
+    fx, tree, codons = load_golden(name)
+    z, fpatt, pi = O.patterns(codons)
+    t, _ = as_model_a(fx, tree)
+    x = np.array(fx["x"])
+    nb = tree.nbranch
+    pb = O.Problem(t, z, fpatt, pi, nthreads=4)
+    n = len(x)
+    eh = 2 * fx["small_diff"] * (np.abs(x) + 1)
+    D = np.zeros((n, len(fpatt)))
+    for i in range(n):
+        for sgn in (-1.0, 1.0):
+            x1 = x.copy()
+            x1[i] += sgn * eh[i]
+            om, pr = _site_x_classes(x1, nb, fx["model"])
+            D[i] += sgn * pb.site_classes(x1[:nb], x1[nb], om, pr)[2] / (2 * eh[i])
+    H = -(D * fpatt[None, :]) @ D.T
+    V = np.linalg.inv(-0.5 * (H + H.T))
+    se = np.where(np.diag(V) > 0, np.sqrt(np.abs(np.diag(V))), -1.0)
+    ref = np.array(fx["se_6dp"])
+    assert np.all(np.abs(se - ref) <= 5.01e-7 + 5e-5 * np.abs(ref))

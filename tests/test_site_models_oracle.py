@@ -99,20 +99,6 @@ def test_site_model_neb_matches_codeml(name):
     assert np.max(np.abs(site - np.array(fx["neb_site_post_5dp"]))) <= 5.01e-6
 
 
-@pytest.mark.parametrize("name", [n for n in site_model_names() if n.startswith(("msM2a", "msM3"))])
-def test_site_model_se_matches_codeml(name):
-    """codeml's SEs (getSE = 1) under M2a and M3: their x is model A's /
-    model B's on the all-foreground tree, so the model-A / model-B estimator
-    gives them (print rounding plus 5e-5 of the value)."""
-    fx, tree, codons = load_golden(name)
-    z, fpatt, pi = O.patterns(codons)
-    t, x = as_model_a(fx, tree)
-    pb = O.Problem(t, z, fpatt, pi, nthreads=4, model_b=fx["model"] == "M3")
-    g, H, se = pb.opg_se(x, small_diff=fx["small_diff"])
-    ref = np.array(fx["se_6dp"])
-    assert np.all(np.abs(se - ref) <= 5.01e-7 + 5e-5 * np.abs(ref))
-
-
 def _site_x_classes(x, nb, model):
     """(omegas, props) of a site model at codeml's x (oracle's quantiles)."""
     r = x[nb + 1:]
@@ -128,17 +114,18 @@ def _site_x_classes(x, nb, model):
     return np.append(om, r[3]), np.append(pr * r[0], 1 - r[0])
 
 
-@pytest.mark.parametrize("name", site_model_names())
+@pytest.mark.parametrize("name", [n for n in site_model_names() if "24x400" not in n])
 def test_site_model_se_generic_matches_codeml(name):
-    """codeml's getSE = 1 SEs under every site model (M1a, M2a, M3, M7, M8),
-    by the estimator over the oracle's K whole-tree classes at the perturbed
-    x: print rounding plus 5e-5 of the value."""
+    """codeml's getSE = 1 SEs under the site models (M1a, M2a, M3, M7), by
+    the estimator over the oracle's K whole-tree classes at the perturbed x:
+    print rounding plus 5e-5 of the value (the smaller fixtures; the GPU test
+    takes all six, M8 included, against codeml's SEs)."""
     fx, tree, codons = load_golden(name)
     z, fpatt, pi = O.patterns(codons)
     t, _ = as_model_a(fx, tree)
     x = np.array(fx["x"])
     nb = tree.nbranch
-    pb = O.Problem(t, z, fpatt, pi, nthreads=4)
+    pb = O.Problem(t, z, fpatt, pi, nthreads=O.max_threads())
     n = len(x)
     eh = 2 * fx["small_diff"] * (np.abs(x) + 1)
     D = np.zeros((n, len(fpatt)))

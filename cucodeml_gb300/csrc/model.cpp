@@ -122,6 +122,14 @@ void tridiagonalize(int n, double *a, double *d, double *e, double *qt) {
     }
 }
 
+// sqrt(a^2 + b^2): the plain form when the sum of squares is comfortably
+// inside the double range (always, for rate matrices), std::hypot otherwise;
+// the plain form is about twice as fast and within an ulp
+inline double norm2(double a, double b) {
+    const double s = a * a + b * b;
+    return (s > 1e-290 && s < 1e290) ? std::sqrt(s) : std::hypot(a, b);
+}
+
 // Implicit-shift QL on the tridiagonal (d, e), e[k] coupling k and k+1.
 // zt holds the transform transposed (row i = column i of the matrix the
 // rotations multiply from the right), so that each rotation combines two
@@ -139,14 +147,14 @@ int ql_implicit(int n, double *d, double *e, double *zt) {
             if (m != l) {
                 if (iter++ == 60) return -1;
                 double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-                double r = std::hypot(g, 1.0);
+                double r = norm2(g, 1.0);
                 g = d[m] - d[l] + e[l] / (g + std::copysign(r, g));
                 double s = 1, c = 1, p = 0;
                 int i;
                 bool underflow = false;
                 for (i = m - 1; i >= l; i--) {
                     double f = s * e[i], b = c * e[i];
-                    r = std::hypot(f, g);
+                    r = norm2(f, g);
                     e[i + 1] = r;
                     if (r == 0.0) {
                         d[i + 1] -= p;

@@ -239,6 +239,15 @@ def batched_leg(args, dev):
     return out
 
 
+def max_over_ranks(vals, device):
+    """Each value's maximum over the ranks of the process group (the slowest
+    replica's times; one all-reduce)."""
+    import torch
+    t = torch.tensor(list(vals), dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 def secondary_leg(fn, *a):
     """A leg beside the headline (BEB, standard errors): its failure is
     reported in its own object and does not take the headline line down."""
@@ -707,9 +716,7 @@ def main():
         dev_ms = lk.replay(args.steps, True)
     kernels_per_eval = r.kernels
     if ws > 1:
-        t = torch.tensor([dev_ms, e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_ms, e2e_s = float(t[0]), float(t[1])
+        dev_ms, e2e_s = max_over_ranks([dev_ms, e2e_s], "cuda")
     value = ws * args.steps / (dev_ms * 1e-3)
     e2e_value = ws * args.steps / e2e_s
 

@@ -136,3 +136,35 @@ def test_beta_classes_reject_bad_parameters():
             api.beta_classes(p, q)
     L = _lib.load()
     assert L.gb_beta_classes(1.0, 1.0, 0, None, None) == -1          # GB_ERR_ARG
+
+
+def _null_args(argtypes):
+    """Arguments for one call: null pointers and arrays of null pointers,
+    1 for integers and 1.0 for doubles."""
+    out = []
+    for t in argtypes:
+        if t in (C.c_int, C.c_double):
+            out.append(t(1))
+        elif isinstance(t, type) and issubclass(t, C.Array):
+            out.append(t())
+        else:
+            out.append(None)
+    return out
+
+
+# entries whose first argument is a gb_handle * or gb_batch *
+HANDLE_ENTRIES = sorted(n for n, (_, a) in _lib.SIGNATURES.items()
+                        if a and a[0] is C.c_void_p and n != "gb_lnL_noalloc")
+
+
+def test_handle_entries_reject_a_null_handle():
+    """Every entry taking a handle or batch returns an error code (and, where
+    it sets one, a reason) for a null one before any device work, so a caller
+    that lost its handle gets a status, not a crash."""
+    L = _lib.load()
+    assert len(HANDLE_ENTRIES) >= 30
+    for name in HANDLE_ENTRIES:
+        rc = getattr(L, name)(*_null_args(_lib.SIGNATURES[name][1]))
+        assert rc < 0, name
+        if name not in ("gb_nscale", "gb_batch_size"):
+            assert L.gb_last_error().decode(), name

@@ -168,3 +168,90 @@ def test_handle_entries_reject_a_null_handle():
         assert rc < 0, name
         if name not in ("gb_nscale", "gb_batch_size"):
             assert L.gb_last_error().decode(), name
+
+
+def _raw_problem(tree, z, fpatt, pi, keep):
+    """A gb_problem over numpy copies (kept alive in `keep`)."""
+    ip, ub = C.POINTER(C.c_int), C.POINTER(C.c_ubyte)
+    father = np.ascontiguousarray(tree.father, dtype=np.int32)
+    label = np.ascontiguousarray(tree.label, dtype=np.int32)
+    z = np.ascontiguousarray(z, dtype=np.uint8)
+    fpatt = np.ascontiguousarray(fpatt, dtype=np.float64)
+    pi = np.ascontiguousarray(pi, dtype=np.float64)
+    keep += [father, label, z, fpatt, pi]
+    dp = C.POINTER(C.c_double)
+    prob = _lib.Problem(tree.ns, tree.nnode, tree.root, father.ctypes.data_as(ip), label.ctypes.data_as(ip),
+                        len(fpatt), z.ctypes.data_as(ub), fpatt.ctypes.data_as(dp), pi.ctypes.data_as(dp),
+                        None, _lib.GB_PREC_FP64, 0)
+    return prob, father, label, z, fpatt, pi
+
+
+def _internal_pair(tree):
+    """Two internal nodes other than the root, the second a son of the first."""
+    for n in range(tree.ns, tree.nnode):
+        f = int(tree.father[n])
+        if n != tree.root and f != tree.root and f >= tree.ns:
+            return f, n
+    raise AssertionError("tree too small")
+
+
+def _one_son(fa, t):
+    """Move a son of internal node n to another internal node m outside its
+    subtree, both with two sons and neither the root: n is left with one."""
+    sons = {a: [s for s in range(t.nnode) if s != t.root and fa[s] == a] for a in range(t.ns, t.nnode)}
+    for n in range(t.ns, t.nnode):
+        if n == t.root or len(sons[n]) != 2:
+            continue
+        s = sons[n][0]
+        below = {s}
+        for v in range(t.nnode):           # nodes in the subtree of s
+            a = v
+            while a != t.root and a not in below:
+                a = int(fa[a])
+            if a in below:
+                below.add(v)
+        for m in range(t.ns, t.nnode):
+            if m not in (n, t.root) and m not in below and len(sons[m]) == 2:
+                fa[s] = m
+                return
+    raise AssertionError("tree too small")
+
+
+# case -> (how the problem is spoiled, the reason gb_last_error gives)
+BAD_PROBLEMS = {
+    "root has a father": (lambda p, fa, la, z, fp, pi, t: fa.__setitem__(t.root, t.ns), "root must be"),
+    "root is a tip": (lambda p, fa, la, z, fp, pi, t: setattr(p, "root", 0), "root must be"),
+    "father out of range": (lambda p, fa, la, z, fp, pi, t: fa.__setitem__(0, t.nnode + 5), "father out of range"),
+    "father is a tip": (lambda p, fa, la, z, fp, pi, t: fa.__setitem__(1, 0), "father out of range or a tip"),
+    "four sons": (lambda p, fa, la, z, fp, pi, t: fa.__setitem__(_internal_pair(t)[1], t.root), "more than 3 sons"),
+    "label 2": (lambda p, fa, la, z, fp, pi, t: la.__setitem__(0, 2), "labels must be 0 or 1"),
+    "internal node with one son": (lambda p, fa, la, z, fp, pi, t: _one_son(fa, t), "< 2 sons"),
+    "cycle off the root": (lambda p, fa, la, z, fp, pi, t: fa.__setitem__(_internal_pair(t)[0], _internal_pair(t)[1]),
+                           "not connected"),
+    "no patterns": (lambda p, fa, la, z, fp, pi, t: setattr(p, "npatt", 0), "sizes too small"),
+    "null z": (lambda p, fa, la, z, fp, pi, t: setattr(p, "z", None), "missing arrays"),
+    "two taxa": (lambda p, fa, la, z, fp, pi, t: setattr(p, "ns", 2), "sizes too small"),
+    "codon id 61": (lambda p, fa, la, z, fp, pi, t: z.__setitem__((0, 0), 61), "codon id >= 61"),
+    "pi zero": (lambda p, fa, la, z, fp, pi, t: pi.__setitem__(5, 0.0), "pi must be positive"),
+    "negative count": (lambda p, fa, la, z, fp, pi, t: fp.__setitem__(0, -1.0), "fpatt must be >= 0"),
+    "NaN count": (lambda p, fa, la, z, fp, pi, t: fp.__setitem__(1, float("nan")), "fpatt must be >= 0"),
+}
+
+
+@pytest.mark.parametrize("case", sorted(BAD_PROBLEMS))
+def test_create_rejects_malformed_problems_on_the_host(case):
+    """gb_create checks the tree (one father per node, the root's -1, 2-3
+    sons at internal nodes, tips 0..ns-1, connected), the branch labels, the
+    codon ids, pi and the pattern counts before it looks for a device:
+    GB_ERR_ARG with a reason, here without a GPU as on a GPU machine."""
+    L = _lib.load()
+    fx, tree, codons = load_golden("c8x300_s1")
+    z, fpatt, pi = O.patterns(codons)
+    keep = []
+    prob, fa, la, zz, fp, pp = _raw_problem(tree, z, fpatt, pi, keep)
+    h = C.c_void_p()
+    spoil, reason = BAD_PROBLEMS[case]
+    spoil(prob, fa, la, zz, fp, pp, tree)
+    rc = L.gb_create(C.byref(prob), C.byref(h))
+    assert rc == -1, (case, rc, L.gb_last_error())
+    assert reason in L.gb_last_error().decode() and not h.value

@@ -2,7 +2,9 @@
 replicas only, so the one exchange is the maximum of each rank's times
 (`max_over_ranks`); and the reference arm under torchrun runs on rank 0 only,
 the other ranks exiting 0 without work."""
+import datetime
 import os
+import socket
 import subprocess
 import sys
 
@@ -15,7 +17,7 @@ def _rank(rank, ws, port, out):
     import torch.distributed as dist
     sys.path.insert(0, ROOT)
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
-    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    dist.init_process_group("gloo", rank=rank, world_size=ws, timeout=datetime.timedelta(seconds=60))
     import bench
     out.put((rank, bench.max_over_ranks([1.0 + rank, 10.0 - rank], "cpu")))
     dist.destroy_process_group()
@@ -24,7 +26,9 @@ def _rank(rank, ws, port, out):
 def test_max_over_ranks_gloo_two_ranks():
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
-    port = 29500 + os.getpid() % 1000
+    with socket.socket() as sk:            # a port that is free now
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
     ps = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
     for p in ps:
         p.start()
